@@ -1,0 +1,134 @@
+/*
+ * gmc.h -- C ABI of the GB300 batched Classic McEliece KEM engine
+ * (libgmc.so). Plain pointers and sizes only; no framework types.
+ *
+ * Parameter-set ids: 0 = mceliece348864, 1 = mceliece460896,
+ * 2 = mceliece6688128, 3 = mceliece6960119, 4 = mceliece8192128.
+ *
+ * Return codes: 0 on success, a negative GMC_E* value on failure. Per-request
+ * decapsulation status (the 6960119 ciphertext-padding rule) goes to the
+ * optional rc[] array, exactly as libmceliece's dec return value.
+ *
+ * Every entry point runs on the calling thread's current CUDA device. There is
+ * no CPU fallback: without a usable GPU the calls return GMC_ECUDA.
+ */
+#ifndef GMC_H
+#define GMC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GMC_OK 0
+#define GMC_EINVAL -1   /* bad argument (set id, null pointer, negative n) */
+#define GMC_ECUDA -2    /* CUDA error (no device, launch failure, ...) */
+#define GMC_ENOMEM -3   /* device allocation failed */
+#define GMC_EKEY -4     /* key handle of the wrong kind or a malformed key */
+
+typedef struct gmc_key gmc_key;
+
+/* ---- parameter sets -------------------------------------------------- */
+int gmc_set_count(void);
+const char *gmc_set_name(int set);
+/* looks up "348864", "mceliece348864", ...; returns the id or GMC_EINVAL */
+int gmc_set_id(const char *name);
+/* out[8] = m, n, t, mt, k, public-key bytes, secret-key bytes, ciphertext bytes */
+int gmc_set_sizes(int set, long long *out);
+
+/* ---- resident keys ---------------------------------------------------
+ * Replaces, for a batch, the per-call key argument of
+ * mceliece_kem_<set>_enc(c,k,pk) / _dec(k,c,sk)
+ * (libmceliece api: mc:crypto_kem/348864/vec/wrap_enc.c:4, wrap_dec.c:4;
+ * harness use: mceliece-gpu-params/main.cu:19-21, 191-202, 279-323).
+ * The key bytes are copied; the caller's buffer may be reused at once. */
+int gmc_pk_load(gmc_key **out, int set, const unsigned char *pk);
+int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk);
+void gmc_key_free(gmc_key *key);
+int gmc_key_set(const gmc_key *key);
+
+/* ---- batched encapsulation --------------------------------------------
+ * n requests against one public key. seeds: n x 32 bytes; request i draws its
+ * randomness from the seed chain state_0 = seeds[i], each randombytes call of
+ * libmceliece's enc returning SHAKE256({64}||state, len) and advancing
+ * state = out[0:32]. With libmceliece's randombytes interposed by that chain
+ * the outputs are byte-identical to mceliece_kem_<set>_enc
+ * (mc:crypto_kem/348864/vec/encrypt.c:41-90, kem_enc.c:18).
+ * c: n x ct bytes, k: n x 32 bytes, rc (optional): n ints (enc return value,
+ * -1 only for a 6960119 key with nonzero padding bits, as the library).
+ * _dev: all pointers are device pointers, work is queued on `stream`
+ * (a cudaStream_t, 0 = default stream) and the call returns without waiting.
+ * Without _dev: host pointers; the call copies in, runs and copies out. */
+int gmc_enc_batch_dev(const gmc_key *pk, unsigned char *c, unsigned char *k, const unsigned char *seeds,
+                      long long n, int *rc, void *stream);
+int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char *k, const unsigned char *seeds,
+                  long long n, int *rc);
+
+/* ---- batched decapsulation ---------------------------------------------
+ * n ciphertexts against one secret key (mc:crypto_kem/348864/vec/kem_dec.c:19,
+ * implicit rejection; 6960119 padding rule mc:crypto_kem/6960119/vec/kem_dec.c:21).
+ * k: n x 32 bytes; rc (optional): per-request dec return value (0, or -1 with
+ * k = 0xff..ff for a 6960119 ciphertext whose padding bits are set). */
+int gmc_dec_batch_dev(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc,
+                      void *stream);
+int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc);
+
+/* ---- libmceliece calling convention (one request per call) --------------
+ * Same signatures and results as mceliece_kem_<set>_enc / _dec
+ * (mc:crypto_kem/<set>/vec/wrap_enc.c:4, wrap_dec.c:4). enc draws one 32-byte
+ * seed from the randombytes source (default: the OS generator) and runs the
+ * GPU seed chain. dec tolerates k == c and k == sk (outputs written last). */
+int gmc_kem_348864_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_348864_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+int gmc_kem_460896_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_460896_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+int gmc_kem_6688128_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6688128_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+int gmc_kem_6960119_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6960119_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+int gmc_kem_8192128_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_8192128_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+
+/* randombytes source of the one-request enc entry points
+ * (librandombytes' randombytes(), rb:include/randombytes.h:10). NULL restores
+ * the OS generator. */
+typedef void (*gmc_randombytes_fn)(void *ctx, unsigned char *out, long long len);
+void gmc_set_randombytes(gmc_randombytes_fn fn, void *ctx);
+
+/* ---- engine selection and diagnostics ----------------------------------- */
+#define GMC_GEMM_POPC 0   /* CUDA-core AND/XOR + popcount */
+#define GMC_GEMM_B1MMA 1  /* legacy mma.sync m8n8k128 .b1 AND.POPC */
+#define GMC_GEMM_TC 2     /* tcgen05 (5th-gen tensor cores), 0/1 operands in FP8, TMEM accumulators */
+int gmc_set_gemm_engine(int engine);
+int gmc_get_gemm_engine(void);
+
+/* Stage outputs of a decapsulation batch (device pointers): the 2t packed
+ * syndromes (s_words per request), the error vectors (e_words per request)
+ * and the decode flags. For the staged parity tests. */
+int gmc_dec_stages_dev(const gmc_key *sk, const unsigned char *c, long long n, unsigned int *synd,
+                       int synd_words, unsigned int *e, int e_words, int *ok, void *stream);
+/* Stage outputs of an encapsulation batch: error vectors and raw syndromes
+ * T*e[mt:n] (device pointers). */
+int gmc_enc_stages_dev(const gmc_key *pk, const unsigned char *seeds, long long n, unsigned int *e,
+                       int e_words, unsigned int *synd, int synd_words, void *stream);
+/* Raw GF(2) product Out[i] = A * X[i] on the selected engine (device
+ * pointers, layouts as documented in the engine: rows_pad % 128 == 0,
+ * kw_pad % 8 == 0, n_pad % 64 == 0, lda/ldx >= kw_pad). */
+int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int rows_pad, const unsigned int *X, int ldx,
+                     long long n_pad, int kw_pad, unsigned int *out, int ldo, int out_words, long long n,
+                     void *stream);
+
+/* Host-only views of the per-key / per-field tables the engine uploads (no
+ * GPU needed): support L[n], L_i^(2^d) [n], front-end matrix F (returns its
+ * word count; *ldf = its row stride), GF(2^m) exp[2q-1]/log[q] and the
+ * additive-FFT constants (alpha_log[q], twist_log[2^(d+1)]). */
+int gmc_host_sk_tables(int set, const unsigned char *sk, unsigned short *L, unsigned short *Lpow, unsigned int *F,
+                       long long f_words, int *ldf);
+int gmc_host_field_tables(int set, unsigned short *gexp, unsigned short *glog, unsigned short *alpha_log,
+                          unsigned short *twist_log);
+
+const char *gmc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

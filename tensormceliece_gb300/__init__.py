@@ -1,0 +1,236 @@
+"""GB300 batched Classic McEliece KEM engine: Python mirror of the C ABI (include/gmc.h).
+
+The engine is libgmc.so, built in-tree by tensormceliece_gb300.build. This module
+loads it with ctypes and exposes the libmceliece-shaped calls
+(``kem_enc``/``kem_dec`` per set) and the batched, resident-key calls
+(``PublicKey``/``SecretKey`` with ``enc_batch``/``dec_batch``). There is no CPU
+fallback: if the library or a GPU is missing the calls raise ``GmcError``.
+
+Buffers: host calls take/return ``bytes``/numpy ``uint8`` arrays; the ``*_dev``
+calls take raw device pointers (ints), e.g. ``torch.Tensor.data_ptr()``, and a
+``cudaStream_t`` handle (``torch.cuda.current_stream().cuda_stream``).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "SETS", "GmcError", "lib", "set_id", "set_sizes", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
+    "set_gemm_engine", "get_gemm_engine", "set_randombytes", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC",
+]
+
+SETS = ("348864", "460896", "6688128", "6960119", "8192128")
+GEMM_POPC, GEMM_B1MMA, GEMM_TC = 0, 1, 2
+_ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad key"}
+
+_lib = None
+
+
+class GmcError(RuntimeError):
+    pass
+
+
+def lib():
+    """Loads libgmc.so (building it first when the sources are newer)."""
+    global _lib
+    if _lib is None:
+        path = _build.LIB
+        if not os.path.exists(path) or os.environ.get("GMC_AUTOBUILD", "1") == "1":
+            path = _build.build()
+        L = ctypes.CDLL(path)
+        c_u8p = ctypes.c_void_p
+        L.gmc_set_name.restype = ctypes.c_char_p
+        L.gmc_last_error.restype = ctypes.c_char_p
+        L.gmc_set_id.argtypes = [ctypes.c_char_p]
+        L.gmc_set_sizes.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+        L.gmc_pk_load.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, c_u8p]
+        L.gmc_sk_load.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, c_u8p]
+        L.gmc_key_free.argtypes = [ctypes.c_void_p]
+        L.gmc_key_free.restype = None
+        for fn in ("gmc_enc_batch", "gmc_enc_batch_dev"):
+            f = getattr(L, fn)
+            f.argtypes = [ctypes.c_void_p, c_u8p, c_u8p, c_u8p, ctypes.c_longlong, ctypes.c_void_p] + (
+                [ctypes.c_void_p] if fn.endswith("_dev") else [])
+        for fn in ("gmc_dec_batch", "gmc_dec_batch_dev"):
+            f = getattr(L, fn)
+            f.argtypes = [ctypes.c_void_p, c_u8p, c_u8p, ctypes.c_longlong, ctypes.c_void_p] + (
+                [ctypes.c_void_p] if fn.endswith("_dev") else [])
+        L.gmc_dec_stages_dev.argtypes = [ctypes.c_void_p, c_u8p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        L.gmc_enc_stages_dev.argtypes = [ctypes.c_void_p, c_u8p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.gmc_gf2_gemm_dev.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_int, ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p]
+        for s in SETS:
+            for op in ("enc", "dec"):
+                getattr(L, f"gmc_kem_{s}_{op}").argtypes = [c_u8p, c_u8p, c_u8p]
+        L.gmc_set_randombytes.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gmc_set_randombytes.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(rc, what):
+    if rc < 0:
+        msg = lib().gmc_last_error().decode(errors="replace")
+        raise GmcError(f"{what}: {_ERRORS.get(rc, rc)} ({msg})")
+    return rc
+
+
+def set_id(name):
+    name = str(name)
+    if name.startswith("mceliece"):
+        name = name[len("mceliece"):]
+    if name not in SETS:
+        raise GmcError(f"unknown parameter set {name!r}")
+    return SETS.index(name)
+
+
+def set_sizes(s):
+    """dict with m, n, t, mt, k, pk_bytes, sk_bytes, ct_bytes for a set (name or id)."""
+    sid = s if isinstance(s, int) else set_id(s)
+    out = (ctypes.c_longlong * 8)()
+    _check(lib().gmc_set_sizes(sid, out), "gmc_set_sizes")
+    keys = ("m", "n", "t", "mt", "k", "pk_bytes", "sk_bytes", "ct_bytes")
+    return dict(zip(keys, [int(v) for v in out]))
+
+
+def _u8(buf, n=None):
+    a = np.frombuffer(buf, dtype=np.uint8) if isinstance(buf, (bytes, bytearray)) else np.ascontiguousarray(
+        buf, dtype=np.uint8)
+    if n is not None and a.size != n:
+        raise GmcError(f"expected {n} bytes, got {a.size}")
+    return a
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _Key:
+    _kind = None
+
+    def __init__(self, set_name, key_bytes):
+        self.set = set_id(set_name) if not isinstance(set_name, int) else set_name
+        self.sizes = set_sizes(self.set)
+        nbytes = self.sizes["pk_bytes" if self._kind == "pk" else "sk_bytes"]
+        raw = _u8(key_bytes, nbytes)
+        h = ctypes.c_void_p()
+        loader = lib().gmc_pk_load if self._kind == "pk" else lib().gmc_sk_load
+        _check(loader(ctypes.byref(h), self.set, _ptr(raw)), f"gmc_{self._kind}_load")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gmc_key_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PublicKey(_Key):
+    """Device-resident public key: batched encapsulation."""
+    _kind = "pk"
+
+    def enc_batch(self, seeds):
+        """seeds: n x 32 bytes -> (ct [n, ct_bytes] uint8, K [n, 32] uint8, rc [n] int32)."""
+        s = _u8(seeds)
+        n = s.size // 32
+        if s.size != 32 * n:
+            raise GmcError("seeds must be a multiple of 32 bytes")
+        c = np.zeros((n, self.sizes["ct_bytes"]), np.uint8)
+        k = np.zeros((n, 32), np.uint8)
+        rc = np.zeros(n, np.int32)
+        _check(lib().gmc_enc_batch(self._h, _ptr(c), _ptr(k), _ptr(s), n, _ptr(rc)), "gmc_enc_batch")
+        return c, k, rc
+
+    def enc_batch_dev(self, c_ptr, k_ptr, seeds_ptr, n, rc_ptr=0, stream=0):
+        return _check(lib().gmc_enc_batch_dev(self._h, c_ptr, k_ptr, seeds_ptr, n, rc_ptr or None, stream or None),
+                      "gmc_enc_batch_dev")
+
+
+class SecretKey(_Key):
+    """Device-resident secret key: batched decapsulation."""
+    _kind = "sk"
+
+    def dec_batch(self, cts):
+        """cts: n x ct_bytes -> (K [n, 32] uint8, rc [n] int32)."""
+        cb = self.sizes["ct_bytes"]
+        c = _u8(cts)
+        n = c.size // cb
+        if c.size != cb * n:
+            raise GmcError(f"ciphertexts must be a multiple of {cb} bytes")
+        k = np.zeros((n, 32), np.uint8)
+        rc = np.zeros(n, np.int32)
+        _check(lib().gmc_dec_batch(self._h, _ptr(k), _ptr(c), n, _ptr(rc)), "gmc_dec_batch")
+        return k, rc
+
+    def dec_batch_dev(self, k_ptr, c_ptr, n, rc_ptr=0, stream=0):
+        return _check(lib().gmc_dec_batch_dev(self._h, k_ptr, c_ptr, n, rc_ptr or None, stream or None),
+                      "gmc_dec_batch_dev")
+
+
+def kem_enc(set_name, pk):
+    """libmceliece-shaped enc: returns (rc, ct, K); randomness from the randombytes source."""
+    sz = set_sizes(set_name)
+    c = np.zeros(sz["ct_bytes"], np.uint8)
+    k = np.zeros(32, np.uint8)
+    p = _u8(pk, sz["pk_bytes"])
+    name = SETS[set_name] if isinstance(set_name, int) else SETS[set_id(set_name)]
+    rc = getattr(lib(), f"gmc_kem_{name}_enc")(_ptr(c), _ptr(k), _ptr(p))
+    if rc < -1:
+        _check(rc, f"gmc_kem_{name}_enc")
+    return rc, c.tobytes(), k.tobytes()
+
+
+def kem_dec(set_name, ct, sk):
+    """libmceliece-shaped dec: returns (rc, K)."""
+    sz = set_sizes(set_name)
+    c = _u8(ct, sz["ct_bytes"])
+    s = _u8(sk, sz["sk_bytes"])
+    k = np.zeros(32, np.uint8)
+    name = SETS[set_name] if isinstance(set_name, int) else SETS[set_id(set_name)]
+    rc = getattr(lib(), f"gmc_kem_{name}_dec")(_ptr(k), _ptr(c), _ptr(s))
+    if rc < -1:
+        _check(rc, f"gmc_kem_{name}_dec")
+    return rc, k.tobytes()
+
+
+def set_gemm_engine(engine):
+    _check(lib().gmc_set_gemm_engine(int(engine)), "gmc_set_gemm_engine")
+
+
+def get_gemm_engine():
+    return lib().gmc_get_gemm_engine()
+
+
+_RNG_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_ubyte), ctypes.c_longlong)
+_rng_keepalive = None
+
+
+def set_randombytes(fn):
+    """fn(n) -> bytes of length n, or None for the OS generator (one-request enc only)."""
+    global _rng_keepalive
+    if fn is None:
+        lib().gmc_set_randombytes(None, None)
+        _rng_keepalive = None
+        return
+
+    def cb(_ctx, out, n):
+        data = fn(int(n))
+        ctypes.memmove(out, data, int(n))
+
+    _rng_keepalive = _RNG_CB(cb)
+    lib().gmc_set_randombytes(ctypes.cast(_rng_keepalive, ctypes.c_void_p), None)

@@ -1,0 +1,567 @@
+// Engine: resident keys, per-batch launch sequences, and the C ABI of gmc.h.
+//
+// Encapsulation of n requests (one public key):
+//   sample (n threads)            seeds -> e (n bits), e[mt:n] (GEMM operand)
+//   gf2_gemm (T x e[mt:n])        -> raw syndromes
+//   finalize (n threads)          c = e[0:mt] ^ syndrome, K = H(1,e,c)
+// Decapsulation of n ciphertexts (one secret key):
+//   pack_ct                       ct bytes -> words
+//   gf2_gemm (F x c)              -> 2t syndromes of the Goppa code
+//   decode (one warp per request) BM, additive FFT, error, re-encryption check
+//   dec_tail (n threads)          K = H(b, e or s, c)
+// Reference flow: mceliece-gpu-params/main.cu:228-239 (encaps), 352-370 (decaps).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include <sys/random.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gmc.h"
+#include "host_keys.h"
+#include "kernels.h"
+
+using namespace gmc;
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+static int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+static int cuda_fail(cudaError_t e, const char *where) {
+  return fail(GMC_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define GMC_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call);  \
+  } while (0)
+
+extern "C" const char *gmc_last_error(void) { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------- keys
+struct gmc_key {
+  int set = 0;
+  int kind = 0;  // 0 public, 1 secret
+  int device = 0;
+  // public key
+  uint32_t *T = nullptr;
+  int lda = 0, rows_pad = 0, kw_pad = 0, pad_bad = 0;
+  // secret key
+  uint32_t *F = nullptr;
+  int ldf = 0, frows_pad = 0, cw_pad = 0;
+  uint16_t *tabs = nullptr;  // L | LL | LW2 | Lpow, n each
+  uint8_t *s = nullptr;
+  DecKeyDev dk{};
+};
+
+static int g_engine = GEMM_POPC;
+
+// per (device, set) field and FFT tables
+struct FieldEntry {
+  uint16_t *buf = nullptr;
+  FieldDev fd{};
+};
+static std::mutex g_field_mu;
+static std::map<std::pair<int, int>, FieldEntry> g_fields;
+
+static int get_field(int set, FieldDev *out) {
+  int dev = 0;
+  GMC_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_field_mu);
+  auto key = std::make_pair(dev, set);
+  auto it = g_fields.find(key);
+  if (it != g_fields.end()) {
+    *out = it->second.fd;
+    return GMC_OK;
+  }
+  const gmc_setinfo &S = set_info(set);
+  const HostField &F = host_field(S.m);
+  FftTables ft = build_fft_tables(S.m, S.fft_d);
+  std::vector<uint16_t> all;
+  const size_t o_exp = 0, o_log = o_exp + F.exp.size(), o_alpha = o_log + F.log.size(),
+               o_twist = o_alpha + ft.alpha_log.size();
+  all.insert(all.end(), F.exp.begin(), F.exp.end());
+  all.insert(all.end(), F.log.begin(), F.log.end());
+  all.insert(all.end(), ft.alpha_log.begin(), ft.alpha_log.end());
+  all.insert(all.end(), ft.twist_log.begin(), ft.twist_log.end());
+  FieldEntry e;
+  GMC_CUDA(cudaMalloc(&e.buf, all.size() * 2));
+  GMC_CUDA(cudaMemcpy(e.buf, all.data(), all.size() * 2, cudaMemcpyHostToDevice));
+  e.fd.gexp = e.buf + o_exp;
+  e.fd.glog = e.buf + o_log;
+  e.fd.fft_alpha_log = e.buf + o_alpha;
+  e.fd.fft_twist_log = e.buf + o_twist;
+  g_fields[key] = e;
+  *out = e.fd;
+  return GMC_OK;
+}
+
+static bool valid_set(int set) { return set >= 0 && set < GMC_NSETS; }
+
+extern "C" int gmc_set_count(void) { return GMC_NSETS; }
+extern "C" const char *gmc_set_name(int set) { return valid_set(set) ? set_info(set).name : nullptr; }
+extern "C" int gmc_set_id(const char *name) {
+  if (!name) return GMC_EINVAL;
+  if (!strncmp(name, "mceliece", 8)) name += 8;
+  for (int i = 0; i < GMC_NSETS; i++)
+    if (!strcmp(name, set_info(i).name)) return i;
+  return GMC_EINVAL;
+}
+extern "C" int gmc_set_sizes(int set, long long *out) {
+  if (!valid_set(set) || !out) return fail(GMC_EINVAL, "gmc_set_sizes: bad argument");
+  const gmc_setinfo &S = set_info(set);
+  out[0] = S.m; out[1] = S.n; out[2] = S.t; out[3] = S.mt; out[4] = S.k;
+  out[5] = S.pk_bytes; out[6] = S.sk_bytes; out[7] = S.synd_bytes;
+  return GMC_OK;
+}
+
+extern "C" int gmc_pk_load(gmc_key **out, int set, const unsigned char *pk) {
+  if (!out || !pk || !valid_set(set)) return fail(GMC_EINVAL, "gmc_pk_load: bad argument");
+  *out = nullptr;
+  PkHost h;
+  build_pk(set, pk, h);
+  gmc_key *k = new gmc_key();
+  k->set = set;
+  k->kind = 0;
+  cudaGetDevice(&k->device);
+  k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad;
+  cudaError_t e = cudaMalloc(&k->T, h.T.size() * 4);
+  if (e != cudaSuccess) { delete k; return cuda_fail(e, "gmc_pk_load: cudaMalloc"); }
+  e = cudaMemcpy(k->T, h.T.data(), h.T.size() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(k->T); delete k; return cuda_fail(e, "gmc_pk_load: copy"); }
+  *out = k;
+  return GMC_OK;
+}
+
+extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
+  if (!out || !sk || !valid_set(set)) return fail(GMC_EINVAL, "gmc_sk_load: bad argument");
+  *out = nullptr;
+  SkHost h;
+  if (build_sk(set, sk, h)) return fail(GMC_EKEY, "gmc_sk_load: Goppa polynomial vanishes on the support");
+  const gmc_setinfo &S = set_info(set);
+  gmc_key *k = new gmc_key();
+  k->set = set;
+  k->kind = 1;
+  cudaGetDevice(&k->device);
+  k->ldf = h.ldf; k->frows_pad = h.frows_pad; k->cw_pad = h.cw_pad;
+  const size_t n = S.n;
+  cudaError_t e = cudaMalloc(&k->F, h.F.size() * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&k->tabs, 4 * n * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&k->s, S.e_bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(k->F, h.F.data(), h.F.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->tabs, h.L.data(), n * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->tabs + n, h.LL.data(), n * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 2 * n, h.LW2.data(), n * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 3 * n, h.Lpow.data(), n * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->s, h.s.data(), S.e_bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s);
+    delete k;
+    return cuda_fail(e, "gmc_sk_load");
+  }
+  k->dk.L = k->tabs;
+  k->dk.LL = k->tabs + n;
+  k->dk.LW2 = k->tabs + 2 * n;
+  k->dk.Lpow = k->tabs + 3 * n;
+  k->dk.s = k->s;
+  *out = k;
+  return GMC_OK;
+}
+
+extern "C" void gmc_key_free(gmc_key *key) {
+  if (!key) return;
+  cudaFree(key->T);
+  cudaFree(key->F);
+  cudaFree(key->tabs);
+  cudaFree(key->s);
+  delete key;
+}
+
+extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set : GMC_EINVAL; }
+
+extern "C" int gmc_set_gemm_engine(int engine) {
+  if (engine < GEMM_POPC || engine > GEMM_TC) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
+  g_engine = engine;
+  return GMC_OK;
+}
+extern "C" int gmc_get_gemm_engine(void) { return g_engine; }
+
+// ---------------------------------------------------------------- workspace
+// Stream-ordered scratch: allocated from the device's default memory pool on
+// the caller's stream and released on it after the last kernel.
+struct Scratch {
+  cudaStream_t st;
+  std::vector<void *> ptrs;
+  explicit Scratch(cudaStream_t s) : st(s) {}
+  cudaError_t get(void **p, size_t bytes) {
+    cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, st);
+    if (e == cudaSuccess) ptrs.push_back(*p);
+    return e;
+  }
+  ~Scratch() {
+    for (void *p : ptrs) cudaFreeAsync(p, st);
+  }
+};
+
+struct EncDims {
+  int lde, ldx, lds;
+  long long n_pad;
+};
+static EncDims enc_dims(const gmc_key *pk, long long n) {
+  const gmc_setinfo &S = set_info(pk->set);
+  EncDims d;
+  d.lde = round_up((S.n + 31) / 32, 4);
+  d.ldx = pk->kw_pad;
+  d.lds = round_up((S.mt + 31) / 32, 4);
+  d.n_pad = (n + kGemmOpTile - 1) / kGemmOpTile * kGemmOpTile;
+  return d;
+}
+
+template <int SET>
+static cudaError_t enc_sample_gemm(const gmc_key *pk, const uint8_t *seeds, long long n, uint32_t *E, uint32_t *Ens,
+                                   uint32_t *S, const EncDims &d, cudaStream_t st) {
+  using p = P<SET>;
+  cudaError_t e = launch_sample<SET>(seeds, n, E, d.lde, Ens, d.ldx, st);
+  if (e != cudaSuccess) return e;
+  return launch_gf2_gemm(g_engine, pk->T, pk->lda, pk->rows_pad, Ens, d.ldx, d.n_pad, pk->kw_pad, S, d.lds, p::mw,
+                         n, st);
+}
+
+template <int SET>
+static cudaError_t enc_run(const gmc_key *pk, uint8_t *c, uint8_t *k, const uint8_t *seeds, long long n,
+                           cudaStream_t st, Scratch &scr) {
+  EncDims d = enc_dims(pk, n);
+  uint32_t *E, *Ens, *S;
+  cudaError_t e;
+  if ((e = scr.get((void **)&E, (size_t)n * d.lde * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&Ens, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&S, (size_t)n * d.lds * 4)) != cudaSuccess) return e;
+  if ((e = enc_sample_gemm<SET>(pk, seeds, n, E, Ens, S, d, st)) != cudaSuccess) return e;
+  return launch_finalize<SET>(E, d.lde, S, d.lds, c, k, n, pk->pad_bad, st);
+}
+
+struct DecDims {
+  int ldx, lds2, lde;
+  long long n_pad;
+};
+static DecDims dec_dims(const gmc_key *sk, long long n) {
+  const gmc_setinfo &S = set_info(sk->set);
+  DecDims d;
+  d.ldx = sk->cw_pad;
+  d.lds2 = round_up((2 * S.t * S.m + 31) / 32, 4);
+  d.lde = round_up((S.n + 31) / 32, 4);
+  d.n_pad = (n + kGemmOpTile - 1) / kGemmOpTile * kGemmOpTile;
+  return d;
+}
+
+template <int SET>
+static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long long n, uint32_t *X, uint32_t *S2,
+                                    uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
+  using p = P<SET>;
+  FieldDev fd;
+  if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
+  cudaError_t e = launch_pack_ct<SET>(c, n, X, d.ldx, st);
+  if (e != cudaSuccess) return e;
+  e = launch_gf2_gemm(g_engine, sk->F, sk->ldf, sk->frows_pad, X, d.ldx, d.n_pad, sk->cw_pad, S2, d.lds2, p::s2w,
+                      n, st);
+  if (e != cudaSuccess) return e;
+  return launch_decode<SET>(S2, d.lds2, sk->dk, fd, n, E, d.lde, ok, st);
+}
+
+template <int SET>
+static cudaError_t dec_run(const gmc_key *sk, uint8_t *k, const uint8_t *c, long long n, int *rc, cudaStream_t st,
+                           Scratch &scr) {
+  DecDims d = dec_dims(sk, n);
+  uint32_t *X, *S2, *E;
+  int *ok;
+  cudaError_t e;
+  if ((e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&S2, (size_t)n * d.lds2 * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&E, (size_t)n * d.lde * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&ok, (size_t)n * 4)) != cudaSuccess) return e;
+  if ((e = dec_front_decode<SET>(sk, c, n, X, S2, E, ok, d, st)) != cudaSuccess) return e;
+  return launch_dec_tail<SET>(E, d.lde, ok, c, sk->dk, k, rc, n, st);
+}
+
+#define GMC_DISPATCH(set, call) \
+  switch (set) {                \
+    case 0: { constexpr int S_ = 0; call; } break; \
+    case 1: { constexpr int S_ = 1; call; } break; \
+    case 2: { constexpr int S_ = 2; call; } break; \
+    case 3: { constexpr int S_ = 3; call; } break; \
+    default: { constexpr int S_ = 4; call; } break; \
+  }
+
+static int check_key(const gmc_key *key, int kind, const char *fn) {
+  if (!key) return fail(GMC_EINVAL, std::string(fn) + ": null key");
+  if (key->kind != kind) return fail(GMC_EKEY, std::string(fn) + ": wrong key kind");
+  return GMC_OK;
+}
+
+__global__ void fill_int_kernel(int *p, long long n, int v) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+extern "C" int gmc_enc_batch_dev(const gmc_key *pk, unsigned char *c, unsigned char *k, const unsigned char *seeds,
+                                 long long n, int *rc, void *stream) {
+  int r = check_key(pk, 0, "gmc_enc_batch_dev");
+  if (r) return r;
+  if (n < 0 || (n && (!c || !k || !seeds))) return fail(GMC_EINVAL, "gmc_enc_batch_dev: bad argument");
+  if (!n) return GMC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  {
+    Scratch scr(st);
+    GMC_DISPATCH(pk->set, e = enc_run<S_>(pk, c, k, seeds, n, st, scr));
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_enc_batch_dev");
+  if (rc) {
+    fill_int_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rc, n, pk->pad_bad ? -1 : 0);
+    GMC_CUDA(cudaGetLastError());
+  }
+  return GMC_OK;
+}
+
+extern "C" int gmc_dec_batch_dev(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc,
+                                 void *stream) {
+  int r = check_key(sk, 1, "gmc_dec_batch_dev");
+  if (r) return r;
+  if (n < 0 || (n && (!c || !k))) return fail(GMC_EINVAL, "gmc_dec_batch_dev: bad argument");
+  if (!n) return GMC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  {
+    Scratch scr(st);
+    GMC_DISPATCH(sk->set, e = dec_run<S_>(sk, k, c, n, rc, st, scr));
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_batch_dev");
+  return GMC_OK;
+}
+
+// host-pointer variants: own stream, copies in, run, copies out
+extern "C" int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char *k, const unsigned char *seeds,
+                             long long n, int *rc) {
+  int r = check_key(pk, 0, "gmc_enc_batch");
+  if (r) return r;
+  if (n < 0 || (n && (!c || !k || !seeds))) return fail(GMC_EINVAL, "gmc_enc_batch: bad argument");
+  if (!n) return GMC_OK;
+  const gmc_setinfo &S = set_info(pk->set);
+  cudaStream_t st;
+  GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  uint8_t *d_seeds = nullptr, *d_c = nullptr, *d_k = nullptr;
+  int *d_rc = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_seeds, (size_t)n * 32, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_c, (size_t)n * S.synd_bytes, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_k, (size_t)n * 32, st);
+  if (e == cudaSuccess && rc) e = cudaMallocAsync(&d_rc, (size_t)n * 4, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_seeds, seeds, (size_t)n * 32, cudaMemcpyHostToDevice, st);
+  int res = GMC_OK;
+  if (e == cudaSuccess) {
+    res = gmc_enc_batch_dev(pk, d_c, d_k, d_seeds, n, d_rc, st);
+    if (res == GMC_OK) {
+      e = cudaMemcpyAsync(c, d_c, (size_t)n * S.synd_bytes, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(k, d_k, (size_t)n * 32, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess && rc) e = cudaMemcpyAsync(rc, d_rc, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    }
+  }
+  cudaFreeAsync(d_seeds, st); cudaFreeAsync(d_c, st); cudaFreeAsync(d_k, st);
+  if (d_rc) cudaFreeAsync(d_rc, st);
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (res != GMC_OK) return res;
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_enc_batch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "gmc_enc_batch: sync");
+  return GMC_OK;
+}
+
+extern "C" int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc) {
+  int r = check_key(sk, 1, "gmc_dec_batch");
+  if (r) return r;
+  if (n < 0 || (n && (!c || !k))) return fail(GMC_EINVAL, "gmc_dec_batch: bad argument");
+  if (!n) return GMC_OK;
+  const gmc_setinfo &S = set_info(sk->set);
+  cudaStream_t st;
+  GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  uint8_t *d_c = nullptr, *d_k = nullptr;
+  int *d_rc = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_c, (size_t)n * S.synd_bytes, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_k, (size_t)n * 32, st);
+  if (e == cudaSuccess && rc) e = cudaMallocAsync(&d_rc, (size_t)n * 4, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, (size_t)n * S.synd_bytes, cudaMemcpyHostToDevice, st);
+  int res = GMC_OK;
+  if (e == cudaSuccess) {
+    res = gmc_dec_batch_dev(sk, d_k, d_c, n, d_rc, st);
+    if (res == GMC_OK) {
+      e = cudaMemcpyAsync(k, d_k, (size_t)n * 32, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess && rc) e = cudaMemcpyAsync(rc, d_rc, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    }
+  }
+  cudaFreeAsync(d_c, st); cudaFreeAsync(d_k, st);
+  if (d_rc) cudaFreeAsync(d_rc, st);
+  cudaError_t e2 = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (res != GMC_OK) return res;
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_batch");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "gmc_dec_batch: sync");
+  return GMC_OK;
+}
+
+// ---------------------------------------------------------------- stages
+extern "C" int gmc_dec_stages_dev(const gmc_key *sk, const unsigned char *c, long long n, unsigned int *synd,
+                                  int synd_words, unsigned int *ev, int e_words, int *ok, void *stream) {
+  int r = check_key(sk, 1, "gmc_dec_stages_dev");
+  if (r) return r;
+  if (n <= 0 || !c || !synd || !ev || !ok) return fail(GMC_EINVAL, "gmc_dec_stages_dev: bad argument");
+  DecDims d = dec_dims(sk, n);
+  if (synd_words != d.lds2 || e_words != d.lde) return fail(GMC_EINVAL, "gmc_dec_stages_dev: row strides");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  {
+    Scratch scr(st);
+    uint32_t *X;
+    e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4);
+    if (e == cudaSuccess) GMC_DISPATCH(sk->set, e = dec_front_decode<S_>(sk, c, n, X, synd, ev, ok, d, st));
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_stages_dev");
+  return GMC_OK;
+}
+
+extern "C" int gmc_enc_stages_dev(const gmc_key *pk, const unsigned char *seeds, long long n, unsigned int *ev,
+                                  int e_words, unsigned int *synd, int synd_words, void *stream) {
+  int r = check_key(pk, 0, "gmc_enc_stages_dev");
+  if (r) return r;
+  if (n <= 0 || !seeds || !ev || !synd) return fail(GMC_EINVAL, "gmc_enc_stages_dev: bad argument");
+  EncDims d = enc_dims(pk, n);
+  if (e_words != d.lde || synd_words != d.lds) return fail(GMC_EINVAL, "gmc_enc_stages_dev: row strides");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  {
+    Scratch scr(st);
+    uint32_t *Ens;
+    e = scr.get((void **)&Ens, (size_t)d.n_pad * d.ldx * 4);
+    if (e == cudaSuccess) GMC_DISPATCH(pk->set, e = enc_sample_gemm<S_>(pk, seeds, n, ev, Ens, synd, d, st));
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_enc_stages_dev");
+  return GMC_OK;
+}
+
+extern "C" int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int rows_pad, const unsigned int *X,
+                                int ldx, long long n_pad, int kw_pad, unsigned int *out, int ldo, int out_words,
+                                long long n, void *stream) {
+  if (!A || !X || !out || n < 0 || lda < kw_pad || ldx < kw_pad || ldo < out_words)
+    return fail(GMC_EINVAL, "gmc_gf2_gemm_dev: bad argument");
+  cudaError_t e = launch_gf2_gemm(engine, A, lda, rows_pad, X, ldx, n_pad, kw_pad, out, ldo, out_words, n,
+                                  (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "gmc_gf2_gemm_dev");
+  return GMC_OK;
+}
+
+// ---------------------------------------------------------------- one-request API
+static std::mutex g_rng_mu;
+static gmc_randombytes_fn g_rng = nullptr;
+static void *g_rng_ctx = nullptr;
+
+extern "C" void gmc_set_randombytes(gmc_randombytes_fn fn, void *ctx) {
+  std::lock_guard<std::mutex> lk(g_rng_mu);
+  g_rng = fn;
+  g_rng_ctx = ctx;
+}
+
+static int draw_seed(uint8_t seed[32]) {
+  gmc_randombytes_fn fn;
+  void *ctx;
+  {
+    std::lock_guard<std::mutex> lk(g_rng_mu);
+    fn = g_rng;
+    ctx = g_rng_ctx;
+  }
+  if (fn) {
+    fn(ctx, seed, 32);
+    return GMC_OK;
+  }
+  size_t got = 0;
+  while (got < 32) {
+    ssize_t r = getrandom(seed + got, 32 - got, 0);
+    if (r <= 0) return fail(GMC_ECUDA, "randombytes: getrandom failed");
+    got += (size_t)r;
+  }
+  return GMC_OK;
+}
+
+static int one_enc(int set, unsigned char *c, unsigned char *k, const unsigned char *pk) {
+  uint8_t seed[32];
+  int r = draw_seed(seed);
+  if (r) return r;
+  gmc_key *h = nullptr;
+  if ((r = gmc_pk_load(&h, set, pk)) != GMC_OK) return r;
+  int rc = 0;
+  r = gmc_enc_batch(h, c, k, seed, 1, &rc);
+  gmc_key_free(h);
+  return r ? r : rc;
+}
+
+static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsigned char *sk) {
+  const gmc_setinfo &S = set_info(set);
+  std::vector<uint8_t> cc(c, c + S.synd_bytes);  // k may alias c or sk
+  gmc_key *h = nullptr;
+  int r = gmc_sk_load(&h, set, sk);
+  if (r) return r;
+  uint8_t kk[32];
+  int rc = 0;
+  r = gmc_dec_batch(h, kk, cc.data(), 1, &rc);
+  gmc_key_free(h);
+  if (r) return r;
+  memcpy(k, kk, 32);
+  return rc;
+}
+
+#define GMC_ONE(NAME, SET)                                                                               \
+  extern "C" int gmc_kem_##NAME##_enc(unsigned char *c, unsigned char *k, const unsigned char *pk) {    \
+    return one_enc(SET, c, k, pk);                                                                      \
+  }                                                                                                     \
+  extern "C" int gmc_kem_##NAME##_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk) { \
+    return one_dec(SET, k, c, sk);                                                                      \
+  }
+GMC_ONE(348864, 0)
+GMC_ONE(460896, 1)
+GMC_ONE(6688128, 2)
+GMC_ONE(6960119, 3)
+GMC_ONE(8192128, 4)
+
+// ---------------------------------------------------------------- host-only views
+// Per-key tables exactly as uploaded, for host-side checks (no GPU needed).
+extern "C" int gmc_host_sk_tables(int set, const unsigned char *sk, unsigned short *L, unsigned short *Lpow,
+                                  unsigned int *F, long long f_words, int *ldf) {
+  if (!valid_set(set) || !sk) return fail(GMC_EINVAL, "gmc_host_sk_tables: bad argument");
+  SkHost h;
+  if (build_sk(set, sk, h)) return fail(GMC_EKEY, "gmc_host_sk_tables: bad key");
+  const gmc_setinfo &S = set_info(set);
+  if (L) memcpy(L, h.L.data(), (size_t)S.n * 2);
+  if (Lpow) memcpy(Lpow, h.Lpow.data(), (size_t)S.n * 2);
+  if (ldf) *ldf = h.ldf;
+  if (F) {
+    if (f_words < (long long)h.F.size()) return fail(GMC_EINVAL, "gmc_host_sk_tables: F too small");
+    memcpy(F, h.F.data(), h.F.size() * 4);
+  }
+  return (int)h.F.size();
+}
+
+extern "C" int gmc_host_field_tables(int set, unsigned short *gexp, unsigned short *glog, unsigned short *alpha_log,
+                                     unsigned short *twist_log) {
+  if (!valid_set(set)) return fail(GMC_EINVAL, "gmc_host_field_tables: bad set");
+  const gmc_setinfo &S = set_info(set);
+  const HostField &F = host_field(S.m);
+  FftTables ft = build_fft_tables(S.m, S.fft_d);
+  if (gexp) memcpy(gexp, F.exp.data(), F.exp.size() * 2);
+  if (glog) memcpy(glog, F.log.data(), F.log.size() * 2);
+  if (alpha_log) memcpy(alpha_log, ft.alpha_log.data(), ft.alpha_log.size() * 2);
+  if (twist_log) memcpy(twist_log, ft.twist_log.data(), ft.twist_log.size() * 2);
+  return GMC_OK;
+}

@@ -1,0 +1,53 @@
+// Host-side per-key and per-field setup for the GPU engine: everything here
+// runs once per loaded key (or once per field), never per request.
+#pragma once
+#include <stdint.h>
+#include <vector>
+#include "params.h"
+
+namespace gmc {
+
+const gmc_setinfo &set_info(int set);
+
+// GF(2^m) with log/antilog tables in the device layout: exp has 2q-1 entries
+// (exp[2q-2] = 0), log[0] = 2q-2 (sentinel), so a*b = exp[min(la+lb, 2q-2)].
+struct HostField {
+  int m = 0, q = 0;
+  uint32_t poly = 0;
+  std::vector<uint16_t> exp, log;
+  void init(int m_);
+  uint16_t mul(uint16_t a, uint16_t b) const;
+  uint16_t inv(uint16_t a) const;
+  uint16_t sq(uint16_t a) const { return mul(a, a); }
+  int zero_log() const { return 2 * q - 2; }
+};
+const HostField &host_field(int m);
+
+// Additive-FFT constants for (m, d): per level l the log of the first basis
+// element's powers (twist) and of the butterfly constants alpha_{l,c'}.
+struct FftTables {
+  std::vector<uint16_t> twist_log;  // levels concatenated, 2^(d-l) each (2^(d+1) total)
+  std::vector<uint16_t> alpha_log;  // levels concatenated, 2^(m-l-1) each (padded to 2^m)
+};
+FftTables build_fft_tables(int m, int d);
+
+// Public key -> row-major T words for the syndrome GEMM.
+struct PkHost {
+  std::vector<uint32_t> T;  // rows_pad x lda
+  int lda = 0, rows_pad = 0, kw_pad = 0;
+  int pad_bad = 0;          // 6960119: nonzero pk padding bits
+};
+void build_pk(int set, const uint8_t *pk, PkHost &out);
+
+// Secret key -> support, logs, front-end matrix F.
+struct SkHost {
+  std::vector<uint16_t> L, LL, LW2, Lpow;   // [n]
+  std::vector<uint8_t> s;                   // [n/8]
+  std::vector<uint32_t> F;                  // frows_pad x ldf
+  int ldf = 0, frows_pad = 0, cw_pad = 0;
+};
+int build_sk(int set, const uint8_t *sk, SkHost &out);
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace gmc

@@ -1,0 +1,59 @@
+// Kernel launchers of the engine (host-callable, templated per parameter set).
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "params.h"
+
+namespace gmc {
+
+constexpr int kSampleThreads = 64;
+constexpr int kTailThreads = 128;
+constexpr int kDecodeWarps = 4;
+
+// GF(2) GEMM engines for Out[op] = parity(A[row] & X[op]) over KW words.
+enum GemmEngine { GEMM_POPC = 0, GEMM_B1MMA = 1, GEMM_TC = 2 };
+
+// Tiling of every engine: A padded to a multiple of kGemmRowTile rows and X
+// to a multiple of kGemmOpTile requests, K to a multiple of kGemmKTile words.
+constexpr int kGemmRowTile = 128;
+constexpr int kGemmOpTile = 64;
+constexpr int kGemmKTile = 8;
+
+cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx,
+                            long long n_pad, int kw_pad, uint32_t *Out, int ldo, int out_words, long long N,
+                            cudaStream_t st);
+
+template <int SET>
+cudaError_t launch_sample(const uint8_t *seeds, long long N, uint32_t *E, int lde, uint32_t *Ens, int ldx,
+                          cudaStream_t st);
+template <int SET>
+cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
+                            long long N, int pk_bad, cudaStream_t st);
+
+// Per-key decapsulation state on the device (built once per secret key).
+struct DecKeyDev {
+  const uint16_t *L;     // support element of each code position [n]
+  const uint16_t *LL;    // log L_i (zero sentinel when L_i = 0) [n]
+  const uint16_t *LW2;   // log of 1/g(L_i)^2 [n]
+  const uint16_t *Lpow;  // L_i^(2^fft_d) when the locator's leading term is separate [n]
+  const uint8_t *s;      // implicit-rejection string [n/8]
+};
+
+// Per-field / per-set device tables (shared by all keys of a set).
+struct FieldDev {
+  const uint16_t *gexp;   // [2q-1]
+  const uint16_t *glog;   // [q]
+  const uint16_t *fft_alpha_log;  // concatenated per level l = 0..d-1: [2^(m-l-1)]
+  const uint16_t *fft_twist_log;  // concatenated per level l = 0..d-1: [2^(d-l)]
+};
+
+template <int SET>
+cudaError_t launch_pack_ct(const uint8_t *C, long long N, uint32_t *X, int ldx, cudaStream_t st);
+template <int SET>
+cudaError_t launch_decode(const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd, long long N, uint32_t *E,
+                          int lde, int *ok, cudaStream_t st);
+template <int SET>
+cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, DecKeyDev key,
+                            uint8_t *K, int *rc, long long N, cudaStream_t st);
+
+}  // namespace gmc

@@ -1,0 +1,373 @@
+// Decapsulation kernels.
+//
+//  pack_ct     ciphertext bytes -> 32-bit words (the front-end GEMM operand)
+//  decode      one warp per request: 2t syndromes (from the front-end GEMM)
+//              -> Berlekamp-Massey -> additive FFT over all 2^m field
+//              elements -> error positions at the key's support -> weight
+//              and re-encryption (syndrome) check
+//  dec_tail    K = SHAKE256(b || (e or s) || c), implicit rejection, and the
+//              6960119 ciphertext-padding rule
+//
+// Reference behaviour: decrypt / operation_dec of libmceliece
+// (mceliece-gpu-params/ref/348864.cuh:3251-3406, 3615-3650;
+// mc:crypto_kem/348864/vec/decrypt.c:135, kem_dec.c:19;
+// mc:crypto_kem/6960119/vec/kem_dec.c:21-78). Only the outcome is defined
+// there: a weight-t error with the received syndrome is unique, so any exact
+// decoder yields the same session key. The BM update rule follows the
+// library's (mc:crypto_kem/348864/vec/bm.c:156), so locators agree with the
+// oracle's stage output as well.
+#include "kernels.h"
+#include "device_common.cuh"
+
+namespace gmc {
+
+__device__ __forceinline__ uint32_t warp_xor(uint32_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v ^= __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------- pack_ct
+template <int SET>
+__global__ void pack_ct_kernel(const uint8_t *__restrict__ C, long long N, uint32_t *__restrict__ X, int ldx) {
+  using p = P<SET>;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long op = idx / ldx;
+  const int w = (int)(idx % ldx);
+  if (op >= N) return;
+  const uint8_t *c = C + op * p::synd_bytes;
+  uint32_t v = 0;
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    int x = 4 * w + b;
+    if (x < p::synd_bytes) v |= (uint32_t)c[x] << (8 * b);
+  }
+  X[op * ldx + w] = v;
+}
+
+// ---------------------------------------------------------------- decode
+template <int SET>
+struct DecodeLayout {
+  using p = P<SET>;
+  static constexpr int Q = p::q, D = p::fft_d;
+  // block-shared tables (u16 units)
+  static constexpr int exp_off = 0, exp_len = 2 * Q;
+  static constexpr int log_off = exp_off + exp_len, log_len = Q;
+  static constexpr int alpha_off = log_off + log_len, alpha_len = Q;   // sum_l 2^(m-l-1) < Q
+  static constexpr int twist_off = alpha_off + alpha_len, twist_len = 2 << D;
+  static constexpr int shared_u16 = twist_off + twist_len;
+  // per-warp region (u32 units): e words, then V[Q] u16, s[2t] u16, slog[2t] u16
+  static constexpr int ewp = (p::ew + 1) & ~1;
+  static constexpr int warp_u32 = ewp + Q / 2 + p::t + p::t;
+  static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u32 * 4; }
+};
+
+template <int SET>
+__global__ void __launch_bounds__(kDecodeWarps * 32) decode_kernel(const uint32_t *__restrict__ S2, int lds2,
+                                                                    DecKeyDev key, FieldDev fd, long long N,
+                                                                    uint32_t *__restrict__ E, int lde,
+                                                                    int *__restrict__ okout) {
+  using p = P<SET>;
+  using LY = DecodeLayout<SET>;
+  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
+  constexpr int ZL = GFLog<M>::zero_log;
+  constexpr int NS = (T + 1 + 31) / 32;  // locator slots per lane
+  constexpr int NSY = (2 * T + 31) / 32; // syndrome slots per lane
+  constexpr int NW = (p::n + 31) / 32;
+  extern __shared__ __align__(16) uint32_t dsm[];
+  uint16_t *sh16 = reinterpret_cast<uint16_t *>(dsm);
+  uint16_t *gexp = sh16 + LY::exp_off;
+  uint16_t *glog = sh16 + LY::log_off;
+  uint16_t *alog = sh16 + LY::alpha_off;
+  uint16_t *tlog = sh16 + LY::twist_off;
+  for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) { glog[i] = fd.glog[i]; alog[i] = fd.fft_alpha_log[i]; }
+  for (int i = threadIdx.x; i < (2 << D); i += blockDim.x) tlog[i] = fd.fft_twist_log[i];
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *wbase = dsm + LY::shared_u16 / 2 + warp * LY::warp_u32;
+  uint32_t *esm = wbase;
+  uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::ewp);
+  uint16_t *ssm = V + Q;
+  uint16_t *slog = ssm + 2 * T;
+
+  const long long nwarps = (long long)gridDim.x * kDecodeWarps;
+  for (long long op = (long long)blockIdx.x * kDecodeWarps + warp; op < N; op += nwarps) {
+    // 1. unpack the 2t syndromes (m bits each) produced by the front end
+    const uint32_t *srow = S2 + op * lds2;
+#pragma unroll
+    for (int k = 0; k < NSY; k++) {
+      const int j = lane + 32 * k;
+      if (j < 2 * T) {
+        const int b = j * M, w = b >> 5, sh = b & 31;
+        uint32_t v = srow[w] >> sh;
+        if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
+        v &= Q - 1;
+        ssm[j] = (uint16_t)v;
+        slog[j] = glog[v];
+      }
+    }
+    __syncwarp();
+
+    // 2. Berlekamp-Massey: coefficient i = lane + 32k of C and B per lane
+    uint16_t C[NS], B[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const int i = lane + 32 * k;
+      C[k] = (i == 0);
+      B[k] = (i == 1);
+    }
+    int L = 0;
+    uint32_t b = 1;
+#pragma unroll 1
+    for (int n = 0; n < 2 * T; n++) {
+      const int lim = n < T ? n : T;
+      uint32_t dp = 0;
+#pragma unroll
+      for (int k = 0; k < NS; k++) {
+        const int i = lane + 32 * k;
+        if (i <= lim) dp ^= gf_mul_log<M>(gexp, glog[C[k]], slog[n - i]);
+      }
+      const uint32_t d = warp_xor(dp);
+      const bool upd = d && (n >= 2 * L);
+      uint16_t Tk[NS];
+      if (d) {
+        int lf = (int)glog[d] - (int)glog[b];
+        if (lf < 0) lf += Q - 1;
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+          Tk[k] = C[k];
+          C[k] ^= gf_mul_log<M>(gexp, lf, glog[B[k]]);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < NS; k++) Tk[k] = C[k];
+      }
+      if (upd) {
+        L = n + 1 - L;
+        b = d;
+#pragma unroll
+        for (int k = 0; k < NS; k++) B[k] = Tk[k];
+      }
+      // B <- x * B (coefficient i takes i-1)
+      uint16_t nb[NS];
+#pragma unroll
+      for (int k = 0; k < NS; k++) {
+        uint16_t up = (uint16_t)__shfl_up_sync(0xffffffffu, B[k], 1);
+        uint16_t wrap = (uint16_t)__shfl_sync(0xffffffffu, k ? B[k ? k - 1 : 0] : 0, 31);
+        nb[k] = lane ? up : (k ? wrap : 0);
+      }
+#pragma unroll
+      for (int k = 0; k < NS; k++) B[k] = nb[k];
+    }
+
+    // 3. locator sigma(x) = sum_deg C[t-deg] x^deg into the FFT coefficient slots
+    for (int x = lane; x < (1 << D); x += 32) V[x] = 0;
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const int i = lane + 32 * k;
+      const int deg = T - i;
+      if (i <= T && deg < (1 << D)) V[deg] = C[k];
+    }
+    __syncwarp();
+
+    // 4. additive FFT, top-down: twist by the level's first basis element and
+    //    radix-convert g(x) = g0(x^2+x) + x g1(x^2+x); children interleave
+    //    (even/odd coefficients) so no data moves between levels.
+#pragma unroll 1
+    for (int l = 0; l < D; l++) {
+      const int sz = 1 << (D - l);
+      if (l) {
+        const uint16_t *tw = tlog + ((2 << D) - (2 << (D - l)));
+        for (int x = lane; x < (1 << D); x += 32) V[x] = gf_mul_log<M>(gexp, glog[V[x]], tw[x >> l]);
+        __syncwarp();
+      }
+#pragma unroll 1
+      for (int s = sz; s >= 4; s >>= 1) {
+        const int tau = s >> 2;
+        for (int it = lane; it < (1 << D) / 4; it += 32) {
+          const int path = it & ((1 << l) - 1), rest = it >> l;
+          const int u = rest % tau, bl = rest / tau;
+          const int i2 = bl * s + 2 * tau + u;
+          V[path + (i2 << l)] ^= V[path + ((i2 + tau) << l)];
+        }
+        __syncwarp();
+        for (int it = lane; it < (1 << D) / 4; it += 32) {
+          const int path = it & ((1 << l) - 1), rest = it >> l;
+          const int u = rest % tau, bl = rest / tau;
+          const int i1 = bl * s + tau + u;
+          V[path + (i1 << l)] ^= V[path + ((i1 + tau) << l)];
+        }
+        __syncwarp();
+      }
+    }
+    //    bottom-up: leaves are constants over their coset; butterflies with
+    //    per-level constants alpha_{l,c'} (log form, zero sentinel).
+    for (int x = (1 << D) + lane; x < Q; x += 32) V[x] = V[x & ((1 << D) - 1)];
+    __syncwarp();
+#pragma unroll 1
+    for (int l = D - 1; l >= 0; l--) {
+      const uint16_t *al = alog + (Q - (Q >> l));
+      const int h = 1 << l;
+      for (int u = lane; u < Q / 2; u += 32) {
+        const int path = u & (h - 1), cp = u >> l;
+        const int x = path + (cp << (l + 1));
+        uint16_t a = V[x];
+        const uint16_t bb = V[x + h];
+        a ^= gf_mul_log<M>(gexp, al[cp], glog[bb]);
+        V[x] = a;
+        V[x + h] = a ^ bb;
+      }
+      __syncwarp();
+    }
+
+    // 5. error positions: sigma(L_i) == 0 (+ L_i^(2^d) for the separate leading term)
+    int weight = 0;
+#pragma unroll 1
+    for (int it = 0; it < NW; it++) {
+      const int i = it * 32 + lane;
+      bool err = false;
+      if (i < p::n) {
+        uint16_t v = V[key.L[i]];
+        if (p::lead) v ^= key.Lpow[i];
+        err = (v == 0);
+      }
+      const uint32_t w = __ballot_sync(0xffffffffu, err);
+      if (lane == 0) esm[it] = w;
+      weight += __popc(w);
+    }
+    __syncwarp();
+
+    // 6. re-encryption: syndromes of the found error must equal the received ones
+    bool ok = (weight == T);
+    if (ok) {
+      uint32_t sc[NSY];
+#pragma unroll
+      for (int k = 0; k < NSY; k++) sc[k] = 0;
+#pragma unroll 1
+      for (int it = 0; it < NW; it++) {
+        uint32_t w = esm[it];
+        while (w) {
+          const int bit = __ffs(w) - 1;
+          w &= w - 1;
+          const int i = it * 32 + bit;
+          const int ll = key.LL[i], lw = key.LW2[i];
+          if (ll == ZL) {  // L_i = 0: only the j = 0 term
+            if (lane == 0) sc[0] ^= gexp[lw];
+          } else {
+#pragma unroll
+            for (int k = 0; k < NSY; k++) {
+              const int j = lane + 32 * k;
+              sc[k] ^= gexp[fold_mod<M>(lw + j * ll)];
+            }
+          }
+        }
+      }
+      bool mism = false;
+#pragma unroll
+      for (int k = 0; k < NSY; k++) {
+        const int j = lane + 32 * k;
+        if (j < 2 * T && sc[k] != ssm[j]) mism = true;
+      }
+      ok = !__any_sync(0xffffffffu, mism);
+    }
+    uint32_t *erow = E + op * lde;
+    for (int it = lane; it < NW; it += 32) erow[it] = esm[it];
+    if (lane == 0) okout[op] = ok ? 1 : 0;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- tail
+template <int SET>
+__global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *__restrict__ E, int lde,
+                                                                const int *__restrict__ okin,
+                                                                const uint8_t *__restrict__ Cin, DecKeyDev key,
+                                                                uint8_t *__restrict__ K, int *__restrict__ rc,
+                                                                long long N) {
+  using p = P<SET>;
+  const long long op = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (op >= N) return;
+  const bool ok = okin[op] != 0;
+  const uint32_t *e = E + op * lde;
+  const uint8_t *c = Cin + op * p::synd_bytes;
+  auto ebyte = [&](int x) -> uint32_t {
+    return ok ? ((e[x >> 2] >> (8 * (x & 3))) & 0xFFu) : (uint32_t)key.s[x];
+  };
+  auto lane = [&](int i) -> uint64_t {
+    uint64_t v = 0;
+    for (int bb = 0; bb < 8; bb++) {
+      const int x = 8 * i + bb;
+      uint32_t byte;
+      if (x == 0) byte = ok ? 1u : 0u;
+      else if (x <= p::e_bytes) byte = ebyte(x - 1);
+      else if (x < p::pre_bytes) byte = c[x - 1 - p::e_bytes];
+      else byte = 0;
+      v |= (uint64_t)byte << (8 * bb);
+    }
+    return v;
+  };
+  uint64_t h[4];
+  shake256_32<p::pre_bytes>(h, lane);
+  bool pad_bad = false;
+  if (p::mt % 8) pad_bad = (c[p::synd_bytes - 1] >> (p::mt % 8)) != 0;
+  uint8_t *k = K + op * 32;
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int bb = 0; bb < 8; bb++) k[8 * i + bb] = pad_bad ? 0xFF : (uint8_t)(h[i] >> (8 * bb));
+  if (rc) rc[op] = pad_bad ? -1 : 0;
+}
+
+// ---------------------------------------------------------------- launchers
+template <int SET>
+cudaError_t launch_pack_ct(const uint8_t *C, long long N, uint32_t *X, int ldx, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  const long long total = N * ldx;
+  pack_ct_kernel<SET><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, N, X, ldx);
+  return cudaGetLastError();
+}
+
+template <int SET>
+cudaError_t launch_decode(const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd, long long N, uint32_t *E,
+                          int lde, int *ok, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  const int smem = DecodeLayout<SET>::bytes(kDecodeWarps);
+  cudaError_t err = cudaFuncSetAttribute(decode_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (err != cudaSuccess) return err;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, decode_kernel<SET>, kDecodeWarps * 32, smem);
+  if (per_sm < 1) per_sm = 1;
+  long long need = (N + kDecodeWarps - 1) / kDecodeWarps;
+  long long blocks = (long long)sms * per_sm;
+  if (blocks > need) blocks = need;
+  decode_kernel<SET><<<(unsigned)blocks, kDecodeWarps * 32, smem, st>>>(S2, lds2, key, fd, N, E, lde, ok);
+  return cudaGetLastError();
+}
+
+template <int SET>
+cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, DecKeyDev key,
+                            uint8_t *K, int *rc, long long N, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  dec_tail_kernel<SET><<<(unsigned)((N + kTailThreads - 1) / kTailThreads), kTailThreads, 0, st>>>(
+      E, lde, ok, C, key, K, rc, N);
+  return cudaGetLastError();
+}
+
+#define GMC_INST_DEC(SET)                                                                                       \
+  template cudaError_t launch_pack_ct<SET>(const uint8_t *, long long, uint32_t *, int, cudaStream_t);          \
+  template cudaError_t launch_decode<SET>(const uint32_t *, int, DecKeyDev, FieldDev, long long, uint32_t *,   \
+                                          int, int *, cudaStream_t);                                            \
+  template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, DecKeyDev,    \
+                                            uint8_t *, int *, long long, cudaStream_t);
+GMC_INST_DEC(0)
+GMC_INST_DEC(1)
+GMC_INST_DEC(2)
+GMC_INST_DEC(3)
+GMC_INST_DEC(4)
+
+}  // namespace gmc
