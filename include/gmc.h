@@ -72,19 +72,32 @@ int gmc_dec_batch_dev(const gmc_key *sk, unsigned char *k, const unsigned char *
                       void *stream);
 int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc);
 
+/* ---- key generation -----------------------------------------------------
+ * Keys in libmceliece's format (mc:crypto_kem/348864/vec/kem_keypair.c:20):
+ * the keypair whose single 32-byte randombytes draw returns seed32.
+ * pk/sk buffers of the set's public/secret-key size. Runs on the host (key
+ * generation is outside the batched enc/dec path). */
+int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32);
+
 /* ---- libmceliece calling convention (one request per call) --------------
  * Same signatures and results as mceliece_kem_<set>_enc / _dec
- * (mc:crypto_kem/<set>/vec/wrap_enc.c:4, wrap_dec.c:4). enc draws one 32-byte
+ * (mc:crypto_kem/<set>/vec/wrap_keypair.c:4, wrap_enc.c:4, wrap_dec.c:4). keypair
+ * and enc draw one 32-byte seed each from the randombytes source; enc draws
  * seed from the randombytes source (default: the OS generator) and runs the
  * GPU seed chain. dec tolerates k == c and k == sk (outputs written last). */
+void gmc_kem_348864_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_348864_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_348864_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_460896_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_460896_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_460896_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6688128_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_6688128_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_6688128_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6960119_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_6960119_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_6960119_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_8192128_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_8192128_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_8192128_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
 
@@ -125,6 +138,13 @@ int gmc_host_sk_tables(int set, const unsigned char *sk, unsigned short *L, unsi
                        long long f_words, int *ldf);
 int gmc_host_field_tables(int set, unsigned short *gexp, unsigned short *glog, unsigned short *alpha_log,
                           unsigned short *twist_log);
+
+/* Per-kernel device timing of the batches launched while enabled (events
+ * recorded on the launching stream around every kernel; not during stream
+ * capture). gmc_prof_enable(1) clears previous records. gmc_prof_report
+ * writes lines "<kernel> <launches> <total ms>" and returns the kernel count. */
+int gmc_prof_enable(int on);
+int gmc_prof_report(char *buf, int len);
 
 const char *gmc_last_error(void);
 

@@ -18,7 +18,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = [
-    "SETS", "GmcError", "lib", "set_id", "set_sizes", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
+    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
     "set_gemm_engine", "get_gemm_engine", "set_randombytes", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC",
 ]
 
@@ -68,6 +68,10 @@ def lib():
         for s in SETS:
             for op in ("enc", "dec"):
                 getattr(L, f"gmc_kem_{s}_{op}").argtypes = [c_u8p, c_u8p, c_u8p]
+        L.gmc_keypair_seed.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p]
+        for s in SETS:
+            getattr(L, f"gmc_kem_{s}_keypair").argtypes = [c_u8p, c_u8p]
+            getattr(L, f"gmc_kem_{s}_keypair").restype = None
         L.gmc_set_randombytes.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gmc_set_randombytes.restype = None
         _lib = L
@@ -180,6 +184,20 @@ class SecretKey(_Key):
     def dec_batch_dev(self, k_ptr, c_ptr, n, rc_ptr=0, stream=0):
         return _check(lib().gmc_dec_batch_dev(self._h, k_ptr, c_ptr, n, rc_ptr or None, stream or None),
                       "gmc_dec_batch_dev")
+
+
+def keypair(set_name, seed32=None):
+    """(pk, sk) as uint8 arrays; seed32 = the keypair's single randombytes draw (None: randombytes source)."""
+    sid = set_name if isinstance(set_name, int) else set_id(set_name)
+    sz = set_sizes(sid)
+    pk = np.zeros(sz["pk_bytes"], np.uint8)
+    sk = np.zeros(sz["sk_bytes"], np.uint8)
+    if seed32 is None:
+        getattr(lib(), f"gmc_kem_{SETS[sid]}_keypair")(_ptr(pk), _ptr(sk))
+    else:
+        seed = _u8(bytes(seed32), 32)
+        _check(lib().gmc_keypair_seed(sid, _ptr(pk), _ptr(sk), _ptr(seed)), "gmc_keypair_seed")
+    return pk, sk
 
 
 def kem_enc(set_name, pk):

@@ -62,6 +62,64 @@ struct gmc_key {
 
 static int g_engine = GEMM_POPC;
 
+// ---------------------------------------------------------------- profiler
+// Optional per-kernel timing: when enabled, an event is recorded on the
+// launching stream before the first and after every kernel of a batch, and
+// gmc_prof_report() turns consecutive pairs into per-kernel device times.
+struct ProfMark {
+  const char *name;  // kernel that ended at this event (nullptr: batch start)
+  cudaEvent_t ev;
+};
+static std::mutex g_prof_mu;
+static bool g_prof = false;
+static std::vector<ProfMark> g_marks;
+
+static void prof_mark(const char *name, cudaStream_t st) {
+  if (!g_prof) return;
+  cudaStreamCaptureStatus cs;
+  if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) return;
+  cudaEvent_t ev;
+  if (cudaEventCreate(&ev) != cudaSuccess) return;
+  cudaEventRecord(ev, st);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_marks.push_back({name, ev});
+}
+
+extern "C" int gmc_prof_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (auto &mk : g_marks) cudaEventDestroy(mk.ev);
+  g_marks.clear();
+  g_prof = on != 0;
+  return GMC_OK;
+}
+
+extern "C" int gmc_prof_report(char *buf, int len) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  std::map<std::string, std::pair<int, double>> agg;
+  std::vector<std::string> order;
+  for (size_t i = 1; i < g_marks.size(); i++) {
+    if (!g_marks[i].name) continue;
+    if (cudaEventSynchronize(g_marks[i].ev) != cudaSuccess) return fail(GMC_ECUDA, "gmc_prof_report: sync");
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, g_marks[i - 1].ev, g_marks[i].ev) != cudaSuccess) continue;
+    std::string nm = g_marks[i].name;
+    if (!agg.count(nm)) order.push_back(nm);
+    agg[nm].first += 1;
+    agg[nm].second += ms;
+  }
+  std::string out;
+  for (auto &nm : order) {
+    char line[160];
+    snprintf(line, sizeof line, "%s %d %.6f\n", nm.c_str(), agg[nm].first, agg[nm].second);
+    out += line;
+  }
+  if (buf && len > 0) {
+    strncpy(buf, out.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)order.size();
+}
+
 // per (device, set) field and FFT tables
 struct FieldEntry {
   uint16_t *buf = nullptr;
@@ -227,10 +285,14 @@ template <int SET>
 static cudaError_t enc_sample_gemm(const gmc_key *pk, const uint8_t *seeds, long long n, uint32_t *E, uint32_t *Ens,
                                    uint32_t *S, const EncDims &d, cudaStream_t st) {
   using p = P<SET>;
+  prof_mark(nullptr, st);
   cudaError_t e = launch_sample<SET>(seeds, n, E, d.lde, Ens, d.ldx, st);
   if (e != cudaSuccess) return e;
-  return launch_gf2_gemm(g_engine, pk->T, pk->lda, pk->rows_pad, Ens, d.ldx, d.n_pad, pk->kw_pad, S, d.lds, p::mw,
-                         n, st);
+  prof_mark("enc_sample", st);
+  e = launch_gf2_gemm(g_engine, pk->T, pk->lda, pk->rows_pad, Ens, d.ldx, d.n_pad, pk->kw_pad, S, d.lds, p::mw, n,
+                      st);
+  prof_mark("enc_syndrome_gemm", st);
+  return e;
 }
 
 template <int SET>
@@ -243,7 +305,9 @@ static cudaError_t enc_run(const gmc_key *pk, uint8_t *c, uint8_t *k, const uint
   if ((e = scr.get((void **)&Ens, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
   if ((e = scr.get((void **)&S, (size_t)n * d.lds * 4)) != cudaSuccess) return e;
   if ((e = enc_sample_gemm<SET>(pk, seeds, n, E, Ens, S, d, st)) != cudaSuccess) return e;
-  return launch_finalize<SET>(E, d.lde, S, d.lds, c, k, n, pk->pad_bad, st);
+  e = launch_finalize<SET>(E, d.lde, S, d.lds, c, k, n, pk->pad_bad, st);
+  prof_mark("enc_finalize_hash", st);
+  return e;
 }
 
 struct DecDims {
@@ -266,12 +330,17 @@ static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long lo
   using p = P<SET>;
   FieldDev fd;
   if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
+  prof_mark(nullptr, st);
   cudaError_t e = launch_pack_ct<SET>(c, n, X, d.ldx, st);
   if (e != cudaSuccess) return e;
+  prof_mark("dec_pack_ct", st);
   e = launch_gf2_gemm(g_engine, sk->F, sk->ldf, sk->frows_pad, X, d.ldx, d.n_pad, sk->cw_pad, S2, d.lds2, p::s2w,
                       n, st);
   if (e != cudaSuccess) return e;
-  return launch_decode<SET>(S2, d.lds2, sk->dk, fd, n, E, d.lde, ok, st);
+  prof_mark("dec_front_gemm", st);
+  e = launch_decode<SET>(S2, d.lds2, sk->dk, fd, n, E, d.lde, ok, st);
+  prof_mark("dec_bm_fft_reenc", st);
+  return e;
 }
 
 template <int SET>
@@ -286,7 +355,9 @@ static cudaError_t dec_run(const gmc_key *sk, uint8_t *k, const uint8_t *c, long
   if ((e = scr.get((void **)&E, (size_t)n * d.lde * 4)) != cudaSuccess) return e;
   if ((e = scr.get((void **)&ok, (size_t)n * 4)) != cudaSuccess) return e;
   if ((e = dec_front_decode<SET>(sk, c, n, X, S2, E, ok, d, st)) != cudaSuccess) return e;
-  return launch_dec_tail<SET>(E, d.lde, ok, c, sk->dk, k, rc, n, st);
+  e = launch_dec_tail<SET>(E, d.lde, ok, c, sk->dk, k, rc, n, st);
+  prof_mark("dec_tail_hash", st);
+  return e;
 }
 
 #define GMC_DISPATCH(set, call) \
@@ -522,7 +593,23 @@ static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsi
   return rc;
 }
 
+extern "C" int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32) {
+  if (!valid_set(set) || !pk || !sk || !seed32) return fail(GMC_EINVAL, "gmc_keypair_seed: bad argument");
+  if (host_keypair(set, pk, sk, seed32)) return fail(GMC_EKEY, "gmc_keypair_seed: key generation failed");
+  return GMC_OK;
+}
+
+static int one_keypair(int set, unsigned char *pk, unsigned char *sk) {
+  uint8_t seed[32];
+  int r = draw_seed(seed);
+  if (r) return r;
+  return gmc_keypair_seed(set, pk, sk, seed);
+}
+
 #define GMC_ONE(NAME, SET)                                                                               \
+  extern "C" void gmc_kem_##NAME##_keypair(unsigned char *pk, unsigned char *sk) {                      \
+    one_keypair(SET, pk, sk);                                                                           \
+  }                                                                                                     \
   extern "C" int gmc_kem_##NAME##_enc(unsigned char *c, unsigned char *k, const unsigned char *pk) {    \
     return one_enc(SET, c, k, pk);                                                                      \
   }                                                                                                     \

@@ -1,6 +1,7 @@
 // Host-side per-key and per-field setup for the GPU engine: everything here
 // runs once per loaded key (or once per field), never per request.
 #pragma once
+#include <stddef.h>
 #include <stdint.h>
 #include <vector>
 #include "params.h"
@@ -47,6 +48,11 @@ struct SkHost {
   int ldf = 0, frows_pad = 0, cw_pad = 0;
 };
 int build_sk(int set, const uint8_t *sk, SkHost &out);
+
+// Key generation in libmceliece's format (host); delta32 is the single
+// 32-byte randombytes draw of the library's keypair.
+int host_keypair(int set, uint8_t *pk, uint8_t *sk, const uint8_t delta32[32]);
+void host_shake256(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen);
 
 inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
