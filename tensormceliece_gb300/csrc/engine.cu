@@ -326,7 +326,7 @@ static DecDims dec_dims(const gmc_key *sk, long long n) {
 
 template <int SET>
 static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long long n, uint32_t *X, uint32_t *S2,
-                                    uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
+                                    uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
   using p = P<SET>;
   FieldDev fd;
   if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
@@ -338,8 +338,11 @@ static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long lo
                       n, st);
   if (e != cudaSuccess) return e;
   prof_mark("dec_front_gemm", st);
-  e = launch_decode<SET>(S2, d.lds2, sk->dk, fd, n, E, d.lde, ok, st);
-  prof_mark("dec_bm_fft_reenc", st);
+  e = launch_dec_bm<SET>(S2, d.lds2, fd, n, Sig, st);
+  if (e != cudaSuccess) return e;
+  prof_mark("dec_bm", st);
+  e = launch_dec_root<SET>(Sig, S2, d.lds2, sk->dk, fd, n, E, d.lde, ok, st);
+  prof_mark("dec_fft_roots_reenc", st);
   return e;
 }
 
@@ -348,13 +351,15 @@ static cudaError_t dec_run(const gmc_key *sk, uint8_t *k, const uint8_t *c, long
                            Scratch &scr) {
   DecDims d = dec_dims(sk, n);
   uint32_t *X, *S2, *E;
+  uint16_t *Sig;
   int *ok;
   cudaError_t e;
   if ((e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
   if ((e = scr.get((void **)&S2, (size_t)n * d.lds2 * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&Sig, (size_t)n * (2u << P<SET>::fft_d))) != cudaSuccess) return e;
   if ((e = scr.get((void **)&E, (size_t)n * d.lde * 4)) != cudaSuccess) return e;
   if ((e = scr.get((void **)&ok, (size_t)n * 4)) != cudaSuccess) return e;
-  if ((e = dec_front_decode<SET>(sk, c, n, X, S2, E, ok, d, st)) != cudaSuccess) return e;
+  if ((e = dec_front_decode<SET>(sk, c, n, X, S2, Sig, E, ok, d, st)) != cudaSuccess) return e;
   e = launch_dec_tail<SET>(E, d.lde, ok, c, sk->dk, k, rc, n, st);
   prof_mark("dec_tail_hash", st);
   return e;
@@ -497,8 +502,10 @@ extern "C" int gmc_dec_stages_dev(const gmc_key *sk, const unsigned char *c, lon
   {
     Scratch scr(st);
     uint32_t *X;
+    uint16_t *Sig = nullptr;
     e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4);
-    if (e == cudaSuccess) GMC_DISPATCH(sk->set, e = dec_front_decode<S_>(sk, c, n, X, synd, ev, ok, d, st));
+    if (e == cudaSuccess) e = scr.get((void **)&Sig, (size_t)n * 256);
+    if (e == cudaSuccess) GMC_DISPATCH(sk->set, e = dec_front_decode<S_>(sk, c, n, X, synd, Sig, ev, ok, d, st));
   }
   if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_stages_dev");
   return GMC_OK;

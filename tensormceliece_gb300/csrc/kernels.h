@@ -8,7 +8,8 @@ namespace gmc {
 
 constexpr int kSampleThreads = 64;
 constexpr int kTailThreads = 128;
-constexpr int kDecodeWarps = 4;
+constexpr int kBMWarps = 16;    // Berlekamp-Massey kernel: warps per block
+constexpr int kRootWarps = 8;   // root-finding kernel: warps per block
 
 // GF(2) GEMM engines for Out[op] = parity(A[row] & X[op]) over KW words.
 enum GemmEngine { GEMM_POPC = 0, GEMM_B1MMA = 1, GEMM_TC = 2 };
@@ -49,9 +50,15 @@ struct FieldDev {
 
 template <int SET>
 cudaError_t launch_pack_ct(const uint8_t *C, long long N, uint32_t *X, int ldx, cudaStream_t st);
+// Berlekamp-Massey: S2 (2t packed syndromes) -> Sig [N][2^fft_d] u16, the
+// error locator's coefficients by degree (the leading x^t term is implicit
+// when t = 2^fft_d).
 template <int SET>
-cudaError_t launch_decode(const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd, long long N, uint32_t *E,
-                          int lde, int *ok, cudaStream_t st);
+cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, long long N, uint16_t *Sig, cudaStream_t st);
+// Root finding + weight + re-encryption check: Sig -> E (error vectors), ok.
+template <int SET>
+cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd,
+                            long long N, uint32_t *E, int lde, int *ok, cudaStream_t st);
 template <int SET>
 cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, DecKeyDev key,
                             uint8_t *K, int *rc, long long N, cudaStream_t st);

@@ -45,37 +45,155 @@ __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, long long N, uint3
   X[op * ldx + w] = v;
 }
 
-// ---------------------------------------------------------------- decode
+// ---------------------------------------------------------------- BM
+// One warp per request (persistent grid). Coefficient i of C (connection
+// polynomial) and B lives in lane i%32, slot i/32. Only the GF(2^m) tables
+// sit in shared memory, so many warps share an SM.
+// Degree bounds used to skip empty slots (exact, also for undecodable input):
+// before iteration n, deg C <= L and deg B <= n+1-L (B is the last connection
+// polynomial before a length change, pre-shifted), so the discrepancy needs
+// coefficients i <= min(L, t) and the update i <= min(max(L, n+1-L), t).
 template <int SET>
-struct DecodeLayout {
+struct BMLayout {
+  using p = P<SET>;
+  static constexpr int Q = p::q;
+  static constexpr int exp_off = 0, log_off = 2 * Q;
+  static constexpr int shared_u16 = 3 * Q;
+  static constexpr int warp_u16 = 2 * p::t;  // log s_j
+  static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u16 * 2; }
+};
+
+template <int SET>
+__global__ void __launch_bounds__(kBMWarps * 32) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
+                                                               FieldDev fd, long long N,
+                                                               uint16_t *__restrict__ Sig) {
+  using p = P<SET>;
+  using LY = BMLayout<SET>;
+  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
+  constexpr int NS = (T + 1 + 31) / 32;
+  constexpr int NSY = (2 * T + 31) / 32;
+  constexpr int SIG = 1 << D;
+  extern __shared__ __align__(16) uint16_t bsm[];
+  uint16_t *gexp = bsm + LY::exp_off;
+  uint16_t *glog = bsm + LY::log_off;
+  for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint16_t *slog = bsm + LY::shared_u16 + warp * LY::warp_u16;
+  const long long nwarps = (long long)gridDim.x * kBMWarps;
+  for (long long op = (long long)blockIdx.x * kBMWarps + warp; op < N; op += nwarps) {
+    const uint32_t *srow = S2 + op * lds2;
+#pragma unroll
+    for (int k = 0; k < NSY; k++) {
+      const int j = lane + 32 * k;
+      if (j < 2 * T) {
+        const int b = j * M, w = b >> 5, sh = b & 31;
+        uint32_t v = srow[w] >> sh;
+        if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
+        slog[j] = glog[v & (Q - 1)];
+      }
+    }
+    __syncwarp();
+    uint16_t C[NS], B[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const int i = lane + 32 * k;
+      C[k] = (i == 0);
+      B[k] = (i == 1);
+    }
+    int L = 0;
+    uint32_t lb = 0;  // log b, b = 1
+#pragma unroll 1
+    for (int n = 0; n < 2 * T; n++) {
+      const int bd = L < T ? L : T;                       // discrepancy: i <= min(L, t) (L <= n)
+      int bu = (L > n + 1 - L) ? L : n + 1 - L;           // update: i <= min(max(L, n+1-L), t)
+      bu = bu < T ? bu : T;
+      uint32_t dp = 0;
+#pragma unroll
+      for (int k = 0; k < NS; k++) {
+        if (32 * k <= bd) {
+          const int i = lane + 32 * k;
+          if (i <= bd) dp ^= gf_mul_log<M>(gexp, glog[C[k]], slog[n - i]);
+        }
+      }
+      const uint32_t d = warp_xor(dp);
+      if (d) {
+        const bool upd = (n >= 2 * L);
+        int lf = (int)glog[d] - (int)lb;
+        if (lf < 0) lf += Q - 1;
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+          if (32 * k <= bu) {
+            const uint16_t c = C[k];
+            C[k] = c ^ gf_mul_log<M>(gexp, lf, glog[B[k]]);
+            if (upd) B[k] = c;
+          }
+        }
+        if (upd) {
+          L = n + 1 - L;
+          lb = glog[d];
+        }
+      }
+      // B <- x * B (coefficient i takes i-1); slots above the bound stay zero.
+      // Descending slot order: slot k reads slot k-1 before that one shifts.
+#pragma unroll
+      for (int k = NS - 1; k >= 0; k--) {
+        if (32 * k <= bu + 1) {
+          const uint16_t up = (uint16_t)__shfl_up_sync(0xffffffffu, B[k], 1);
+          const uint16_t wrap = (uint16_t)__shfl_sync(0xffffffffu, k ? B[k ? k - 1 : 0] : 0, 31);
+          B[k] = lane ? up : (k ? wrap : 0);
+        }
+      }
+    }
+    // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d)
+    uint16_t *sig = Sig + op * SIG;
+    for (int x = lane; x < SIG; x += 32)
+      if (x > T) sig[x] = 0;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const int i = lane + 32 * k;
+      const int deg = T - i;
+      if (i <= T && deg < SIG) sig[deg] = C[k];
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- root finding
+// One warp per request: additive FFT of sigma over all 2^m field elements
+// (Gao-Mateer, basis beta_i = 2^i so point c is the element c), the error
+// positions sigma(L_i) = 0 at the key's support, the weight and the
+// re-encryption check (syndromes of the found error equal the received ones).
+template <int SET>
+struct RootLayout {
   using p = P<SET>;
   static constexpr int Q = p::q, D = p::fft_d;
-  // block-shared tables (u16 units)
   static constexpr int exp_off = 0, exp_len = 2 * Q;
   static constexpr int log_off = exp_off + exp_len, log_len = Q;
-  static constexpr int alpha_off = log_off + log_len, alpha_len = Q;   // sum_l 2^(m-l-1) < Q
+  static constexpr int alpha_off = log_off + log_len, alpha_len = Q;
   static constexpr int twist_off = alpha_off + alpha_len, twist_len = 2 << D;
   static constexpr int shared_u16 = twist_off + twist_len;
-  // per-warp region (u32 units): e words, then V[Q] u16, s[2t] u16, slog[2t] u16
   static constexpr int ewp = (p::ew + 1) & ~1;
-  static constexpr int warp_u32 = ewp + Q / 2 + p::t + p::t;
+  static constexpr int warp_u32 = ewp + Q / 2 + p::t;  // e words | V[Q] u16 | s[2t] u16
   static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u32 * 4; }
 };
 
 template <int SET>
-__global__ void __launch_bounds__(kDecodeWarps * 32) decode_kernel(const uint32_t *__restrict__ S2, int lds2,
-                                                                    DecKeyDev key, FieldDev fd, long long N,
-                                                                    uint32_t *__restrict__ E, int lde,
-                                                                    int *__restrict__ okout) {
+__global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_t *__restrict__ Sig,
+                                                                   const uint32_t *__restrict__ S2, int lds2,
+                                                                   DecKeyDev key, FieldDev fd, long long N,
+                                                                   uint32_t *__restrict__ E, int lde,
+                                                                   int *__restrict__ okout) {
   using p = P<SET>;
-  using LY = DecodeLayout<SET>;
+  using LY = RootLayout<SET>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
   constexpr int ZL = GFLog<M>::zero_log;
-  constexpr int NS = (T + 1 + 31) / 32;  // locator slots per lane
-  constexpr int NSY = (2 * T + 31) / 32; // syndrome slots per lane
+  constexpr int NSY = (2 * T + 31) / 32;
   constexpr int NW = (p::n + 31) / 32;
-  extern __shared__ __align__(16) uint32_t dsm[];
-  uint16_t *sh16 = reinterpret_cast<uint16_t *>(dsm);
+  constexpr int SIG = 1 << D;
+  extern __shared__ __align__(16) uint32_t rsm[];
+  uint16_t *sh16 = reinterpret_cast<uint16_t *>(rsm);
   uint16_t *gexp = sh16 + LY::exp_off;
   uint16_t *glog = sh16 + LY::log_off;
   uint16_t *alog = sh16 + LY::alpha_off;
@@ -86,131 +204,57 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) decode_kernel(const uint32_
   __syncthreads();
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *wbase = dsm + LY::shared_u16 / 2 + warp * LY::warp_u32;
+  uint32_t *wbase = rsm + LY::shared_u16 / 2 + warp * LY::warp_u32;
   uint32_t *esm = wbase;
   uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::ewp);
   uint16_t *ssm = V + Q;
-  uint16_t *slog = ssm + 2 * T;
 
-  const long long nwarps = (long long)gridDim.x * kDecodeWarps;
-  for (long long op = (long long)blockIdx.x * kDecodeWarps + warp; op < N; op += nwarps) {
-    // 1. unpack the 2t syndromes (m bits each) produced by the front end
-    const uint32_t *srow = S2 + op * lds2;
-#pragma unroll
-    for (int k = 0; k < NSY; k++) {
-      const int j = lane + 32 * k;
-      if (j < 2 * T) {
-        const int b = j * M, w = b >> 5, sh = b & 31;
-        uint32_t v = srow[w] >> sh;
-        if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
-        v &= Q - 1;
-        ssm[j] = (uint16_t)v;
-        slog[j] = glog[v];
-      }
-    }
+  const long long nwarps = (long long)gridDim.x * kRootWarps;
+  for (long long op = (long long)blockIdx.x * kRootWarps + warp; op < N; op += nwarps) {
+    const uint16_t *sig = Sig + op * SIG;
+    for (int x = lane; x < SIG; x += 32) V[x] = sig[x];
     __syncwarp();
-
-    // 2. Berlekamp-Massey: coefficient i = lane + 32k of C and B per lane
-    uint16_t C[NS], B[NS];
-#pragma unroll
-    for (int k = 0; k < NS; k++) {
-      const int i = lane + 32 * k;
-      C[k] = (i == 0);
-      B[k] = (i == 1);
-    }
-    int L = 0;
-    uint32_t b = 1;
-#pragma unroll 1
-    for (int n = 0; n < 2 * T; n++) {
-      const int lim = n < T ? n : T;
-      uint32_t dp = 0;
-#pragma unroll
-      for (int k = 0; k < NS; k++) {
-        const int i = lane + 32 * k;
-        if (i <= lim) dp ^= gf_mul_log<M>(gexp, glog[C[k]], slog[n - i]);
-      }
-      const uint32_t d = warp_xor(dp);
-      const bool upd = d && (n >= 2 * L);
-      uint16_t Tk[NS];
-      if (d) {
-        int lf = (int)glog[d] - (int)glog[b];
-        if (lf < 0) lf += Q - 1;
-#pragma unroll
-        for (int k = 0; k < NS; k++) {
-          Tk[k] = C[k];
-          C[k] ^= gf_mul_log<M>(gexp, lf, glog[B[k]]);
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < NS; k++) Tk[k] = C[k];
-      }
-      if (upd) {
-        L = n + 1 - L;
-        b = d;
-#pragma unroll
-        for (int k = 0; k < NS; k++) B[k] = Tk[k];
-      }
-      // B <- x * B (coefficient i takes i-1)
-      uint16_t nb[NS];
-#pragma unroll
-      for (int k = 0; k < NS; k++) {
-        uint16_t up = (uint16_t)__shfl_up_sync(0xffffffffu, B[k], 1);
-        uint16_t wrap = (uint16_t)__shfl_sync(0xffffffffu, k ? B[k ? k - 1 : 0] : 0, 31);
-        nb[k] = lane ? up : (k ? wrap : 0);
-      }
-#pragma unroll
-      for (int k = 0; k < NS; k++) B[k] = nb[k];
-    }
-
-    // 3. locator sigma(x) = sum_deg C[t-deg] x^deg into the FFT coefficient slots
-    for (int x = lane; x < (1 << D); x += 32) V[x] = 0;
-    __syncwarp();
-#pragma unroll
-    for (int k = 0; k < NS; k++) {
-      const int i = lane + 32 * k;
-      const int deg = T - i;
-      if (i <= T && deg < (1 << D)) V[deg] = C[k];
-    }
-    __syncwarp();
-
-    // 4. additive FFT, top-down: twist by the level's first basis element and
-    //    radix-convert g(x) = g0(x^2+x) + x g1(x^2+x); children interleave
-    //    (even/odd coefficients) so no data moves between levels.
+    // top-down: twist by the level's first basis element, then radix-convert
+    // g(x) = g0(x^2+x) + x g1(x^2+x); children interleave (even/odd) in place
 #pragma unroll 1
     for (int l = 0; l < D; l++) {
       const int sz = 1 << (D - l);
       if (l) {
         const uint16_t *tw = tlog + ((2 << D) - (2 << (D - l)));
-        for (int x = lane; x < (1 << D); x += 32) V[x] = gf_mul_log<M>(gexp, glog[V[x]], tw[x >> l]);
+        for (int x = lane; x < SIG; x += 32) V[x] = gf_mul_log<M>(gexp, glog[V[x]], tw[x >> l]);
         __syncwarp();
       }
 #pragma unroll 1
       for (int s = sz; s >= 4; s >>= 1) {
         const int tau = s >> 2;
-        for (int it = lane; it < (1 << D) / 4; it += 32) {
+        for (int it = lane; it < SIG / 4; it += 32) {
           const int path = it & ((1 << l) - 1), rest = it >> l;
-          const int u = rest % tau, bl = rest / tau;
+          const int u = rest & (tau - 1), bl = rest / tau;
           const int i2 = bl * s + 2 * tau + u;
           V[path + (i2 << l)] ^= V[path + ((i2 + tau) << l)];
         }
         __syncwarp();
-        for (int it = lane; it < (1 << D) / 4; it += 32) {
+        for (int it = lane; it < SIG / 4; it += 32) {
           const int path = it & ((1 << l) - 1), rest = it >> l;
-          const int u = rest % tau, bl = rest / tau;
+          const int u = rest & (tau - 1), bl = rest / tau;
           const int i1 = bl * s + tau + u;
           V[path + (i1 << l)] ^= V[path + ((i1 + tau) << l)];
         }
         __syncwarp();
       }
     }
-    //    bottom-up: leaves are constants over their coset; butterflies with
-    //    per-level constants alpha_{l,c'} (log form, zero sentinel).
-    for (int x = (1 << D) + lane; x < Q; x += 32) V[x] = V[x & ((1 << D) - 1)];
+    // bottom-up: leaves are constant over their coset, then butterflies
+    // (a, b) -> (a + alpha_{l,c'} b, a + alpha_{l,c'} b + b) per level
+    {
+      uint32_t *V32 = reinterpret_cast<uint32_t *>(V);
+      for (int x = SIG / 2 + lane; x < Q / 2; x += 32) V32[x] = V32[x & (SIG / 2 - 1)];
+    }
     __syncwarp();
 #pragma unroll 1
     for (int l = D - 1; l >= 0; l--) {
       const uint16_t *al = alog + (Q - (Q >> l));
       const int h = 1 << l;
+#pragma unroll 4
       for (int u = lane; u < Q / 2; u += 32) {
         const int path = u & (h - 1), cp = u >> l;
         const int x = path + (cp << (l + 1));
@@ -222,10 +266,9 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) decode_kernel(const uint32_
       }
       __syncwarp();
     }
-
-    // 5. error positions: sigma(L_i) == 0 (+ L_i^(2^d) for the separate leading term)
+    // error positions: sigma(L_i) == 0, with L_i^(2^d) for the separate leading term
     int weight = 0;
-#pragma unroll 1
+#pragma unroll 2
     for (int it = 0; it < NW; it++) {
       const int i = it * 32 + lane;
       bool err = false;
@@ -239,10 +282,20 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) decode_kernel(const uint32_
       weight += __popc(w);
     }
     __syncwarp();
-
-    // 6. re-encryption: syndromes of the found error must equal the received ones
     bool ok = (weight == T);
     if (ok) {
+      // received syndromes (m bits each) of this request
+      const uint32_t *srow = S2 + op * lds2;
+#pragma unroll
+      for (int k = 0; k < NSY; k++) {
+        const int j = lane + 32 * k;
+        if (j < 2 * T) {
+          const int b = j * M, w = b >> 5, sh = b & 31;
+          uint32_t v = srow[w] >> sh;
+          if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
+          ssm[j] = (uint16_t)(v & (Q - 1));
+        }
+      }
       uint32_t sc[NSY];
 #pragma unroll
       for (int k = 0; k < NSY; k++) sc[k] = 0;
@@ -254,17 +307,22 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) decode_kernel(const uint32_
           w &= w - 1;
           const int i = it * 32 + bit;
           const int ll = key.LL[i], lw = key.LW2[i];
-          if (ll == ZL) {  // L_i = 0: only the j = 0 term
+          if (ll == ZL) {  // L_i = 0 contributes only to s_0
             if (lane == 0) sc[0] ^= gexp[lw];
           } else {
+            // log(w2_i L_i^j) for j = lane + 32k, stepping by 32 log L_i mod 2^m - 1
+            int idx = fold_mod<M>(lw + lane * ll);
+            const int step = fold_mod<M>(32 * ll);
 #pragma unroll
             for (int k = 0; k < NSY; k++) {
-              const int j = lane + 32 * k;
-              sc[k] ^= gexp[fold_mod<M>(lw + j * ll)];
+              sc[k] ^= gexp[idx];
+              idx += step;
+              idx = idx >= Q - 1 ? idx - (Q - 1) : idx;
             }
           }
         }
       }
+      __syncwarp();
       bool mism = false;
 #pragma unroll
       for (int k = 0; k < NSY; k++) {
@@ -330,22 +388,38 @@ cudaError_t launch_pack_ct(const uint8_t *C, long long N, uint32_t *X, int ldx, 
   return cudaGetLastError();
 }
 
-template <int SET>
-cudaError_t launch_decode(const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd, long long N, uint32_t *E,
-                          int lde, int *ok, cudaStream_t st) {
-  if (N <= 0) return cudaSuccess;
-  const int smem = DecodeLayout<SET>::bytes(kDecodeWarps);
-  cudaError_t err = cudaFuncSetAttribute(decode_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (err != cudaSuccess) return err;
+template <typename K>
+static int persistent_blocks(K kernel, int threads, int smem, long long work_items, int items_per_block) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, decode_kernel<SET>, kDecodeWarps * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
   if (per_sm < 1) per_sm = 1;
-  long long need = (N + kDecodeWarps - 1) / kDecodeWarps;
+  long long need = (work_items + items_per_block - 1) / items_per_block;
   long long blocks = (long long)sms * per_sm;
-  if (blocks > need) blocks = need;
-  decode_kernel<SET><<<(unsigned)blocks, kDecodeWarps * 32, smem, st>>>(S2, lds2, key, fd, N, E, lde, ok);
+  return (int)(blocks < need ? blocks : need);
+}
+
+template <int SET>
+cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, long long N, uint16_t *Sig, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  const int smem_bm = BMLayout<SET>::bytes(kBMWarps);
+  cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bm);
+  if (err != cudaSuccess) return err;
+  const int gb = persistent_blocks(dec_bm_kernel<SET>, kBMWarps * 32, smem_bm, N, kBMWarps);
+  dec_bm_kernel<SET><<<gb, kBMWarps * 32, smem_bm, st>>>(S2, lds2, fd, N, Sig);
+  return cudaGetLastError();
+}
+
+template <int SET>
+cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd,
+                            long long N, uint32_t *E, int lde, int *ok, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  const int smem_rt = RootLayout<SET>::bytes(kRootWarps);
+  cudaError_t err = cudaFuncSetAttribute(dec_root_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_rt);
+  if (err != cudaSuccess) return err;
+  const int gr = persistent_blocks(dec_root_kernel<SET>, kRootWarps * 32, smem_rt, N, kRootWarps);
+  dec_root_kernel<SET><<<gr, kRootWarps * 32, smem_rt, st>>>(Sig, S2, lds2, key, fd, N, E, lde, ok);
   return cudaGetLastError();
 }
 
@@ -360,8 +434,9 @@ cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uin
 
 #define GMC_INST_DEC(SET)                                                                                       \
   template cudaError_t launch_pack_ct<SET>(const uint8_t *, long long, uint32_t *, int, cudaStream_t);          \
-  template cudaError_t launch_decode<SET>(const uint32_t *, int, DecKeyDev, FieldDev, long long, uint32_t *,   \
-                                          int, int *, cudaStream_t);                                            \
+  template cudaError_t launch_dec_bm<SET>(const uint32_t *, int, FieldDev, long long, uint16_t *, cudaStream_t); \
+  template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, DecKeyDev, FieldDev,        \
+                                            long long, uint32_t *, int, int *, cudaStream_t);                    \
   template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, DecKeyDev,    \
                                             uint8_t *, int *, long long, cudaStream_t);
 GMC_INST_DEC(0)
