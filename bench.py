@@ -42,7 +42,7 @@ N_DEFAULT = 65536
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gmc", choices=["gmc", "reference"])
     ap.add_argument("--set", default=SET_DEFAULT)
@@ -138,11 +138,11 @@ def cpu_baseline(sid, pk, sk, cts_host, seeds_host, c_gpu, k_gpu, kdec_gpu, thre
     t0 = time.perf_counter()
     O.dec_batch(sid, sk, cts_host[:threads], threads=threads)
     t_dec1 = (time.perf_counter() - t0) / threads
-    n_dec = int(min(len(cts_host), max(threads, 6.0 * threads / max(t_dec1, 1e-6))))
+    n_dec = int(min(len(cts_host), max(threads, 6.0 / max(t_dec1, 1e-9))))
     t0 = time.perf_counter()
     O.enc_batch(sid, pk, seeds_host[:threads], threads=threads)
     t_enc1 = (time.perf_counter() - t0) / threads
-    n_enc = int(min(len(seeds_host), max(threads, 3.0 * threads / max(t_enc1, 1e-6))))
+    n_enc = int(min(len(seeds_host), max(threads, 3.0 / max(t_enc1, 1e-9))))
     t0 = time.perf_counter()
     oc, ok_, _ = O.enc_batch(sid, pk, seeds_host[:n_enc], threads=threads)
     t_enc = time.perf_counter() - t0

@@ -55,7 +55,7 @@ struct gmc_key {
   // secret key
   uint32_t *F = nullptr;
   int ldf = 0, frows_pad = 0, cw_pad = 0;
-  uint16_t *tabs = nullptr;  // L | LL | LW2 | Lpow, n each
+  uint16_t *tabs = nullptr;  // L | LL | LW2 (n each) | invL (2^m)
   uint8_t *s = nullptr;
   DecKeyDev dk{};
 };
@@ -148,6 +148,10 @@ static int get_field(int set, FieldDev *out) {
   all.insert(all.end(), F.log.begin(), F.log.end());
   all.insert(all.end(), ft.alpha_log.begin(), ft.alpha_log.end());
   all.insert(all.end(), ft.twist_log.begin(), ft.twist_log.end());
+  const size_t o_frlo = all.size();
+  all.insert(all.end(), ft.frob_lo.begin(), ft.frob_lo.end());
+  const size_t o_frhi = all.size();
+  all.insert(all.end(), ft.frob_hi.begin(), ft.frob_hi.end());
   FieldEntry e;
   GMC_CUDA(cudaMalloc(&e.buf, all.size() * 2));
   GMC_CUDA(cudaMemcpy(e.buf, all.data(), all.size() * 2, cudaMemcpyHostToDevice));
@@ -155,6 +159,8 @@ static int get_field(int set, FieldDev *out) {
   e.fd.glog = e.buf + o_log;
   e.fd.fft_alpha_log = e.buf + o_alpha;
   e.fd.fft_twist_log = e.buf + o_twist;
+  e.fd.frob_lo = e.buf + o_frlo;
+  e.fd.frob_hi = e.buf + o_frhi;
   g_fields[key] = e;
   *out = e.fd;
   return GMC_OK;
@@ -210,13 +216,14 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   k->ldf = h.ldf; k->frows_pad = h.frows_pad; k->cw_pad = h.cw_pad;
   const size_t n = S.n;
   cudaError_t e = cudaMalloc(&k->F, h.F.size() * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&k->tabs, 4 * n * 2);
+  const size_t q = (size_t)S.q;
+  if (e == cudaSuccess) e = cudaMalloc(&k->tabs, (3 * n + q) * 2);
   if (e == cudaSuccess) e = cudaMalloc(&k->s, S.e_bytes);
   if (e == cudaSuccess) e = cudaMemcpy(k->F, h.F.data(), h.F.size() * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs, h.L.data(), n * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs + n, h.LL.data(), n * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 2 * n, h.LW2.data(), n * 2, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 3 * n, h.Lpow.data(), n * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 3 * n, h.invL.data(), q * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->s, h.s.data(), S.e_bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s);
@@ -226,7 +233,7 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   k->dk.L = k->tabs;
   k->dk.LL = k->tabs + n;
   k->dk.LW2 = k->tabs + 2 * n;
-  k->dk.Lpow = k->tabs + 3 * n;
+  k->dk.invL = k->tabs + 3 * n;
   k->dk.s = k->s;
   *out = k;
   return GMC_OK;

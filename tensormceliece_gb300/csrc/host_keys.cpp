@@ -145,6 +145,14 @@ FftTables build_fft_tables(int m, int d) {
     for (int i = 1; i < dim; i++) nb[i - 1] = (uint16_t)(F.sq(delta[i]) ^ delta[i]);
     beta = nb;
   }
+  auto frob = [&](uint16_t a) {
+    for (int r = 0; r < d; r++) a = F.sq(a);
+    return a;
+  };
+  t.frob_lo.resize(1 << d);
+  for (int x = 0; x < (1 << d); x++) t.frob_lo[x] = frob((uint16_t)x);
+  t.frob_hi.resize(1 << (m - d));
+  for (int c = 0; c < (1 << (m - d)); c++) t.frob_hi[c] = frob((uint16_t)(c << d));
   return t;
 }
 
@@ -199,6 +207,7 @@ int build_sk(int set, const uint8_t *sk, SkHost &out) {
   for (int s = m - 2; s >= 0; s--) { layer(s, cb); cb += q >> 4; }
 
   out.L.resize(n); out.LL.resize(n); out.LW2.resize(n); out.Lpow.resize(n);
+  out.invL.assign(q, 0xFFFF);
   std::vector<uint16_t> w2(n);
   const int d = S.fft_d;
   for (int i = 0; i < n; i++) {
@@ -208,6 +217,7 @@ int build_sk(int set, const uint8_t *sk, SkHost &out) {
     if (!v) return -1;  // g has a root on the support: not a valid key
     w2[i] = F.inv(F.mul(v, v));
     out.L[i] = a;
+    out.invL[a] = (uint16_t)i;
     out.LL[i] = F.log[a];
     out.LW2[i] = F.log[w2[i]];
     uint16_t pw = a;

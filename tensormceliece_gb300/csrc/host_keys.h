@@ -29,6 +29,8 @@ const HostField &host_field(int m);
 struct FftTables {
   std::vector<uint16_t> twist_log;  // levels concatenated, 2^(d-l) each (2^(d+1) total)
   std::vector<uint16_t> alpha_log;  // levels concatenated, 2^(m-l-1) each (padded to 2^m)
+  std::vector<uint16_t> frob_lo;    // x^(2^d), x < 2^d
+  std::vector<uint16_t> frob_hi;    // (c 2^d)^(2^d), c < 2^(m-d)
 };
 FftTables build_fft_tables(int m, int d);
 
@@ -43,6 +45,7 @@ void build_pk(int set, const uint8_t *pk, PkHost &out);
 // Secret key -> support, logs, front-end matrix F.
 struct SkHost {
   std::vector<uint16_t> L, LL, LW2, Lpow;   // [n]
+  std::vector<uint16_t> invL;               // [2^m]: position of each field element, 0xFFFF if none
   std::vector<uint8_t> s;                   // [n/8]
   std::vector<uint32_t> F;                  // frows_pad x ldf
   int ldf = 0, frows_pad = 0, cw_pad = 0;

@@ -9,7 +9,7 @@ namespace gmc {
 constexpr int kSampleThreads = 64;
 constexpr int kTailThreads = 128;
 constexpr int kBMWarps = 16;    // Berlekamp-Massey kernel: warps per block
-constexpr int kRootWarps = 8;   // root-finding kernel: warps per block
+constexpr int kRootWarps = 16;  // root-finding kernel: warps per block
 
 // GF(2) GEMM engines for Out[op] = parity(A[row] & X[op]) over KW words.
 enum GemmEngine { GEMM_POPC = 0, GEMM_B1MMA = 1, GEMM_TC = 2 };
@@ -36,7 +36,7 @@ struct DecKeyDev {
   const uint16_t *L;     // support element of each code position [n]
   const uint16_t *LL;    // log L_i (zero sentinel when L_i = 0) [n]
   const uint16_t *LW2;   // log of 1/g(L_i)^2 [n]
-  const uint16_t *Lpow;  // L_i^(2^fft_d) when the locator's leading term is separate [n]
+  const uint16_t *invL;  // code position of each field element, 0xFFFF off the support [2^m]
   const uint8_t *s;      // implicit-rejection string [n/8]
 };
 
@@ -46,6 +46,8 @@ struct FieldDev {
   const uint16_t *glog;   // [q]
   const uint16_t *fft_alpha_log;  // concatenated per level l = 0..d-1: [2^(m-l-1)]
   const uint16_t *fft_twist_log;  // concatenated per level l = 0..d-1: [2^(d-l)]
+  const uint16_t *frob_lo;  // x^(2^d) for x < 2^d
+  const uint16_t *frob_hi;  // (c 2^d)^(2^d) for c < 2^(m-d)
 };
 
 template <int SET>

@@ -163,19 +163,31 @@ __global__ void __launch_bounds__(kBMWarps * 32) dec_bm_kernel(const uint32_t *_
 // ---------------------------------------------------------------- root finding
 // One warp per request: additive FFT of sigma over all 2^m field elements
 // (Gao-Mateer, basis beta_i = 2^i so point c is the element c), the error
-// positions sigma(L_i) = 0 at the key's support, the weight and the
-// re-encryption check (syndromes of the found error equal the received ones).
+// positions, the weight and the re-encryption check.
+// The top-down part (twist + radix conversion) turns the 2^d coefficients
+// into 2^d leaf constants. Every bottom-up butterfly level has stride < 2^d,
+// so the 2^m evaluations split into 2^(m-d) independent chunks of 2^d
+// consecutive elements that all start from the same leaves: the warp walks
+// the chunks in a 2^d-entry shared buffer. A root (sigma(a) = 0, with a^(2^d)
+// added for the separate leading term via Frobenius tables, since
+// (hi + lo)^(2^d) = hi^(2^d) + lo^(2^d)) is mapped to its code position
+// through the key's inverse support table; only roots touch that table.
 template <int SET>
 struct RootLayout {
   using p = P<SET>;
-  static constexpr int Q = p::q, D = p::fft_d;
+  static constexpr int Q = p::q, D = p::fft_d, SIG = 1 << D, NC = Q >> D;
   static constexpr int exp_off = 0, exp_len = 2 * Q;
   static constexpr int log_off = exp_off + exp_len, log_len = Q;
   static constexpr int alpha_off = log_off + log_len, alpha_len = Q;
   static constexpr int twist_off = alpha_off + alpha_len, twist_len = 2 << D;
-  static constexpr int shared_u16 = twist_off + twist_len;
+  static constexpr int frlo_off = twist_off + twist_len, frlo_len = SIG;
+  static constexpr int frhi_off = frlo_off + frlo_len, frhi_len = NC;
+  static constexpr int shared_u16 = (frhi_off + frhi_len + 1) & ~1;
   static constexpr int ewp = (p::ew + 1) & ~1;
-  static constexpr int warp_u32 = ewp + Q / 2 + p::t;  // e words | V[Q] u16 | s[2t] u16
+  // per warp (u32): e words | roots [t] (pos << 16 | element) | count | V[SIG] u16 | s[2t] u16
+  static constexpr int roots_off = ewp, cnt_off = roots_off + p::t, v_off = cnt_off + 2;
+  static constexpr int s_off = v_off + SIG / 2;
+  static constexpr int warp_u32 = s_off + p::t;
   static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u32 * 4; }
 };
 
@@ -187,32 +199,39 @@ __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_
                                                                    int *__restrict__ okout) {
   using p = P<SET>;
   using LY = RootLayout<SET>;
-  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
-  constexpr int ZL = GFLog<M>::zero_log;
+  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d, SIG = LY::SIG, NC = LY::NC;
   constexpr int NSY = (2 * T + 31) / 32;
   constexpr int NW = (p::n + 31) / 32;
-  constexpr int SIG = 1 << D;
+  constexpr int VPL = SIG / 32;  // chunk values per lane
   extern __shared__ __align__(16) uint32_t rsm[];
   uint16_t *sh16 = reinterpret_cast<uint16_t *>(rsm);
   uint16_t *gexp = sh16 + LY::exp_off;
   uint16_t *glog = sh16 + LY::log_off;
   uint16_t *alog = sh16 + LY::alpha_off;
   uint16_t *tlog = sh16 + LY::twist_off;
+  uint16_t *frlo = sh16 + LY::frlo_off;
+  uint16_t *frhi = sh16 + LY::frhi_off;
   for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
   for (int i = threadIdx.x; i < Q; i += blockDim.x) { glog[i] = fd.glog[i]; alog[i] = fd.fft_alpha_log[i]; }
   for (int i = threadIdx.x; i < (2 << D); i += blockDim.x) tlog[i] = fd.fft_twist_log[i];
+  for (int i = threadIdx.x; i < SIG; i += blockDim.x) frlo[i] = fd.frob_lo[i];
+  for (int i = threadIdx.x; i < NC; i += blockDim.x) frhi[i] = fd.frob_hi[i];
   __syncthreads();
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t *wbase = rsm + LY::shared_u16 / 2 + warp * LY::warp_u32;
   uint32_t *esm = wbase;
-  uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::ewp);
-  uint16_t *ssm = V + Q;
+  uint32_t *roots = wbase + LY::roots_off;
+  uint32_t *cnt = wbase + LY::cnt_off;
+  uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::v_off);
+  uint16_t *ssm = reinterpret_cast<uint16_t *>(wbase + LY::s_off);
 
   const long long nwarps = (long long)gridDim.x * kRootWarps;
   for (long long op = (long long)blockIdx.x * kRootWarps + warp; op < N; op += nwarps) {
     const uint16_t *sig = Sig + op * SIG;
     for (int x = lane; x < SIG; x += 32) V[x] = sig[x];
+    for (int w = lane; w < NW; w += 32) esm[w] = 0;
+    if (lane == 0) *cnt = 0;
     __syncwarp();
     // top-down: twist by the level's first basis element, then radix-convert
     // g(x) = g0(x^2+x) + x g1(x^2+x); children interleave (even/odd) in place
@@ -243,45 +262,56 @@ __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_
         __syncwarp();
       }
     }
-    // bottom-up: leaves are constant over their coset, then butterflies
-    // (a, b) -> (a + alpha_{l,c'} b, a + alpha_{l,c'} b + b) per level
-    {
-      uint32_t *V32 = reinterpret_cast<uint32_t *>(V);
-      for (int x = SIG / 2 + lane; x < Q / 2; x += 32) V32[x] = V32[x & (SIG / 2 - 1)];
-    }
+    uint16_t leaf[VPL];
+#pragma unroll
+    for (int j = 0; j < VPL; j++) leaf[j] = V[lane + 32 * j];
     __syncwarp();
+
+    // bottom-up, one chunk of 2^d consecutive field elements at a time
+    int weight = 0;
 #pragma unroll 1
-    for (int l = D - 1; l >= 0; l--) {
-      const uint16_t *al = alog + (Q - (Q >> l));
-      const int h = 1 << l;
-#pragma unroll 4
-      for (int u = lane; u < Q / 2; u += 32) {
-        const int path = u & (h - 1), cp = u >> l;
-        const int x = path + (cp << (l + 1));
-        uint16_t a = V[x];
-        const uint16_t bb = V[x + h];
-        a ^= gf_mul_log<M>(gexp, al[cp], glog[bb]);
-        V[x] = a;
-        V[x + h] = a ^ bb;
+    for (int c = 0; c < NC; c++) {
+#pragma unroll
+      for (int j = 0; j < VPL; j++) V[lane + 32 * j] = leaf[j];
+      __syncwarp();
+#pragma unroll
+      for (int l = D - 1; l >= 0; l--) {
+        const uint16_t *al = alog + (Q - (Q >> l)) + (c << (D - 1 - l));
+        const int h = 1 << l;
+#pragma unroll
+        for (int it = 0; it < SIG / 64; it++) {
+          const int u = lane + 32 * it;
+          const int path = u & (h - 1), cpl = u >> l;
+          const int x = path + (cpl << (l + 1));
+          uint16_t a = V[x];
+          const uint16_t bb = V[x + h];
+          a ^= gf_mul_log<M>(gexp, al[cpl], glog[bb]);
+          V[x] = a;
+          V[x + h] = a ^ bb;
+        }
+        __syncwarp();
+      }
+#pragma unroll
+      for (int j = 0; j < VPL; j++) {
+        const int xl = lane + 32 * j;
+        const int elt = (c << D) | xl;
+        uint16_t v = V[xl];
+        if (p::lead) v ^= frhi[c] ^ frlo[xl];
+        bool hit = false;
+        if (v == 0) {
+          const uint32_t pos = key.invL[elt];
+          if (pos < (uint32_t)p::n) {
+            hit = true;
+            atomicOr(&esm[pos >> 5], 1u << (pos & 31));
+            const uint32_t slot = atomicAdd(cnt, 1u);
+            if (slot < (uint32_t)T) roots[slot] = (pos << 16) | (uint32_t)elt;
+          }
+        }
+        weight += __popc(__ballot_sync(0xffffffffu, hit));
       }
       __syncwarp();
     }
-    // error positions: sigma(L_i) == 0, with L_i^(2^d) for the separate leading term
-    int weight = 0;
-#pragma unroll 2
-    for (int it = 0; it < NW; it++) {
-      const int i = it * 32 + lane;
-      bool err = false;
-      if (i < p::n) {
-        uint16_t v = V[key.L[i]];
-        if (p::lead) v ^= key.Lpow[i];
-        err = (v == 0);
-      }
-      const uint32_t w = __ballot_sync(0xffffffffu, err);
-      if (lane == 0) esm[it] = w;
-      weight += __popc(w);
-    }
-    __syncwarp();
+
     bool ok = (weight == T);
     if (ok) {
       // received syndromes (m bits each) of this request
@@ -296,29 +326,27 @@ __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_
           ssm[j] = (uint16_t)(v & (Q - 1));
         }
       }
+      // syndromes of the found error: sum over roots of w2_i L_i^j
       uint32_t sc[NSY];
 #pragma unroll
       for (int k = 0; k < NSY; k++) sc[k] = 0;
 #pragma unroll 1
-      for (int it = 0; it < NW; it++) {
-        uint32_t w = esm[it];
-        while (w) {
-          const int bit = __ffs(w) - 1;
-          w &= w - 1;
-          const int i = it * 32 + bit;
-          const int ll = key.LL[i], lw = key.LW2[i];
-          if (ll == ZL) {  // L_i = 0 contributes only to s_0
-            if (lane == 0) sc[0] ^= gexp[lw];
-          } else {
-            // log(w2_i L_i^j) for j = lane + 32k, stepping by 32 log L_i mod 2^m - 1
-            int idx = fold_mod<M>(lw + lane * ll);
-            const int step = fold_mod<M>(32 * ll);
+      for (int r = 0; r < T; r++) {
+        const uint32_t rv = roots[r];
+        const int elt = rv & 0xFFFF, pos = rv >> 16;
+        const int lw = key.LW2[pos];
+        if (elt == 0) {  // L_i = 0 contributes only to s_0
+          if (lane == 0) sc[0] ^= gexp[lw];
+        } else {
+          const int ll = glog[elt];
+          // log(w2_i L_i^j) for j = lane + 32k, stepping by 32 log L_i mod 2^m - 1
+          int idx = fold_mod<M>(lw + lane * ll);
+          const int step = fold_mod<M>(32 * ll);
 #pragma unroll
-            for (int k = 0; k < NSY; k++) {
-              sc[k] ^= gexp[idx];
-              idx += step;
-              idx = idx >= Q - 1 ? idx - (Q - 1) : idx;
-            }
+          for (int k = 0; k < NSY; k++) {
+            sc[k] ^= gexp[idx];
+            idx += step;
+            idx = idx >= Q - 1 ? idx - (Q - 1) : idx;
           }
         }
       }
