@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--set", default=SET_DEFAULT)
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--flip", type=float, default=0.10)
-    ap.add_argument("--engine", default="popc", choices=["popc", "b1mma", "tc"])
+    ap.add_argument("--engine", default="tc", choices=["popc", "b1mma", "tc"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()

@@ -113,6 +113,9 @@ void gmc_set_randombytes(gmc_randombytes_fn fn, void *ctx);
 #define GMC_GEMM_TC 2     /* tcgen05 (5th-gen tensor cores), 0/1 operands in FP8, TMEM accumulators */
 int gmc_set_gemm_engine(int engine);
 int gmc_get_gemm_engine(void);
+/* Reads and clears the tensor-core engine's error word on the current device:
+ * 1 when a CTA gave up on a bounded wait (its outputs are then invalid). */
+int gmc_tc_status(void);
 
 /* Stage outputs of a decapsulation batch (device pointers): the 2t packed
  * syndromes (s_words per request), the error vectors (e_words per request)
@@ -125,7 +128,7 @@ int gmc_enc_stages_dev(const gmc_key *pk, const unsigned char *seeds, long long 
                        int e_words, unsigned int *synd, int synd_words, void *stream);
 /* Raw GF(2) product Out[i] = A * X[i] on the selected engine (device
  * pointers, layouts as documented in the engine: rows_pad % 128 == 0,
- * kw_pad % 8 == 0, n_pad % 64 == 0, lda/ldx >= kw_pad). */
+ * kw_pad % 8 == 0, n_pad % 256 == 0, lda/ldx >= kw_pad; X has n_pad rows). */
 int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int rows_pad, const unsigned int *X, int ldx,
                      long long n_pad, int kw_pad, unsigned int *out, int ldo, int out_words, long long n,
                      void *stream);

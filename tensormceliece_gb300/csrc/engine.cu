@@ -56,11 +56,13 @@ struct gmc_key {
   uint32_t *F = nullptr;
   int ldf = 0, frows_pad = 0, cw_pad = 0;
   uint16_t *tabs = nullptr;  // L | LL | LW2 (n each) | invL (2^m)
+  uint8_t *a8 = nullptr;     // FP8 stage images of T (public) or F (secret) for the tensor-core engine
+  std::mutex *a8_mu = nullptr;
   uint8_t *s = nullptr;
   DecKeyDev dk{};
 };
 
-static int g_engine = GEMM_POPC;
+static int g_engine = GEMM_TC;
 
 // ---------------------------------------------------------------- profiler
 // Optional per-kernel timing: when enabled, an event is recorded on the
@@ -168,6 +170,70 @@ static int get_field(int set, FieldDev *out) {
 
 static bool valid_set(int set) { return set >= 0 && set < GMC_NSETS; }
 
+// Per-device error word of the tensor-core engine (a CTA that gave up on a
+// bounded wait sets it to 1); gmc_tc_status() reads and clears it.
+static std::mutex g_err_mu;
+static std::map<int, int *> g_err_words;
+static int *tc_err_word() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  auto it = g_err_words.find(dev);
+  if (it != g_err_words.end()) return it->second;
+  int *w = nullptr;
+  if (cudaMalloc(&w, sizeof(int)) != cudaSuccess) return nullptr;
+  cudaMemset(w, 0, sizeof(int));
+  g_err_words[dev] = w;
+  return w;
+}
+
+extern "C" int gmc_tc_status(void) {
+  int *w = tc_err_word();
+  if (!w) return fail(GMC_ECUDA, "gmc_tc_status: no device");
+  int v = 0;
+  GMC_CUDA(cudaMemcpy(&v, w, sizeof(int), cudaMemcpyDeviceToHost));
+  GMC_CUDA(cudaMemset(w, 0, sizeof(int)));
+  return v;
+}
+
+// FP8 stage images of the key matrix, built on first use by the tensor-core engine.
+static cudaError_t key_a8(const gmc_key *kc, cudaStream_t st, const uint8_t **out) {
+  gmc_key *k = const_cast<gmc_key *>(kc);
+  std::lock_guard<std::mutex> lk(*k->a8_mu);
+  if (!k->a8) {
+    const uint32_t *A = k->kind == 0 ? k->T : k->F;
+    const int lda = k->kind == 0 ? k->lda : k->ldf, rows = k->kind == 0 ? k->rows_pad : k->frows_pad;
+    const int kw = k->kind == 0 ? k->kw_pad : k->cw_pad;
+    uint8_t *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, tc_a8_bytes(rows, kw));
+    if (e != cudaSuccess) return e;
+    e = launch_expand_a(A, lda, rows, kw, p, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return e;
+    }
+    k->a8 = p;
+  }
+  *out = k->a8;
+  return cudaSuccess;
+}
+
+static cudaError_t key_gemm(const gmc_key *k, const uint32_t *X, int ldx, long long n_pad, uint32_t *Out, int ldo,
+                            int out_words, long long n, cudaStream_t st) {
+  const uint32_t *A = k->kind == 0 ? k->T : k->F;
+  const int lda = k->kind == 0 ? k->lda : k->ldf, rows = k->kind == 0 ? k->rows_pad : k->frows_pad;
+  const int kw = k->kind == 0 ? k->kw_pad : k->cw_pad;
+  const uint8_t *a8 = nullptr;
+  int *err = nullptr;
+  if (g_engine == GEMM_TC) {
+    cudaError_t e = key_a8(k, st, &a8);
+    if (e != cudaSuccess) return e;
+    if (!(err = tc_err_word())) return cudaErrorMemoryAllocation;
+  }
+  return launch_gf2_gemm(g_engine, A, a8, lda, rows, X, ldx, n_pad, kw, Out, ldo, out_words, n, err, st);
+}
+
 extern "C" int gmc_set_count(void) { return GMC_NSETS; }
 extern "C" const char *gmc_set_name(int set) { return valid_set(set) ? set_info(set).name : nullptr; }
 extern "C" int gmc_set_id(const char *name) {
@@ -191,14 +257,15 @@ extern "C" int gmc_pk_load(gmc_key **out, int set, const unsigned char *pk) {
   PkHost h;
   build_pk(set, pk, h);
   gmc_key *k = new gmc_key();
+  k->a8_mu = new std::mutex();
   k->set = set;
   k->kind = 0;
   cudaGetDevice(&k->device);
   k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad;
   cudaError_t e = cudaMalloc(&k->T, h.T.size() * 4);
-  if (e != cudaSuccess) { delete k; return cuda_fail(e, "gmc_pk_load: cudaMalloc"); }
+  if (e != cudaSuccess) { delete k->a8_mu; delete k; return cuda_fail(e, "gmc_pk_load: cudaMalloc"); }
   e = cudaMemcpy(k->T, h.T.data(), h.T.size() * 4, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(k->T); delete k; return cuda_fail(e, "gmc_pk_load: copy"); }
+  if (e != cudaSuccess) { cudaFree(k->T); delete k->a8_mu; delete k; return cuda_fail(e, "gmc_pk_load: copy"); }
   *out = k;
   return GMC_OK;
 }
@@ -210,6 +277,7 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   if (build_sk(set, sk, h)) return fail(GMC_EKEY, "gmc_sk_load: Goppa polynomial vanishes on the support");
   const gmc_setinfo &S = set_info(set);
   gmc_key *k = new gmc_key();
+  k->a8_mu = new std::mutex();
   k->set = set;
   k->kind = 1;
   cudaGetDevice(&k->device);
@@ -227,6 +295,7 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   if (e == cudaSuccess) e = cudaMemcpy(k->s, h.s.data(), S.e_bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s);
+    delete k->a8_mu;
     delete k;
     return cuda_fail(e, "gmc_sk_load");
   }
@@ -241,6 +310,8 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
 
 extern "C" void gmc_key_free(gmc_key *key) {
   if (!key) return;
+  cudaFree(key->a8);
+  delete key->a8_mu;
   cudaFree(key->T);
   cudaFree(key->F);
   cudaFree(key->tabs);
@@ -284,7 +355,7 @@ static EncDims enc_dims(const gmc_key *pk, long long n) {
   d.lde = round_up((S.n + 31) / 32, 4);
   d.ldx = pk->kw_pad;
   d.lds = round_up((S.mt + 31) / 32, 4);
-  d.n_pad = (n + kGemmOpTile - 1) / kGemmOpTile * kGemmOpTile;
+  d.n_pad = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
   return d;
 }
 
@@ -296,8 +367,7 @@ static cudaError_t enc_sample_gemm(const gmc_key *pk, const uint8_t *seeds, long
   cudaError_t e = launch_sample<SET>(seeds, n, E, d.lde, Ens, d.ldx, st);
   if (e != cudaSuccess) return e;
   prof_mark("enc_sample", st);
-  e = launch_gf2_gemm(g_engine, pk->T, pk->lda, pk->rows_pad, Ens, d.ldx, d.n_pad, pk->kw_pad, S, d.lds, p::mw, n,
-                      st);
+  e = key_gemm(pk, Ens, d.ldx, d.n_pad, S, d.lds, p::mw, n, st);
   prof_mark("enc_syndrome_gemm", st);
   return e;
 }
@@ -327,7 +397,7 @@ static DecDims dec_dims(const gmc_key *sk, long long n) {
   d.ldx = sk->cw_pad;
   d.lds2 = round_up((2 * S.t * S.m + 31) / 32, 4);
   d.lde = round_up((S.n + 31) / 32, 4);
-  d.n_pad = (n + kGemmOpTile - 1) / kGemmOpTile * kGemmOpTile;
+  d.n_pad = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
   return d;
 }
 
@@ -341,8 +411,7 @@ static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long lo
   cudaError_t e = launch_pack_ct<SET>(c, n, X, d.ldx, st);
   if (e != cudaSuccess) return e;
   prof_mark("dec_pack_ct", st);
-  e = launch_gf2_gemm(g_engine, sk->F, sk->ldf, sk->frows_pad, X, d.ldx, d.n_pad, sk->cw_pad, S2, d.lds2, p::s2w,
-                      n, st);
+  e = key_gemm(sk, X, d.ldx, d.n_pad, S2, d.lds2, p::s2w, n, st);
   if (e != cudaSuccess) return e;
   prof_mark("dec_front_gemm", st);
   e = launch_dec_bm<SET>(S2, d.lds2, fd, n, Sig, st);
@@ -542,8 +611,18 @@ extern "C" int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int 
                                 long long n, void *stream) {
   if (!A || !X || !out || n < 0 || lda < kw_pad || ldx < kw_pad || ldo < out_words)
     return fail(GMC_EINVAL, "gmc_gf2_gemm_dev: bad argument");
-  cudaError_t e = launch_gf2_gemm(engine, A, lda, rows_pad, X, ldx, n_pad, kw_pad, out, ldo, out_words, n,
-                                  (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t *a8 = nullptr;
+  int *err = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (engine == GEMM_TC) {  // one-off FP8 image of A for this call
+    if (!(err = tc_err_word())) return fail(GMC_ECUDA, "gmc_gf2_gemm_dev: error word");
+    e = cudaMallocAsync(&a8, tc_a8_bytes(rows_pad, kw_pad), st);
+    if (e == cudaSuccess) e = launch_expand_a(A, lda, rows_pad, kw_pad, a8, st);
+  }
+  if (e == cudaSuccess)
+    e = launch_gf2_gemm(engine, A, a8, lda, rows_pad, X, ldx, n_pad, kw_pad, out, ldo, out_words, n, err, st);
+  if (a8) cudaFreeAsync(a8, st);
   if (e != cudaSuccess) return cuda_fail(e, "gmc_gf2_gemm_dev");
   return GMC_OK;
 }

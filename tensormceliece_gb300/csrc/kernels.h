@@ -20,9 +20,28 @@ constexpr int kGemmRowTile = 128;
 constexpr int kGemmOpTile = 64;
 constexpr int kGemmKTile = 8;
 
-cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx,
-                            long long n_pad, int kw_pad, uint32_t *Out, int ldo, int out_words, long long N,
-                            cudaStream_t st);
+// Request-operand buffers (X) are padded to a multiple of kGemmOpPad rows.
+constexpr int kGemmOpPad = 256;
+
+// tcgen05 engine tiling: CTA tile kTcM rows x kTcN requests, kTcKB bits of K
+// per pipeline stage (4 MMAs of K = 32), kTcStages stage buffers.
+constexpr int kTcM = 128;
+constexpr int kTcN = 256;
+constexpr int kTcKB = 128;
+constexpr int kTcStages = 3;
+
+// A8: the key matrix pre-expanded to FP8 stage images (GEMM_TC only);
+// err: device word set to 1 when a tensor-core CTA gave up on a bounded wait.
+cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, const uint8_t *A8, int lda, int rows_pad,
+                            const uint32_t *X, int ldx, long long n_pad, int kw_pad, uint32_t *Out, int ldo,
+                            int out_words, long long N, int *err, cudaStream_t st);
+size_t tc_a8_bytes(int rows_pad, int kw_pad);
+cudaError_t launch_expand_a(const uint32_t *A, int lda, int rows_pad, int kw_pad, uint8_t *A8, cudaStream_t st);
+cudaError_t launch_gf2_gemm_tc(const uint8_t *A8, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
+                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, int *err,
+                               cudaStream_t st);
+cudaError_t launch_gf2_gemm_b1(const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
+                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, cudaStream_t st);
 
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, long long N, uint32_t *E, int lde, uint32_t *Ens, int ldx,

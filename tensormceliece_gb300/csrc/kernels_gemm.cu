@@ -90,21 +90,25 @@ __global__ void __launch_bounds__(POPC_THREADS) gf2_gemm_popc(const uint32_t *__
   }
 }
 
-cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx,
-                            long long n_pad, int kw_pad, uint32_t *Out, int ldo, int out_words, long long N,
-                            cudaStream_t st) {
+cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, const uint8_t *A8, int lda, int rows_pad,
+                            const uint32_t *X, int ldx, long long n_pad, int kw_pad, uint32_t *Out, int ldo,
+                            int out_words, long long N, int *err, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
   if (rows_pad % kGemmRowTile || n_pad % kGemmOpTile || kw_pad % kGemmKTile || lda % 4 || ldx % 4 ||
-      n_pad < N)
+      n_pad < N || lda < kw_pad || ldx < kw_pad)
     return cudaErrorInvalidValue;
-  dim3 grid((unsigned)((N + kGemmOpTile - 1) / kGemmOpTile), rows_pad / kGemmRowTile);
   switch (engine) {
+    case GEMM_TC:
+      return launch_gf2_gemm_tc(A8, rows_pad, X, ldx, n_pad, kw_pad, Out, ldo, out_words, N, err, st);
+    case GEMM_B1MMA:
+      return launch_gf2_gemm_b1(A, lda, rows_pad, X, ldx, n_pad, kw_pad, Out, ldo, out_words, N, st);
     case GEMM_POPC:
-    default:
+    default: {
+      dim3 grid((unsigned)((N + kGemmOpTile - 1) / kGemmOpTile), rows_pad / kGemmRowTile);
       gf2_gemm_popc<<<grid, POPC_THREADS, 0, st>>>(A, lda, X, ldx, kw_pad, Out, ldo, out_words, N);
-      break;
+      return cudaGetLastError();
+    }
   }
-  return cudaGetLastError();
 }
 
 }  // namespace gmc

@@ -1,0 +1,383 @@
+// Tensor-core engines for the batched GF(2) products Out[op] = A * X[op].
+//
+// GEMM_TC: 5th-generation tensor cores (tcgen05). 0/1 operands carried as FP8
+// e4m3 (0x00 / 0x38 = 1.0) through tcgen05.mma .kind::f8f6f4 with FP32
+// accumulators in tensor memory. Sums of products are integer counts <= K
+// (at most 6656 here), exact in FP32, so parity = (int)acc & 1. (.kind::i8 is
+// not available on sm_103a.)
+//   A (key matrix, fixed per key) is pre-expanded once into FP8 tiles laid
+//   out exactly as the shared-memory image of one pipeline stage, so a stage
+//   is one cp.async.bulk (TMA engine) completing on an mbarrier.
+//   X (request bits) is expanded to FP8 by the CUDA cores into the same
+//   canonical layout (no-swizzle K-major: 8-row x 16-byte core matrices,
+//   K-adjacent core matrices 128 B apart, row groups 1024 B apart).
+//   One thread issues 4 MMAs (K = 32 each) per 128-bit K stage and commits
+//   them to an mbarrier that releases the stage buffers. The epilogue reads
+//   the accumulators with tcgen05.ld and packs 32 parities per ballot.
+//   Every wait is bounded (about 2 s of globaltimer); on expiry the CTA sets
+//   the error word, stops issuing, waits (bounded) for its own copies and
+//   MMAs, frees its tensor memory and returns.
+//
+// GEMM_B1MMA: the legacy 1-bit path, mma.sync m8n8k128 .b1 AND.POPC (the
+// reference's engine family, mceliece-gpu-params/tc_kernels.cuh:97-123).
+#include "kernels.h"
+
+namespace gmc {
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+// bounded wait on an mbarrier phase; false when the limit expired
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// Shared-memory matrix descriptor (tcgen05): start, leading- and stride-
+// dimension byte offsets (16-byte units), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor, .kind::f8f6f4: D = F32 (bits 4-5 = 1), A = B = E4M3
+// (bits 7-9, 10-12 = 0), both K-major (bits 15, 16 = 0), N >> 3 at bit 17,
+// M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_f8f6f4_e4m3(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+#define GMC_TMEM_LD32(taddr, r)                                                                                 \
+  asm volatile(                                                                                                 \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"  \
+      "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                                        \
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),         \
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),   \
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), \
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])  \
+      : "r"(taddr))
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 4 bits -> 4 FP8 bytes (bit i -> byte i = 0x38 or 0)
+__device__ __forceinline__ uint32_t expand4(uint32_t v) {
+  return ((v * 0x00204081u) & 0x01010101u) * 0x38u;
+}
+
+// ---------------------------------------------------------------- tcgen05 engine
+constexpr int TC_THREADS = 128;
+constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
+constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
+constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 256;
+constexpr uint32_t TC_TMEM_COLS = kTcN;    // FP32 accumulator: 128 lanes x kTcN columns
+
+__global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const uint8_t *__restrict__ A8, int kstages,
+                                                              const uint32_t *__restrict__ X, int ldx,
+                                                              uint32_t *__restrict__ Out, int ldo, int out_words,
+                                                              long long N, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t tsm[];
+  uint8_t *As = tsm;
+  uint8_t *Xs = tsm + kTcStages * TC_A_BYTES;
+  uint64_t *bar_a = reinterpret_cast<uint64_t *>(Xs + kTcStages * TC_X_BYTES);
+  uint64_t *bar_mma = bar_a + kTcStages;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + kTcStages);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long op0 = (long long)blockIdx.x * kTcN;
+  const int mtile = blockIdx.y;
+  if (tid == 0) {
+    for (int i = 0; i < kTcStages; i++) {
+      mbar_init(&bar_a[i], 1);
+      mbar_init(&bar_mma[i], 1);
+    }
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, TC_TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint8_t *Atile = A8 + (size_t)mtile * kstages * TC_A_BYTES;
+  constexpr uint32_t idesc = idesc_f8f6f4_e4m3(kTcM, kTcN);
+
+  int issued = 0;  // stages whose MMAs were committed (thread 0's view)
+  int copies = 0;  // stages whose A copy was issued
+  // each thread expands whole 128-bit stage rows r = tid + 128 j (j < kTcN/128);
+  // the 16-byte loads for stage s+1 are issued before stage s is expanded
+  constexpr int RPT = kTcN / TC_THREADS;
+  uint4 xnext[RPT];
+  const uint32_t *xrow0 = X + (size_t)(op0 + tid) * ldx;
+#pragma unroll
+  for (int j = 0; j < RPT; j++) xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_THREADS * ldx);
+  for (int s = 0; s < kstages; s++) {
+    const int buf = s % kTcStages;
+    const uint32_t use = (uint32_t)(s / kTcStages);
+    bool ok = true;
+    if (s >= kTcStages) ok = mbar_wait(&bar_mma[buf], (use - 1) & 1);  // stage s-kTcStages released the buffers
+    if (!ok) *abort_flag = 1;
+    if (__syncthreads_or(*abort_flag)) break;
+    if (tid == 0) {
+      mbar_expect_tx(&bar_a[buf], TC_A_BYTES);
+      bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &bar_a[buf]);
+      copies = s + 1;
+    }
+    // request bits -> FP8 core matrices (row r, 16-bit chunk kc at
+    // ((r/8)*8 + kc)*128 + (r%8)*16)
+    uint8_t *xb = Xs + buf * TC_X_BYTES;
+    uint4 xcur[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; j++) xcur[j] = xnext[j];
+    if (s + 1 < kstages) {
+#pragma unroll
+      for (int j = 0; j < RPT; j++)
+        xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_THREADS * ldx + 4 * (s + 1));
+    }
+#pragma unroll
+    for (int j = 0; j < RPT; j++) {
+      const int r = tid + j * TC_THREADS;
+      const uint32_t wv[4] = {xcur[j].x, xcur[j].y, xcur[j].z, xcur[j].w};
+      uint8_t *rb = xb + (r >> 3) * 1024 + (r & 7) * 16;
+#pragma unroll
+      for (int kc = 0; kc < 8; kc++) {
+        const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
+        uint4 v;
+        v.x = expand4(bits & 0xFu);
+        v.y = expand4((bits >> 4) & 0xFu);
+        v.z = expand4((bits >> 8) & 0xFu);
+        v.w = expand4((bits >> 12) & 0xFu);
+        *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
+      }
+    }
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      if (!mbar_wait(&bar_a[buf], use & 1)) {
+        *abort_flag = 1;
+      } else {
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(As + buf * TC_A_BYTES), x0 = smem_u32(xb);
+#pragma unroll
+        for (int kk = 0; kk < kTcKB / 32; kk++) {
+          const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
+          const uint64_t bd = smem_desc(x0 + kk * 256, 128, 1024);
+          mma_f8(tmem, ad, bd, idesc, (s > 0 || kk > 0) ? 1u : 0u);
+        }
+        mma_commit(&bar_mma[buf]);
+        issued = s + 1;
+      }
+    }
+  }
+  // drain: the last committed stage completes after all earlier MMAs
+  __shared__ int last_issued, last_copy;
+  if (tid == 0) { last_issued = issued; last_copy = copies; }
+  __syncthreads();
+  bool ok = true;
+  if (last_issued > 0) {
+    const int s = last_issued - 1;
+    ok = mbar_wait(&bar_mma[s % kTcStages], (uint32_t)(s / kTcStages) & 1);
+  }
+  if (tid == 0 && last_copy > last_issued) {  // a copy issued without its MMAs (abort): let it land
+    const int s = last_copy - 1;
+    mbar_wait(&bar_a[s % kTcStages], (uint32_t)(s / kTcStages) & 1);
+  }
+  const int good = __syncthreads_and(ok && !*abort_flag && last_issued == kstages);
+  tc_fence_after();
+  if (good) {
+    // epilogue: warp w owns accumulator lanes (rows) 32w..32w+31
+#pragma unroll 1
+    for (int cb = 0; cb < kTcN / 32; cb++) {
+      uint32_t r[32];
+      GMC_TMEM_LD32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * cb), r);
+      tmem_ld_wait();
+      uint32_t mine = 0;
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const uint32_t par = (uint32_t)__float2int_rz(__uint_as_float(r[j])) & 1u;
+        const uint32_t word = __ballot_sync(0xffffffffu, par);
+        if (lane == j) mine = word;
+      }
+      const long long op = op0 + 32 * cb + lane;
+      const int wd = mtile * (kTcM / 32) + warp;
+      if (op < N && wd < out_words) Out[op * ldo + wd] = mine;
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
+// A (packed bits, rows_pad x lda words) -> FP8 stage images:
+// [m-tile][stage][row group g][16-byte chunk kc][row r&7][16 bytes]
+__global__ void expand_a_kernel(const uint32_t *__restrict__ A, int lda, int rows_pad, int kstages,
+                                uint8_t *__restrict__ A8) {
+  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (row, 16-bit chunk)
+  const long long total = (long long)rows_pad * kstages * 8;
+  if (item >= total) return;
+  const int row = (int)(item / (kstages * 8));
+  const int rest = (int)(item % (kstages * 8));
+  const int s = rest >> 3, kc = rest & 7;
+  const uint32_t w = A[(size_t)row * lda + 4 * s + (kc >> 1)];
+  const uint32_t bits = (kc & 1) ? (w >> 16) : (w & 0xFFFFu);
+  uint4 v;
+  v.x = expand4(bits & 0xFu);
+  v.y = expand4((bits >> 4) & 0xFu);
+  v.z = expand4((bits >> 8) & 0xFu);
+  v.w = expand4((bits >> 12) & 0xFu);
+  const int mt = row / kTcM, rr = row % kTcM;
+  const size_t off = ((size_t)mt * kstages + s) * TC_A_BYTES + ((rr >> 3) * 8 + kc) * 128 + (rr & 7) * 16;
+  *reinterpret_cast<uint4 *>(A8 + off) = v;
+}
+
+size_t tc_a8_bytes(int rows_pad, int kw_pad) { return (size_t)rows_pad * kw_pad * 32; }
+
+cudaError_t launch_expand_a(const uint32_t *A, int lda, int rows_pad, int kw_pad, uint8_t *A8, cudaStream_t st) {
+  if (rows_pad % kTcM || kw_pad % (kTcKB / 32)) return cudaErrorInvalidValue;
+  const int kstages = kw_pad / (kTcKB / 32);
+  const long long total = (long long)rows_pad * kstages * 8;
+  expand_a_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(A, lda, rows_pad, kstages, A8);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gf2_gemm_tc(const uint8_t *A8, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
+                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, int *err,
+                               cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  if (!A8 || !err || rows_pad % kTcM || kw_pad % (kTcKB / 32) || n_pad % kTcN || n_pad < N || ldx < kw_pad)
+    return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(gf2_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+  if (e != cudaSuccess) return e;
+  dim3 grid((unsigned)((N + kTcN - 1) / kTcN), rows_pad / kTcM);
+  gf2_gemm_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(A8, kw_pad / (kTcKB / 32), X, ldx, Out, ldo, out_words, N, err);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- legacy b1 MMA engine
+// Warp tile 32 rows x 32 requests (4 x 4 m8n8k128 MMAs per 128-bit K step),
+// 4 warps per block covering 128 rows. Fragments come straight from global
+// memory (L1/L2): A row (lane/4) bits 32*(lane%4).., B column (lane/4) the same.
+__global__ void __launch_bounds__(128) gf2_gemm_b1(const uint32_t *__restrict__ A, int lda,
+                                                    const uint32_t *__restrict__ X, int ldx, int kw_pad,
+                                                    uint32_t *__restrict__ Out, int ldo, int out_words,
+                                                    long long N) {
+  __shared__ uint32_t words[4][32];  // per warp: output word (32 rows) per request
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.y * 128 + warp * 32;
+  const long long op0 = (long long)blockIdx.x * 32;
+  int acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j][0] = acc[i][j][1] = 0;
+  const int fr = lane >> 2, fk = lane & 3;
+  for (int k = 0; k < kw_pad; k += 4) {
+    uint32_t a[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) a[i] = A[(size_t)(row0 + 8 * i + fr) * lda + k + fk];
+#pragma unroll
+    for (int j = 0; j < 4; j++) b[j] = X[(size_t)(op0 + 8 * j + fr) * ldx + k + fk];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        asm volatile(
+            "mma.sync.aligned.m8n8k128.row.col.s32.b1.b1.s32.and.popc {%0,%1}, {%2}, {%3}, {%0,%1};"
+            : "+r"(acc[i][j][0]), "+r"(acc[i][j][1])
+            : "r"(a[i]), "r"(b[j]));
+  }
+  // D fragment: row (lane/4) + 8i, request 2(lane%4) + e + 8j
+  words[warp][lane] = 0;
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+      for (int e = 0; e < 2; e++)
+        if (acc[i][j][e] & 1) atomicOr(&words[warp][8 * j + 2 * fk + e], 1u << (8 * i + fr));
+  __syncwarp();
+  const long long op = op0 + lane;
+  const int wd = row0 / 32;
+  if (op < N && wd < out_words) Out[op * ldo + wd] = words[warp][lane];
+}
+
+cudaError_t launch_gf2_gemm_b1(const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
+                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  if (rows_pad % 128 || kw_pad % 4 || n_pad < (N + 31) / 32 * 32) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)((N + 31) / 32), rows_pad / 128);
+  gf2_gemm_b1<<<grid, 128, 0, st>>>(A, lda, X, ldx, kw_pad, Out, ldo, out_words, N);
+  return cudaGetLastError();
+}
+
+}  // namespace gmc

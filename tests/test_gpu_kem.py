@@ -214,3 +214,27 @@ def test_full_size_roundtrip(gmc, keys, sid):
     oc, okey, _ = O.enc_batch(sid, pk, seeds[idx], threads=THREADS)
     assert (c[idx] == oc).all() and (k[idx] == okey).all()
     assert len({bytes(x) for x in k[:4096]}) == 4096
+
+
+@pytest.mark.parametrize("engine", ["tc", "b1mma"])
+@pytest.mark.parametrize("sid", range(5), ids=SETS)
+def test_kem_parity_per_gemm_engine(gmc, keys, sid, engine):
+    """Encapsulation and decapsulation byte-exact with the tensor-core and legacy 1-bit GEMM engines."""
+    pk, sk = keys(sid)
+    eng = {"tc": gmc.GEMM_TC, "b1mma": gmc.GEMM_B1MMA}[engine]
+    prev = gmc.get_gemm_engine()
+    gmc.set_gemm_engine(eng)
+    try:
+        n = 300
+        seeds = request_seeds(sid, n, b"engine")
+        c, k, rc = gmc.PublicKey(sid, pk).enc_batch(seeds)
+        oc, okey, _ = O.enc_batch(sid, pk, seeds, threads=THREADS)
+        assert (c == oc).all() and (k == okey).all()
+        cts, _ = flipped_and_random(sid, oc, seed=5)
+        k2, rc2 = gmc.SecretKey(sid, sk).dec_batch(cts)
+        ok2, orc2 = O.dec_batch(sid, sk, cts, threads=THREADS)
+        assert (k2 == ok2).all() and (rc2 == orc2).all()
+        if eng == gmc.GEMM_TC:
+            assert gmc.lib().gmc_tc_status() == 0
+    finally:
+        gmc.set_gemm_engine(prev)
