@@ -133,6 +133,23 @@ int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int rows_pad, c
                      long long n_pad, int kw_pad, unsigned int *out, int ldo, int out_words, long long n,
                      void *stream);
 
+/* ---- batched decapsulation without device allocation --------------------
+ * No counterpart in the reference. For callers that cannot call cudaMalloc:
+ * a process whose device memory belongs to another allocator with a fixed
+ * budget, or a latency-critical path where cudaMalloc/cudaFree would
+ * synchronize the device. Same inputs, outputs and results as
+ * gmc_dec_batch_dev (device pointers, caller stream), but all intermediates
+ * live in a fixed file-scope device array of about 7.6 MiB (plus 330 KB of
+ * field tables) that every GPU loading the library keeps until exit; the
+ * front-end product runs on the CUDA-core engine. At most
+ * GMC_NOALLOC_MAX_REQUESTS ciphertexts per call (larger n: GMC_EINVAL).
+ * The first call on a device does a one-time set-up (symbol lookup and a
+ * synchronous table copy): make it before any stream capture. Calls share the
+ * array: calls that overlap on the GPU race, so order them on one stream. */
+#define GMC_NOALLOC_MAX_REQUESTS 4096
+int gmc_dec_batch_noalloc(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc,
+                          void *stream);
+
 /* Host-only views of the per-key / per-field tables the engine uploads (no
  * GPU needed): support L[n], L_i^(2^d) [n], front-end matrix F (returns its
  * word count; *ldf = its row stride), GF(2^m) exp[2q-1]/log[q] and the

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/gmc.h"
+#include "engine_internal.h"
 #include "host_keys.h"
 #include "kernels.h"
 
@@ -43,24 +44,10 @@ static int cuda_fail(cudaError_t e, const char *where) {
   } while (0)
 
 extern "C" const char *gmc_last_error(void) { return g_last_error.c_str(); }
+void gmc::set_last_error(const char *msg) { g_last_error = msg; }
 
 // ---------------------------------------------------------------- keys
-struct gmc_key {
-  int set = 0;
-  int kind = 0;  // 0 public, 1 secret
-  int device = 0;
-  // public key
-  uint32_t *T = nullptr;
-  int lda = 0, rows_pad = 0, kw_pad = 0, pad_bad = 0;
-  // secret key
-  uint32_t *F = nullptr;
-  int ldf = 0, frows_pad = 0, cw_pad = 0;
-  uint16_t *tabs = nullptr;  // L | LL | LW2 (n each) | invL (2^m)
-  uint8_t *a8 = nullptr;     // FP8 stage images of T (public) or F (secret) for the tensor-core engine
-  std::mutex *a8_mu = nullptr;
-  uint8_t *s = nullptr;
-  DecKeyDev dk{};
-};
+// (struct gmc_key: engine_internal.h)
 
 static int g_engine = GEMM_TC;
 

@@ -1,0 +1,192 @@
+// Batched decapsulation that allocates no device memory.
+//
+// Some callers cannot call cudaMalloc: a host process whose device memory is
+// owned by another allocator with a fixed budget (for example a serving
+// framework that reserved the GPU's memory up front), or a latency-critical
+// path where cudaMalloc/cudaFree would synchronize the device and stall other
+// streams. For them gmc_dec_batch_noalloc runs the same decapsulation kernels
+// as gmc_dec_batch_dev, but every intermediate buffer (ciphertext words, the
+// 2t syndromes, the error locators, the error vectors, the decode flags) is
+// carved from one file-scope device array of fixed size, and the per-set
+// field and FFT tables come from a second one. Nothing here calls cudaMalloc,
+// cudaMallocAsync, cudaFree or an allocating library routine; the front-end
+// GF(2) product uses the CUDA-core engine, which needs no extra buffers.
+//
+// Set-up: the first call on a device (with that device current) looks up the
+// device addresses of the two arrays with cudaGetSymbolAddress and copies the
+// field tables into the second one (cudaMemcpy, synchronous). Make that first
+// call before any stream capture. Later calls do no set-up.
+//
+// All calls share the arrays and the arrays keep the last call's contents.
+// Every intermediate is written in full before it is read, so nothing has to
+// start at zero. Calls whose work overlaps on the GPU (different streams or
+// threads without ordering between them) race on the shared scratch: order
+// them (one stream, or events) or use gmc_dec_batch_dev instead.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/gmc.h"
+#include "engine_internal.h"
+#include "host_keys.h"
+#include "kernels.h"
+
+using namespace gmc;
+
+namespace {
+
+constexpr long long kMaxRequests = GMC_NOALLOC_MAX_REQUESTS;
+
+constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// scratch of one decapsulation batch of n requests for a set
+template <int SET>
+struct DecScratch {
+  using p = P<SET>;
+  static constexpr int ldx = (p::cw + kGemmKTile - 1) / kGemmKTile * kGemmKTile;
+  static constexpr int lds2 = (p::s2w + 3) / 4 * 4;
+  static constexpr int lde = (p::ew + 3) / 4 * 4;
+  static constexpr size_t x_bytes(long long n) {
+    return align256((size_t)((n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad) * ldx * 4);
+  }
+  static constexpr size_t s2_bytes(long long n) { return align256((size_t)n * lds2 * 4); }
+  static constexpr size_t sig_bytes(long long n) { return align256((size_t)n * (2u << p::fft_d)); }
+  static constexpr size_t e_bytes(long long n) { return align256((size_t)n * lde * 4); }
+  static constexpr size_t ok_bytes(long long n) { return align256((size_t)n * 4); }
+  static constexpr size_t total(long long n) {
+    return x_bytes(n) + s2_bytes(n) + sig_bytes(n) + e_bytes(n) + ok_bytes(n);
+  }
+};
+
+constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
+constexpr size_t kScratchBytes =
+    cmax(cmax(cmax(DecScratch<0>::total(kMaxRequests), DecScratch<1>::total(kMaxRequests)),
+              cmax(DecScratch<2>::total(kMaxRequests), DecScratch<3>::total(kMaxRequests))),
+         DecScratch<4>::total(kMaxRequests));
+
+// per-set field/FFT tables: exp (2q-1) | log (q) | alpha (q) | twist (2^(d+1)) | frob_lo (2^d) | frob_hi (2^(m-d))
+constexpr int kFieldSlot = 2 * 8192 + 8192 + 8192 + 256 + 128 + 64 + 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+static __device__ __align__(256) uint16_t g_noalloc_fields[GMC_NSETS][kFieldSlot];
+
+namespace {
+
+struct DeviceSetup {
+  unsigned char *scratch = nullptr;
+  uint16_t *fields = nullptr;
+  FieldDev fd[GMC_NSETS];
+};
+
+std::mutex g_setup_mu;
+std::vector<std::pair<int, DeviceSetup>> g_setups;  // per device (set-up done)
+
+int set_error(int code, const char *msg) {
+  gmc::set_last_error(msg);
+  return code;
+}
+
+// once per device: symbol addresses, field tables copied into the static array
+int device_setup(const DeviceSetup **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: no device");
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  for (auto &e : g_setups)
+    if (e.first == dev) {
+      *out = &e.second;
+      return GMC_OK;
+    }
+  DeviceSetup su;
+  if (cudaGetSymbolAddress((void **)&su.scratch, g_noalloc_scratch) != cudaSuccess ||
+      cudaGetSymbolAddress((void **)&su.fields, g_noalloc_fields) != cudaSuccess)
+    return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: cudaGetSymbolAddress failed");
+  for (int set = 0; set < GMC_NSETS; set++) {
+    const gmc_setinfo &S = set_info(set);
+    const HostField &F = host_field(S.m);
+    FftTables ft = build_fft_tables(S.m, S.fft_d);
+    std::vector<uint16_t> all(kFieldSlot, 0);
+    size_t o = 0;
+    auto put = [&](const std::vector<uint16_t> &v) {
+      size_t at = o;
+      memcpy(all.data() + o, v.data(), v.size() * 2);
+      o += v.size();
+      return at;
+    };
+    const size_t o_exp = put(F.exp), o_log = put(F.log), o_alpha = put(ft.alpha_log), o_twist = put(ft.twist_log),
+                 o_flo = put(ft.frob_lo), o_fhi = put(ft.frob_hi);
+    if (o > (size_t)kFieldSlot) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: field table slot too small");
+    uint16_t *base = su.fields + (size_t)set * kFieldSlot;
+    if (cudaMemcpy(base, all.data(), all.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess)
+      return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: field table copy failed");
+    su.fd[set].gexp = base + o_exp;
+    su.fd[set].glog = base + o_log;
+    su.fd[set].fft_alpha_log = base + o_alpha;
+    su.fd[set].fft_twist_log = base + o_twist;
+    su.fd[set].frob_lo = base + o_flo;
+    su.fd[set].frob_hi = base + o_fhi;
+  }
+  g_setups.push_back({dev, su});
+  *out = &g_setups.back().second;
+  return GMC_OK;
+}
+
+template <int SET>
+cudaError_t run(const DeviceSetup &su, const gmc_key *sk, uint8_t *k, const uint8_t *c, long long n, int *rc,
+                cudaStream_t st) {
+  using D = DecScratch<SET>;
+  unsigned char *q = su.scratch;
+  uint32_t *X = reinterpret_cast<uint32_t *>(q);
+  q += D::x_bytes(n);
+  uint32_t *S2 = reinterpret_cast<uint32_t *>(q);
+  q += D::s2_bytes(n);
+  uint16_t *Sig = reinterpret_cast<uint16_t *>(q);
+  q += D::sig_bytes(n);
+  uint32_t *E = reinterpret_cast<uint32_t *>(q);
+  q += D::e_bytes(n);
+  int *ok = reinterpret_cast<int *>(q);
+  const long long n_pad = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
+  cudaError_t e = launch_pack_ct<SET>(c, n, X, D::ldx, st);
+  if (e == cudaSuccess)
+    e = launch_gf2_gemm(GEMM_POPC, sk->F, nullptr, sk->ldf, sk->frows_pad, X, D::ldx, n_pad, sk->cw_pad, S2, D::lds2,
+                        P<SET>::s2w, n, nullptr, st);
+  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, D::lds2, su.fd[SET], n, Sig, st);
+  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, D::lds2, sk->dk, su.fd[SET], n, E, D::lde, ok, st);
+  if (e == cudaSuccess) e = launch_dec_tail<SET>(E, D::lde, ok, c, sk->dk, k, rc, n, st);
+  return e;
+}
+
+}  // namespace
+
+extern "C" int gmc_dec_batch_noalloc(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n,
+                                     int *rc, void *stream) {
+  if (!sk || sk->kind != 1) return set_error(GMC_EKEY, "gmc_dec_batch_noalloc: needs a secret-key handle");
+  if (n < 0 || (n && (!k || !c))) return set_error(GMC_EINVAL, "gmc_dec_batch_noalloc: bad argument");
+  if (n > kMaxRequests)
+    return set_error(GMC_EINVAL, "gmc_dec_batch_noalloc: more than GMC_NOALLOC_MAX_REQUESTS requests; split the "
+                                 "batch or use gmc_dec_batch_dev");
+  const DeviceSetup *su = nullptr;
+  int r = device_setup(&su);
+  if (r) return r;
+  if (!n) return GMC_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (sk->set) {
+    case 0: e = run<0>(*su, sk, k, c, n, rc, st); break;
+    case 1: e = run<1>(*su, sk, k, c, n, rc, st); break;
+    case 2: e = run<2>(*su, sk, k, c, n, rc, st); break;
+    case 3: e = run<3>(*su, sk, k, c, n, rc, st); break;
+    default: e = run<4>(*su, sk, k, c, n, rc, st); break;
+  }
+  if (e != cudaSuccess) {
+    gmc::set_last_error((std::string("gmc_dec_batch_noalloc: ") + cudaGetErrorString(e)).c_str());
+    return GMC_ECUDA;
+  }
+  return GMC_OK;
+}
