@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--engine", default="tc", choices=["popc", "b1mma", "tc"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-grouped", action="store_true", help="skip the mixed-key grouped-launch measurement")
     return ap.parse_args()
 
 
@@ -208,6 +209,82 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+MIX_SETS = [0, 0, 1, 1, 2, 3, 4, 4]  # 2x348864, 2x460896, 6688128, 6960119, 2x8192128
+
+
+def zipf_counts(total, k, s=1.2, seed=11):
+    w = 1.0 / np.arange(1, k + 1) ** s
+    w = w[np.random.default_rng(seed).permutation(k)]
+    c = np.floor(total * w / w.sum()).astype(int)
+    c[0] += total - c.sum()
+    return c
+
+
+def grouped_mix(gmc, torch, dev, total, steps, warmup):
+    """8 keys over the five sets, Zipf(1.2) request counts summing to `total`, each key's requests
+    split 50/50 enc/dec: one plain batched call per (key, op) vs one grouped CUDA-graph launch."""
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(77)
+    counts = zipf_counts(total, len(MIX_SETS))
+    keys, bufs, groups = [], [], []
+    for i, sid in enumerate(MIX_SETS):
+        z = gmc.set_sizes(sid)
+        pk, sk = gmc.keypair(sid, bytes([i + 1]) * 32)
+        P, S = gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)
+        ne = int(counts[i]) // 2
+        nd = int(counts[i]) - ne
+        seeds = torch.randint(0, 256, (max(ne, 1), 32), dtype=torch.uint8, device=dev, generator=gen)
+        c = torch.empty((max(ne, 1), z["ct_bytes"]), dtype=torch.uint8, device=dev)
+        k = torch.empty((max(ne, 1), 32), dtype=torch.uint8, device=dev)
+        s2 = torch.randint(0, 256, (max(nd, 1), 32), dtype=torch.uint8, device=dev, generator=gen)
+        cts = torch.empty((max(nd, 1), z["ct_bytes"]), dtype=torch.uint8, device=dev)
+        kd = torch.empty((max(nd, 1), 32), dtype=torch.uint8, device=dev)
+        kt = torch.empty((max(nd, 1), 32), dtype=torch.uint8, device=dev)
+        P.enc_batch_dev(cts.data_ptr(), kt.data_ptr(), s2.data_ptr(), nd, 0, st)  # valid ciphertexts
+        keys.append((P, S))
+        bufs.append((seeds, c, k, cts, kd, ne, nd))
+        groups.append((P, ne, seeds.data_ptr(), c.data_ptr(), k.data_ptr(), 0))
+        groups.append((S, nd, cts.data_ptr(), 0, kd.data_ptr(), 0))
+    torch.cuda.synchronize()
+
+    def plain():
+        for (P, S), (seeds, c, k, cts, kd, ne, nd) in zip(keys, bufs):
+            P.enc_batch_dev(c.data_ptr(), k.data_ptr(), seeds.data_ptr(), ne, 0, st)
+            S.dec_batch_dev(kd.data_ptr(), cts.data_ptr(), nd, 0, st)
+
+    plan = gmc.Plan(groups)
+
+    def timed(fn):
+        for _ in range(max(3, warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_plain = timed(plain)
+    k_plain = [b[2].clone() for b in bufs] + [b[4].clone() for b in bufs]
+    ms_group = timed(lambda: plan.launch(st))
+    k_group = [b[2] for b in bufs] + [b[4] for b in bufs]
+    same = all(torch.equal(a, b) for a, b in zip(k_plain, k_group))
+    info = plan.info()
+    plan.close()
+    return {
+        "workload": f"{len(MIX_SETS)} keys over the five sets (2x348864, 2x460896, 6688128, 6960119, 2x8192128), "
+                    f"Zipf(1.2) request counts summing to {total}, 50/50 enc/dec",
+        "counts": [int(x) for x in counts],
+        "plain_ms": ms_plain, "plain_ops_s": total / (ms_plain / 1e3),
+        "grouped_ms": ms_group, "grouped_ops_s": total / (ms_group / 1e3),
+        "speedup": ms_plain / ms_group, "pipelines": info["pipelines"], "outputs_identical": same,
+    }
+
+
 def main():
     args = parse()
     rank, local_rank, world = dist_env()
@@ -328,6 +405,9 @@ def main():
         "clocks": clk,
         "wall_s_timed_loop": wall,
     }
+
+    if rank == 0 and not args.no_grouped:
+        line["grouped"] = grouped_mix(gmc, torch, dev, N, max(5, args.steps // 2), args.warmup)
 
     if rank == 0 and not args.no_e2e:
         # end to end through the host-pointer C ABI (pinned host buffers)

@@ -79,6 +79,31 @@ int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned char *c, l
  * generation is outside the batched enc/dec path). */
 int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32);
 
+/* ---- grouped launches over many keys and parameter sets -------------------
+ * A group is one key's batch: a public key with n seeds (encapsulation) or a
+ * secret key with n ciphertexts (decapsulation), device buffers. A plan
+ * buckets its groups by (parameter set, enc/dec) into pipelines of up to 16
+ * keys, each running the kernels once for all of its keys (uneven counts per
+ * key are fine), and captures all pipelines as parallel branches of one CUDA
+ * graph; gmc_plan_launch replays it with one cudaGraphLaunch. Outputs land in
+ * each group's buffers, identical to per-key gmc_{enc,dec}_batch_dev calls.
+ * The plan owns its scratch; the groups' buffers must stay valid while it is
+ * launched. (Replaces the per-key launch loop of the reference harness,
+ * mceliece-gpu-params/main.cu:228-370.) */
+typedef struct gmc_group {
+  const gmc_key *key;       /* public key: encapsulation; secret key: decapsulation */
+  long long n;              /* requests */
+  const unsigned char *in;  /* enc: n x 32 seeds; dec: n x ct ciphertexts */
+  unsigned char *ct;        /* enc: n x ct ciphertexts out; dec: unused */
+  unsigned char *k;         /* n x 32 session keys out */
+  int *rc;                  /* optional n return codes */
+} gmc_group;
+typedef struct gmc_plan gmc_plan;
+int gmc_plan_create(gmc_plan **plan, const gmc_group *groups, int ngroups);
+int gmc_plan_launch(gmc_plan *plan, void *stream);
+int gmc_plan_info(const gmc_plan *plan, int *pipelines, long long *padded_rows);
+void gmc_plan_free(gmc_plan *plan);
+
 /* ---- libmceliece calling convention (one request per call) --------------
  * Same signatures and results as mceliece_kem_<set>_enc / _dec
  * (mc:crypto_kem/<set>/vec/wrap_keypair.c:4, wrap_enc.c:4, wrap_dec.c:4). keypair

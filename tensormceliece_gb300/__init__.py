@@ -18,7 +18,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = [
-    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
+    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "Plan", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
     "set_gemm_engine", "get_gemm_engine", "set_randombytes", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC",
 ]
 
@@ -72,6 +72,11 @@ def lib():
         for s in SETS:
             getattr(L, f"gmc_kem_{s}_keypair").argtypes = [c_u8p, c_u8p]
             getattr(L, f"gmc_kem_{s}_keypair").restype = None
+        L.gmc_plan_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_int]
+        L.gmc_plan_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.gmc_plan_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]
+        L.gmc_plan_free.argtypes = [ctypes.c_void_p]
+        L.gmc_plan_free.restype = None
         L.gmc_set_randombytes.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gmc_set_randombytes.restype = None
         _lib = L
@@ -184,6 +189,49 @@ class SecretKey(_Key):
     def dec_batch_dev(self, k_ptr, c_ptr, n, rc_ptr=0, stream=0):
         return _check(lib().gmc_dec_batch_dev(self._h, k_ptr, c_ptr, n, rc_ptr or None, stream or None),
                       "gmc_dec_batch_dev")
+
+
+class _Group(ctypes.Structure):
+    _fields_ = [("key", ctypes.c_void_p), ("n", ctypes.c_longlong), ("in_", ctypes.c_void_p),
+                ("ct", ctypes.c_void_p), ("k", ctypes.c_void_p), ("rc", ctypes.c_void_p)]
+
+
+class Plan:
+    """A grouped launch over many keys (and parameter sets): one CUDA graph replay per launch().
+
+    groups: iterable of (key, n, in_ptr, ct_ptr, k_ptr, rc_ptr) with device pointers; key is a PublicKey
+    (encapsulation of n seeds) or SecretKey (decapsulation of n ciphertexts).
+    """
+
+    def __init__(self, groups):
+        arr = (_Group * len(groups))()
+        self._keys = []
+        for i, (key, n, inp, ct, k, rc) in enumerate(groups):
+            self._keys.append(key)
+            arr[i] = _Group(key.handle, n, inp, ct or None, k, rc or None)
+        h = ctypes.c_void_p()
+        _check(lib().gmc_plan_create(ctypes.byref(h), ctypes.cast(arr, ctypes.c_void_p), len(groups)),
+               "gmc_plan_create")
+        self._h = h
+
+    def launch(self, stream=0):
+        _check(lib().gmc_plan_launch(self._h, stream or None), "gmc_plan_launch")
+
+    def info(self):
+        p, r = ctypes.c_int(), ctypes.c_longlong()
+        _check(lib().gmc_plan_info(self._h, ctypes.byref(p), ctypes.byref(r)), "gmc_plan_info")
+        return {"pipelines": p.value, "padded_rows": r.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gmc_plan_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def keypair(set_name, seed32=None):

@@ -206,20 +206,6 @@ static cudaError_t key_a8(const gmc_key *kc, cudaStream_t st, const uint8_t **ou
   return cudaSuccess;
 }
 
-static cudaError_t key_gemm(const gmc_key *k, const uint32_t *X, int ldx, long long n_pad, uint32_t *Out, int ldo,
-                            int out_words, long long n, cudaStream_t st) {
-  const uint32_t *A = k->kind == 0 ? k->T : k->F;
-  const int lda = k->kind == 0 ? k->lda : k->ldf, rows = k->kind == 0 ? k->rows_pad : k->frows_pad;
-  const int kw = k->kind == 0 ? k->kw_pad : k->cw_pad;
-  const uint8_t *a8 = nullptr;
-  int *err = nullptr;
-  if (g_engine == GEMM_TC) {
-    cudaError_t e = key_a8(k, st, &a8);
-    if (e != cudaSuccess) return e;
-    if (!(err = tc_err_word())) return cudaErrorMemoryAllocation;
-  }
-  return launch_gf2_gemm(g_engine, A, a8, lda, rows, X, ldx, n_pad, kw, Out, ldo, out_words, n, err, st);
-}
 
 extern "C" int gmc_set_count(void) { return GMC_NSETS; }
 extern "C" const char *gmc_set_name(int set) { return valid_set(set) ? set_info(set).name : nullptr; }
@@ -336,27 +322,57 @@ struct EncDims {
   int lde, ldx, lds;
   long long n_pad;
 };
-static EncDims enc_dims(const gmc_key *pk, long long n) {
-  const gmc_setinfo &S = set_info(pk->set);
+static EncDims enc_dims(int set, int kw_pad, long long rows) {
+  const gmc_setinfo &S = set_info(set);
   EncDims d;
   d.lde = round_up((S.n + 31) / 32, 4);
-  d.ldx = pk->kw_pad;
+  d.ldx = kw_pad;
   d.lds = round_up((S.mt + 31) / 32, 4);
-  d.n_pad = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
+  d.n_pad = (rows + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
   return d;
+}
+static EncDims enc_dims(const gmc_key *pk, long long n) { return enc_dims(pk->set, pk->kw_pad, n); }
+
+// Key matrices of a segment list (FP8 images built first when the engine needs them).
+static cudaError_t gemm_keys(const gmc_key *const *keys, int nkeys, int engine, cudaStream_t st, GemmKeys *gk,
+                             int **err) {
+  *gk = GemmKeys{};
+  *err = nullptr;
+  for (int i = 0; i < nkeys; i++) {
+    gk->A[i] = keys[i]->kind == 0 ? keys[i]->T : keys[i]->F;
+    if (engine == GEMM_TC) {
+      cudaError_t e = key_a8(keys[i], st, &gk->A8[i]);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  if (engine == GEMM_TC && !(*err = tc_err_word())) return cudaErrorMemoryAllocation;
+  return cudaSuccess;
+}
+
+// encapsulation kernels for the segments of one set: seeds / c / k rows in padded row space
+template <int SET>
+static cudaError_t enc_sample_gemm_seg(const Segs &segs, const gmc_key *ref, const GemmKeys &gk, int engine, int *err,
+                                       const uint8_t *seeds, uint32_t *E, uint32_t *Ens, uint32_t *S,
+                                       const EncDims &d, cudaStream_t st) {
+  using p = P<SET>;
+  prof_mark(nullptr, st);
+  cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, st);
+  if (e != cudaSuccess) return e;
+  prof_mark("enc_sample", st);
+  e = launch_gf2_gemm_seg(engine, gk, segs, ref->lda, ref->rows_pad, Ens, d.ldx, ref->kw_pad, S, d.lds, p::mw, err,
+                          st);
+  prof_mark("enc_syndrome_gemm", st);
+  return e;
 }
 
 template <int SET>
 static cudaError_t enc_sample_gemm(const gmc_key *pk, const uint8_t *seeds, long long n, uint32_t *E, uint32_t *Ens,
                                    uint32_t *S, const EncDims &d, cudaStream_t st) {
-  using p = P<SET>;
-  prof_mark(nullptr, st);
-  cudaError_t e = launch_sample<SET>(seeds, n, E, d.lde, Ens, d.ldx, st);
+  GemmKeys gk;
+  int *err;
+  cudaError_t e = gemm_keys(&pk, 1, g_engine, st, &gk, &err);
   if (e != cudaSuccess) return e;
-  prof_mark("enc_sample", st);
-  e = key_gemm(pk, Ens, d.ldx, d.n_pad, S, d.lds, p::mw, n, st);
-  prof_mark("enc_syndrome_gemm", st);
-  return e;
+  return enc_sample_gemm_seg<SET>(one_segment(n), pk, gk, g_engine, err, seeds, E, Ens, S, d, st);
 }
 
 template <int SET>
@@ -365,11 +381,11 @@ static cudaError_t enc_run(const gmc_key *pk, uint8_t *c, uint8_t *k, const uint
   EncDims d = enc_dims(pk, n);
   uint32_t *E, *Ens, *S;
   cudaError_t e;
-  if ((e = scr.get((void **)&E, (size_t)n * d.lde * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&E, (size_t)d.n_pad * d.lde * 4)) != cudaSuccess) return e;
   if ((e = scr.get((void **)&Ens, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
-  if ((e = scr.get((void **)&S, (size_t)n * d.lds * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&S, (size_t)d.n_pad * d.lds * 4)) != cudaSuccess) return e;
   if ((e = enc_sample_gemm<SET>(pk, seeds, n, E, Ens, S, d, st)) != cudaSuccess) return e;
-  e = launch_finalize<SET>(E, d.lde, S, d.lds, c, k, n, pk->pad_bad, st);
+  e = launch_finalize<SET>(E, d.lde, S, d.lds, c, k, one_segment(n), pk->pad_bad ? 1u : 0u, st);
   prof_mark("enc_finalize_hash", st);
   return e;
 }
@@ -378,35 +394,51 @@ struct DecDims {
   int ldx, lds2, lde;
   long long n_pad;
 };
-static DecDims dec_dims(const gmc_key *sk, long long n) {
-  const gmc_setinfo &S = set_info(sk->set);
+static DecDims dec_dims(int set, int cw_pad, long long rows) {
+  const gmc_setinfo &S = set_info(set);
   DecDims d;
-  d.ldx = sk->cw_pad;
+  d.ldx = cw_pad;
   d.lds2 = round_up((2 * S.t * S.m + 31) / 32, 4);
   d.lde = round_up((S.n + 31) / 32, 4);
-  d.n_pad = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
+  d.n_pad = (rows + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
   return d;
+}
+static DecDims dec_dims(const gmc_key *sk, long long n) { return dec_dims(sk->set, sk->cw_pad, n); }
+
+// decapsulation kernels up to the decode flags for the segments of one set
+template <int SET>
+static cudaError_t dec_front_decode_seg(const Segs &segs, const gmc_key *ref, const GemmKeys &gk, const DecKeys &dk,
+                                        int engine, int *err, const uint8_t *c, uint32_t *X, uint32_t *S2,
+                                        uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
+  using p = P<SET>;
+  FieldDev fd;
+  if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
+  prof_mark(nullptr, st);
+  cudaError_t e = launch_pack_ct<SET>(c, segs, X, d.ldx, st);
+  if (e != cudaSuccess) return e;
+  prof_mark("dec_pack_ct", st);
+  e = launch_gf2_gemm_seg(engine, gk, segs, ref->ldf, ref->frows_pad, X, d.ldx, ref->cw_pad, S2, d.lds2, p::s2w, err,
+                          st);
+  if (e != cudaSuccess) return e;
+  prof_mark("dec_front_gemm", st);
+  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st);
+  if (e != cudaSuccess) return e;
+  prof_mark("dec_bm", st);
+  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st);
+  prof_mark("dec_fft_roots_reenc", st);
+  return e;
 }
 
 template <int SET>
 static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long long n, uint32_t *X, uint32_t *S2,
                                     uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
-  using p = P<SET>;
-  FieldDev fd;
-  if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
-  prof_mark(nullptr, st);
-  cudaError_t e = launch_pack_ct<SET>(c, n, X, d.ldx, st);
+  GemmKeys gk;
+  int *err;
+  cudaError_t e = gemm_keys(&sk, 1, g_engine, st, &gk, &err);
   if (e != cudaSuccess) return e;
-  prof_mark("dec_pack_ct", st);
-  e = key_gemm(sk, X, d.ldx, d.n_pad, S2, d.lds2, p::s2w, n, st);
-  if (e != cudaSuccess) return e;
-  prof_mark("dec_front_gemm", st);
-  e = launch_dec_bm<SET>(S2, d.lds2, fd, n, Sig, st);
-  if (e != cudaSuccess) return e;
-  prof_mark("dec_bm", st);
-  e = launch_dec_root<SET>(Sig, S2, d.lds2, sk->dk, fd, n, E, d.lde, ok, st);
-  prof_mark("dec_fft_roots_reenc", st);
-  return e;
+  DecKeys dk{};
+  dk.k[0] = sk->dk;
+  return dec_front_decode_seg<SET>(one_segment(n), sk, gk, dk, g_engine, err, c, X, S2, Sig, E, ok, d, st);
 }
 
 template <int SET>
@@ -418,12 +450,14 @@ static cudaError_t dec_run(const gmc_key *sk, uint8_t *k, const uint8_t *c, long
   int *ok;
   cudaError_t e;
   if ((e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
-  if ((e = scr.get((void **)&S2, (size_t)n * d.lds2 * 4)) != cudaSuccess) return e;
-  if ((e = scr.get((void **)&Sig, (size_t)n * (2u << P<SET>::fft_d))) != cudaSuccess) return e;
-  if ((e = scr.get((void **)&E, (size_t)n * d.lde * 4)) != cudaSuccess) return e;
-  if ((e = scr.get((void **)&ok, (size_t)n * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&S2, (size_t)d.n_pad * d.lds2 * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&Sig, (size_t)d.n_pad * (2u << P<SET>::fft_d))) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&E, (size_t)d.n_pad * d.lde * 4)) != cudaSuccess) return e;
+  if ((e = scr.get((void **)&ok, (size_t)d.n_pad * 4)) != cudaSuccess) return e;
   if ((e = dec_front_decode<SET>(sk, c, n, X, S2, Sig, E, ok, d, st)) != cudaSuccess) return e;
-  e = launch_dec_tail<SET>(E, d.lde, ok, c, sk->dk, k, rc, n, st);
+  DecKeys dk{};
+  dk.k[0] = sk->dk;
+  e = launch_dec_tail<SET>(E, d.lde, ok, c, dk, k, rc, one_segment(n), st);
   prof_mark("dec_tail_hash", st);
   return e;
 }
@@ -567,7 +601,7 @@ extern "C" int gmc_dec_stages_dev(const gmc_key *sk, const unsigned char *c, lon
     uint32_t *X;
     uint16_t *Sig = nullptr;
     e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4);
-    if (e == cudaSuccess) e = scr.get((void **)&Sig, (size_t)n * 256);
+    if (e == cudaSuccess) e = scr.get((void **)&Sig, (size_t)d.n_pad * 256);
     if (e == cudaSuccess) GMC_DISPATCH(sk->set, e = dec_front_decode<S_>(sk, c, n, X, synd, Sig, ev, ok, d, st));
   }
   if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_stages_dev");
@@ -730,5 +764,224 @@ extern "C" int gmc_host_field_tables(int set, unsigned short *gexp, unsigned sho
   if (glog) memcpy(glog, F.log.data(), F.log.size() * 2);
   if (alpha_log) memcpy(alpha_log, ft.alpha_log.data(), ft.alpha_log.size() * 2);
   if (twist_log) memcpy(twist_log, ft.twist_log.data(), ft.twist_log.size() * 2);
+  return GMC_OK;
+}
+
+// ---------------------------------------------------------------- grouped plans
+// A plan is a fixed set of request groups (key, op, n, device buffers). Groups
+// are bucketed by (parameter set, enc/dec) into pipelines of at most kMaxSegs
+// keys; each pipeline gathers its groups' inputs into one padded buffer
+// (segment starts at multiples of kGemmOpPad), runs the segment-aware kernels
+// once for all its keys, and scatters the outputs back. All pipelines are
+// captured as parallel branches of one CUDA graph; gmc_plan_launch replays it
+// with a single cudaGraphLaunch.
+struct PlanPipe {
+  int set = 0, kind = 0;  // kind 0 enc, 1 dec
+  std::vector<int> groups;
+  Segs segs{};
+  uint32_t pk_bad_mask = 0;
+  uint8_t *in = nullptr, *ct = nullptr, *k = nullptr;
+  int *rc = nullptr;
+  uint32_t *w0 = nullptr, *w1 = nullptr, *w2 = nullptr, *w3 = nullptr;  // intermediates
+  uint16_t *sig = nullptr;
+  int *ok = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
+struct gmc_plan {
+  int device = 0;
+  int engine = GEMM_TC;
+  std::vector<gmc_group> groups;
+  std::vector<PlanPipe> pipes;
+  std::vector<void *> allocs;
+  cudaStream_t cap = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+static void plan_release(gmc_plan *p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  for (auto &pp : p->pipes) {
+    if (pp.st) cudaStreamDestroy(pp.st);
+    if (pp.done) cudaEventDestroy(pp.done);
+  }
+  if (p->fork) cudaEventDestroy(p->fork);
+  if (p->cap) cudaStreamDestroy(p->cap);
+  for (void *a : p->allocs) cudaFree(a);
+  delete p;
+}
+
+extern "C" void gmc_plan_free(gmc_plan *plan) { plan_release(plan); }
+
+template <int SET>
+static cudaError_t plan_pipe_kernels(gmc_plan *p, PlanPipe &pp) {
+  const gmc_key *keys[kMaxSegs];
+  for (size_t i = 0; i < pp.groups.size(); i++) keys[i] = p->groups[pp.groups[i]].key;
+  const gmc_key *ref = keys[0];
+  GemmKeys gk;
+  int *err;
+  cudaError_t e = gemm_keys(keys, (int)pp.groups.size(), p->engine, pp.st, &gk, &err);
+  if (e != cudaSuccess) return e;
+  const long long rows = seg_rows(pp.segs);
+  if (pp.kind == 0) {
+    EncDims d = enc_dims(SET, ref->kw_pad, rows);
+    e = enc_sample_gemm_seg<SET>(pp.segs, ref, gk, p->engine, err, pp.in, pp.w0, pp.w1, pp.w2, d, pp.st);
+    if (e == cudaSuccess)
+      e = launch_finalize<SET>(pp.w0, d.lde, pp.w2, d.lds, pp.ct, pp.k, pp.segs, pp.pk_bad_mask, pp.st);
+  } else {
+    DecDims d = dec_dims(SET, ref->cw_pad, rows);
+    DecKeys dk{};
+    for (size_t i = 0; i < pp.groups.size(); i++) dk.k[i] = keys[i]->dk;
+    e = dec_front_decode_seg<SET>(pp.segs, ref, gk, dk, p->engine, err, pp.in, pp.w0, pp.w1, pp.sig, pp.w2, pp.ok, d,
+                                  pp.st);
+    if (e == cudaSuccess) e = launch_dec_tail<SET>(pp.w2, d.lde, pp.ok, pp.in, dk, pp.k, pp.rc, pp.segs, pp.st);
+  }
+  return e;
+}
+
+static cudaError_t plan_alloc(gmc_plan *p, void **ptr, size_t bytes) {
+  cudaError_t e = cudaMalloc(ptr, bytes ? bytes : 16);
+  if (e == cudaSuccess) p->allocs.push_back(*ptr);
+  return e;
+}
+
+extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngroups) {
+  if (!out || !groups || ngroups <= 0) return fail(GMC_EINVAL, "gmc_plan_create: bad argument");
+  *out = nullptr;
+  for (int i = 0; i < ngroups; i++) {
+    const gmc_group &g = groups[i];
+    if (!g.key || g.n < 0 || (g.n && (!g.in || !g.k || (g.key->kind == 0 && !g.ct))))
+      return fail(GMC_EINVAL, "gmc_plan_create: bad group");
+  }
+  gmc_plan *p = new gmc_plan();
+  cudaGetDevice(&p->device);
+  p->engine = g_engine;
+  p->groups.assign(groups, groups + ngroups);
+  // bucket by (set, kind), at most kMaxSegs groups per pipeline
+  for (int i = 0; i < ngroups; i++) {
+    const gmc_group &g = groups[i];
+    if (!g.n) continue;
+    PlanPipe *dst = nullptr;
+    for (auto &pp : p->pipes)
+      if (pp.set == g.key->set && pp.kind == g.key->kind && pp.groups.size() < (size_t)kMaxSegs) dst = &pp;
+    if (!dst) {
+      p->pipes.emplace_back();
+      dst = &p->pipes.back();
+      dst->set = g.key->set;
+      dst->kind = g.key->kind;
+    }
+    dst->groups.push_back(i);
+  }
+  cudaError_t e = cudaSuccess;
+  for (auto &pp : p->pipes) {
+    const gmc_setinfo &S = set_info(pp.set);
+    pp.segs = Segs{};
+    pp.segs.nseg = (int)pp.groups.size();
+    long long row = 0;
+    for (size_t j = 0; j < pp.groups.size(); j++) {
+      const gmc_group &g = p->groups[pp.groups[j]];
+      pp.segs.row0[j] = row;
+      pp.segs.nreq[j] = g.n;
+      row += (g.n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
+      if (pp.kind == 0 && g.key->pad_bad) pp.pk_bad_mask |= 1u << j;
+    }
+    pp.segs.row0[pp.groups.size()] = row;
+    const gmc_key *ref = p->groups[pp.groups[0]].key;
+    const size_t in_b = pp.kind == 0 ? 32 : (size_t)S.synd_bytes;
+    if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.in, row * in_b);
+    if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.k, row * 32);
+    if (pp.kind == 0) {
+      EncDims d = enc_dims(pp.set, ref->kw_pad, row);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.ct, row * S.synd_bytes);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w0, row * d.lde * 4);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w1, row * d.ldx * 4);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w2, row * d.lds * 4);
+    } else {
+      DecDims d = dec_dims(pp.set, ref->cw_pad, row);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.rc, row * 4);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w0, row * d.ldx * 4);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w1, row * d.lds2 * 4);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.sig, row * (2u << S.fft_d));
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w2, row * d.lde * 4);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.ok, row * 4);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pp.st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pp.done, cudaEventDisableTiming);
+    // per-set tables and FP8 key images exist before capture
+    FieldDev fd;
+    if (e == cudaSuccess && pp.kind == 1 && get_field(pp.set, &fd) != GMC_OK) e = cudaErrorUnknown;
+    if (e == cudaSuccess && p->engine == GEMM_TC)
+      for (int gi : pp.groups) {
+        const uint8_t *a8;
+        if ((e = key_a8(p->groups[gi].key, pp.st, &a8)) != cudaSuccess) break;
+      }
+    if (e == cudaSuccess && p->engine == GEMM_TC && !tc_err_word()) e = cudaErrorMemoryAllocation;
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    plan_release(p);
+    return cuda_fail(e, "gmc_plan_create: setup");
+  }
+  // capture: fork to one stream per pipeline, gather, kernels, scatter, join
+  e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) e = cudaEventRecord(p->fork, p->cap);
+  for (auto &pp : p->pipes) {
+    if (e != cudaSuccess) break;
+    const gmc_setinfo &S = set_info(pp.set);
+    const size_t in_b = pp.kind == 0 ? 32 : (size_t)S.synd_bytes;
+    e = cudaStreamWaitEvent(pp.st, p->fork, 0);
+    for (size_t j = 0; j < pp.groups.size() && e == cudaSuccess; j++) {
+      const gmc_group &g = p->groups[pp.groups[j]];
+      e = cudaMemcpyAsync(pp.in + pp.segs.row0[j] * in_b, g.in, g.n * in_b, cudaMemcpyDeviceToDevice, pp.st);
+    }
+    if (e == cudaSuccess) GMC_DISPATCH(pp.set, e = plan_pipe_kernels<S_>(p, pp));
+    for (size_t j = 0; j < pp.groups.size() && e == cudaSuccess; j++) {
+      const gmc_group &g = p->groups[pp.groups[j]];
+      const long long r0 = pp.segs.row0[j];
+      e = cudaMemcpyAsync(g.k, pp.k + r0 * 32, g.n * 32, cudaMemcpyDeviceToDevice, pp.st);
+      if (e == cudaSuccess && pp.kind == 0)
+        e = cudaMemcpyAsync(g.ct, pp.ct + r0 * S.synd_bytes, g.n * S.synd_bytes, cudaMemcpyDeviceToDevice, pp.st);
+      if (e == cudaSuccess && g.rc) {
+        if (pp.kind == 0)
+          e = cudaMemsetAsync(g.rc, g.key->pad_bad ? 0xFF : 0, g.n * 4, pp.st);  // -1 or 0
+        else
+          e = cudaMemcpyAsync(g.rc, pp.rc + r0, g.n * 4, cudaMemcpyDeviceToDevice, pp.st);
+      }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(pp.done, pp.st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(p->cap, pp.done, 0);
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(p->cap, &graph);
+  if (e == cudaSuccess) e = e2;
+  p->graph = graph;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  if (e != cudaSuccess) {
+    plan_release(p);
+    return cuda_fail(e, "gmc_plan_create: capture");
+  }
+  *out = p;
+  return GMC_OK;
+}
+
+extern "C" int gmc_plan_launch(gmc_plan *plan, void *stream) {
+  if (!plan || !plan->exec) return fail(GMC_EINVAL, "gmc_plan_launch: bad plan");
+  GMC_CUDA(cudaGraphLaunch(plan->exec, (cudaStream_t)stream));
+  return GMC_OK;
+}
+
+extern "C" int gmc_plan_info(const gmc_plan *plan, int *pipelines, long long *padded_rows) {
+  if (!plan) return fail(GMC_EINVAL, "gmc_plan_info: bad plan");
+  if (pipelines) *pipelines = (int)plan->pipes.size();
+  if (padded_rows) {
+    long long r = 0;
+    for (auto &pp : plan->pipes) r += seg_rows(pp.segs);
+    *padded_rows = r;
+  }
   return GMC_OK;
 }

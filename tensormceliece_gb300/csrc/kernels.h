@@ -11,6 +11,36 @@ constexpr int kTailThreads = 128;
 constexpr int kBMWarps = 16;    // Berlekamp-Massey kernel: warps per block
 constexpr int kRootWarps = 16;  // root-finding kernel: warps per block
 
+// ---------------------------------------------------------------- segments
+// A launch covers up to kMaxSegs segments (one key each) laid out back to back
+// in "padded row" space: segment s owns rows [row0[s], row0[s+1]), its live
+// requests are the first nreq[s] of them, row0[] are multiples of kGemmOpPad
+// (so no GEMM tile straddles two keys). Rows past a segment's live count are
+// never read from or written to caller buffers. A single-key batch of n
+// requests is the one-segment case {row0 = {0, round_up(n, kGemmOpPad)}}.
+constexpr int kMaxSegs = 16;
+struct Segs {
+  int nseg;
+  long long row0[kMaxSegs + 1];
+  long long nreq[kMaxSegs];
+};
+#ifdef __CUDACC__
+__host__ __device__ inline long long seg_rows(const Segs &S) { return S.row0[S.nseg]; }
+__device__ inline int seg_find(const Segs &S, long long row) {
+  int s = 0;
+#pragma unroll 1
+  for (int i = 1; i < S.nseg; i++)
+    if (row >= S.row0[i]) s = i;
+  return s;
+}
+// segment of a row and whether it is a live request
+__device__ inline bool seg_live(const Segs &S, long long row, int *seg) {
+  const int s = seg_find(S, row);
+  *seg = s;
+  return row < S.row0[S.nseg] && row - S.row0[s] < S.nreq[s];
+}
+#endif
+
 // GF(2) GEMM engines for Out[op] = parity(A[row] & X[op]) over KW words.
 enum GemmEngine { GEMM_POPC = 0, GEMM_B1MMA = 1, GEMM_TC = 2 };
 
@@ -30,25 +60,38 @@ constexpr int kTcN = 256;
 constexpr int kTcKB = 128;
 constexpr int kTcStages = 3;
 
-// A8: the key matrix pre-expanded to FP8 stage images (GEMM_TC only);
-// err: device word set to 1 when a tensor-core CTA gave up on a bounded wait.
+// Key matrices of the segments of a GEMM launch (same shape for all: one set).
+// A8: the key matrix pre-expanded to FP8 stage images (GEMM_TC only).
+struct GemmKeys {
+  const uint32_t *A[kMaxSegs];
+  const uint8_t *A8[kMaxSegs];
+};
+// Out rows follow X rows (padded row space). err: device word set to 1 when a
+// tensor-core CTA gave up on a bounded wait.
+cudaError_t launch_gf2_gemm_seg(int engine, const GemmKeys &keys, const Segs &segs, int lda, int rows_pad,
+                                const uint32_t *X, int ldx, int kw_pad, uint32_t *Out, int ldo, int out_words,
+                                int *err, cudaStream_t st);
+// single-key form: X has n_pad rows (multiple of kGemmOpPad), N live requests
 cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, const uint8_t *A8, int lda, int rows_pad,
                             const uint32_t *X, int ldx, long long n_pad, int kw_pad, uint32_t *Out, int ldo,
                             int out_words, long long N, int *err, cudaStream_t st);
 size_t tc_a8_bytes(int rows_pad, int kw_pad);
 cudaError_t launch_expand_a(const uint32_t *A, int lda, int rows_pad, int kw_pad, uint8_t *A8, cudaStream_t st);
-cudaError_t launch_gf2_gemm_tc(const uint8_t *A8, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
-                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, int *err,
-                               cudaStream_t st);
-cudaError_t launch_gf2_gemm_b1(const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
-                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, cudaStream_t st);
+cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_pad, const uint32_t *X, int ldx,
+                               int kw_pad, uint32_t *Out, int ldo, int out_words, int *err, cudaStream_t st);
+cudaError_t launch_gf2_gemm_b1(const GemmKeys &keys, const Segs &segs, int lda, int rows_pad, const uint32_t *X,
+                               int ldx, int kw_pad, uint32_t *Out, int ldo, int out_words, cudaStream_t st);
+Segs one_segment(long long n);
 
+// Encapsulation: seeds / C / K rows in padded row space; E, Ens, S have
+// seg_rows(segs) rows. pk_bad_mask bit s: segment s's public key has
+// nonzero padding bits (6960119), its c and K are zeroed.
 template <int SET>
-cudaError_t launch_sample(const uint8_t *seeds, long long N, uint32_t *E, int lde, uint32_t *Ens, int ldx,
+cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           cudaStream_t st);
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
-                            long long N, int pk_bad, cudaStream_t st);
+                            const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st);
 
 // Per-key decapsulation state on the device (built once per secret key).
 struct DecKeyDev {
@@ -69,19 +112,27 @@ struct FieldDev {
   const uint16_t *frob_hi;  // (c 2^d)^(2^d) for c < 2^(m-d)
 };
 
+// Per-key decapsulation tables of the segments of a launch.
+struct DecKeys {
+  DecKeyDev k[kMaxSegs];
+};
+
+// Decapsulation: C / K / rc rows in padded row space; X, S2, Sig, E, ok have
+// seg_rows(segs) rows.
 template <int SET>
-cudaError_t launch_pack_ct(const uint8_t *C, long long N, uint32_t *X, int ldx, cudaStream_t st);
+cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int ldx, cudaStream_t st);
 // Berlekamp-Massey: S2 (2t packed syndromes) -> Sig [N][2^fft_d] u16, the
 // error locator's coefficients by degree (the leading x^t term is implicit
 // when t = 2^fft_d).
 template <int SET>
-cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, long long N, uint16_t *Sig, cudaStream_t st);
+cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
+                          cudaStream_t st);
 // Root finding + weight + re-encryption check: Sig -> E (error vectors), ok.
 template <int SET>
-cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd,
-                            long long N, uint32_t *E, int lde, int *ok, cudaStream_t st);
+cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
+                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st);
 template <int SET>
-cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, DecKeyDev key,
-                            uint8_t *K, int *rc, long long N, cudaStream_t st);
+cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, const DecKeys &keys,
+                            uint8_t *K, int *rc, const Segs &segs, cudaStream_t st);
 
 }  // namespace gmc

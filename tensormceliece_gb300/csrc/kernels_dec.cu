@@ -29,18 +29,21 @@ __device__ __forceinline__ uint32_t warp_xor(uint32_t v) {
 
 // ---------------------------------------------------------------- pack_ct
 template <int SET>
-__global__ void pack_ct_kernel(const uint8_t *__restrict__ C, long long N, uint32_t *__restrict__ X, int ldx) {
+__global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, uint32_t *__restrict__ X, int ldx) {
   using p = P<SET>;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long op = idx / ldx;
   const int w = (int)(idx % ldx);
-  if (op >= N) return;
-  const uint8_t *c = C + op * p::synd_bytes;
-  uint32_t v = 0;
+  if (op >= seg_rows(segs)) return;
+  int seg;
+  uint32_t v = 0;  // rows past a segment's live requests stay zero
+  if (seg_live(segs, op, &seg)) {
+    const uint8_t *c = C + op * p::synd_bytes;
 #pragma unroll
-  for (int b = 0; b < 4; b++) {
-    int x = 4 * w + b;
-    if (x < p::synd_bytes) v |= (uint32_t)c[x] << (8 * b);
+    for (int b = 0; b < 4; b++) {
+      int x = 4 * w + b;
+      if (x < p::synd_bytes) v |= (uint32_t)c[x] << (8 * b);
+    }
   }
   X[op * ldx + w] = v;
 }
@@ -64,12 +67,13 @@ struct BMLayout {
 };
 
 template <int SET>
-__global__ void __launch_bounds__(kBMWarps * 32) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
-                                                               FieldDev fd, long long N,
-                                                               uint16_t *__restrict__ Sig) {
+__global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
+                                                                  FieldDev fd, const Segs segs,
+                                                                  uint16_t *__restrict__ Sig) {
   using p = P<SET>;
   using LY = BMLayout<SET>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
+  constexpr int ZL = GFLog<M>::zero_log;
   constexpr int NS = (T + 1 + 31) / 32;
   constexpr int NSY = (2 * T + 31) / 32;
   constexpr int SIG = 1 << D;
@@ -81,8 +85,11 @@ __global__ void __launch_bounds__(kBMWarps * 32) dec_bm_kernel(const uint32_t *_
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint16_t *slog = bsm + LY::shared_u16 + warp * LY::warp_u16;
+  const long long N = seg_rows(segs);
   const long long nwarps = (long long)gridDim.x * kBMWarps;
   for (long long op = (long long)blockIdx.x * kBMWarps + warp; op < N; op += nwarps) {
+    int seg;
+    if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
     const uint32_t *srow = S2 + op * lds2;
 #pragma unroll
     for (int k = 0; k < NSY; k++) {
@@ -95,12 +102,15 @@ __global__ void __launch_bounds__(kBMWarps * 32) dec_bm_kernel(const uint32_t *_
       }
     }
     __syncwarp();
-    uint16_t C[NS], B[NS];
+    // C in normal form plus its log (the discrepancy multiplies by s via
+    // logs); B only through its log (the update multiplies it by d/b).
+    uint16_t C[NS], lC[NS], lB[NS];
 #pragma unroll
     for (int k = 0; k < NS; k++) {
       const int i = lane + 32 * k;
       C[k] = (i == 0);
-      B[k] = (i == 1);
+      lC[k] = (i == 0) ? 0 : ZL;
+      lB[k] = (i == 1) ? 0 : ZL;
     }
     int L = 0;
     uint32_t lb = 0;  // log b, b = 1
@@ -114,35 +124,38 @@ __global__ void __launch_bounds__(kBMWarps * 32) dec_bm_kernel(const uint32_t *_
       for (int k = 0; k < NS; k++) {
         if (32 * k <= bd) {
           const int i = lane + 32 * k;
-          if (i <= bd) dp ^= gf_mul_log<M>(gexp, glog[C[k]], slog[n - i]);
+          if (i <= bd) dp ^= gf_mul_log<M>(gexp, lC[k], slog[n - i]);
         }
       }
       const uint32_t d = warp_xor(dp);
       if (d) {
         const bool upd = (n >= 2 * L);
-        int lf = (int)glog[d] - (int)lb;
+        const int ld = glog[d];
+        int lf = ld - (int)lb;
         if (lf < 0) lf += Q - 1;
 #pragma unroll
         for (int k = 0; k < NS; k++) {
           if (32 * k <= bu) {
-            const uint16_t c = C[k];
-            C[k] = c ^ gf_mul_log<M>(gexp, lf, glog[B[k]]);
-            if (upd) B[k] = c;
+            const uint16_t lc_old = lC[k];
+            C[k] ^= gf_mul_log<M>(gexp, lf, lB[k]);
+            lC[k] = glog[C[k]];
+            if (upd) lB[k] = lc_old;
           }
         }
         if (upd) {
           L = n + 1 - L;
-          lb = glog[d];
+          lb = ld;
         }
       }
-      // B <- x * B (coefficient i takes i-1); slots above the bound stay zero.
-      // Descending slot order: slot k reads slot k-1 before that one shifts.
+      // B <- x * B (coefficient i takes i-1; log of the new B_0 = 0 is the
+      // zero sentinel); slots above the bound stay zero. Descending slot
+      // order: slot k reads slot k-1 before that one shifts.
 #pragma unroll
       for (int k = NS - 1; k >= 0; k--) {
         if (32 * k <= bu + 1) {
-          const uint16_t up = (uint16_t)__shfl_up_sync(0xffffffffu, B[k], 1);
-          const uint16_t wrap = (uint16_t)__shfl_sync(0xffffffffu, k ? B[k ? k - 1 : 0] : 0, 31);
-          B[k] = lane ? up : (k ? wrap : 0);
+          const uint16_t up = (uint16_t)__shfl_up_sync(0xffffffffu, lB[k], 1);
+          const uint16_t wrap = (uint16_t)__shfl_sync(0xffffffffu, k ? lB[k ? k - 1 : 0] : ZL, 31);
+          lB[k] = lane ? up : (k ? wrap : (uint16_t)ZL);
         }
       }
     }
@@ -194,7 +207,7 @@ struct RootLayout {
 template <int SET>
 __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_t *__restrict__ Sig,
                                                                    const uint32_t *__restrict__ S2, int lds2,
-                                                                   DecKeyDev key, FieldDev fd, long long N,
+                                                                   const DecKeys keys, FieldDev fd, const Segs segs,
                                                                    uint32_t *__restrict__ E, int lde,
                                                                    int *__restrict__ okout) {
   using p = P<SET>;
@@ -226,8 +239,12 @@ __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_
   uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::v_off);
   uint16_t *ssm = reinterpret_cast<uint16_t *>(wbase + LY::s_off);
 
+  const long long N = seg_rows(segs);
   const long long nwarps = (long long)gridDim.x * kRootWarps;
   for (long long op = (long long)blockIdx.x * kRootWarps + warp; op < N; op += nwarps) {
+    int seg;
+    if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
+    const DecKeyDev &key = keys.k[seg];
     const uint16_t *sig = Sig + op * SIG;
     for (int x = lane; x < SIG; x += 32) V[x] = sig[x];
     for (int w = lane; w < NW; w += 32) esm[w] = 0;
@@ -370,12 +387,14 @@ __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_
 template <int SET>
 __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *__restrict__ E, int lde,
                                                                 const int *__restrict__ okin,
-                                                                const uint8_t *__restrict__ Cin, DecKeyDev key,
+                                                                const uint8_t *__restrict__ Cin, const DecKeys keys,
                                                                 uint8_t *__restrict__ K, int *__restrict__ rc,
-                                                                long long N) {
+                                                                const Segs segs) {
   using p = P<SET>;
   const long long op = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (op >= N) return;
+  int seg;
+  if (!seg_live(segs, op, &seg)) return;
+  const DecKeyDev &key = keys.k[seg];
   const bool ok = okin[op] != 0;
   const uint32_t *e = E + op * lde;
   const uint8_t *c = Cin + op * p::synd_bytes;
@@ -409,10 +428,11 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
 
 // ---------------------------------------------------------------- launchers
 template <int SET>
-cudaError_t launch_pack_ct(const uint8_t *C, long long N, uint32_t *X, int ldx, cudaStream_t st) {
+cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int ldx, cudaStream_t st) {
+  const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   const long long total = N * ldx;
-  pack_ct_kernel<SET><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, N, X, ldx);
+  pack_ct_kernel<SET><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, segs, X, ldx);
   return cudaGetLastError();
 }
 
@@ -429,44 +449,49 @@ static int persistent_blocks(K kernel, int threads, int smem, long long work_ite
 }
 
 template <int SET>
-cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, long long N, uint16_t *Sig, cudaStream_t st) {
+cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
+                          cudaStream_t st) {
+  const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   const int smem_bm = BMLayout<SET>::bytes(kBMWarps);
   cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bm);
   if (err != cudaSuccess) return err;
   const int gb = persistent_blocks(dec_bm_kernel<SET>, kBMWarps * 32, smem_bm, N, kBMWarps);
-  dec_bm_kernel<SET><<<gb, kBMWarps * 32, smem_bm, st>>>(S2, lds2, fd, N, Sig);
+  dec_bm_kernel<SET><<<gb, kBMWarps * 32, smem_bm, st>>>(S2, lds2, fd, segs, Sig);
   return cudaGetLastError();
 }
 
 template <int SET>
-cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, DecKeyDev key, FieldDev fd,
-                            long long N, uint32_t *E, int lde, int *ok, cudaStream_t st) {
+cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
+                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st) {
+  const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   const int smem_rt = RootLayout<SET>::bytes(kRootWarps);
   cudaError_t err = cudaFuncSetAttribute(dec_root_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_rt);
   if (err != cudaSuccess) return err;
   const int gr = persistent_blocks(dec_root_kernel<SET>, kRootWarps * 32, smem_rt, N, kRootWarps);
-  dec_root_kernel<SET><<<gr, kRootWarps * 32, smem_rt, st>>>(Sig, S2, lds2, key, fd, N, E, lde, ok);
+  dec_root_kernel<SET><<<gr, kRootWarps * 32, smem_rt, st>>>(Sig, S2, lds2, keys, fd, segs, E, lde, ok);
   return cudaGetLastError();
 }
 
 template <int SET>
-cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, DecKeyDev key,
-                            uint8_t *K, int *rc, long long N, cudaStream_t st) {
+cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, const DecKeys &keys,
+                            uint8_t *K, int *rc, const Segs &segs, cudaStream_t st) {
+  const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   dec_tail_kernel<SET><<<(unsigned)((N + kTailThreads - 1) / kTailThreads), kTailThreads, 0, st>>>(
-      E, lde, ok, C, key, K, rc, N);
+      E, lde, ok, C, keys, K, rc, segs);
   return cudaGetLastError();
 }
 
 #define GMC_INST_DEC(SET)                                                                                       \
-  template cudaError_t launch_pack_ct<SET>(const uint8_t *, long long, uint32_t *, int, cudaStream_t);          \
-  template cudaError_t launch_dec_bm<SET>(const uint32_t *, int, FieldDev, long long, uint16_t *, cudaStream_t); \
-  template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, DecKeyDev, FieldDev,        \
-                                            long long, uint32_t *, int, int *, cudaStream_t);                    \
-  template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, DecKeyDev,    \
-                                            uint8_t *, int *, long long, cudaStream_t);
+  template cudaError_t launch_pack_ct<SET>(const uint8_t *, const Segs &, uint32_t *, int, cudaStream_t);       \
+  template cudaError_t launch_dec_bm<SET>(const uint32_t *, int, FieldDev, const Segs &, uint16_t *,             \
+                                         cudaStream_t);                                                          \
+  template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, const DecKeys &, FieldDev,  \
+                                            const Segs &, uint32_t *, int, int *, cudaStream_t);                 \
+  template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, const DecKeys &, \
+                                            uint8_t *, int *, const Segs &, cudaStream_t);
 GMC_INST_DEC(0)
 GMC_INST_DEC(1)
 GMC_INST_DEC(2)

@@ -19,19 +19,22 @@ namespace gmc {
 // sort-and-compare: only the set of positions matters). The bitmap is the
 // error vector e itself and is written out with the block's coalesced store.
 template <int SET>
-__global__ void __launch_bounds__(kSampleThreads) sample_kernel(const uint8_t *__restrict__ seeds, long long N,
+__global__ void __launch_bounds__(kSampleThreads) sample_kernel(const uint8_t *__restrict__ seeds, const Segs segs,
                                                                 uint32_t *__restrict__ E, int lde,
                                                                 uint32_t *__restrict__ Ens, int ldx) {
   using p = P<SET>;
   constexpr int EWS = p::ew | 1;  // odd stride: bitmaps of neighbouring threads start in different banks
   extern __shared__ uint32_t sm[];
   uint32_t *bm = sm + threadIdx.x * EWS;
+  const long long N = seg_rows(segs);
   const long long op0 = (long long)blockIdx.x * blockDim.x;
   const long long op = op0 + threadIdx.x;
+  int seg;
+  const bool live = seg_live(segs, op, &seg);
 
   for (int w = 0; w < p::ew; w++) bm[w] = 0;
 
-  if (op < N) {
+  if (live) {
     uint64_t st[4];
     const uint8_t *sd = seeds + 32 * op;
 #pragma unroll
@@ -85,18 +88,21 @@ __global__ void __launch_bounds__(kSampleThreads) sample_kernel(const uint8_t *_
       st[0] = nst[0]; st[1] = nst[1]; st[2] = nst[2]; st[3] = nst[3];
     }
   }
+  __shared__ unsigned char live_rows[kSampleThreads];
+  live_rows[threadIdx.x] = live;
   __syncthreads();
   // coalesced copy-out of the block's error vectors, and of e[mt:n] shifted
-  // to bit 0 (the GEMM operand)
+  // to bit 0 (the GEMM operand); rows past a segment's live requests are skipped
   const int nthreads = blockDim.x;
   const long long nops = (N - op0) < nthreads ? (N - op0) : nthreads;
   for (long long idx = threadIdx.x; idx < nops * p::ew; idx += nthreads) {
     int r = (int)(idx / p::ew), w = (int)(idx % p::ew);
-    E[(op0 + r) * lde + w] = sm[r * EWS + w];
+    if (live_rows[r]) E[(op0 + r) * lde + w] = sm[r * EWS + w];
   }
   constexpr int sh = p::mt % 32, w0 = p::mt / 32;
   for (long long idx = threadIdx.x; idx < nops * p::kw; idx += nthreads) {
     int r = (int)(idx / p::kw), w = (int)(idx % p::kw);
+    if (!live_rows[r]) continue;
     uint32_t lo = sm[r * EWS + w0 + w];
     uint32_t hi = (w0 + w + 1 < p::ew) ? sm[r * EWS + w0 + w + 1] : 0u;
     Ens[(op0 + r) * ldx + w] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
@@ -111,10 +117,12 @@ template <int SET>
 __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *__restrict__ E, int lde,
                                                                 const uint32_t *__restrict__ S, int lds,
                                                                 uint8_t *__restrict__ C, uint8_t *__restrict__ K,
-                                                                long long N, int pk_bad) {
+                                                                const Segs segs, uint32_t pk_bad_mask) {
   using p = P<SET>;
   const long long op = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (op >= N) return;
+  int seg;
+  if (!seg_live(segs, op, &seg)) return;
+  const bool pk_bad = (pk_bad_mask >> seg) & 1u;
   const uint32_t *e = E + op * lde;
   const uint32_t *sy = S + op * lds;
   // c words (mt bits, tail bits cleared)
@@ -172,31 +180,33 @@ template <int SET>
 static int sample_smem_bytes() { return kSampleThreads * (P<SET>::ew | 1) * 4; }
 
 template <int SET>
-cudaError_t launch_sample(const uint8_t *seeds, long long N, uint32_t *E, int lde, uint32_t *Ens, int ldx,
+cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           cudaStream_t st) {
+  const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   int smem = sample_smem_bytes<SET>();
   cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (err != cudaSuccess) return err;
   long long blocks = (N + kSampleThreads - 1) / kSampleThreads;
-  sample_kernel<SET><<<(unsigned)blocks, kSampleThreads, smem, st>>>(seeds, N, E, lde, Ens, ldx);
+  sample_kernel<SET><<<(unsigned)blocks, kSampleThreads, smem, st>>>(seeds, segs, E, lde, Ens, ldx);
   return cudaGetLastError();
 }
 
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
-                            long long N, int pk_bad, cudaStream_t st) {
+                            const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st) {
+  const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   long long blocks = (N + kTailThreads - 1) / kTailThreads;
-  finalize_kernel<SET><<<(unsigned)blocks, kTailThreads, 0, st>>>(E, lde, S, lds, C, K, N, pk_bad);
+  finalize_kernel<SET><<<(unsigned)blocks, kTailThreads, 0, st>>>(E, lde, S, lds, C, K, segs, pk_bad_mask);
   return cudaGetLastError();
 }
 
 #define GMC_INST_ENC(SET)                                                                                        \
-  template cudaError_t launch_sample<SET>(const uint8_t *, long long, uint32_t *, int, uint32_t *, int,          \
+  template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int,       \
                                           cudaStream_t);                                                         \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
-                                            long long, int, cudaStream_t);
+                                            const Segs &, uint32_t, cudaStream_t);
 GMC_INST_ENC(0)
 GMC_INST_ENC(1)
 GMC_INST_ENC(2)

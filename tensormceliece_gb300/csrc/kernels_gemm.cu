@@ -20,15 +20,17 @@ namespace gmc {
 constexpr int POPC_THREADS = 128;
 constexpr int POPC_OPS_PER_WARP = 16;
 
-__global__ void __launch_bounds__(POPC_THREADS) gf2_gemm_popc(const uint32_t *__restrict__ A, int lda,
+__global__ void __launch_bounds__(POPC_THREADS) gf2_gemm_popc(const GemmKeys keys, const Segs segs, int lda,
                                                                const uint32_t *__restrict__ X, int ldx, int kw_pad,
-                                                               uint32_t *__restrict__ Out, int ldo, int out_words,
-                                                               long long N) {
+                                                               uint32_t *__restrict__ Out, int ldo, int out_words) {
   __shared__ uint32_t As[2][kGemmKTile][kGemmRowTile];
   __shared__ __align__(16) uint32_t Xs[2][kGemmOpTile][kGemmKTile];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long op0 = (long long)blockIdx.x * kGemmOpTile;
   const int row0 = blockIdx.y * kGemmRowTile;
+  const int seg = seg_find(segs, op0);  // a tile never straddles segments
+  const uint32_t *__restrict__ A = keys.A[seg];
+  const long long live_end = segs.row0[seg] + segs.nreq[seg];
   const uint32_t *Arow = A + (size_t)(row0 + tid) * lda;          // this thread stages row tid
   const uint32_t *Xrow = X + (size_t)(op0 + (tid >> 1)) * ldx + 4 * (tid & 1);
 
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(POPC_THREADS) gf2_gemm_popc(const uint32_t *__
     }
   if (lane < POPC_OPS_PER_WARP) {
     const long long op = op0 + warp * POPC_OPS_PER_WARP + lane;
-    if (op < N) {
+    if (op < live_end) {
 #pragma unroll
       for (int g = 0; g < 4; g++) {
         const int word = row0 / 32 + g;
@@ -90,25 +92,50 @@ __global__ void __launch_bounds__(POPC_THREADS) gf2_gemm_popc(const uint32_t *__
   }
 }
 
+Segs one_segment(long long n) {
+  Segs s{};
+  s.nseg = 1;
+  s.row0[0] = 0;
+  s.row0[1] = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
+  s.nreq[0] = n;
+  return s;
+}
+
+cudaError_t launch_gf2_gemm_seg(int engine, const GemmKeys &keys, const Segs &segs, int lda, int rows_pad,
+                                const uint32_t *X, int ldx, int kw_pad, uint32_t *Out, int ldo, int out_words,
+                                int *err, cudaStream_t st) {
+  const long long rows = seg_rows(segs);
+  if (rows <= 0) return cudaSuccess;
+  if (segs.nseg < 1 || segs.nseg > kMaxSegs || rows_pad % kGemmRowTile || kw_pad % kGemmKTile || lda % 4 ||
+      ldx % 4 || lda < kw_pad || ldx < kw_pad)
+    return cudaErrorInvalidValue;
+  for (int i = 0; i <= segs.nseg; i++)
+    if (segs.row0[i] % kGemmOpPad) return cudaErrorInvalidValue;
+  switch (engine) {
+    case GEMM_TC:
+      return launch_gf2_gemm_tc(keys, segs, rows_pad, X, ldx, kw_pad, Out, ldo, out_words, err, st);
+    case GEMM_B1MMA:
+      return launch_gf2_gemm_b1(keys, segs, lda, rows_pad, X, ldx, kw_pad, Out, ldo, out_words, st);
+    case GEMM_POPC:
+    default: {
+      dim3 grid((unsigned)(rows / kGemmOpTile), rows_pad / kGemmRowTile);
+      gf2_gemm_popc<<<grid, POPC_THREADS, 0, st>>>(keys, segs, lda, X, ldx, kw_pad, Out, ldo, out_words);
+      return cudaGetLastError();
+    }
+  }
+}
+
 cudaError_t launch_gf2_gemm(int engine, const uint32_t *A, const uint8_t *A8, int lda, int rows_pad,
                             const uint32_t *X, int ldx, long long n_pad, int kw_pad, uint32_t *Out, int ldo,
                             int out_words, long long N, int *err, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
-  if (rows_pad % kGemmRowTile || n_pad % kGemmOpTile || kw_pad % kGemmKTile || lda % 4 || ldx % 4 ||
-      n_pad < N || lda < kw_pad || ldx < kw_pad)
-    return cudaErrorInvalidValue;
-  switch (engine) {
-    case GEMM_TC:
-      return launch_gf2_gemm_tc(A8, rows_pad, X, ldx, n_pad, kw_pad, Out, ldo, out_words, N, err, st);
-    case GEMM_B1MMA:
-      return launch_gf2_gemm_b1(A, lda, rows_pad, X, ldx, n_pad, kw_pad, Out, ldo, out_words, N, st);
-    case GEMM_POPC:
-    default: {
-      dim3 grid((unsigned)((N + kGemmOpTile - 1) / kGemmOpTile), rows_pad / kGemmRowTile);
-      gf2_gemm_popc<<<grid, POPC_THREADS, 0, st>>>(A, lda, X, ldx, kw_pad, Out, ldo, out_words, N);
-      return cudaGetLastError();
-    }
-  }
+  if (n_pad < N || n_pad % kGemmOpPad) return cudaErrorInvalidValue;
+  GemmKeys keys{};
+  keys.A[0] = A;
+  keys.A8[0] = A8;
+  Segs segs = one_segment(N);
+  segs.row0[1] = n_pad;
+  return launch_gf2_gemm_seg(engine, keys, segs, lda, rows_pad, X, ldx, kw_pad, Out, ldo, out_words, err, st);
 }
 
 }  // namespace gmc

@@ -135,10 +135,10 @@ constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
 constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 256;
 constexpr uint32_t TC_TMEM_COLS = kTcN;    // FP32 accumulator: 128 lanes x kTcN columns
 
-__global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const uint8_t *__restrict__ A8, int kstages,
+__global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys, const Segs segs, int kstages,
                                                               const uint32_t *__restrict__ X, int ldx,
                                                               uint32_t *__restrict__ Out, int ldo, int out_words,
-                                                              long long N, int *__restrict__ err) {
+                                                              int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t *As = tsm;
   uint8_t *Xs = tsm + kTcStages * TC_A_BYTES;
@@ -150,6 +150,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const uint8_t *__re
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long op0 = (long long)blockIdx.x * kTcN;
   const int mtile = blockIdx.y;
+  const int seg = seg_find(segs, op0);  // a tile never straddles segments
+  const uint8_t *__restrict__ A8 = keys.A8[seg];
+  const long long live_end = segs.row0[seg] + segs.nreq[seg];
   if (tid == 0) {
     for (int i = 0; i < kTcStages; i++) {
       mbar_init(&bar_a[i], 1);
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const uint8_t *__re
       }
       const long long op = op0 + 32 * cb + lane;
       const int wd = mtile * (kTcM / 32) + warp;
-      if (op < N && wd < out_words) Out[op * ldo + wd] = mine;
+      if (op < live_end && wd < out_words) Out[op * ldo + wd] = mine;
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
@@ -309,16 +312,17 @@ cudaError_t launch_expand_a(const uint32_t *A, int lda, int rows_pad, int kw_pad
   return cudaGetLastError();
 }
 
-cudaError_t launch_gf2_gemm_tc(const uint8_t *A8, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
-                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, int *err,
-                               cudaStream_t st) {
-  if (N <= 0) return cudaSuccess;
-  if (!A8 || !err || rows_pad % kTcM || kw_pad % (kTcKB / 32) || n_pad % kTcN || n_pad < N || ldx < kw_pad)
-    return cudaErrorInvalidValue;
+cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_pad, const uint32_t *X, int ldx,
+                               int kw_pad, uint32_t *Out, int ldo, int out_words, int *err, cudaStream_t st) {
+  const long long rows = seg_rows(segs);
+  if (rows <= 0) return cudaSuccess;
+  if (!err || rows_pad % kTcM || kw_pad % (kTcKB / 32) || rows % kTcN || ldx < kw_pad) return cudaErrorInvalidValue;
+  for (int i = 0; i < segs.nseg; i++)
+    if (!keys.A8[i]) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(gf2_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((N + kTcN - 1) / kTcN), rows_pad / kTcM);
-  gf2_gemm_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(A8, kw_pad / (kTcKB / 32), X, ldx, Out, ldo, out_words, N, err);
+  dim3 grid((unsigned)(rows / kTcN), rows_pad / kTcM);
+  gf2_gemm_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(keys, segs, kw_pad / (kTcKB / 32), X, ldx, Out, ldo, out_words, err);
   return cudaGetLastError();
 }
 
@@ -326,14 +330,16 @@ cudaError_t launch_gf2_gemm_tc(const uint8_t *A8, int rows_pad, const uint32_t *
 // Warp tile 32 rows x 32 requests (4 x 4 m8n8k128 MMAs per 128-bit K step),
 // 4 warps per block covering 128 rows. Fragments come straight from global
 // memory (L1/L2): A row (lane/4) bits 32*(lane%4).., B column (lane/4) the same.
-__global__ void __launch_bounds__(128) gf2_gemm_b1(const uint32_t *__restrict__ A, int lda,
+__global__ void __launch_bounds__(128) gf2_gemm_b1(const GemmKeys keys, const Segs segs, int lda,
                                                     const uint32_t *__restrict__ X, int ldx, int kw_pad,
-                                                    uint32_t *__restrict__ Out, int ldo, int out_words,
-                                                    long long N) {
+                                                    uint32_t *__restrict__ Out, int ldo, int out_words) {
   __shared__ uint32_t words[4][32];  // per warp: output word (32 rows) per request
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row0 = blockIdx.y * 128 + warp * 32;
   const long long op0 = (long long)blockIdx.x * 32;
+  const int seg = seg_find(segs, op0);
+  const uint32_t *__restrict__ A = keys.A[seg];
+  const long long live_end = segs.row0[seg] + segs.nreq[seg];
   int acc[4][4][2];
 #pragma unroll
   for (int i = 0; i < 4; i++)
@@ -368,15 +374,16 @@ __global__ void __launch_bounds__(128) gf2_gemm_b1(const uint32_t *__restrict__ 
   __syncwarp();
   const long long op = op0 + lane;
   const int wd = row0 / 32;
-  if (op < N && wd < out_words) Out[op * ldo + wd] = words[warp][lane];
+  if (op < live_end && wd < out_words) Out[op * ldo + wd] = words[warp][lane];
 }
 
-cudaError_t launch_gf2_gemm_b1(const uint32_t *A, int lda, int rows_pad, const uint32_t *X, int ldx, long long n_pad,
-                               int kw_pad, uint32_t *Out, int ldo, int out_words, long long N, cudaStream_t st) {
-  if (N <= 0) return cudaSuccess;
-  if (rows_pad % 128 || kw_pad % 4 || n_pad < (N + 31) / 32 * 32) return cudaErrorInvalidValue;
-  dim3 grid((unsigned)((N + 31) / 32), rows_pad / 128);
-  gf2_gemm_b1<<<grid, 128, 0, st>>>(A, lda, X, ldx, kw_pad, Out, ldo, out_words, N);
+cudaError_t launch_gf2_gemm_b1(const GemmKeys &keys, const Segs &segs, int lda, int rows_pad, const uint32_t *X,
+                               int ldx, int kw_pad, uint32_t *Out, int ldo, int out_words, cudaStream_t st) {
+  const long long rows = seg_rows(segs);
+  if (rows <= 0) return cudaSuccess;
+  if (rows_pad % 128 || kw_pad % 4 || rows % 32) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)(rows / 32), rows_pad / 128);
+  gf2_gemm_b1<<<grid, 128, 0, st>>>(keys, segs, lda, X, ldx, kw_pad, Out, ldo, out_words);
   return cudaGetLastError();
 }
 

@@ -151,14 +151,18 @@ cudaError_t run(const DeviceSetup &su, const gmc_key *sk, uint8_t *k, const uint
   uint32_t *E = reinterpret_cast<uint32_t *>(q);
   q += D::e_bytes(n);
   int *ok = reinterpret_cast<int *>(q);
-  const long long n_pad = (n + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
-  cudaError_t e = launch_pack_ct<SET>(c, n, X, D::ldx, st);
+  const Segs segs = one_segment(n);  // only the first n rows are live and written
+  GemmKeys gk{};
+  gk.A[0] = sk->F;
+  DecKeys dk{};
+  dk.k[0] = sk->dk;
+  cudaError_t e = launch_pack_ct<SET>(c, segs, X, D::ldx, st);
   if (e == cudaSuccess)
-    e = launch_gf2_gemm(GEMM_POPC, sk->F, nullptr, sk->ldf, sk->frows_pad, X, D::ldx, n_pad, sk->cw_pad, S2, D::lds2,
-                        P<SET>::s2w, n, nullptr, st);
-  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, D::lds2, su.fd[SET], n, Sig, st);
-  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, D::lds2, sk->dk, su.fd[SET], n, E, D::lde, ok, st);
-  if (e == cudaSuccess) e = launch_dec_tail<SET>(E, D::lde, ok, c, sk->dk, k, rc, n, st);
+    e = launch_gf2_gemm_seg(GEMM_POPC, gk, segs, sk->ldf, sk->frows_pad, X, D::ldx, sk->cw_pad, S2, D::lds2,
+                            P<SET>::s2w, nullptr, st);
+  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, D::lds2, su.fd[SET], segs, Sig, st);
+  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, D::lds2, dk, su.fd[SET], segs, E, D::lde, ok, st);
+  if (e == cudaSuccess) e = launch_dec_tail<SET>(E, D::lde, ok, c, dk, k, rc, segs, st);
   return e;
 }
 
