@@ -48,10 +48,15 @@ def parse():
     ap.add_argument("--set", default=SET_DEFAULT)
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--flip", type=float, default=0.10)
-    ap.add_argument("--engine", default="tc", choices=["popc", "b1mma", "tc"])
+    ap.add_argument("--engine", default="auto", choices=["auto", "popc", "b1mma", "tc"],
+                    help="auto: per-set configuration (autotuned when --tune, else defaults)")
+    ap.add_argument("--tune", action="store_true", help="autotune every set used before measuring")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-grouped", action="store_true", help="skip the mixed-key grouped-launch measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serve-seconds", type=float, default=3.0, help="seconds per serving load level (60 = the "
+                    "full serving configuration)")
     return ap.parse_args()
 
 
@@ -285,6 +290,50 @@ def grouped_mix(gmc, torch, dev, total, steps, warmup):
     }
 
 
+def serving(gmc, torch, seconds):
+    """16 device-resident key pairs over the five sets, 50/50 enc/dec, Poisson arrivals at 10/50/90% of the
+    measured peak; p50/p99 latency (arrival to completion) against sequential one-request calls."""
+    pairs = []
+    for i in range(16):
+        sid = i % 5
+        pk, sk = gmc.keypair(sid, bytes([0x40 + i]) * 32)
+        pairs.append((gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)))
+    srv = gmc.Server(max_batch=65536, slots=3, mem_fraction=0.4)
+    for P, S in pairs:
+        srv.add_key(P)
+        srv.add_key(S)
+    peak = srv.loadgen(pairs, rate=2e8, seconds=max(1.0, seconds / 2), seed=1)  # overload: saturated throughput
+    levels = {}
+    for frac in (0.1, 0.5, 0.9):
+        r = srv.loadgen(pairs, rate=frac * peak["ops_s"], seconds=seconds, seed=int(frac * 100))
+        levels[f"{int(frac * 100)}%"] = {k: r[k] for k in ("offered_rate", "ops_s", "p50_ms", "p99_ms", "mean_batch",
+                                                             "completed", "submitted")}
+    srv.close()
+    # sequential one-request calls (libmceliece calling convention, resident keys, host buffers)
+    lat = []
+    rng = np.random.default_rng(3)
+    for i in range(100):
+        P, S = pairs[i % 16]
+        z = P.sizes
+        seed = rng.integers(0, 256, (1, 32), dtype=np.uint8)
+        t0 = time.perf_counter()
+        if i % 2 == 0:
+            P.enc_batch(seed)
+        else:
+            c, _, _ = pairs[i % 16][0].enc_batch(seed)  # untimed ciphertext for this dec
+            t0 = time.perf_counter()
+            S.dec_batch(c)
+        lat.append((time.perf_counter() - t0) * 1e3)
+    lat = np.array(lat)
+    return {
+        "workload": "16 key pairs (sets uniform over the five), 50/50 enc/dec, Poisson arrivals, "
+                    f"{seconds:.0f} s per load level, latency = arrival to completion",
+        "peak_ops_s": peak["ops_s"], "peak_mean_batch": peak["mean_batch"], "levels": levels,
+        "sequential_one_request": {"ops_s": 1e3 / lat.mean(), "p50_ms": float(np.percentile(lat, 50)),
+                                   "p99_ms": float(np.percentile(lat, 99))},
+    }
+
+
 def main():
     args = parse()
     rank, local_rank, world = dist_env()
@@ -302,7 +351,13 @@ def main():
     dev = torch.device("cuda", local_rank)
     L = gmc.lib()
     L.gmc_prof_report.argtypes = [ctypes.c_char_p, ctypes.c_int]
-    gmc.set_gemm_engine({"popc": gmc.GEMM_POPC, "b1mma": gmc.GEMM_B1MMA, "tc": gmc.GEMM_TC}[args.engine])
+    gmc.set_gemm_engine({"auto": -1, "popc": gmc.GEMM_POPC, "b1mma": gmc.GEMM_B1MMA, "tc": gmc.GEMM_TC}[args.engine])
+    tuning = {}
+    if args.tune:
+        for sname in sorted({args.set} | ({gmc.SETS[s] for s in MIX_SETS} if not args.no_grouped else set())):
+            t0 = time.perf_counter()
+            tuning[sname] = gmc.autotune(sname, args.n)
+            tuning[sname]["seconds"] = round(time.perf_counter() - t0, 2)
     sid = gmc.set_id(args.set)
     z = gmc.set_sizes(sid)
     N = args.n
@@ -398,7 +453,8 @@ def main():
                                f"decapsulations ({int(args.flip * 100)}% with one flipped bit) per step, "
                                f"one resident key pair", "set": args.set, "n_per_gpu": N,
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MiB write) between timed steps",
-                   "gemm_engine": args.engine},
+                   "gemm_engine": args.engine,
+                   "tuning": {k: gmc.tune_get(k) for k in gmc.SETS} if not tuning else tuning},
         "gpu_launches": launches_per_step * args.steps,
         "kernels": kernels,
         "roofline": roofline,
@@ -408,6 +464,8 @@ def main():
 
     if rank == 0 and not args.no_grouped:
         line["grouped"] = grouped_mix(gmc, torch, dev, N, max(5, args.steps // 2), args.warmup)
+    if rank == 0 and not args.no_serving:
+        line["serving"] = serving(gmc, torch, args.serve_seconds)
 
     if rank == 0 and not args.no_e2e:
         # end to end through the host-pointer C ABI (pinned host buffers)

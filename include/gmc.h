@@ -104,6 +104,40 @@ int gmc_plan_launch(gmc_plan *plan, void *stream);
 int gmc_plan_info(const gmc_plan *plan, int *pipelines, long long *padded_rows);
 void gmc_plan_free(gmc_plan *plan);
 
+/* ---- serving loop (continuous batching) -----------------------------------
+ * gmc_server_create: `slots` batches may be in flight at once (each with its
+ * own stream, device arena and pinned staging); a batch holds at most
+ * max_batch requests and only what fits its arena (arenas take at most
+ * mem_fraction of the device memory free at creation: admission by free
+ * memory). Keys must be registered (gmc_server_add_key) before requests use
+ * them; their device state is completed at registration.
+ * gmc_server_submit queues one request with host buffers (in: 32-byte seed for
+ * a public key, ciphertext for a secret key; ct out for a public key; k out;
+ * optional rc) and returns at once; *done (optional) becomes 1 when the
+ * outputs are written (-1 on failure). A dispatcher thread forms each batch
+ * from everything queued when a slot frees up, so requests that arrive while
+ * others run join the next batch. Results equal the one-request calls.
+ * gmc_server_stats out[8]: completed, batches, mean batch size, p50 ms,
+ * p99 ms (arrival to completion), ops/s since the first arrival, errors,
+ * slots. gmc_server_loadgen drives the server with Poisson arrivals at `rate`
+ * requests/s for `seconds` over npairs (public, secret) key pairs, a fraction
+ * enc_fraction of them encapsulations, and writes out[8]: submitted,
+ * completed, achieved ops/s, p50 ms, p99 ms, mean batch, batches, offered
+ * rate. */
+typedef struct gmc_server gmc_server;
+int gmc_server_create(gmc_server **server, long long max_batch, int slots, double mem_fraction);
+int gmc_server_add_key(gmc_server *server, const gmc_key *key);
+int gmc_server_submit(gmc_server *server, const gmc_key *key, const unsigned char *in, unsigned char *ct,
+                      unsigned char *k, int *rc, int *done);
+int gmc_server_drain(gmc_server *server, double timeout_s);
+int gmc_server_stats(gmc_server *server, double *out);
+int gmc_server_reset_stats(gmc_server *server);
+int gmc_server_loadgen(gmc_server *server, const gmc_key *const *pks, const gmc_key *const *sks, int npairs,
+                       double rate, double seconds, double enc_fraction, unsigned long long seed, double *out);
+void gmc_server_destroy(gmc_server *server);
+/* message of the server's last failed batch ("" if none) */
+const char *gmc_server_error(gmc_server *server);
+
 /* ---- libmceliece calling convention (one request per call) --------------
  * Same signatures and results as mceliece_kem_<set>_enc / _dec
  * (mc:crypto_kem/<set>/vec/wrap_keypair.c:4, wrap_enc.c:4, wrap_dec.c:4). keypair
@@ -136,8 +170,23 @@ void gmc_set_randombytes(gmc_randombytes_fn fn, void *ctx);
 #define GMC_GEMM_POPC 0   /* CUDA-core AND/XOR + popcount */
 #define GMC_GEMM_B1MMA 1  /* legacy mma.sync m8n8k128 .b1 AND.POPC */
 #define GMC_GEMM_TC 2     /* tcgen05 (5th-gen tensor cores), 0/1 operands in FP8, TMEM accumulators */
+/* Forces one GEMM engine for every set (-1 restores the per-set choices);
+ * gmc_get_gemm_engine returns the override or -1. */
 int gmc_set_gemm_engine(int engine);
 int gmc_get_gemm_engine(void);
+
+/* ---- autotuner --------------------------------------------------------------
+ * Per parameter set: the GEMM engine of the encapsulation syndrome and of the
+ * decapsulation front end, and the sampler block size (32/64/128). Defaults:
+ * tcgen05, tcgen05, 64. gmc_autotune times every candidate on this GPU with a
+ * batch of n requests (median of 5), keeps the fastest and, when cache_path is
+ * given, writes the choices of all tuned sets to that JSON file;
+ * gmc_autotune_load applies such a file (returns the number of sets loaded).
+ * gmc_tune_get returns 1 when the set's configuration was tuned or loaded. */
+int gmc_autotune(int set, long long n, const char *cache_path);
+int gmc_autotune_load(const char *cache_path);
+int gmc_tune_set(int set, int enc_engine, int dec_engine, int sample_threads);
+int gmc_tune_get(int set, int *enc_engine, int *dec_engine, int *sample_threads);
 /* Reads and clears the tensor-core engine's error word on the current device:
  * 1 when a CTA gave up on a bounded wait (its outputs are then invalid). */
 int gmc_tc_status(void);

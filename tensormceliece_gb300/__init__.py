@@ -18,8 +18,9 @@ import numpy as np
 from . import build as _build
 
 __all__ = [
-    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "Plan", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
-    "set_gemm_engine", "get_gemm_engine", "set_randombytes", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC",
+    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "Plan", "Server", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
+    "set_gemm_engine", "get_gemm_engine", "set_randombytes", "autotune", "autotune_load", "tune_get",
+    "tune_set", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC",
 ]
 
 SETS = ("348864", "460896", "6688128", "6960119", "8192128")
@@ -77,6 +78,24 @@ def lib():
         L.gmc_plan_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]
         L.gmc_plan_free.argtypes = [ctypes.c_void_p]
         L.gmc_plan_free.restype = None
+        L.gmc_autotune.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_char_p]
+        L.gmc_autotune_load.argtypes = [ctypes.c_char_p]
+        L.gmc_tune_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.gmc_tune_get.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                   ctypes.POINTER(ctypes.c_int)]
+        vp = ctypes.c_void_p
+        L.gmc_server_create.argtypes = [ctypes.POINTER(vp), ctypes.c_longlong, ctypes.c_int, ctypes.c_double]
+        L.gmc_server_add_key.argtypes = [vp, vp]
+        L.gmc_server_submit.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.gmc_server_drain.argtypes = [vp, ctypes.c_double]
+        L.gmc_server_stats.argtypes = [vp, vp]
+        L.gmc_server_reset_stats.argtypes = [vp]
+        L.gmc_server_loadgen.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_ulonglong, vp]
+        L.gmc_server_destroy.argtypes = [vp]
+        L.gmc_server_destroy.restype = None
+        L.gmc_server_error.argtypes = [vp]
+        L.gmc_server_error.restype = ctypes.c_char_p
         L.gmc_set_randombytes.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gmc_set_randombytes.restype = None
         _lib = L
@@ -234,6 +253,62 @@ class Plan:
             pass
 
 
+class Server:
+    """Continuous-batching request loop (gmc_server_*): register keys, submit requests, read statistics."""
+
+    STATS = ("completed", "batches", "mean_batch", "p50_ms", "p99_ms", "ops_s", "errors", "slots")
+    LOADGEN = ("submitted", "completed", "ops_s", "p50_ms", "p99_ms", "mean_batch", "batches", "offered_rate")
+
+    def __init__(self, max_batch=65536, slots=3, mem_fraction=0.5):
+        h = ctypes.c_void_p()
+        _check(lib().gmc_server_create(ctypes.byref(h), int(max_batch), int(slots), float(mem_fraction)),
+               "gmc_server_create")
+        self._h = h
+        self._keys = []
+
+    def add_key(self, key):
+        _check(lib().gmc_server_add_key(self._h, key.handle), "gmc_server_add_key")
+        self._keys.append(key)
+
+    def submit(self, key, in_ptr, ct_ptr, k_ptr, rc_ptr=None, done_ptr=None):
+        """Host pointers; returns at once. *done becomes 1 when outputs are written."""
+        _check(lib().gmc_server_submit(self._h, key.handle, in_ptr, ct_ptr, k_ptr, rc_ptr, done_ptr),
+               "gmc_server_submit")
+
+    def drain(self, timeout_s=60.0):
+        _check(lib().gmc_server_drain(self._h, float(timeout_s)), "gmc_server_drain")
+
+    def stats(self):
+        out = (ctypes.c_double * 8)()
+        _check(lib().gmc_server_stats(self._h, out), "gmc_server_stats")
+        d = dict(zip(self.STATS, list(out)))
+        d["last_error"] = lib().gmc_server_error(self._h).decode(errors="replace")
+        return d
+
+    def reset_stats(self):
+        _check(lib().gmc_server_reset_stats(self._h), "gmc_server_reset_stats")
+
+    def loadgen(self, pairs, rate, seconds, enc_fraction=0.5, seed=1):
+        """pairs: [(PublicKey, SecretKey)] registered with this server. Poisson arrivals at `rate`/s."""
+        pk = (ctypes.c_void_p * len(pairs))(*[p.handle.value for p, _ in pairs])
+        sk = (ctypes.c_void_p * len(pairs))(*[s.handle.value for _, s in pairs])
+        out = (ctypes.c_double * 8)()
+        _check(lib().gmc_server_loadgen(self._h, pk, sk, len(pairs), float(rate), float(seconds),
+                                        float(enc_fraction), int(seed), out), "gmc_server_loadgen")
+        return dict(zip(self.LOADGEN, list(out)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gmc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def keypair(set_name, seed32=None):
     """(pk, sk) as uint8 arrays; seed32 = the keypair's single randombytes draw (None: randombytes source)."""
     sid = set_name if isinstance(set_name, int) else set_id(set_name)
@@ -272,6 +347,32 @@ def kem_dec(set_name, ct, sk):
     if rc < -1:
         _check(rc, f"gmc_kem_{name}_dec")
     return rc, k.tobytes()
+
+
+def autotune(set_name, n=65536, cache_path=None):
+    """Times the candidate configurations for a set on this GPU; returns the chosen configuration."""
+    sid = set_name if isinstance(set_name, int) else set_id(set_name)
+    _check(lib().gmc_autotune(sid, int(n), cache_path.encode() if cache_path else None), "gmc_autotune")
+    return tune_get(sid)
+
+
+def autotune_load(cache_path):
+    return _check(lib().gmc_autotune_load(cache_path.encode()), "gmc_autotune_load")
+
+
+def tune_get(set_name):
+    sid = set_name if isinstance(set_name, int) else set_id(set_name)
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    tuned = _check(lib().gmc_tune_get(sid, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "gmc_tune_get")
+    names = {GEMM_POPC: "popc", GEMM_B1MMA: "b1mma", GEMM_TC: "tc"}
+    return {"enc_engine": names[a.value], "dec_engine": names[b.value], "sample_threads": c.value,
+            "tuned": bool(tuned)}
+
+
+def tune_set(set_name, enc_engine, dec_engine, sample_threads):
+    sid = set_name if isinstance(set_name, int) else set_id(set_name)
+    ids = {"popc": GEMM_POPC, "b1mma": GEMM_B1MMA, "tc": GEMM_TC}
+    _check(lib().gmc_tune_set(sid, ids[enc_engine], ids[dec_engine], int(sample_threads)), "gmc_tune_set")
 
 
 def set_gemm_engine(engine):

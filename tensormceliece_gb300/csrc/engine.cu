@@ -49,7 +49,23 @@ void gmc::set_last_error(const char *msg) { g_last_error = msg; }
 // ---------------------------------------------------------------- keys
 // (struct gmc_key: engine_internal.h)
 
-static int g_engine = GEMM_TC;
+// Per-set launch configuration (autotuned, see gmc_autotune) and an optional
+// global GEMM-engine override (gmc_set_gemm_engine).
+static SetTune g_tune[GMC_NSETS];
+static int g_engine_override = -1;
+static std::mutex g_tune_mu;
+static int engine_for(int set, int op) {
+  if (g_engine_override >= 0) return g_engine_override;
+  return op ? g_tune[set].dec_engine : g_tune[set].enc_engine;
+}
+SetTune gmc::tune_get(int set) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return g_tune[set];
+}
+void gmc::tune_put(int set, const SetTune &t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[set] = t;
+}
 
 // ---------------------------------------------------------------- profiler
 // Optional per-kernel timing: when enabled, an event is recorded on the
@@ -295,11 +311,11 @@ extern "C" void gmc_key_free(gmc_key *key) {
 extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set : GMC_EINVAL; }
 
 extern "C" int gmc_set_gemm_engine(int engine) {
-  if (engine < GEMM_POPC || engine > GEMM_TC) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
-  g_engine = engine;
+  if (engine < -1 || engine > GEMM_TC) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
+  g_engine_override = engine;
   return GMC_OK;
 }
-extern "C" int gmc_get_gemm_engine(void) { return g_engine; }
+extern "C" int gmc_get_gemm_engine(void) { return g_engine_override; }
 
 // ---------------------------------------------------------------- workspace
 // Stream-ordered scratch: allocated from the device's default memory pool on
@@ -356,7 +372,7 @@ static cudaError_t enc_sample_gemm_seg(const Segs &segs, const gmc_key *ref, con
                                        const EncDims &d, cudaStream_t st) {
   using p = P<SET>;
   prof_mark(nullptr, st);
-  cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, st);
+  cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, tune_get(SET).sample_threads, st);
   if (e != cudaSuccess) return e;
   prof_mark("enc_sample", st);
   e = launch_gf2_gemm_seg(engine, gk, segs, ref->lda, ref->rows_pad, Ens, d.ldx, ref->kw_pad, S, d.lds, p::mw, err,
@@ -370,9 +386,10 @@ static cudaError_t enc_sample_gemm(const gmc_key *pk, const uint8_t *seeds, long
                                    uint32_t *S, const EncDims &d, cudaStream_t st) {
   GemmKeys gk;
   int *err;
-  cudaError_t e = gemm_keys(&pk, 1, g_engine, st, &gk, &err);
+  const int engine = engine_for(pk->set, 0);
+  cudaError_t e = gemm_keys(&pk, 1, engine, st, &gk, &err);
   if (e != cudaSuccess) return e;
-  return enc_sample_gemm_seg<SET>(one_segment(n), pk, gk, g_engine, err, seeds, E, Ens, S, d, st);
+  return enc_sample_gemm_seg<SET>(one_segment(n), pk, gk, engine, err, seeds, E, Ens, S, d, st);
 }
 
 template <int SET>
@@ -434,11 +451,12 @@ static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long lo
                                     uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
   GemmKeys gk;
   int *err;
-  cudaError_t e = gemm_keys(&sk, 1, g_engine, st, &gk, &err);
+  const int engine = engine_for(sk->set, 1);
+  cudaError_t e = gemm_keys(&sk, 1, engine, st, &gk, &err);
   if (e != cudaSuccess) return e;
   DecKeys dk{};
   dk.k[0] = sk->dk;
-  return dec_front_decode_seg<SET>(one_segment(n), sk, gk, dk, g_engine, err, c, X, S2, Sig, E, ok, d, st);
+  return dec_front_decode_seg<SET>(one_segment(n), sk, gk, dk, engine, err, c, X, S2, Sig, E, ok, d, st);
 }
 
 template <int SET>
@@ -767,6 +785,20 @@ extern "C" int gmc_host_field_tables(int set, unsigned short *gexp, unsigned sho
   return GMC_OK;
 }
 
+int *gmc::tc_err_word_ptr() { return tc_err_word(); }
+int gmc::field_tables(int set, FieldDev *out) { return get_field(set, out); }
+int gmc::key_prepare_resident(const gmc_key *key) {
+  if (!key) return fail(GMC_EINVAL, "key_prepare_resident: null key");
+  cudaStream_t st;
+  GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  const uint8_t *a8;
+  cudaError_t e = key_a8(key, st, &a8);
+  cudaStreamDestroy(st);
+  if (e != cudaSuccess) return cuda_fail(e, "key_prepare_resident");
+  FieldDev fd;
+  return get_field(key->set, &fd);
+}
+
 // ---------------------------------------------------------------- grouped plans
 // A plan is a fixed set of request groups (key, op, n, device buffers). Groups
 // are bucketed by (parameter set, enc/dec) into pipelines of at most kMaxSegs
@@ -777,6 +809,7 @@ extern "C" int gmc_host_field_tables(int set, unsigned short *gexp, unsigned sho
 // with a single cudaGraphLaunch.
 struct PlanPipe {
   int set = 0, kind = 0;  // kind 0 enc, 1 dec
+  int engine = GEMM_TC;
   std::vector<int> groups;
   Segs segs{};
   uint32_t pk_bad_mask = 0;
@@ -791,7 +824,6 @@ struct PlanPipe {
 
 struct gmc_plan {
   int device = 0;
-  int engine = GEMM_TC;
   std::vector<gmc_group> groups;
   std::vector<PlanPipe> pipes;
   std::vector<void *> allocs;
@@ -824,19 +856,19 @@ static cudaError_t plan_pipe_kernels(gmc_plan *p, PlanPipe &pp) {
   const gmc_key *ref = keys[0];
   GemmKeys gk;
   int *err;
-  cudaError_t e = gemm_keys(keys, (int)pp.groups.size(), p->engine, pp.st, &gk, &err);
+  cudaError_t e = gemm_keys(keys, (int)pp.groups.size(), pp.engine, pp.st, &gk, &err);
   if (e != cudaSuccess) return e;
   const long long rows = seg_rows(pp.segs);
   if (pp.kind == 0) {
     EncDims d = enc_dims(SET, ref->kw_pad, rows);
-    e = enc_sample_gemm_seg<SET>(pp.segs, ref, gk, p->engine, err, pp.in, pp.w0, pp.w1, pp.w2, d, pp.st);
+    e = enc_sample_gemm_seg<SET>(pp.segs, ref, gk, pp.engine, err, pp.in, pp.w0, pp.w1, pp.w2, d, pp.st);
     if (e == cudaSuccess)
       e = launch_finalize<SET>(pp.w0, d.lde, pp.w2, d.lds, pp.ct, pp.k, pp.segs, pp.pk_bad_mask, pp.st);
   } else {
     DecDims d = dec_dims(SET, ref->cw_pad, rows);
     DecKeys dk{};
     for (size_t i = 0; i < pp.groups.size(); i++) dk.k[i] = keys[i]->dk;
-    e = dec_front_decode_seg<SET>(pp.segs, ref, gk, dk, p->engine, err, pp.in, pp.w0, pp.w1, pp.sig, pp.w2, pp.ok, d,
+    e = dec_front_decode_seg<SET>(pp.segs, ref, gk, dk, pp.engine, err, pp.in, pp.w0, pp.w1, pp.sig, pp.w2, pp.ok, d,
                                   pp.st);
     if (e == cudaSuccess) e = launch_dec_tail<SET>(pp.w2, d.lde, pp.ok, pp.in, dk, pp.k, pp.rc, pp.segs, pp.st);
   }
@@ -859,7 +891,6 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
   }
   gmc_plan *p = new gmc_plan();
   cudaGetDevice(&p->device);
-  p->engine = g_engine;
   p->groups.assign(groups, groups + ngroups);
   // bucket by (set, kind), at most kMaxSegs groups per pipeline
   for (int i = 0; i < ngroups; i++) {
@@ -873,6 +904,7 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
       dst = &p->pipes.back();
       dst->set = g.key->set;
       dst->kind = g.key->kind;
+      dst->engine = engine_for(dst->set, dst->kind);
     }
     dst->groups.push_back(i);
   }
@@ -914,12 +946,12 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
     // per-set tables and FP8 key images exist before capture
     FieldDev fd;
     if (e == cudaSuccess && pp.kind == 1 && get_field(pp.set, &fd) != GMC_OK) e = cudaErrorUnknown;
-    if (e == cudaSuccess && p->engine == GEMM_TC)
+    if (e == cudaSuccess && pp.engine == GEMM_TC)
       for (int gi : pp.groups) {
         const uint8_t *a8;
         if ((e = key_a8(p->groups[gi].key, pp.st, &a8)) != cudaSuccess) break;
       }
-    if (e == cudaSuccess && p->engine == GEMM_TC && !tc_err_word()) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess && pp.engine == GEMM_TC && !tc_err_word()) e = cudaErrorMemoryAllocation;
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);

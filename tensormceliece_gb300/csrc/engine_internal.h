@@ -28,4 +28,24 @@ struct gmc_key {
 namespace gmc {
 // sets the calling thread's message returned by gmc_last_error()
 void set_last_error(const char *msg);
+
+// per-parameter-set launch configuration chosen by the autotuner
+struct SetTune {
+  int enc_engine = GEMM_TC;   // GF(2) GEMM engine of the encapsulation syndrome
+  int dec_engine = GEMM_TC;   // GF(2) GEMM engine of the decapsulation front end
+  int sample_threads = 64;    // sampler block size (32, 64 or 128)
+  int tuned = 0;              // 1 when measured on this device
+  double enc_ms = 0, dec_ms = 0;
+  long long n = 0;
+};
+SetTune tune_get(int set);
+void tune_put(int set, const SetTune &t);
+
+// device word of the tensor-core engine's bounded waits (allocated on first use)
+int *tc_err_word_ptr();
+// per-set field / FFT tables of the current device (built on first use)
+int field_tables(int set, FieldDev *out);
+// builds everything a key needs resident on the device for any engine choice
+// (FP8 image of its matrix, per-set tables), so later launches allocate nothing for it
+int key_prepare_resident(const gmc_key *key);
 }  // namespace gmc

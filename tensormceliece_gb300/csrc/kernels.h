@@ -6,7 +6,7 @@
 
 namespace gmc {
 
-constexpr int kSampleThreads = 64;
+constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
 constexpr int kBMWarps = 16;    // Berlekamp-Massey kernel: warps per block
 constexpr int kRootWarps = 16;  // root-finding kernel: warps per block
@@ -88,7 +88,7 @@ Segs one_segment(long long n);
 // nonzero padding bits (6960119), its c and K are zeroed.
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
-                          cudaStream_t st);
+                          int threads, cudaStream_t st);
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
                             const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st);

@@ -19,7 +19,7 @@ namespace gmc {
 // sort-and-compare: only the set of positions matters). The bitmap is the
 // error vector e itself and is written out with the block's coalesced store.
 template <int SET>
-__global__ void __launch_bounds__(kSampleThreads) sample_kernel(const uint8_t *__restrict__ seeds, const Segs segs,
+__global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t *__restrict__ seeds, const Segs segs,
                                                                 uint32_t *__restrict__ E, int lde,
                                                                 uint32_t *__restrict__ Ens, int ldx) {
   using p = P<SET>;
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kSampleThreads) sample_kernel(const uint8_t *_
       st[0] = nst[0]; st[1] = nst[1]; st[2] = nst[2]; st[3] = nst[3];
     }
   }
-  __shared__ unsigned char live_rows[kSampleThreads];
+  __shared__ unsigned char live_rows[kSampleThreadsMax];
   live_rows[threadIdx.x] = live;
   __syncthreads();
   // coalesced copy-out of the block's error vectors, and of e[mt:n] shifted
@@ -177,18 +177,20 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
 
 // ---------------------------------------------------------------- launchers
 template <int SET>
-static int sample_smem_bytes() { return kSampleThreads * (P<SET>::ew | 1) * 4; }
+static int sample_smem_bytes(int threads) { return threads * (P<SET>::ew | 1) * 4; }
 
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
-                          cudaStream_t st) {
+                          int threads, cudaStream_t st) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
-  int smem = sample_smem_bytes<SET>();
-  cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (threads != 32 && threads != 64 && threads != 128) return cudaErrorInvalidValue;
+  const int smem = sample_smem_bytes<SET>(threads);
+  cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         sample_smem_bytes<SET>(kSampleThreadsMax));
   if (err != cudaSuccess) return err;
-  long long blocks = (N + kSampleThreads - 1) / kSampleThreads;
-  sample_kernel<SET><<<(unsigned)blocks, kSampleThreads, smem, st>>>(seeds, segs, E, lde, Ens, ldx);
+  long long blocks = (N + threads - 1) / threads;
+  sample_kernel<SET><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx);
   return cudaGetLastError();
 }
 
@@ -203,7 +205,7 @@ cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int l
 }
 
 #define GMC_INST_ENC(SET)                                                                                        \
-  template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int,       \
+  template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int, int,  \
                                           cudaStream_t);                                                         \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
                                             const Segs &, uint32_t, cudaStream_t);

@@ -222,7 +222,7 @@ def test_kem_parity_per_gemm_engine(gmc, keys, sid, engine):
     """Encapsulation and decapsulation byte-exact with the tensor-core and legacy 1-bit GEMM engines."""
     pk, sk = keys(sid)
     eng = {"tc": gmc.GEMM_TC, "b1mma": gmc.GEMM_B1MMA}[engine]
-    prev = gmc.get_gemm_engine()
+    prev = gmc.get_gemm_engine()  # -1: no override
     gmc.set_gemm_engine(eng)
     try:
         n = 300
