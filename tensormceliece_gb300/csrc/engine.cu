@@ -147,25 +147,24 @@ static int get_field(int set, FieldDev *out) {
   const HostField &F = host_field(S.m);
   FftTables ft = build_fft_tables(S.m, S.fft_d);
   std::vector<uint16_t> all;
-  const size_t o_exp = 0, o_log = o_exp + F.exp.size(), o_alpha = o_log + F.log.size(),
-               o_twist = o_alpha + ft.alpha_log.size();
-  all.insert(all.end(), F.exp.begin(), F.exp.end());
-  all.insert(all.end(), F.log.begin(), F.log.end());
-  all.insert(all.end(), ft.alpha_log.begin(), ft.alpha_log.end());
-  all.insert(all.end(), ft.twist_log.begin(), ft.twist_log.end());
-  const size_t o_frlo = all.size();
-  all.insert(all.end(), ft.frob_lo.begin(), ft.frob_lo.end());
-  const size_t o_frhi = all.size();
-  all.insert(all.end(), ft.frob_hi.begin(), ft.frob_hi.end());
+  // u16 tables, then the bit-sliced u32 tables at even (4-byte aligned) offsets
+  auto put = [&](const std::vector<uint16_t> &v) {
+    if (all.size() & 1) all.push_back(0);
+    const size_t at = all.size();
+    all.insert(all.end(), v.begin(), v.end());
+    return at;
+  };
+  const size_t o_exp = put(F.exp), o_log = put(F.log), o_twist = put(ft.twist_log), o_frlo = put(ft.frob_lo),
+               o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs);
   FieldEntry e;
   GMC_CUDA(cudaMalloc(&e.buf, all.size() * 2));
   GMC_CUDA(cudaMemcpy(e.buf, all.data(), all.size() * 2, cudaMemcpyHostToDevice));
   e.fd.gexp = e.buf + o_exp;
   e.fd.glog = e.buf + o_log;
-  e.fd.fft_alpha_log = e.buf + o_alpha;
   e.fd.fft_twist_log = e.buf + o_twist;
   e.fd.frob_lo = e.buf + o_frlo;
-  e.fd.frob_hi = e.buf + o_frhi;
+  e.fd.fft_alpha_bs = reinterpret_cast<const uint32_t *>(e.buf + o_abs);
+  e.fd.frob_hi_bs = reinterpret_cast<const uint32_t *>(e.buf + o_fhbs);
   g_fields[key] = e;
   *out = e.fd;
   return GMC_OK;

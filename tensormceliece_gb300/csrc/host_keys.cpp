@@ -153,6 +153,33 @@ FftTables build_fft_tables(int m, int d) {
   for (int x = 0; x < (1 << d); x++) t.frob_lo[x] = frob((uint16_t)x);
   t.frob_hi.resize(1 << (m - d));
   for (int c = 0; c < (1 << (m - d)); c++) t.frob_hi[c] = frob((uint16_t)(c << d));
+
+  // bit-sliced forms: 32 chunks per word
+  const int H = (1 << (m - d)) / 32;
+  auto put_word = [](std::vector<uint16_t> &v, size_t w, uint32_t x) {
+    v[2 * w] = (uint16_t)(x & 0xFFFFu);
+    v[2 * w + 1] = (uint16_t)(x >> 16);
+  };
+  t.alpha_bs.assign((size_t)2 * ((1 << d) - 1) * H * m, 0);
+  for (int l = 0, aoff = 0; l < d; aoff += 1 << (m - l - 1), l++)
+    for (int xh = 0; xh < (1 << (d - 1 - l)); xh++)
+      for (int h = 0; h < H; h++)
+        for (int b = 0; b < m; b++) {
+          uint32_t w = 0;
+          for (int k = 0; k < 32; k++) {
+            const int c = 32 * h + k;
+            const uint16_t a = F.exp[t.alpha_log[aoff + (c << (d - 1 - l)) + xh]];
+            w |= (uint32_t)((a >> b) & 1) << k;
+          }
+          put_word(t.alpha_bs, ((size_t)((1 << d) - (1 << (d - l)) + xh) * H + h) * m + b, w);
+        }
+  t.frob_hi_bs.assign((size_t)2 * H * m, 0);
+  for (int h = 0; h < H; h++)
+    for (int b = 0; b < m; b++) {
+      uint32_t w = 0;
+      for (int k = 0; k < 32; k++) w |= (uint32_t)((t.frob_hi[32 * h + k] >> b) & 1) << k;
+      put_word(t.frob_hi_bs, (size_t)h * m + b, w);
+    }
   return t;
 }
 

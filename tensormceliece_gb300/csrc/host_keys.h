@@ -31,6 +31,14 @@ struct FftTables {
   std::vector<uint16_t> alpha_log;  // levels concatenated, 2^(m-l-1) each (padded to 2^m)
   std::vector<uint16_t> frob_lo;    // x^(2^d), x < 2^d
   std::vector<uint16_t> frob_hi;    // (c 2^d)^(2^d), c < 2^(m-d)
+  // Bit-sliced copies for the chunked bottom-up pass, where bit k of a 32-bit
+  // word belongs to chunk c = 32 h + k (h < 2^(m-d) / 32) and plane b holds
+  // bit b of the field element. Stored as u32 words split into (low, high)
+  // u16 halves so they travel in the u16 table buffers.
+  //   alpha_bs[((2^d - 2^(d-l) + xh) * H + h) * m + b]: alpha_{l, (c << (d-1-l)) + xh}, xh < 2^(d-1-l)
+  //   frob_hi_bs[h * m + b]: frob_hi[c]
+  std::vector<uint16_t> alpha_bs;
+  std::vector<uint16_t> frob_hi_bs;
 };
 FftTables build_fft_tables(int m, int d);
 

@@ -9,7 +9,7 @@ namespace gmc {
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
 constexpr int kBMWarps = 16;    // Berlekamp-Massey kernel: warps per block
-constexpr int kRootWarps = 16;  // root-finding kernel: warps per block
+constexpr int kRootWarps = 8;  // root-finding kernel: warps per block
 
 // ---------------------------------------------------------------- segments
 // A launch covers up to kMaxSegs segments (one key each) laid out back to back
@@ -106,10 +106,11 @@ struct DecKeyDev {
 struct FieldDev {
   const uint16_t *gexp;   // [2q-1]
   const uint16_t *glog;   // [q]
-  const uint16_t *fft_alpha_log;  // concatenated per level l = 0..d-1: [2^(m-l-1)]
   const uint16_t *fft_twist_log;  // concatenated per level l = 0..d-1: [2^(d-l)]
-  const uint16_t *frob_lo;  // x^(2^d) for x < 2^d
-  const uint16_t *frob_hi;  // (c 2^d)^(2^d) for c < 2^(m-d)
+  const uint16_t *frob_lo;        // x^(2^d) for x < 2^d
+  // bit-sliced over 32 chunks per word (bit k: chunk 32 h + k), plane b = bit b
+  const uint32_t *fft_alpha_bs;   // [(2^d - 2^(d-l) + xh) * H + h][m]: alpha_{l, (c << (d-1-l)) + xh}
+  const uint32_t *frob_hi_bs;     // [h][m]: (c 2^d)^(2^d)
 };
 
 // Per-key decapsulation tables of the segments of a launch.

@@ -180,59 +180,116 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
 // The top-down part (twist + radix conversion) turns the 2^d coefficients
 // into 2^d leaf constants. Every bottom-up butterfly level has stride < 2^d,
 // so the 2^m evaluations split into 2^(m-d) independent chunks of 2^d
-// consecutive elements that all start from the same leaves: the warp walks
-// the chunks in a 2^d-entry shared buffer. A root (sigma(a) = 0, with a^(2^d)
-// added for the separate leading term via Frobenius tables, since
-// (hi + lo)^(2^d) = hi^(2^d) + lo^(2^d)) is mapped to its code position
-// through the key's inverse support table; only roots touch that table.
+// consecutive elements that all start from the same leaves.
+// The bottom-up pass is bit-sliced over the chunks: a 32-bit word carries one
+// bit plane of the same element slot of 32 chunks, so a butterfly of 32
+// chunks is one bit-sliced GF(2^m) product (m^2 AND-XOR steps and the
+// reduction) instead of 64 table lookups. Lane and register slot together
+// address the 2^d slots; a level whose pair bit is a lane bit first swaps
+// that lane bit with the register bit of the oldest finished level (one
+// shuffle per plane of half the slots), so every butterfly is in-register.
+// A root (sigma(a) = 0, with a^(2^d) added for the separate leading term via
+// Frobenius tables, since (hi + lo)^(2^d) = hi^(2^d) + lo^(2^d)) is mapped to
+// its code position through the key's inverse support table; only roots touch
+// that table.
 template <int SET>
 struct RootLayout {
   using p = P<SET>;
-  static constexpr int Q = p::q, D = p::fft_d, SIG = 1 << D, NC = Q >> D;
+  static constexpr int Q = p::q, D = p::fft_d, SIG = 1 << D, NC = Q >> D, NH = NC / 32, M = p::m;
   static constexpr int exp_off = 0, exp_len = 2 * Q;
   static constexpr int log_off = exp_off + exp_len, log_len = Q;
-  static constexpr int alpha_off = log_off + log_len, alpha_len = Q;
-  static constexpr int twist_off = alpha_off + alpha_len, twist_len = 2 << D;
+  static constexpr int twist_off = log_off + log_len, twist_len = 2 << D;
   static constexpr int frlo_off = twist_off + twist_len, frlo_len = SIG;
-  static constexpr int frhi_off = frlo_off + frlo_len, frhi_len = NC;
-  static constexpr int shared_u16 = (frhi_off + frhi_len + 1) & ~1;
+  static constexpr int shared_u16 = (frlo_off + frlo_len + 1) & ~1;
+  // u32 region: bit-sliced alpha, bit-sliced frob_hi
+  static constexpr int abs_off = shared_u16 / 2, abs_len = (SIG - 1) * NH * M;
+  static constexpr int fhbs_off = abs_off + abs_len, fhbs_len = NH * M;
+  static constexpr int shared_u32 = fhbs_off + fhbs_len;
   static constexpr int ewp = (p::ew + 1) & ~1;
   // per warp (u32): e words | roots [t] (pos << 16 | element) | count | V[SIG] u16 | s[2t] u16
   static constexpr int roots_off = ewp, cnt_off = roots_off + p::t, v_off = cnt_off + 2;
   static constexpr int s_off = v_off + SIG / 2;
   static constexpr int warp_u32 = s_off + p::t;
-  static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u32 * 4; }
+  static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
 };
 
+// Chunk-slot index held by (lane, register slot j) while level l is processed
+// (after that level's swap). Register bits hold slot bits L .. L+LOGV-1 (slot
+// bit e in register bit e % LOGV), lane bits below L hold slot bits below L,
+// lane bits from L on hold slot bits from L+LOGV on; L = min(l, D - LOGV).
+template <int D, int LOGV>
+__device__ __forceinline__ int chunk_slot(int l, int lane, int j) {
+  const int L = l < D - LOGV ? l : D - LOGV;
+  int x = (lane & ((1 << L) - 1)) | ((lane >> L) << (L + LOGV));
+#pragma unroll
+  for (int e = 0; e < LOGV; e++) x |= ((j >> ((L + e) % LOGV)) & 1) << (L + e);
+  return x;
+}
+
+// r = a * b in GF(2^M), bit-sliced (plane i = bit i of 32 elements), Horner
+// over the planes of a (read from shared memory one plane per step):
+// r <- r x + a_j b, where r x reduces by x^M = x^4 + x^3 + x + 1 (M = 13) or
+// x^3 + 1 (M = 12), the field polynomials of the log/antilog tables.
+// M^2 AND-XOR steps plus 3 (1) XORs per step; only r and b stay live.
+template <int M>
+__device__ __forceinline__ void bs_mul(uint32_t (&r)[M], const uint32_t *__restrict__ a, const uint32_t (&b)[M]) {
+  {
+    const uint32_t aj = a[M - 1];
+#pragma unroll
+    for (int i = 0; i < M; i++) r[i] = b[i] & aj;
+  }
+#pragma unroll
+  for (int j = M - 2; j >= 0; j--) {
+    const uint32_t top = r[M - 1];
+#pragma unroll
+    for (int i = M - 1; i > 0; i--) r[i] = r[i - 1];
+    r[0] = top;
+    if (M == 13) {
+      r[1] ^= top;
+      r[3] ^= top;
+      r[4] ^= top;
+    } else {
+      r[3] ^= top;
+    }
+    const uint32_t aj = a[j];
+#pragma unroll
+    for (int i = 0; i < M; i++) r[i] ^= b[i] & aj;
+  }
+}
+
 template <int SET>
-__global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_t *__restrict__ Sig,
+__global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint16_t *__restrict__ Sig,
                                                                    const uint32_t *__restrict__ S2, int lds2,
                                                                    const DecKeys keys, FieldDev fd, const Segs segs,
                                                                    uint32_t *__restrict__ E, int lde,
                                                                    int *__restrict__ okout) {
   using p = P<SET>;
   using LY = RootLayout<SET>;
-  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d, SIG = LY::SIG, NC = LY::NC;
+  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d, SIG = LY::SIG, NH = LY::NH;
   constexpr int NSY = (2 * T + 31) / 32;
   constexpr int NW = (p::n + 31) / 32;
-  constexpr int VPL = SIG / 32;  // chunk values per lane
+  constexpr int VPL = SIG / 32;  // chunk slots per lane
+  constexpr int LOGV = (VPL == 4) ? 2 : 1;
+  static_assert(VPL == (1 << LOGV) && (LY::NC % 32) == 0, "chunk geometry");
+  static_assert(M == 12 || M == 13, "field polynomial");
   extern __shared__ __align__(16) uint32_t rsm[];
   uint16_t *sh16 = reinterpret_cast<uint16_t *>(rsm);
   uint16_t *gexp = sh16 + LY::exp_off;
   uint16_t *glog = sh16 + LY::log_off;
-  uint16_t *alog = sh16 + LY::alpha_off;
   uint16_t *tlog = sh16 + LY::twist_off;
   uint16_t *frlo = sh16 + LY::frlo_off;
-  uint16_t *frhi = sh16 + LY::frhi_off;
+  uint32_t *abs_ = rsm + LY::abs_off;
+  uint32_t *fhbs = rsm + LY::fhbs_off;
   for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
-  for (int i = threadIdx.x; i < Q; i += blockDim.x) { glog[i] = fd.glog[i]; alog[i] = fd.fft_alpha_log[i]; }
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
   for (int i = threadIdx.x; i < (2 << D); i += blockDim.x) tlog[i] = fd.fft_twist_log[i];
   for (int i = threadIdx.x; i < SIG; i += blockDim.x) frlo[i] = fd.frob_lo[i];
-  for (int i = threadIdx.x; i < NC; i += blockDim.x) frhi[i] = fd.frob_hi[i];
+  for (int i = threadIdx.x; i < LY::abs_len; i += blockDim.x) abs_[i] = fd.fft_alpha_bs[i];
+  for (int i = threadIdx.x; i < LY::fhbs_len; i += blockDim.x) fhbs[i] = fd.frob_hi_bs[i];
   __syncthreads();
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *wbase = rsm + LY::shared_u16 / 2 + warp * LY::warp_u32;
+  uint32_t *wbase = rsm + LY::shared_u32 + warp * LY::warp_u32;
   uint32_t *esm = wbase;
   uint32_t *roots = wbase + LY::roots_off;
   uint32_t *cnt = wbase + LY::cnt_off;
@@ -279,55 +336,87 @@ __global__ void __launch_bounds__(kRootWarps * 32) dec_root_kernel(const uint16_
         __syncwarp();
       }
     }
-    uint16_t leaf[VPL];
+    uint32_t leaf[VPL];
 #pragma unroll
-    for (int j = 0; j < VPL; j++) leaf[j] = V[lane + 32 * j];
+    for (int j = 0; j < VPL; j++) leaf[j] = V[chunk_slot<D, LOGV>(D - 1, lane, j)];
     __syncwarp();
 
-    // bottom-up, one chunk of 2^d consecutive field elements at a time
     int weight = 0;
 #pragma unroll 1
-    for (int c = 0; c < NC; c++) {
+    for (int h = 0; h < NH; h++) {
+      uint32_t v[VPL][M];
 #pragma unroll
-      for (int j = 0; j < VPL; j++) V[lane + 32 * j] = leaf[j];
-      __syncwarp();
+      for (int j = 0; j < VPL; j++)
+#pragma unroll
+        for (int b = 0; b < M; b++) v[j][b] = 0u - ((leaf[j] >> b) & 1u);
 #pragma unroll
       for (int l = D - 1; l >= 0; l--) {
-        const uint16_t *al = alog + (Q - (Q >> l)) + (c << (D - 1 - l));
-        const int h = 1 << l;
+        const int rb = 1 << (l % LOGV);  // register bit that pairs at this level
+        if (l < D - LOGV) {
+          // lane bit l <-> register bit rb: the lane with lane bit 0 keeps its
+          // slots with register bit 0 and trades the others with its partner
+          const bool lo = ((lane >> l) & 1) == 0;
 #pragma unroll
-        for (int it = 0; it < SIG / 64; it++) {
-          const int u = lane + 32 * it;
-          const int path = u & (h - 1), cpl = u >> l;
-          const int x = path + (cpl << (l + 1));
-          uint16_t a = V[x];
-          const uint16_t bb = V[x + h];
-          a ^= gf_mul_log<M>(gexp, al[cpl], glog[bb]);
-          V[x] = a;
-          V[x + h] = a ^ bb;
+          for (int j = 0; j < VPL; j++) {
+            if (j & rb) continue;
+#pragma unroll
+            for (int b = 0; b < M; b++) {
+              const uint32_t send = lo ? v[j | rb][b] : v[j][b];
+              const uint32_t got = __shfl_xor_sync(0xffffffffu, send, 1 << l);
+              if (lo) v[j | rb][b] = got;
+              else v[j][b] = got;
+            }
+          }
         }
-        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < VPL; j++) {
+          if (j & rb) continue;
+          const int xh = chunk_slot<D, LOGV>(l, lane, j) >> (l + 1);
+          const uint32_t *ap = abs_ + (((SIG - (SIG >> l)) + xh) * NH + h) * M;
+          uint32_t pr[M];
+          bs_mul<M>(pr, ap, v[j | rb]);
+#pragma unroll
+          for (int b = 0; b < M; b++) {
+            v[j][b] ^= pr[b];
+            v[j | rb][b] ^= v[j][b];
+          }
+        }
+      }
+      // zero planes -> roots; slot VPL * lane + j of chunk 32 h + k
+      uint32_t zero[VPL];
+#pragma unroll
+      for (int j = 0; j < VPL; j++) {
+        // read here, not hoisted out of the chunk loop (the root stores below
+        // may alias), so the per-plane masks are not held across it
+        const uint32_t frl = p::lead ? frlo[VPL * lane + j] : 0u;  // final mapping: slot VPL * lane + j
+        uint32_t nz = 0;
+#pragma unroll
+        for (int b = 0; b < M; b++) {
+          uint32_t w = v[j][b];
+          if (p::lead) w ^= fhbs[h * M + b] ^ (0u - ((frl >> b) & 1u));
+          nz |= w;
+        }
+        zero[j] = ~nz;
       }
 #pragma unroll
       for (int j = 0; j < VPL; j++) {
-        const int xl = lane + 32 * j;
-        const int elt = (c << D) | xl;
-        uint16_t v = V[xl];
-        if (p::lead) v ^= frhi[c] ^ frlo[xl];
-        bool hit = false;
-        if (v == 0) {
+        uint32_t z = zero[j];
+        while (z) {
+          const int k = __ffs(z) - 1;
+          z &= z - 1;
+          const int elt = ((32 * h + k) << D) | (VPL * lane + j);
           const uint32_t pos = key.invL[elt];
           if (pos < (uint32_t)p::n) {
-            hit = true;
+            weight++;
             atomicOr(&esm[pos >> 5], 1u << (pos & 31));
             const uint32_t slot = atomicAdd(cnt, 1u);
             if (slot < (uint32_t)T) roots[slot] = (pos << 16) | (uint32_t)elt;
           }
         }
-        weight += __popc(__ballot_sync(0xffffffffu, hit));
       }
-      __syncwarp();
     }
+    weight = __reduce_add_sync(0xffffffffu, weight);
+    __syncwarp();
 
     bool ok = (weight == T);
     if (ok) {

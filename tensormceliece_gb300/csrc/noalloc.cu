@@ -69,8 +69,10 @@ constexpr size_t kScratchBytes =
               cmax(DecScratch<2>::total(kMaxRequests), DecScratch<3>::total(kMaxRequests))),
          DecScratch<4>::total(kMaxRequests));
 
-// per-set field/FFT tables: exp (2q-1) | log (q) | alpha (q) | twist (2^(d+1)) | frob_lo (2^d) | frob_hi (2^(m-d))
-constexpr int kFieldSlot = 2 * 8192 + 8192 + 8192 + 256 + 128 + 64 + 64;
+// per-set field/FFT tables (u16 entries): exp (2q-1) | log (q) | twist (2^(d+1)) | frob_lo (2^d) |
+// bit-sliced alpha (2 (2^d - 1) 2 m) | bit-sliced frob_hi (2 * 2 m), u32 tables at even offsets
+constexpr int kFieldSlot = 2 * 8192 + 8192 + 256 + 128 + 2 * 127 * 2 * 13 + 2 * 2 * 13 + 16;
+static_assert(kFieldSlot % 2 == 0, "per-set slots must keep the u32 tables 4-byte aligned");
 
 }  // namespace
 
@@ -113,24 +115,30 @@ int device_setup(const DeviceSetup **out) {
     FftTables ft = build_fft_tables(S.m, S.fft_d);
     std::vector<uint16_t> all(kFieldSlot, 0);
     size_t o = 0;
+    bool fits = true;
     auto put = [&](const std::vector<uint16_t> &v) {
-      size_t at = o;
+      o += o & 1;  // u32 tables start 4-byte aligned
+      const size_t at = o;
+      if (o + v.size() > all.size()) {
+        fits = false;
+        return at;
+      }
       memcpy(all.data() + o, v.data(), v.size() * 2);
       o += v.size();
       return at;
     };
-    const size_t o_exp = put(F.exp), o_log = put(F.log), o_alpha = put(ft.alpha_log), o_twist = put(ft.twist_log),
-                 o_flo = put(ft.frob_lo), o_fhi = put(ft.frob_hi);
-    if (o > (size_t)kFieldSlot) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: field table slot too small");
+    const size_t o_exp = put(F.exp), o_log = put(F.log), o_twist = put(ft.twist_log), o_flo = put(ft.frob_lo),
+                 o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs);
+    if (!fits) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: field table slot too small");
     uint16_t *base = su.fields + (size_t)set * kFieldSlot;
     if (cudaMemcpy(base, all.data(), all.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess)
       return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: field table copy failed");
     su.fd[set].gexp = base + o_exp;
     su.fd[set].glog = base + o_log;
-    su.fd[set].fft_alpha_log = base + o_alpha;
     su.fd[set].fft_twist_log = base + o_twist;
     su.fd[set].frob_lo = base + o_flo;
-    su.fd[set].frob_hi = base + o_fhi;
+    su.fd[set].fft_alpha_bs = reinterpret_cast<const uint32_t *>(base + o_abs);
+    su.fd[set].frob_hi_bs = reinterpret_cast<const uint32_t *>(base + o_fhbs);
   }
   g_setups.push_back({dev, su});
   *out = &g_setups.back().second;
