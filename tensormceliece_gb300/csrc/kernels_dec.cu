@@ -50,19 +50,28 @@ __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, u
 
 // ---------------------------------------------------------------- BM
 // One warp per request (persistent grid). Coefficient i of C (connection
-// polynomial) and B lives in lane i%32, slot i/32. Only the GF(2^m) tables
-// sit in shared memory, so many warps share an SM.
+// polynomial) lives in lane i%32, slot i/32, as its normal value and its log.
+// B = x^s B' is kept unshifted: B' (the connection polynomial before the last
+// length change, as logs) sits in a per-warp shared array behind a guard of
+// 2t zero logs, so B_i is the entry at i - s and the per-iteration shift is
+// s += 1. The syndrome logs sit behind a 32-entry zero guard, so the
+// discrepancy reads s_{n-i} for every lane of an active slot without a
+// per-lane test (C_i = 0 above deg C). Coefficients above t are never
+// updated, as in the library's fixed-size arrays.
 // Degree bounds used to skip empty slots (exact, also for undecodable input):
-// before iteration n, deg C <= L and deg B <= n+1-L (B is the last connection
-// polynomial before a length change, pre-shifted), so the discrepancy needs
+// before iteration n, deg C <= L and deg B <= n+1-L, so the discrepancy needs
 // coefficients i <= min(L, t) and the update i <= min(max(L, n+1-L), t).
 template <int SET>
 struct BMLayout {
   using p = P<SET>;
-  static constexpr int Q = p::q;
+  static constexpr int Q = p::q, T = p::t;
+  static constexpr int NS = (T + 1 + 31) / 32;
   static constexpr int exp_off = 0, log_off = 2 * Q;
   static constexpr int shared_u16 = 3 * Q;
-  static constexpr int warp_u16 = 2 * p::t;  // log s_j
+  static constexpr int sguard = 32, bguard = 2 * T;
+  static constexpr int s_off = 0, s_len = sguard + 2 * T;          // per warp, u16
+  static constexpr int b_off = s_len, b_len = bguard + 32 * NS;
+  static constexpr int warp_u16 = (s_len + b_len + 1) & ~1;
   static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u16 * 2; }
 };
 
@@ -74,7 +83,7 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
   using LY = BMLayout<SET>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
   constexpr int ZL = GFLog<M>::zero_log;
-  constexpr int NS = (T + 1 + 31) / 32;
+  constexpr int NS = LY::NS;
   constexpr int NSY = (2 * T + 31) / 32;
   constexpr int SIG = 1 << D;
   extern __shared__ __align__(16) uint16_t bsm[];
@@ -82,9 +91,13 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
   uint16_t *glog = bsm + LY::log_off;
   for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
   for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint16_t *slog = bsm + LY::shared_u16 + warp * LY::warp_u16;
+  uint16_t *wsm = bsm + LY::shared_u16 + warp * LY::warp_u16;
+  uint16_t *slog = wsm + LY::s_off + LY::sguard;  // slog[-32 .. -1] = zero logs
+  uint16_t *blog = wsm + LY::b_off + LY::bguard;  // blog[-2t .. -1] = zero logs
+  for (int i = lane; i < LY::sguard; i += 32) wsm[LY::s_off + i] = (uint16_t)ZL;
+  for (int i = lane; i < LY::bguard; i += 32) wsm[LY::b_off + i] = (uint16_t)ZL;
+  __syncthreads();
   const long long N = seg_rows(segs);
   const long long nwarps = (long long)gridDim.x * kBMWarps;
   for (long long op = (long long)blockIdx.x * kBMWarps + warp; op < N; op += nwarps) {
@@ -101,18 +114,18 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
         slog[j] = glog[v & (Q - 1)];
       }
     }
+    // B' = 1, s = 1 (B = x)
+#pragma unroll
+    for (int k = 0; k < NS; k++) blog[lane + 32 * k] = (lane + 32 * k == 0) ? 0 : (uint16_t)ZL;
     __syncwarp();
-    // C in normal form plus its log (the discrepancy multiplies by s via
-    // logs); B only through its log (the update multiplies it by d/b).
-    uint16_t C[NS], lC[NS], lB[NS];
+    uint32_t C[NS], lC[NS];
 #pragma unroll
     for (int k = 0; k < NS; k++) {
       const int i = lane + 32 * k;
       C[k] = (i == 0);
       lC[k] = (i == 0) ? 0 : ZL;
-      lB[k] = (i == 1) ? 0 : ZL;
     }
-    int L = 0;
+    int L = 0, sft = 1;
     uint32_t lb = 0;  // log b, b = 1
 #pragma unroll 1
     for (int n = 0; n < 2 * T; n++) {
@@ -120,44 +133,42 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
       int bu = (L > n + 1 - L) ? L : n + 1 - L;           // update: i <= min(max(L, n+1-L), t)
       bu = bu < T ? bu : T;
       uint32_t dp = 0;
+      const uint16_t *sn = slog + n - lane;
 #pragma unroll
-      for (int k = 0; k < NS; k++) {
-        if (32 * k <= bd) {
-          const int i = lane + 32 * k;
-          if (i <= bd) dp ^= gf_mul_log<M>(gexp, lC[k], slog[n - i]);
-        }
-      }
-      const uint32_t d = warp_xor(dp);
+      for (int k = 0; k < NS; k++)
+        if (32 * k <= bd) dp ^= gf_mul_log<M>(gexp, lC[k], sn[-32 * k]);
+      const uint32_t d = __reduce_xor_sync(0xffffffffu, dp);
       if (d) {
         const bool upd = (n >= 2 * L);
         const int ld = glog[d];
         int lf = ld - (int)lb;
         if (lf < 0) lf += Q - 1;
+        const uint16_t *bs = blog + lane - sft;
+        uint32_t lco[NS];
 #pragma unroll
         for (int k = 0; k < NS; k++) {
+          lco[k] = lC[k];
           if (32 * k <= bu) {
-            const uint16_t lc_old = lC[k];
-            C[k] ^= gf_mul_log<M>(gexp, lf, lB[k]);
-            lC[k] = glog[C[k]];
-            if (upd) lB[k] = lc_old;
+            const uint32_t f = gf_mul_log<M>(gexp, lf, bs[32 * k]);
+            const bool in = (k < NS - 1) || (lane + 32 * k <= T);  // coefficients above t stay zero
+            if (in) {
+              C[k] ^= f;
+              lC[k] = glog[C[k]];
+            }
           }
         }
         if (upd) {
+          __syncwarp();  // every lane has read B' before it is replaced
+#pragma unroll
+          for (int k = 0; k < NS; k++)
+            if (32 * k <= bu) blog[lane + 32 * k] = (uint16_t)lco[k];
+          __syncwarp();
           L = n + 1 - L;
           lb = ld;
+          sft = 0;
         }
       }
-      // B <- x * B (coefficient i takes i-1; log of the new B_0 = 0 is the
-      // zero sentinel); slots above the bound stay zero. Descending slot
-      // order: slot k reads slot k-1 before that one shifts.
-#pragma unroll
-      for (int k = NS - 1; k >= 0; k--) {
-        if (32 * k <= bu + 1) {
-          const uint16_t up = (uint16_t)__shfl_up_sync(0xffffffffu, lB[k], 1);
-          const uint16_t wrap = (uint16_t)__shfl_sync(0xffffffffu, k ? lB[k ? k - 1 : 0] : ZL, 31);
-          lB[k] = lane ? up : (k ? wrap : (uint16_t)ZL);
-        }
-      }
+      sft++;
     }
     // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d)
     uint16_t *sig = Sig + op * SIG;
@@ -167,7 +178,7 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
     for (int k = 0; k < NS; k++) {
       const int i = lane + 32 * k;
       const int deg = T - i;
-      if (i <= T && deg < SIG) sig[deg] = C[k];
+      if (i <= T && deg < SIG) sig[deg] = (uint16_t)C[k];
     }
     __syncwarp();
   }
