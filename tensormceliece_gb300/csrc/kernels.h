@@ -58,7 +58,7 @@ constexpr int kGemmOpPad = 256;
 constexpr int kTcM = 128;
 constexpr int kTcN = 256;
 constexpr int kTcKB = 128;
-constexpr int kTcStages = 3;
+constexpr int kTcStages = 4;
 
 // Key matrices of the segments of a GEMM launch (same shape for all: one set).
 // A8: the key matrix pre-expanded to FP8 stage images (GEMM_TC only).

@@ -11,9 +11,13 @@
 //   X (request bits) is expanded to FP8 by the CUDA cores into the same
 //   canonical layout (no-swizzle K-major: 8-row x 16-byte core matrices,
 //   K-adjacent core matrices 128 B apart, row groups 1024 B apart).
-//   One thread issues 4 MMAs (K = 32 each) per 128-bit K stage and commits
-//   them to an mbarrier that releases the stage buffers. The epilogue reads
-//   the accumulators with tcgen05.ld and packs 32 parities per ballot.
+//   Warp roles: four expander warps write the X stages, one warp's lane 0
+//   issues the A copies, another's lane 0 issues 4 MMAs (K = 32 each) per
+//   128-bit K stage. Stages hand over through mbarriers only: A full (copy
+//   bytes landed), X full (128 expander arrivals), empty (the MMA commit that
+//   releases both buffers), so expansion, copies and MMAs of different stages
+//   overlap. The expander warps then read the accumulators with tcgen05.ld
+//   and pack 32 parities per ballot.
 //   Every wait is bounded (about 2 s of globaltimer); on expiry the CTA sets
 //   the error word, stops issuing, waits (bounded) for its own copies and
 //   MMAs, frees its tensor memory and returns.
@@ -129,11 +133,18 @@ __device__ __forceinline__ uint32_t expand4(uint32_t v) {
 }
 
 // ---------------------------------------------------------------- tcgen05 engine
-constexpr int TC_THREADS = 128;
+constexpr int TC_EXP_WARPS = 4;                           // X expanders, then the epilogue
+constexpr int TC_THREADS = (TC_EXP_WARPS + 2) * 32;       // + A producer warp + MMA warp
+constexpr int TC_EXP_THREADS = TC_EXP_WARPS * 32;
 constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
 constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
 constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 256;
 constexpr uint32_t TC_TMEM_COLS = kTcN;    // FP32 accumulator: 128 lanes x kTcN columns
+static_assert(TC_EXP_THREADS == kTcM, "one expander thread per accumulator lane");
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
 __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys, const Segs segs, int kstages,
                                                               const uint32_t *__restrict__ X, int ldx,
@@ -142,10 +153,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t *As = tsm;
   uint8_t *Xs = tsm + kTcStages * TC_A_BYTES;
-  uint64_t *bar_a = reinterpret_cast<uint64_t *>(Xs + kTcStages * TC_X_BYTES);
-  uint64_t *bar_mma = bar_a + kTcStages;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + kTcStages);
+  uint64_t *full_a = reinterpret_cast<uint64_t *>(Xs + kTcStages * TC_X_BYTES);
+  uint64_t *full_x = full_a + kTcStages;
+  uint64_t *empty = full_x + kTcStages;
+  uint64_t *done = empty + kTcStages;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  int *last_copy = reinterpret_cast<int *>(tmem_slot + 2);  // [kTcStages]: last stage copied per buffer
+  int *issued_sh = last_copy + kTcStages;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long op0 = (long long)blockIdx.x * kTcN;
@@ -155,10 +170,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   const long long live_end = segs.row0[seg] + segs.nreq[seg];
   if (tid == 0) {
     for (int i = 0; i < kTcStages; i++) {
-      mbar_init(&bar_a[i], 1);
-      mbar_init(&bar_mma[i], 1);
+      mbar_init(&full_a[i], 1);
+      mbar_init(&full_x[i], TC_EXP_THREADS);
+      mbar_init(&empty[i], 1);
+      last_copy[i] = -1;
     }
+    mbar_init(done, 1);
     *abort_flag = 0;
+    *issued_sh = 0;
     fence_mbar_init();
   }
   if (warp == 0) {
@@ -169,108 +188,115 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint8_t *Atile = A8 + (size_t)mtile * kstages * TC_A_BYTES;
   constexpr uint32_t idesc = idesc_f8f6f4_e4m3(kTcM, kTcN);
 
-  int issued = 0;  // stages whose MMAs were committed (thread 0's view)
-  int copies = 0;  // stages whose A copy was issued
-  // each thread expands whole 128-bit stage rows r = tid + 128 j (j < kTcN/128);
-  // the 16-byte loads for stage s+1 are issued before stage s is expanded
-  constexpr int RPT = kTcN / TC_THREADS;
-  uint4 xnext[RPT];
-  const uint32_t *xrow0 = X + (size_t)(op0 + tid) * ldx;
+  if (warp < TC_EXP_WARPS) {
+    // X expanders: thread tid writes whole 128-bit stage rows r = tid + 128 j;
+    // the 16-byte loads of stage s+1 are in flight while stage s is expanded
+    constexpr int RPT = kTcN / TC_EXP_THREADS;
+    uint4 xnext[RPT];
+    const uint32_t *xrow0 = X + (size_t)(op0 + tid) * ldx;
 #pragma unroll
-  for (int j = 0; j < RPT; j++) xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_THREADS * ldx);
-  for (int s = 0; s < kstages; s++) {
-    const int buf = s % kTcStages;
-    const uint32_t use = (uint32_t)(s / kTcStages);
-    bool ok = true;
-    if (s >= kTcStages) ok = mbar_wait(&bar_mma[buf], (use - 1) & 1);  // stage s-kTcStages released the buffers
-    if (!ok) *abort_flag = 1;
-    if (__syncthreads_or(*abort_flag)) break;
-    if (tid == 0) {
-      mbar_expect_tx(&bar_a[buf], TC_A_BYTES);
-      bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &bar_a[buf]);
-      copies = s + 1;
+    for (int j = 0; j < RPT; j++)
+      xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx);
+    for (int s = 0; s < kstages; s++) {
+      const int buf = s % kTcStages;
+      if (s >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(s / kTcStages - 1) & 1)) *abort_flag = 1;
+      if (*abort_flag) break;
+      uint4 xcur[RPT];
+#pragma unroll
+      for (int j = 0; j < RPT; j++) xcur[j] = xnext[j];
+      if (s + 1 < kstages) {
+#pragma unroll
+        for (int j = 0; j < RPT; j++)
+          xnext[j] =
+              *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx + 4 * (s + 1));
+      }
+      // request bits -> FP8 core matrices (row r, 16-bit chunk kc at
+      // ((r/8)*8 + kc)*128 + (r%8)*16)
+      uint8_t *xb = Xs + buf * TC_X_BYTES;
+#pragma unroll
+      for (int j = 0; j < RPT; j++) {
+        const int r = tid + j * TC_EXP_THREADS;
+        const uint32_t wv[4] = {xcur[j].x, xcur[j].y, xcur[j].z, xcur[j].w};
+        uint8_t *rb = xb + (r >> 3) * 1024 + (r & 7) * 16;
+#pragma unroll
+        for (int kc = 0; kc < 8; kc++) {
+          const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
+          uint4 v;
+          v.x = expand4(bits & 0xFu);
+          v.y = expand4((bits >> 4) & 0xFu);
+          v.z = expand4((bits >> 8) & 0xFu);
+          v.w = expand4((bits >> 12) & 0xFu);
+          *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
+        }
+      }
+      fence_proxy_async();  // generic-proxy writes visible to the tensor core
+      mbar_arrive(&full_x[buf]);
     }
-    // request bits -> FP8 core matrices (row r, 16-bit chunk kc at
-    // ((r/8)*8 + kc)*128 + (r%8)*16)
-    uint8_t *xb = Xs + buf * TC_X_BYTES;
-    uint4 xcur[RPT];
-#pragma unroll
-    for (int j = 0; j < RPT; j++) xcur[j] = xnext[j];
-    if (s + 1 < kstages) {
-#pragma unroll
-      for (int j = 0; j < RPT; j++)
-        xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_THREADS * ldx + 4 * (s + 1));
-    }
-#pragma unroll
-    for (int j = 0; j < RPT; j++) {
-      const int r = tid + j * TC_THREADS;
-      const uint32_t wv[4] = {xcur[j].x, xcur[j].y, xcur[j].z, xcur[j].w};
-      uint8_t *rb = xb + (r >> 3) * 1024 + (r & 7) * 16;
-#pragma unroll
-      for (int kc = 0; kc < 8; kc++) {
-        const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
-        uint4 v;
-        v.x = expand4(bits & 0xFu);
-        v.y = expand4((bits >> 4) & 0xFu);
-        v.z = expand4((bits >> 8) & 0xFu);
-        v.w = expand4((bits >> 12) & 0xFu);
-        *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
+  } else if (warp == TC_EXP_WARPS) {
+    if (lane == 0) {  // A producer: one bulk copy per stage into a free buffer
+      const uint8_t *Atile = A8 + (size_t)mtile * kstages * TC_A_BYTES;
+      for (int s = 0; s < kstages; s++) {
+        const int buf = s % kTcStages;
+        if (s >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(s / kTcStages - 1) & 1)) *abort_flag = 1;
+        if (*abort_flag) break;
+        mbar_expect_tx(&full_a[buf], TC_A_BYTES);
+        bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &full_a[buf]);
+        last_copy[buf] = s;
       }
     }
-    fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      if (!mbar_wait(&bar_a[buf], use & 1)) {
-        *abort_flag = 1;
-      } else {
+  } else {
+    if (lane == 0) {  // MMA issuer
+      int issued = 0;
+      for (int s = 0; s < kstages; s++) {
+        const int buf = s % kTcStages;
+        const uint32_t par = (uint32_t)(s / kTcStages) & 1;
+        if (!mbar_wait(&full_a[buf], par) || !mbar_wait(&full_x[buf], par)) *abort_flag = 1;
+        if (*abort_flag) break;
         tc_fence_after();
-        const uint32_t a0 = smem_u32(As + buf * TC_A_BYTES), x0 = smem_u32(xb);
+        const uint32_t a0 = smem_u32(As + buf * TC_A_BYTES), x0 = smem_u32(Xs + buf * TC_X_BYTES);
 #pragma unroll
         for (int kk = 0; kk < kTcKB / 32; kk++) {
           const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
           const uint64_t bd = smem_desc(x0 + kk * 256, 128, 1024);
           mma_f8(tmem, ad, bd, idesc, (s > 0 || kk > 0) ? 1u : 0u);
         }
-        mma_commit(&bar_mma[buf]);
+        mma_commit(&empty[buf]);
         issued = s + 1;
       }
+      mma_commit(done);  // arrives once every MMA issued above has completed
+      *issued_sh = issued;
     }
   }
-  // drain: the last committed stage completes after all earlier MMAs
-  __shared__ int last_issued, last_copy;
-  if (tid == 0) { last_issued = issued; last_copy = copies; }
   __syncthreads();
-  bool ok = true;
-  if (last_issued > 0) {
-    const int s = last_issued - 1;
-    ok = mbar_wait(&bar_mma[s % kTcStages], (uint32_t)(s / kTcStages) & 1);
+  // drain: the MMAs (done barrier) and any A copy still landing
+  bool ok = mbar_wait(done, 0);
+  if (warp == TC_EXP_WARPS && lane == 0) {
+    for (int b = 0; b < kTcStages; b++)
+      if (last_copy[b] >= 0 && !mbar_wait(&full_a[b], (uint32_t)(last_copy[b] / kTcStages) & 1)) ok = false;
   }
-  if (tid == 0 && last_copy > last_issued) {  // a copy issued without its MMAs (abort): let it land
-    const int s = last_copy - 1;
-    mbar_wait(&bar_a[s % kTcStages], (uint32_t)(s / kTcStages) & 1);
-  }
-  const int good = __syncthreads_and(ok && !*abort_flag && last_issued == kstages);
+  const int good = __syncthreads_and(ok && !*abort_flag && *issued_sh == kstages);
   tc_fence_after();
   if (good) {
-    // epilogue: warp w owns accumulator lanes (rows) 32w..32w+31
+    if (warp < TC_EXP_WARPS) {
+      // epilogue: warp w owns accumulator lanes (rows) 32w..32w+31
 #pragma unroll 1
-    for (int cb = 0; cb < kTcN / 32; cb++) {
-      uint32_t r[32];
-      GMC_TMEM_LD32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * cb), r);
-      tmem_ld_wait();
-      uint32_t mine = 0;
+      for (int cb = 0; cb < kTcN / 32; cb++) {
+        uint32_t r[32];
+        GMC_TMEM_LD32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * cb), r);
+        tmem_ld_wait();
+        uint32_t mine = 0;
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const uint32_t par = (uint32_t)__float2int_rz(__uint_as_float(r[j])) & 1u;
-        const uint32_t word = __ballot_sync(0xffffffffu, par);
-        if (lane == j) mine = word;
+        for (int j = 0; j < 32; j++) {
+          const uint32_t par = (uint32_t)__float2int_rz(__uint_as_float(r[j])) & 1u;
+          const uint32_t word = __ballot_sync(0xffffffffu, par);
+          if (lane == j) mine = word;
+        }
+        const long long op = op0 + 32 * cb + lane;
+        const int wd = mtile * (kTcM / 32) + warp;
+        if (op < live_end && wd < out_words) Out[op * ldo + wd] = mine;
       }
-      const long long op = op0 + 32 * cb + lane;
-      const int wd = mtile * (kTcM / 32) + warp;
-      if (op < live_end && wd < out_words) Out[op * ldo + wd] = mine;
     }
   } else if (tid == 0) {
     atomicExch(err, 1);
