@@ -8,7 +8,7 @@ namespace gmc {
 
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
-constexpr int kBMWarps = 16;    // Berlekamp-Massey kernel: warps per block
+constexpr int kBMWarps = 24;    // Berlekamp-Massey kernel: warps per block
 constexpr int kRootWarps = 8;  // root-finding kernel: warps per block
 
 // ---------------------------------------------------------------- segments
@@ -86,9 +86,12 @@ Segs one_segment(long long n);
 // Encapsulation: seeds / C / K rows in padded row space; E, Ens, S have
 // seg_rows(segs) rows. pk_bad_mask bit s: segment s's public key has
 // nonzero padding bits (6960119), its c and K are zeroed.
+// counter: 4 bytes of device scratch (zeroed here, on st) that nothing else
+// touches until the sampler ends; the pipelines lend the first word of the
+// syndrome buffer, which only the following GEMM writes.
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
-                          int threads, cudaStream_t st);
+                          int threads, unsigned int *counter, cudaStream_t st);
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
                             const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st);
@@ -111,6 +114,7 @@ struct FieldDev {
   // bit-sliced over 32 chunks per word (bit k: chunk 32 h + k), plane b = bit b
   const uint32_t *fft_alpha_bs;   // [(2^d - 2^(d-l) + xh) * H + h][m]: alpha_{l, (c << (d-1-l)) + xh}
   const uint32_t *frob_hi_bs;     // [h][m]: (c 2^d)^(2^d)
+  const uint16_t *zech;           // [q]: log(1 + g^k), zech[0] = 3q (zero)
 };
 
 // Per-key decapsulation tables of the segments of a launch.

@@ -50,7 +50,10 @@ __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, u
 
 // ---------------------------------------------------------------- BM
 // One warp per request (persistent grid). Coefficient i of C (connection
-// polynomial) lives in lane i%32, slot i/32, as its normal value and its log.
+// polynomial) lives in lane i%32, slot i/32, as its log only: the update
+// C_i += f B_i is done in the log domain with Zech logarithms,
+// log(a + b) = log a + zech(log b - log a), one table lookup instead of an
+// antilog and a log. Any log at or above the zero sentinel 2q-2 means 0.
 // B = x^s B' is kept unshifted: B' (the connection polynomial before the last
 // length change, as logs) sits in a per-warp shared array behind a guard of
 // 2t zero logs, so B_i is the entry at i - s and the per-iteration shift is
@@ -66,8 +69,8 @@ struct BMLayout {
   using p = P<SET>;
   static constexpr int Q = p::q, T = p::t;
   static constexpr int NS = (T + 1 + 31) / 32;
-  static constexpr int exp_off = 0, log_off = 2 * Q;
-  static constexpr int shared_u16 = 3 * Q;
+  static constexpr int exp_off = 0, log_off = 2 * Q, zech_off = 3 * Q;
+  static constexpr int shared_u16 = 4 * Q;
   static constexpr int sguard = 32, bguard = 2 * T;
   static constexpr int s_off = 0, s_len = sguard + 2 * T;          // per warp, u16
   static constexpr int b_off = s_len, b_len = bguard + 32 * NS;
@@ -76,7 +79,7 @@ struct BMLayout {
 };
 
 template <int SET>
-__global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
+__global__ void __launch_bounds__(kBMWarps * 32, 2) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
                                                                   FieldDev fd, const Segs segs,
                                                                   uint16_t *__restrict__ Sig) {
   using p = P<SET>;
@@ -89,8 +92,12 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
   extern __shared__ __align__(16) uint16_t bsm[];
   uint16_t *gexp = bsm + LY::exp_off;
   uint16_t *glog = bsm + LY::log_off;
+  uint16_t *zech = bsm + LY::zech_off;
   for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
-  for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) {
+    glog[i] = fd.glog[i];
+    zech[i] = fd.zech[i];
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint16_t *wsm = bsm + LY::shared_u16 + warp * LY::warp_u16;
   uint16_t *slog = wsm + LY::s_off + LY::sguard;  // slog[-32 .. -1] = zero logs
@@ -118,13 +125,9 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
 #pragma unroll
     for (int k = 0; k < NS; k++) blog[lane + 32 * k] = (lane + 32 * k == 0) ? 0 : (uint16_t)ZL;
     __syncwarp();
-    uint32_t C[NS], lC[NS];
+    uint32_t lC[NS];
 #pragma unroll
-    for (int k = 0; k < NS; k++) {
-      const int i = lane + 32 * k;
-      C[k] = (i == 0);
-      lC[k] = (i == 0) ? 0 : ZL;
-    }
+    for (int k = 0; k < NS; k++) lC[k] = (lane + 32 * k == 0) ? 0 : ZL;
     int L = 0, sft = 1;
     uint32_t lb = 0;  // log b, b = 1
 #pragma unroll 1
@@ -149,12 +152,20 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
         for (int k = 0; k < NS; k++) {
           lco[k] = lC[k];
           if (32 * k <= bu) {
-            const uint32_t f = gf_mul_log<M>(gexp, lf, bs[32 * k]);
+            // log(C_i + f B_i): p = log(f B_i); zero B_i keeps C_i, zero C_i takes p
+            constexpr uint32_t Q1 = Q - 1;
+            const uint32_t lbi = bs[32 * k], lc = lC[k];
+            uint32_t pl = (uint32_t)lf + lbi;
+            pl = min(pl, pl - Q1);                      // < q-1 when B_i != 0
+            uint32_t kk = pl - lc;                      // log(f B_i / C_i) mod q-1
+            kk = min(kk + Q1, kk);
+            const uint32_t z = zech[min(kk, Q1 - 1)];   // index clamped for the zero cases
+            uint32_t nl = lc + z;
+            nl = min(nl, nl - Q1);                      // >= 2q-2 when the sum is 0
+            nl = (lc >= (uint32_t)ZL) ? pl : nl;
+            nl = (lbi >= (uint32_t)ZL) ? lc : nl;
             const bool in = (k < NS - 1) || (lane + 32 * k <= T);  // coefficients above t stay zero
-            if (in) {
-              C[k] ^= f;
-              lC[k] = glog[C[k]];
-            }
+            if (in) lC[k] = nl;
           }
         }
         if (upd) {
@@ -170,7 +181,8 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
       }
       sft++;
     }
-    // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d)
+    // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d);
+    // coefficients are < 2^m <= 2^13, so bit 15 is free for the length flag
     uint16_t *sig = Sig + op * SIG;
     for (int x = lane; x < SIG; x += 32)
       if (x > T) sig[x] = 0;
@@ -178,7 +190,9 @@ __global__ void __launch_bounds__(kBMWarps * 32, 3) dec_bm_kernel(const uint32_t
     for (int k = 0; k < NS; k++) {
       const int i = lane + 32 * k;
       const int deg = T - i;
-      if (i <= T && deg < SIG) sig[deg] = (uint16_t)C[k];
+      // bit 15 of the constant coefficient flags a final length L > t
+      const uint32_t c = gexp[min(lC[k], (uint32_t)ZL)];
+      if (i <= T && deg < SIG) sig[deg] = (uint16_t)(c | ((deg == 0 && L > T) ? 0x8000u : 0u));
     }
     __syncwarp();
   }
@@ -217,10 +231,9 @@ struct RootLayout {
   static constexpr int fhbs_off = abs_off + abs_len, fhbs_len = NH * M;
   static constexpr int shared_u32 = fhbs_off + fhbs_len;
   static constexpr int ewp = (p::ew + 1) & ~1;
-  // per warp (u32): e words | roots [t] (pos << 16 | element) | count | V[SIG] u16 | s[2t] u16
+  // per warp (u32): e words | roots [t] (pos << 16 | element) | count | V[SIG] u16
   static constexpr int roots_off = ewp, cnt_off = roots_off + p::t, v_off = cnt_off + 2;
-  static constexpr int s_off = v_off + SIG / 2;
-  static constexpr int warp_u32 = s_off + p::t;
+  static constexpr int warp_u32 = v_off + SIG / 2;
   static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
 };
 
@@ -277,7 +290,6 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   using p = P<SET>;
   using LY = RootLayout<SET>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d, SIG = LY::SIG, NH = LY::NH;
-  constexpr int NSY = (2 * T + 31) / 32;
   constexpr int NW = (p::n + 31) / 32;
   constexpr int VPL = SIG / 32;  // chunk slots per lane
   constexpr int LOGV = (VPL == 4) ? 2 : 1;
@@ -305,7 +317,6 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   uint32_t *roots = wbase + LY::roots_off;
   uint32_t *cnt = wbase + LY::cnt_off;
   uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::v_off);
-  uint16_t *ssm = reinterpret_cast<uint16_t *>(wbase + LY::s_off);
 
   const long long N = seg_rows(segs);
   const long long nwarps = (long long)gridDim.x * kRootWarps;
@@ -314,7 +325,8 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
     const DecKeyDev &key = keys.k[seg];
     const uint16_t *sig = Sig + op * SIG;
-    for (int x = lane; x < SIG; x += 32) V[x] = sig[x];
+    const bool long_lfsr = (sig[0] >> 15) != 0;  // BM ended with L > t
+    for (int x = lane; x < SIG; x += 32) V[x] = sig[x] & 0x7FFFu;
     for (int w = lane; w < NW; w += 32) esm[w] = 0;
     if (lane == 0) *cnt = 0;
     __syncwarp();
@@ -429,51 +441,71 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     weight = __reduce_add_sync(0xffffffffu, weight);
     __syncwarp();
 
-    bool ok = (weight == T);
+    // Accept when the t roots lie in the support, BM's length is <= t and the
+    // first t syndromes of the found error equal the received ones. That is
+    // the library's full 2t-syndrome check: with L <= t, the connection
+    // polynomial C (sigma reversed) annihilates the received sequence from
+    // index t on, and also the found error's sequence sum_i w2_i L_i^j (sigma
+    // vanishes at every L_i), so the two sequences agree iff their first t
+    // terms do. With L > t no error of weight <= t has these syndromes (its
+    // locator would be a shorter LFSR), so the library's check fails as well.
+    bool ok = (weight == T) && !long_lfsr;
     if (ok) {
-      // received syndromes (m bits each) of this request
+      constexpr int NSC = (T + 31) / 32;
+      // received syndromes j = lane + 32k < t (m bits each)
       const uint32_t *srow = S2 + op * lds2;
+      uint32_t sr[NSC];
 #pragma unroll
-      for (int k = 0; k < NSY; k++) {
+      for (int k = 0; k < NSC; k++) {
         const int j = lane + 32 * k;
-        if (j < 2 * T) {
+        sr[k] = 0;
+        if (j < T) {
           const int b = j * M, w = b >> 5, sh = b & 31;
           uint32_t v = srow[w] >> sh;
           if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
-          ssm[j] = (uint16_t)(v & (Q - 1));
+          sr[k] = v & (Q - 1);
         }
       }
-      // syndromes of the found error: sum over roots of w2_i L_i^j
-      uint32_t sc[NSY];
+      // per root: log w2_i (key table, global) and log L_i, fetched by all
+      // lanes at once and stored back over the root list as lw << 16 | ll
+      // (ll = 0xFFFF for L_i = 0)
 #pragma unroll
-      for (int k = 0; k < NSY; k++) sc[k] = 0;
-#pragma unroll 1
+      for (int k = 0; k < NSC; k++) {
+        const int r = lane + 32 * k;
+        if (r < T) {
+          const uint32_t rv = roots[r];
+          const int elt = rv & 0xFFFF, pos = rv >> 16;
+          const uint32_t lw = key.LW2[pos];
+          roots[r] = (lw << 16) | (elt ? glog[elt] : 0xFFFFu);
+        }
+      }
+      __syncwarp();
+      // syndromes of the found error: sum over roots of w2_i L_i^j
+      uint32_t sc[NSC];
+#pragma unroll
+      for (int k = 0; k < NSC; k++) sc[k] = 0;
+#pragma unroll 4
       for (int r = 0; r < T; r++) {
         const uint32_t rv = roots[r];
-        const int elt = rv & 0xFFFF, pos = rv >> 16;
-        const int lw = key.LW2[pos];
-        if (elt == 0) {  // L_i = 0 contributes only to s_0
+        const int lw = rv >> 16, ll = rv & 0xFFFF;
+        if (ll == 0xFFFF) {  // L_i = 0 contributes only to s_0
           if (lane == 0) sc[0] ^= gexp[lw];
         } else {
-          const int ll = glog[elt];
           // log(w2_i L_i^j) for j = lane + 32k, stepping by 32 log L_i mod 2^m - 1
           int idx = fold_mod<M>(lw + lane * ll);
           const int step = fold_mod<M>(32 * ll);
 #pragma unroll
-          for (int k = 0; k < NSY; k++) {
+          for (int k = 0; k < NSC; k++) {
             sc[k] ^= gexp[idx];
             idx += step;
             idx = idx >= Q - 1 ? idx - (Q - 1) : idx;
           }
         }
       }
-      __syncwarp();
       bool mism = false;
 #pragma unroll
-      for (int k = 0; k < NSY; k++) {
-        const int j = lane + 32 * k;
-        if (j < 2 * T && sc[k] != ssm[j]) mism = true;
-      }
+      for (int k = 0; k < NSC; k++)
+        if (lane + 32 * k < T && sc[k] != sr[k]) mism = true;
       ok = !__any_sync(0xffffffffu, mism);
     }
     uint32_t *erow = E + op * lde;

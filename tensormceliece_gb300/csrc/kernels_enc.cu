@@ -1,4 +1,4 @@
-// Encapsulation kernels: fixed-weight sampling (thread per request) and the
+// Encapsulation kernels: fixed-weight sampling (lane per request) and the
 // finalize step (ciphertext assembly + session-key hash).
 //
 // Reference behaviour: gen_e / syndrome / operation_enc of libmceliece
@@ -10,45 +10,91 @@
 namespace gmc {
 
 // ---------------------------------------------------------------- sampling
-// One thread per request. Randomness is the per-request seed chain:
-// attempt j draws SHAKE256({64} || state, cand_bytes) and the next state is
-// the first 32 bytes of that draw. Candidates are little-endian 16-bit words
-// masked to m bits; for n < 2^m the first t values below n are kept, else all
-// t. A repeated position rejects the attempt. Duplicate detection uses a
-// per-thread n-bit bitmap in shared memory (equivalent to the library's
-// sort-and-compare: only the set of positions matters). The bitmap is the
-// error vector e itself and is written out with the block's coalesced store.
+// Randomness is the per-request seed chain: attempt j draws
+// SHAKE256({64} || state, cand_bytes) and the next state is the first 32
+// bytes of that draw. Candidates are little-endian 16-bit words masked to m
+// bits; for n < 2^m the first t values below n are kept, else all t. A
+// repeated position rejects the attempt (only the set of positions matters,
+// as in the library's sort-and-compare).
+// Work split: each lane owns one request and runs its Keccak chain; lanes
+// take requests from a launch-wide counter whenever their previous request
+// is done, so a request that needs many attempts does not hold the warp's
+// other lanes idle. After every attempt the warp checks, one lane's
+// candidates at a time, for repeats with a single n-bit bitmap per warp
+// (atomicOr returns the previous word); on success that bitmap is the error
+// vector e, written out by the whole warp (coalesced) together with e[mt:n]
+// shifted to bit 0 (the syndrome GEMM operand). Only the touched bitmap
+// words are cleared.
+template <int SET>
+struct SampleLayout {
+  using p = P<SET>;
+  static constexpr int bm_words = (p::ew + 1) & ~1;
+  static constexpr int cand_u16 = 32 * p::t;  // candidate c of lane l at c*32 + (l ^ 2(c%16))
+  static constexpr int warp_bytes = bm_words * 4 + cand_u16 * 2;
+};
+
+__device__ __forceinline__ int cand_slot(int c, int l) { return c * 32 + (l ^ ((c & 15) << 1)); }
+
 template <int SET>
 __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t *__restrict__ seeds, const Segs segs,
                                                                 uint32_t *__restrict__ E, int lde,
-                                                                uint32_t *__restrict__ Ens, int ldx) {
+                                                                uint32_t *__restrict__ Ens, int ldx,
+                                                                unsigned int *__restrict__ counter) {
   using p = P<SET>;
-  constexpr int EWS = p::ew | 1;  // odd stride: bitmaps of neighbouring threads start in different banks
-  extern __shared__ uint32_t sm[];
-  uint32_t *bm = sm + threadIdx.x * EWS;
+  using LY = SampleLayout<SET>;
+  constexpr int NCW = (p::t + 31) / 32;
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *bm = sm + warp * (LY::warp_bytes / 4);
+  uint16_t *cand = reinterpret_cast<uint16_t *>(bm + LY::bm_words);
+  for (int w = lane; w < LY::bm_words; w += 32) bm[w] = 0;
+  __syncwarp();
   const long long N = seg_rows(segs);
-  const long long op0 = (long long)blockIdx.x * blockDim.x;
-  const long long op = op0 + threadIdx.x;
-  int seg;
-  const bool live = seg_live(segs, op, &seg);
-
-  for (int w = 0; w < p::ew; w++) bm[w] = 0;
-
-  if (live) {
-    uint64_t st[4];
-    const uint8_t *sd = seeds + 32 * op;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-      uint64_t v = 0;
-#pragma unroll
-      for (int b = 0; b < 8; b++) v |= (uint64_t)sd[8 * i + b] << (8 * b);
-      st[i] = v;
-    }
-    constexpr int ncand = p::cand_bytes / 2;     // 16-bit candidates per attempt
-    constexpr int nlanes = (ncand + 3) / 4;      // output lanes holding them
-    constexpr uint32_t mask = p::q - 1;
+  bool has = false, exhausted = false;
+  long long op = 0;
+  uint64_t st[4] = {0, 0, 0, 0};
+  constexpr int ncand = p::cand_bytes / 2;  // 16-bit candidates per attempt
+  constexpr int nlanes = (ncand + 3) / 4;   // output lanes holding them
+  constexpr uint32_t mask = p::q - 1;
+  constexpr int sh = p::mt % 32, w0 = p::mt / 32;
 #pragma unroll 1
-    for (int attempt = 0; attempt < 1000000; attempt++) {
+  while (true) {
+    // lanes without a request take the next ones (rows that are segment gaps are skipped)
+    const uint32_t need = __ballot_sync(0xffffffffu, !has && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned int base = 0;
+      if (lane == leader) base = atomicAdd(counter, (unsigned int)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if ((need >> lane) & 1) {
+        const long long idx = (long long)base + __popc(need & ((1u << lane) - 1));
+        if (idx >= N) {
+          exhausted = true;
+        } else {
+          int seg;
+          op = idx;
+          has = seg_live(segs, idx, &seg);
+          if (has) {
+            const uint8_t *sd = seeds + 32 * idx;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+              uint64_t v = 0;
+#pragma unroll
+              for (int b = 0; b < 8; b++) v |= (uint64_t)sd[8 * i + b] << (8 * b);
+              st[i] = v;
+            }
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, has)) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    // one attempt per lane that holds a request
+    int count = 0;
+    uint64_t nst[4] = {0, 0, 0, 0};
+    if (has) {
       uint64_t s[25];
 #pragma unroll
       for (int i = 0; i < 25; i++) s[i] = 0;
@@ -59,53 +105,80 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
       s[4] = (st[3] >> 56) | (0x1Full << 8);
       s[16] = 0x8000000000000000ull;
       keccak_f1600(s);
-      uint64_t nst[4] = {s[0], s[1], s[2], s[3]};
-      int count = 0;
-      bool bad = false;
+      nst[0] = s[0];
+      nst[1] = s[1];
+      nst[2] = s[2];
+      nst[3] = s[3];
 #pragma unroll 1
-      for (int base = 0; base < nlanes && count < p::t && !bad; base += 17) {
+      for (int base = 0; base < nlanes && count < p::t; base += 17) {
         if (base) keccak_f1600(s);
 #pragma unroll
         for (int i = 0; i < 17; i++) {
           if (base + i < nlanes) {
-            uint64_t l = s[i];
+            const uint64_t l = s[i];
 #pragma unroll
             for (int h = 0; h < 4; h++) {
-              uint32_t v = (uint32_t)(l >> (16 * h)) & mask;
-              bool take = (4 * (base + i) + h < ncand) && (count < p::t) && !bad &&
-                          (p::full || v < (uint32_t)p::n);
+              const uint32_t v = (uint32_t)(l >> (16 * h)) & mask;
+              const bool take = (4 * (base + i) + h < ncand) && (count < p::t) && (p::full || v < (uint32_t)p::n);
               if (take) {
-                uint32_t word = bm[v >> 5], bit = 1u << (v & 31);
-                if (word & bit) bad = true;
-                else { bm[v >> 5] = word | bit; count++; }
+                cand[cand_slot(count, lane)] = (uint16_t)v;
+                count++;
               }
             }
           }
         }
       }
-      if (!bad && count == p::t) break;
-      for (int w = 0; w < p::ew; w++) bm[w] = 0;
-      st[0] = nst[0]; st[1] = nst[1]; st[2] = nst[2]; st[3] = nst[3];
     }
-  }
-  __shared__ unsigned char live_rows[kSampleThreadsMax];
-  live_rows[threadIdx.x] = live;
-  __syncthreads();
-  // coalesced copy-out of the block's error vectors, and of e[mt:n] shifted
-  // to bit 0 (the GEMM operand); rows past a segment's live requests are skipped
-  const int nthreads = blockDim.x;
-  const long long nops = (N - op0) < nthreads ? (N - op0) : nthreads;
-  for (long long idx = threadIdx.x; idx < nops * p::ew; idx += nthreads) {
-    int r = (int)(idx / p::ew), w = (int)(idx % p::ew);
-    if (live_rows[r]) E[(op0 + r) * lde + w] = sm[r * EWS + w];
-  }
-  constexpr int sh = p::mt % 32, w0 = p::mt / 32;
-  for (long long idx = threadIdx.x; idx < nops * p::kw; idx += nthreads) {
-    int r = (int)(idx / p::kw), w = (int)(idx % p::kw);
-    if (!live_rows[r]) continue;
-    uint32_t lo = sm[r * EWS + w0 + w];
-    uint32_t hi = (w0 + w + 1 < p::ew) ? sm[r * EWS + w0 + w + 1] : 0u;
-    Ens[(op0 + r) * ldx + w] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
+    __syncwarp();
+    // repeats, one lane's candidate set at a time
+    uint32_t pend = __ballot_sync(0xffffffffu, has && count == p::t);
+    uint32_t okmask = 0;
+#pragma unroll 1
+    while (pend) {
+      const int r = __ffs(pend) - 1;
+      pend &= pend - 1;
+      uint32_t vv[NCW];
+      bool dup = false;
+#pragma unroll
+      for (int i = 0; i < NCW; i++) {
+        const int c = lane + 32 * i;
+        vv[i] = 0xFFFFFFFFu;
+        if (c < p::t) {
+          const uint32_t v = cand[cand_slot(c, r)];
+          vv[i] = v;
+          const uint32_t bit = 1u << (v & 31);
+          dup |= (atomicOr(&bm[v >> 5], bit) & bit) != 0;
+        }
+      }
+      const bool anydup = __any_sync(0xffffffffu, dup);
+      const long long opr = __shfl_sync(0xffffffffu, op, r);
+      if (!anydup) {
+        okmask |= 1u << r;
+        uint32_t *erow = E + opr * lde;
+        for (int w = lane; w < p::ew; w += 32) erow[w] = bm[w];
+        uint32_t *xrow = Ens + opr * ldx;
+        for (int w = lane; w < p::kw; w += 32) {
+          const uint32_t lo = bm[w0 + w];
+          const uint32_t hi = (w0 + w + 1 < p::ew) ? bm[w0 + w + 1] : 0u;
+          xrow[w] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NCW; i++)
+        if (vv[i] != 0xFFFFFFFFu) bm[vv[i] >> 5] = 0;
+      __syncwarp();
+    }
+    if (has) {
+      if ((okmask >> lane) & 1) {
+        has = false;
+      } else {
+        st[0] = nst[0];
+        st[1] = nst[1];
+        st[2] = nst[2];
+        st[3] = nst[3];
+      }
+    }
   }
 }
 
@@ -177,20 +250,25 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
 
 // ---------------------------------------------------------------- launchers
 template <int SET>
-static int sample_smem_bytes(int threads) { return threads * (P<SET>::ew | 1) * 4; }
-
-template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
-                          int threads, cudaStream_t st) {
+                          int threads, unsigned int *counter, cudaStream_t st) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
-  if (threads != 32 && threads != 64 && threads != 128) return cudaErrorInvalidValue;
-  const int smem = sample_smem_bytes<SET>(threads);
+  if ((threads != 32 && threads != 64 && threads != 128) || !counter) return cudaErrorInvalidValue;
+  const int smem = (threads / 32) * SampleLayout<SET>::warp_bytes;
   cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         sample_smem_bytes<SET>(kSampleThreadsMax));
+                                         (kSampleThreadsMax / 32) * SampleLayout<SET>::warp_bytes);
   if (err != cudaSuccess) return err;
-  long long blocks = (N + threads - 1) / threads;
-  sample_kernel<SET><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx);
+  if ((err = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st)) != cudaSuccess) return err;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sample_kernel<SET>, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  const long long need = (N + threads - 1) / threads;
+  const long long resident = (long long)sms * per_sm;
+  const long long blocks = need < resident ? need : resident;
+  sample_kernel<SET><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx, counter);
   return cudaGetLastError();
 }
 
@@ -206,7 +284,7 @@ cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int l
 
 #define GMC_INST_ENC(SET)                                                                                        \
   template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int, int,  \
-                                          cudaStream_t);                                                         \
+                                          unsigned int *, cudaStream_t);                                         \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
                                             const Segs &, uint32_t, cudaStream_t);
 GMC_INST_ENC(0)

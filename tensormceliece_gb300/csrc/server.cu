@@ -147,7 +147,8 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp) {
     uint32_t bad = 0;
     for (size_t i = 0; i < pp.keys.size(); i++)
       if (pp.keys[i]->pad_bad) bad |= 1u << i;
-    cudaError_t e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, tune.sample_threads, sl.st);
+    cudaError_t e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, tune.sample_threads,
+                                       reinterpret_cast<unsigned int *>(Sy), sl.st);
     if (e == cudaSuccess)
       e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->lda, ref->rows_pad, Ens, kw, ref->kw_pad, Sy, mw, p::mw,
                               tc_err_word_ptr(), sl.st);
