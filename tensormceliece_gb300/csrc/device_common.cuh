@@ -119,6 +119,36 @@ __device__ __forceinline__ void shake256_32(uint64_t out[4], LaneFn lane) {
   for (int i = 0; i < 4; i++) out[i] = s[i];
 }
 
+// ---------------------------------------------------------------- KEM hash preimage
+// 8 bytes of a little-endian word stream from byte offset off >= 0.
+template <typename WordFn>
+__device__ __forceinline__ uint64_t stream_u64(WordFn word, int off) {
+  const int w = off >> 2, sh = 8 * (off & 3);
+  uint64_t v = (uint64_t)word(w) | ((uint64_t)word(w + 1) << 32);
+  if (sh) v = (v >> sh) | ((uint64_t)word(w + 2) << (64 - sh));
+  return v;
+}
+
+// Lane i (bytes 8i .. 8i+7) of the session-key preimage b || e || c, where e
+// has EB bytes given as 32-bit words by eword and c is given as 32-bit words
+// by cword (zero past its length). Lanes inside e or inside c are funnels of
+// three words; only the lane holding the e/c boundary is assembled bytewise.
+template <int EB, typename EWord, typename CWord>
+__device__ __forceinline__ uint64_t kem_preimage_lane(int i, uint32_t b, EWord eword, CWord cword) {
+  const int o = 8 * i;
+  if (o == 0) return (uint64_t)b | (stream_u64(eword, 0) << 8);
+  if (o + 7 <= EB) return stream_u64(eword, o - 1);
+  if (o >= 1 + EB) return stream_u64(cword, o - 1 - EB);
+  uint64_t v = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const int x = o + k - 1;  // byte of e || c
+    const uint32_t byte = x < EB ? (eword(x >> 2) >> (8 * (x & 3))) : (cword((x - EB) >> 2) >> (8 * ((x - EB) & 3)));
+    v |= (uint64_t)(byte & 0xFFu) << (8 * k);
+  }
+  return v;
+}
+
 // ---------------------------------------------------------------- GF(2^m)
 // Log/antilog representation: log[0] = 2q-2 (sentinel), exp has 2q-1 entries
 // with exp[2q-2] = 0, so a*b = exp[min(log a + log b, 2q-2)] without branches.

@@ -275,7 +275,10 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   cudaError_t e = cudaMalloc(&k->F, h.F.size() * 4);
   const size_t q = (size_t)S.q;
   if (e == cudaSuccess) e = cudaMalloc(&k->tabs, (3 * n + q) * 2);
-  if (e == cudaSuccess) e = cudaMalloc(&k->s, S.e_bytes);
+  // s zero-padded to whole 16-byte units: the hash kernels read it as 32-bit words
+  const size_t s_alloc = ((size_t)S.e_bytes + 15) / 16 * 16;
+  if (e == cudaSuccess) e = cudaMalloc(&k->s, s_alloc);
+  if (e == cudaSuccess) e = cudaMemset(k->s, 0, s_alloc);
   if (e == cudaSuccess) e = cudaMemcpy(k->F, h.F.data(), h.F.size() * 4, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs, h.L.data(), n * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs + n, h.LL.data(), n * 2, cudaMemcpyHostToDevice);

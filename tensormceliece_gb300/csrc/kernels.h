@@ -6,6 +6,7 @@
 
 namespace gmc {
 
+constexpr int kSampleWarpsPerSM = 8;     // sampler: resident warps per SM (lanes fetch requests)
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
 constexpr int kBMWarps = 24;    // Berlekamp-Massey kernel: warps per block

@@ -530,22 +530,17 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
   const bool ok = okin[op] != 0;
   const uint32_t *e = E + op * lde;
   const uint8_t *c = Cin + op * p::synd_bytes;
-  auto ebyte = [&](int x) -> uint32_t {
-    return ok ? ((e[x >> 2] >> (8 * (x & 3))) & 0xFFu) : (uint32_t)key.s[x];
-  };
-  auto lane = [&](int i) -> uint64_t {
-    uint64_t v = 0;
-    for (int bb = 0; bb < 8; bb++) {
-      const int x = 8 * i + bb;
-      uint32_t byte;
-      if (x == 0) byte = ok ? 1u : 0u;
-      else if (x <= p::e_bytes) byte = ebyte(x - 1);
-      else if (x < p::pre_bytes) byte = c[x - 1 - p::e_bytes];
-      else byte = 0;
-      v |= (uint64_t)byte << (8 * bb);
-    }
+  // b || (e or s) || c; s is the key's n/8 bytes, stored zero-padded to whole words
+  const uint32_t *sw = reinterpret_cast<const uint32_t *>(key.s);
+  auto eword = [&](int w) -> uint32_t { return ok ? e[w] : sw[w]; };
+  auto cword = [&](int w) -> uint32_t {  // ciphertext rows need not be 4-byte aligned
+    uint32_t v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (4 * w + k < p::synd_bytes) v |= (uint32_t)c[4 * w + k] << (8 * k);
     return v;
   };
+  auto lane = [&](int i) -> uint64_t { return kem_preimage_lane<p::e_bytes>(i, ok ? 1u : 0u, eword, cword); };
   uint64_t h[4];
   shake256_32<p::pre_bytes>(h, lane);
   bool pad_bad = false;

@@ -198,50 +198,20 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
   const bool pk_bad = (pk_bad_mask >> seg) & 1u;
   const uint32_t *e = E + op * lde;
   const uint32_t *sy = S + op * lds;
-  // c words (mt bits, tail bits cleared)
-  uint32_t cw[p::cw];
-#pragma unroll
-  for (int w = 0; w < p::cw; w++) {
-    uint32_t v = (w < p::mw) ? (e[w] ^ sy[w]) : 0u;
+  // c word w: e[0:mt] xor the syndrome, bits from mt on cleared (zero past c)
+  auto cword = [&](int w) -> uint32_t {
+    if (w >= p::mw) return 0u;
+    uint32_t v = e[w] ^ sy[w];
     if (w == p::mt / 32 && (p::mt % 32)) v &= (1u << (p::mt % 32)) - 1u;
-    if (w > (p::mt - 1) / 32) v = 0;
-    cw[w] = v;
-  }
-  // preimage byte x (x < pre_bytes): 1 | e bytes | c bytes
-  auto ebyte = [&](int x) -> uint32_t { return (e[x >> 2] >> (8 * (x & 3))) & 0xFFu; };
-  auto cbyte = [&](int x) -> uint32_t {
-    uint32_t r = 0;
-#pragma unroll
-    for (int w = 0; w < p::cw; w++)
-      if (w == (x >> 2)) r = (cw[w] >> (8 * (x & 3))) & 0xFFu;
-    return r;
-  };
-  auto lane = [&](int i) -> uint64_t {
-    const int o = 8 * i;
-    if (o >= 8 && o + 7 <= p::e_bytes) {
-      // bytes o..o+7 are e[o-1 .. o+6]: funnel of three 32-bit words
-      int x = o - 1;  // x % 4 == 3
-      uint32_t w0 = e[x >> 2], w1 = e[(x >> 2) + 1], w2 = e[(x >> 2) + 2];
-      uint64_t lo = (uint64_t)(w0 >> 24) | ((uint64_t)w1 << 8) | ((uint64_t)(w2 & 0xFFFFFFu) << 40);
-      return lo;
-    }
-    uint64_t v = 0;
-    for (int b = 0; b < 8; b++) {
-      int x = o + b;
-      uint32_t byte;
-      if (x == 0) byte = 1;
-      else if (x <= p::e_bytes) byte = ebyte(x - 1);
-      else if (x < p::pre_bytes) byte = cbyte(x - 1 - p::e_bytes);
-      else byte = 0;
-      v |= (uint64_t)byte << (8 * b);
-    }
     return v;
   };
+  auto eword = [&](int w) -> uint32_t { return e[w]; };
+  auto lane = [&](int i) -> uint64_t { return kem_preimage_lane<p::e_bytes>(i, 1u, eword, cword); };
   uint64_t h[4];
   shake256_32<p::pre_bytes>(h, lane);
   uint8_t *c = C + op * p::synd_bytes;
   uint8_t *k = K + op * 32;
-  for (int x = 0; x < p::synd_bytes; x++) c[x] = pk_bad ? 0 : (uint8_t)cbyte(x);
+  for (int x = 0; x < p::synd_bytes; x++) c[x] = pk_bad ? 0 : (uint8_t)(cword(x >> 2) >> (8 * (x & 3)));
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -265,8 +235,13 @@ cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, i
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sample_kernel<SET>, threads, smem);
   if (per_sm < 1) per_sm = 1;
+  // fewer lanes than requests: a lane that finishes early takes further
+  // requests, so the last slow chains hold few warps (kSampleWarpsPerSM)
+  const int warps = threads / 32;
+  int per_sm_target = (kSampleWarpsPerSM + warps - 1) / warps;
+  if (per_sm_target > per_sm) per_sm_target = per_sm;
   const long long need = (N + threads - 1) / threads;
-  const long long resident = (long long)sms * per_sm;
+  const long long resident = (long long)sms * per_sm_target;
   const long long blocks = need < resident ? need : resident;
   sample_kernel<SET><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx, counter);
   return cudaGetLastError();
