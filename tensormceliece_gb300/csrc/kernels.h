@@ -9,7 +9,7 @@ namespace gmc {
 constexpr int kSampleWarpsPerSM = 8;     // sampler: resident warps per SM (lanes fetch requests)
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
-constexpr int kBMWarps = 24;    // Berlekamp-Massey kernel: warps per block
+constexpr int kBMWarps = 8;     // Berlekamp-Massey kernel: warps per block (32 requests per warp)
 constexpr int kRootWarps = 8;  // root-finding kernel: warps per block
 
 // ---------------------------------------------------------------- segments

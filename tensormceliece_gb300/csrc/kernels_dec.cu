@@ -49,150 +49,233 @@ __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, u
 }
 
 // ---------------------------------------------------------------- BM
-// One warp per request (persistent grid). Coefficient i of C (connection
-// polynomial) lives in lane i%32, slot i/32, as its log only: the update
-// C_i += f B_i is done in the log domain with Zech logarithms,
-// log(a + b) = log a + zech(log b - log a), one table lookup instead of an
-// antilog and a log. Any log at or above the zero sentinel 2q-2 means 0.
-// B = x^s B' is kept unshifted: B' (the connection polynomial before the last
-// length change, as logs) sits in a per-warp shared array behind a guard of
-// 2t zero logs, so B_i is the entry at i - s and the per-iteration shift is
-// s += 1. The syndrome logs sit behind a 32-entry zero guard, so the
-// discrepancy reads s_{n-i} for every lane of an active slot without a
-// per-lane test (C_i = 0 above deg C). Coefficients above t are never
-// updated, as in the library's fixed-size arrays.
-// Degree bounds used to skip empty slots (exact, also for undecodable input):
-// before iteration n, deg C <= L and deg B <= n+1-L, so the discrepancy needs
-// coefficients i <= min(L, t) and the update i <= min(max(L, n+1-L), t).
+// One warp per group of 32 requests, bit-sliced: bit q of every word belongs
+// to request 32g + q, and a GF(2^m) value of all 32 requests is m words
+// (planes). Coefficient i of C (connection polynomial) lives in lane i%32,
+// slot i/32, as m plane registers; B and the syndromes sit in per-warp shared
+// memory as planes. Per iteration n:
+//   d = sum_i C_i s_{n-i}: carry-less plane products accumulated unreduced,
+//       one reduction, then one XOR reduction instruction per plane;
+//   f = d/b per request: lane q extracts its request's d, divides with the
+//       log tables (L and log b are per-request scalars in lane q) and the
+//       32 quotients are sliced back by ballot;
+//   C_i += f B_i (bit-sliced product), and B <- x (upd ? C_old : B) with the
+//       per-request update mask from a ballot.
+// This is the library's update rule (mc:crypto_kem/348864/vec/bm.c:156) on
+// fixed arrays of t+1 coefficients, per request; the slot loops stop at the
+// largest degree bound of the group: before iteration n, deg C <= L and
+// deg B <= n+1-L, so the discrepancy needs i <= min(L, t) and the update
+// i <= min(max(L, n+1-L), t). Rows that are not live run with zero
+// syndromes (d = 0) and write nothing.
 template <int SET>
 struct BMLayout {
   using p = P<SET>;
-  static constexpr int Q = p::q, T = p::t;
+  static constexpr int Q = p::q, T = p::t, M = p::m;
   static constexpr int NS = (T + 1 + 31) / 32;
-  static constexpr int exp_off = 0, log_off = 2 * Q, zech_off = 3 * Q;
-  static constexpr int shared_u16 = 4 * Q;
-  static constexpr int sguard = 32, bguard = 2 * T;
-  static constexpr int s_off = 0, s_len = sguard + 2 * T;          // per warp, u16
-  static constexpr int b_off = s_len, b_len = bguard + 32 * NS;
-  static constexpr int warp_u16 = (s_len + b_len + 1) & ~1;
-  static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u16 * 2; }
+  static constexpr int exp_off = 0, log_off = 2 * Q;           // u16 tables
+  static constexpr int shared_u32 = (3 * Q) / 2;
+  static constexpr int s_words = 2 * T * M;                    // syndrome planes [j][b]
+  static constexpr int b_words = (32 * NS + 1) * M;            // B planes [i][b]
+  static constexpr int warp_u32 = s_words + b_words;
+  static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
+  static_assert(32 * NS * M <= s_words, "C planes are staged in the syndrome area");
 };
 
+// acc (2M-1 planes, unreduced) -> r (M planes) mod the field polynomial
+template <int M>
+__device__ __forceinline__ void bs_reduce(uint32_t (&r)[M], uint32_t (&acc)[2 * M - 1]) {
+#pragma unroll
+  for (int k = 2 * M - 2; k >= M; k--) {
+    if (M == 13) {
+      acc[k - 13] ^= acc[k];
+      acc[k - 12] ^= acc[k];
+      acc[k - 10] ^= acc[k];
+      acc[k - 9] ^= acc[k];
+    } else {
+      acc[k - 12] ^= acc[k];
+      acc[k - 9] ^= acc[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < M; k++) r[k] = acc[k];
+}
+
 template <int SET>
-__global__ void __launch_bounds__(kBMWarps * 32, 2) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
+__global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t *__restrict__ S2, int lds2,
                                                                   FieldDev fd, const Segs segs,
                                                                   uint16_t *__restrict__ Sig) {
   using p = P<SET>;
   using LY = BMLayout<SET>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
-  constexpr int ZL = GFLog<M>::zero_log;
   constexpr int NS = LY::NS;
-  constexpr int NSY = (2 * T + 31) / 32;
   constexpr int SIG = 1 << D;
-  extern __shared__ __align__(16) uint16_t bsm[];
-  uint16_t *gexp = bsm + LY::exp_off;
-  uint16_t *glog = bsm + LY::log_off;
-  uint16_t *zech = bsm + LY::zech_off;
+  static_assert(M == 12 || M == 13, "field polynomial");
+  extern __shared__ __align__(16) uint32_t bsm[];
+  uint16_t *gexp = reinterpret_cast<uint16_t *>(bsm) + LY::exp_off;
+  uint16_t *glog = reinterpret_cast<uint16_t *>(bsm) + LY::log_off;
   for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
-  for (int i = threadIdx.x; i < Q; i += blockDim.x) {
-    glog[i] = fd.glog[i];
-    zech[i] = fd.zech[i];
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint16_t *wsm = bsm + LY::shared_u16 + warp * LY::warp_u16;
-  uint16_t *slog = wsm + LY::s_off + LY::sguard;  // slog[-32 .. -1] = zero logs
-  uint16_t *blog = wsm + LY::b_off + LY::bguard;  // blog[-2t .. -1] = zero logs
-  for (int i = lane; i < LY::sguard; i += 32) wsm[LY::s_off + i] = (uint16_t)ZL;
-  for (int i = lane; i < LY::bguard; i += 32) wsm[LY::b_off + i] = (uint16_t)ZL;
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
   __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *SP = bsm + LY::shared_u32 + warp * LY::warp_u32;
+  uint32_t *BP = SP + LY::s_words;
   const long long N = seg_rows(segs);
-  const long long nwarps = (long long)gridDim.x * kBMWarps;
-  for (long long op = (long long)blockIdx.x * kBMWarps + warp; op < N; op += nwarps) {
+  const long long ngroups = (N + 31) / 32;
+  for (long long g = (long long)blockIdx.x * kBMWarps + warp; g < ngroups; g += (long long)gridDim.x * kBMWarps) {
+    const long long op = g * 32 + lane;
     int seg;
-    if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
+    const bool live = op < N && seg_live(segs, op, &seg);
+    // syndromes -> planes (lane b < M stores plane b of s_j)
     const uint32_t *srow = S2 + op * lds2;
-#pragma unroll
-    for (int k = 0; k < NSY; k++) {
-      const int j = lane + 32 * k;
-      if (j < 2 * T) {
-        const int b = j * M, w = b >> 5, sh = b & 31;
-        uint32_t v = srow[w] >> sh;
+#pragma unroll 1
+    for (int j = 0; j < 2 * T; j++) {
+      uint32_t v = 0;
+      if (live) {
+        const int bb = j * M, w = bb >> 5, sh = bb & 31;
+        v = srow[w] >> sh;
         if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
-        slog[j] = glog[v & (Q - 1)];
       }
+      uint32_t mine = 0;
+#pragma unroll
+      for (int b = 0; b < M; b++) {
+        const uint32_t pl = __ballot_sync(0xffffffffu, (v >> b) & 1u);
+        mine = (lane == b) ? pl : mine;
+      }
+      if (lane < M) SP[j * M + lane] = mine;
     }
-    // B' = 1, s = 1 (B = x)
+    // C = 1, B = x
+    uint32_t C[NS][M];
 #pragma unroll
-    for (int k = 0; k < NS; k++) blog[lane + 32 * k] = (lane + 32 * k == 0) ? 0 : (uint16_t)ZL;
+    for (int k = 0; k < NS; k++)
+#pragma unroll
+      for (int b = 0; b < M; b++) C[k][b] = (k == 0 && lane == 0 && b == 0) ? 0xFFFFFFFFu : 0u;
+    for (int w = lane; w < LY::b_words; w += 32) BP[w] = (w == M) ? 0xFFFFFFFFu : 0u;
     __syncwarp();
-    uint32_t lC[NS];
-#pragma unroll
-    for (int k = 0; k < NS; k++) lC[k] = (lane + 32 * k == 0) ? 0 : ZL;
-    int L = 0, sft = 1;
-    uint32_t lb = 0;  // log b, b = 1
+    int L = 0, lb = 0;  // this lane's request: LFSR length, log b
 #pragma unroll 1
     for (int n = 0; n < 2 * T; n++) {
-      const int bd = L < T ? L : T;                       // discrepancy: i <= min(L, t) (L <= n)
-      int bu = (L > n + 1 - L) ? L : n + 1 - L;           // update: i <= min(max(L, n+1-L), t)
-      bu = bu < T ? bu : T;
-      uint32_t dp = 0;
-      const uint16_t *sn = slog + n - lane;
+      const int Lc = L < T ? L : T;
+      int Lu = (L > n + 1 - L) ? L : n + 1 - L;
+      Lu = Lu < T ? Lu : T;
+      const int bd = (int)__reduce_max_sync(0xffffffffu, live ? (unsigned)Lc : 0u);
+      const int bu = (int)__reduce_max_sync(0xffffffffu, live ? (unsigned)Lu : 0u);
+      // discrepancy planes
+      uint32_t d[M];
+      {
+        uint32_t acc[2 * M - 1];
 #pragma unroll
-      for (int k = 0; k < NS; k++)
-        if (32 * k <= bd) dp ^= gf_mul_log<M>(gexp, lC[k], sn[-32 * k]);
-      const uint32_t d = __reduce_xor_sync(0xffffffffu, dp);
-      if (d) {
-        const bool upd = (n >= 2 * L);
-        const int ld = glog[d];
-        int lf = ld - (int)lb;
-        if (lf < 0) lf += Q - 1;
-        const uint16_t *bs = blog + lane - sft;
-        uint32_t lco[NS];
+        for (int k = 0; k < 2 * M - 1; k++) acc[k] = 0;
 #pragma unroll
         for (int k = 0; k < NS; k++) {
-          lco[k] = lC[k];
-          if (32 * k <= bu) {
-            // log(C_i + f B_i): p = log(f B_i); zero B_i keeps C_i, zero C_i takes p
-            constexpr uint32_t Q1 = Q - 1;
-            const uint32_t lbi = bs[32 * k], lc = lC[k];
-            uint32_t pl = (uint32_t)lf + lbi;
-            pl = min(pl, pl - Q1);                      // < q-1 when B_i != 0
-            uint32_t kk = pl - lc;                      // log(f B_i / C_i) mod q-1
-            kk = min(kk + Q1, kk);
-            const uint32_t z = zech[min(kk, Q1 - 1)];   // index clamped for the zero cases
-            uint32_t nl = lc + z;
-            nl = min(nl, nl - Q1);                      // >= 2q-2 when the sum is 0
-            nl = (lc >= (uint32_t)ZL) ? pl : nl;
-            nl = (lbi >= (uint32_t)ZL) ? lc : nl;
-            const bool in = (k < NS - 1) || (lane + 32 * k <= T);  // coefficients above t stay zero
-            if (in) lC[k] = nl;
+          if (32 * k <= bd) {
+            const int j = n - lane - 32 * k;  // s_j, j < 0 reads as zero
+            const uint32_t jm = j >= 0 ? 0xFFFFFFFFu : 0u;
+            const uint32_t *sp = SP + (j >= 0 ? j : 0) * M;
+#pragma unroll
+            for (int b2 = 0; b2 < M; b2++) {
+              const uint32_t sv = sp[b2] & jm;
+#pragma unroll
+              for (int b1 = 0; b1 < M; b1++) acc[b1 + b2] ^= C[k][b1] & sv;
+            }
           }
         }
-        if (upd) {
-          __syncwarp();  // every lane has read B' before it is replaced
+        bs_reduce<M>(d, acc);
 #pragma unroll
-          for (int k = 0; k < NS; k++)
-            if (32 * k <= bu) blog[lane + 32 * k] = (uint16_t)lco[k];
+        for (int b = 0; b < M; b++) d[b] = __reduce_xor_sync(0xffffffffu, d[b]);
+      }
+      // this lane's request: f = d / b, the update decision
+      uint32_t dq = 0;
+#pragma unroll
+      for (int b = 0; b < M; b++) dq |= ((d[b] >> lane) & 1u) << b;
+      const bool upd = dq != 0 && 2 * L <= n;
+      uint32_t fq = 0;
+      int ld = 0;
+      if (dq) {
+        ld = glog[dq];
+        int lf = ld - lb;
+        if (lf < 0) lf += Q - 1;
+        fq = gexp[lf];
+      }
+      uint32_t f[M];
+#pragma unroll
+      for (int b = 0; b < M; b++) f[b] = __ballot_sync(0xffffffffu, (fq >> b) & 1u);
+      const uint32_t U = __ballot_sync(0xffffffffu, upd);
+      const bool anyf = __any_sync(0xffffffffu, dq != 0);
+      if (upd) {
+        L = n + 1 - L;
+        lb = ld;
+      }
+      // C_i += f B_i; B_{i+1} <- (U ? C_i(old) : B_i); slots in descending
+      // order so slot k's write of B_{32(k+1)} follows slot k+1's read of it
+#pragma unroll
+      for (int k = NS - 1; k >= 0; k--) {
+        if (32 * k <= bu) {
+          const int i = lane + 32 * k;
+          const uint32_t *bp = BP + i * M;
+          uint32_t bi[M];
+#pragma unroll
+          for (int b = 0; b < M; b++) bi[b] = bp[b];
+          __syncwarp();  // every lane holds its B_i before B_{i+1} is replaced
+          const bool in = (k < NS - 1) || (i <= T);  // coefficients above t stay zero
+          uint32_t r[M];
+          if (anyf) {
+            // r = f * B_i, Horner over the planes of f
+#pragma unroll
+            for (int b = 0; b < M; b++) r[b] = bi[b] & f[M - 1];
+#pragma unroll
+            for (int jj = M - 2; jj >= 0; jj--) {
+              const uint32_t top = r[M - 1];
+#pragma unroll
+              for (int b = M - 1; b > 0; b--) r[b] = r[b - 1];
+              r[0] = top;
+              if (M == 13) {
+                r[1] ^= top;
+                r[3] ^= top;
+                r[4] ^= top;
+              } else {
+                r[3] ^= top;
+              }
+#pragma unroll
+              for (int b = 0; b < M; b++) r[b] ^= bi[b] & f[jj];
+            }
+          } else {
+#pragma unroll
+            for (int b = 0; b < M; b++) r[b] = 0;
+          }
+          uint32_t *bq = BP + (i + 1) * M;
+#pragma unroll
+          for (int b = 0; b < M; b++) {
+            const uint32_t cold = C[k][b];
+            if (in) C[k][b] = cold ^ r[b];
+            if (i + 1 <= T) bq[b] = (U & cold) | (~U & bi[b]);
+          }
           __syncwarp();
-          L = n + 1 - L;
-          lb = ld;
-          sft = 0;
         }
       }
-      sft++;
+      if (lane < M) BP[lane] = 0;  // B_0 of x * (...) is zero
+      __syncwarp();
     }
     // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d);
-    // coefficients are < 2^m <= 2^13, so bit 15 is free for the length flag
-    uint16_t *sig = Sig + op * SIG;
-    for (int x = lane; x < SIG; x += 32)
-      if (x > T) sig[x] = 0;
+    // coefficients are < 2^m <= 2^13, so bit 15 of the constant coefficient
+    // is free for the flag of a final length L > t
 #pragma unroll
-    for (int k = 0; k < NS; k++) {
-      const int i = lane + 32 * k;
-      const int deg = T - i;
-      // bit 15 of the constant coefficient flags a final length L > t
-      const uint32_t c = gexp[min(lC[k], (uint32_t)ZL)];
-      if (i <= T && deg < SIG) sig[deg] = (uint16_t)(c | ((deg == 0 && L > T) ? 0x8000u : 0u));
+    for (int k = 0; k < NS; k++)
+#pragma unroll
+      for (int b = 0; b < M; b++) SP[(lane + 32 * k) * M + b] = C[k][b];
+    __syncwarp();
+    if (live) {
+      uint16_t *sig = Sig + op * SIG;
+#pragma unroll 1
+      for (int deg = 0; deg < SIG; deg++) {
+        const int i = T - deg;
+        uint32_t v = 0;
+        if (i >= 0) {
+#pragma unroll
+          for (int b = 0; b < M; b++) v |= ((SP[i * M + b] >> lane) & 1u) << b;
+        }
+        if (deg == 0 && L > T) v |= 0x8000u;
+        sig[deg] = (uint16_t)v;
+      }
     }
     __syncwarp();
   }
@@ -583,7 +666,7 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
   const int smem_bm = BMLayout<SET>::bytes(kBMWarps);
   cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bm);
   if (err != cudaSuccess) return err;
-  const int gb = persistent_blocks(dec_bm_kernel<SET>, kBMWarps * 32, smem_bm, N, kBMWarps);
+  const int gb = persistent_blocks(dec_bm_kernel<SET>, kBMWarps * 32, smem_bm, (N + 31) / 32, kBMWarps);
   dec_bm_kernel<SET><<<gb, kBMWarps * 32, smem_bm, st>>>(S2, lds2, fd, segs, Sig);
   return cudaGetLastError();
 }
