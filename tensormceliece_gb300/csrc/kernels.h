@@ -115,7 +115,6 @@ struct FieldDev {
   // bit-sliced over 32 chunks per word (bit k: chunk 32 h + k), plane b = bit b
   const uint32_t *fft_alpha_bs;   // [(2^d - 2^(d-l) + xh) * H + h][m]: alpha_{l, (c << (d-1-l)) + xh}
   const uint32_t *frob_hi_bs;     // [h][m]: (c 2^d)^(2^d)
-  const uint16_t *zech;           // [q]: log(1 + g^k), zech[0] = 3q (zero)
 };
 
 // Per-key decapsulation tables of the segments of a launch.

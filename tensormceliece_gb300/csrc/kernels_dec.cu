@@ -320,17 +320,27 @@ struct RootLayout {
   static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
 };
 
-// Chunk-slot index held by (lane, register slot j) while level l is processed
-// (after that level's swap). Register bits hold slot bits L .. L+LOGV-1 (slot
-// bit e in register bit e % LOGV), lane bits below L hold slot bits below L,
-// lane bits from L on hold slot bits from L+LOGV on; L = min(l, D - LOGV).
-template <int D, int LOGV>
+// Chunk-slot index held by (lane, register slot j = j0 + 2 j1) while level l
+// of the bottom-up pass is processed (l = -1: after the last level).
+// Register bit 0 pairs at every level but one: a level whose pair bit is a
+// lane bit first swaps that lane bit with register bit 0, whose slot bit
+// (the level before) is finished. D = 7 (4 slots per lane) starts with
+// slot bits 6, 5 in register bits 0, 1 and lane bits 0..4 = slot bits 0..4;
+// level 5 pairs on register bit 1. D = 6 (2 slots) starts with slot bit 5 in
+// register bit 0.
+template <int D>
 __device__ __forceinline__ int chunk_slot(int l, int lane, int j) {
-  const int L = l < D - LOGV ? l : D - LOGV;
-  int x = (lane & ((1 << L) - 1)) | ((lane >> L) << (L + LOGV));
-#pragma unroll
-  for (int e = 0; e < LOGV; e++) x |= ((j >> ((L + e) % LOGV)) & 1) << (L + e);
-  return x;
+  const int j0 = j & 1, j1 = j >> 1;
+  if (D == 7) {
+    if (l >= 5) return lane | (j1 << 5) | (j0 << 6);
+    if (l < 0) return j0 | ((lane & 15) << 1) | (j1 << 5) | ((lane >> 4) << 6);
+    return (lane & ((1 << l) - 1)) | (j0 << l) | (((lane >> l) & ((1 << (4 - l)) - 1)) << (l + 1)) | (j1 << 5) |
+           ((lane >> 4) << 6);
+  } else {
+    if (l >= 5) return lane | (j0 << 5);
+    if (l < 0) return j0 | (lane << 1);
+    return (lane & ((1 << l) - 1)) | (j0 << l) | ((lane >> l) << (l + 1));
+  }
 }
 
 // r = a * b in GF(2^M), bit-sliced (plane i = bit i of 32 elements), Horner
@@ -444,7 +454,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     }
     uint32_t leaf[VPL];
 #pragma unroll
-    for (int j = 0; j < VPL; j++) leaf[j] = V[chunk_slot<D, LOGV>(D - 1, lane, j)];
+    for (int j = 0; j < VPL; j++) leaf[j] = V[chunk_slot<D>(D - 1, lane, j)];
     __syncwarp();
 
     int weight = 0;
@@ -455,36 +465,51 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
       for (int j = 0; j < VPL; j++)
 #pragma unroll
         for (int b = 0; b < M; b++) v[j][b] = 0u - ((leaf[j] >> b) & 1u);
-#pragma unroll
+      // one loop body for every level (a runtime loop keeps the unrolled
+      // bit-sliced products small enough for the instruction cache)
+#pragma unroll 1
       for (int l = D - 1; l >= 0; l--) {
-        const int rb = 1 << (l % LOGV);  // register bit that pairs at this level
+        if (VPL == 4 && l == D - 2) {
+          // pairs on register bit 1 (slot bit 5)
+#pragma unroll
+          for (int j = 0; j < 2; j++) {
+            const int xh = chunk_slot<D>(l, lane, j) >> (l + 1);
+            const uint32_t *ap = abs_ + (((SIG - (SIG >> l)) + xh) * NH + h) * M;
+            uint32_t pr[M];
+            bs_mul<M>(pr, ap, v[j + 2]);
+#pragma unroll
+            for (int b = 0; b < M; b++) {
+              v[j][b] ^= pr[b];
+              v[j + 2][b] ^= v[j][b];
+            }
+          }
+          continue;
+        }
         if (l < D - LOGV) {
-          // lane bit l <-> register bit rb: the lane with lane bit 0 keeps its
+          // lane bit l <-> register bit 0: the lane with lane bit 0 keeps its
           // slots with register bit 0 and trades the others with its partner
           const bool lo = ((lane >> l) & 1) == 0;
 #pragma unroll
-          for (int j = 0; j < VPL; j++) {
-            if (j & rb) continue;
+          for (int j = 0; j < VPL; j += 2) {
 #pragma unroll
             for (int b = 0; b < M; b++) {
-              const uint32_t send = lo ? v[j | rb][b] : v[j][b];
+              const uint32_t send = lo ? v[j + 1][b] : v[j][b];
               const uint32_t got = __shfl_xor_sync(0xffffffffu, send, 1 << l);
-              if (lo) v[j | rb][b] = got;
+              if (lo) v[j + 1][b] = got;
               else v[j][b] = got;
             }
           }
         }
 #pragma unroll
-        for (int j = 0; j < VPL; j++) {
-          if (j & rb) continue;
-          const int xh = chunk_slot<D, LOGV>(l, lane, j) >> (l + 1);
+        for (int j = 0; j < VPL; j += 2) {
+          const int xh = chunk_slot<D>(l, lane, j) >> (l + 1);
           const uint32_t *ap = abs_ + (((SIG - (SIG >> l)) + xh) * NH + h) * M;
           uint32_t pr[M];
-          bs_mul<M>(pr, ap, v[j | rb]);
+          bs_mul<M>(pr, ap, v[j + 1]);
 #pragma unroll
           for (int b = 0; b < M; b++) {
             v[j][b] ^= pr[b];
-            v[j | rb][b] ^= v[j][b];
+            v[j + 1][b] ^= v[j][b];
           }
         }
       }
@@ -494,7 +519,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
       for (int j = 0; j < VPL; j++) {
         // read here, not hoisted out of the chunk loop (the root stores below
         // may alias), so the per-plane masks are not held across it
-        const uint32_t frl = p::lead ? frlo[VPL * lane + j] : 0u;  // final mapping: slot VPL * lane + j
+        const uint32_t frl = p::lead ? frlo[chunk_slot<D>(-1, lane, j)] : 0u;
         uint32_t nz = 0;
 #pragma unroll
         for (int b = 0; b < M; b++) {
@@ -510,7 +535,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
         while (z) {
           const int k = __ffs(z) - 1;
           z &= z - 1;
-          const int elt = ((32 * h + k) << D) | (VPL * lane + j);
+          const int elt = ((32 * h + k) << D) | chunk_slot<D>(-1, lane, j);
           const uint32_t pos = key.invL[elt];
           if (pos < (uint32_t)p::n) {
             weight++;
