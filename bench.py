@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--set", default=SET_DEFAULT)
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--flip", type=float, default=0.10)
-    ap.add_argument("--engine", default="auto", choices=["auto", "popc", "b1mma", "tc"],
+    ap.add_argument("--engine", default="auto", choices=["auto", "popc", "b1mma", "tc", "sparse"],
                     help="auto: per-set configuration (autotuned when --tune, else defaults)")
     ap.add_argument("--tune", action="store_true", help="autotune every set used before measuring")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -124,6 +124,7 @@ def algorithmic_bytes(kernel, z, n):
     s2 = (2 * z["t"] * z["m"] + 31) // 32 * 4
     per = {
         "enc_sample": 32 + ew + kw,
+        "enc_sample_syndrome": 32 + ew + mw,
         "enc_syndrome_gemm": kw + mw,
         "enc_finalize_hash": ew + mw + ct + 32,
         "dec_pack_ct": ct + (ct + 3) // 4 * 4,
@@ -132,7 +133,8 @@ def algorithmic_bytes(kernel, z, n):
         "dec_fft_roots_reenc": 2 * (1 << (6 if z["t"] <= 64 else 7)) + s2 + ew + 4,
         "dec_tail_hash": ew + 4 + ct + 32 + 4,
     }[kernel]
-    fixed = {"enc_syndrome_gemm": z["mt"] * kw, "dec_front_gemm": 2 * z["t"] * z["m"] * ((ct + 3) // 4 * 4)}
+    fixed = {"enc_syndrome_gemm": z["mt"] * kw, "enc_sample_syndrome": z["k"] * mw,
+             "dec_front_gemm": 2 * z["t"] * z["m"] * ((ct + 3) // 4 * 4)}
     return per * n + fixed.get(kernel, 0)
 
 
@@ -351,7 +353,8 @@ def main():
     dev = torch.device("cuda", local_rank)
     L = gmc.lib()
     L.gmc_prof_report.argtypes = [ctypes.c_char_p, ctypes.c_int]
-    gmc.set_gemm_engine({"auto": -1, "popc": gmc.GEMM_POPC, "b1mma": gmc.GEMM_B1MMA, "tc": gmc.GEMM_TC}[args.engine])
+    gmc.set_gemm_engine({"auto": -1, "popc": gmc.GEMM_POPC, "b1mma": gmc.GEMM_B1MMA, "tc": gmc.GEMM_TC,
+                         "sparse": gmc.GEMM_SPARSE}[args.engine])
     tuning = {}
     if args.tune:
         for sname in sorted({args.set} | ({gmc.SETS[s] for s in MIX_SETS} if not args.no_grouped else set())):

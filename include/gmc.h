@@ -170,15 +170,19 @@ void gmc_set_randombytes(gmc_randombytes_fn fn, void *ctx);
 #define GMC_GEMM_POPC 0   /* CUDA-core AND/XOR + popcount */
 #define GMC_GEMM_B1MMA 1  /* legacy mma.sync m8n8k128 .b1 AND.POPC */
 #define GMC_GEMM_TC 2     /* tcgen05 (5th-gen tensor cores), 0/1 operands in FP8, TMEM accumulators */
-/* Forces one GEMM engine for every set (-1 restores the per-set choices);
+#define GMC_GEMM_SPARSE 3 /* encapsulation only: XOR of the public-key columns at e's t positions,
+                             gathered by the sampler (no GEMM launch); the default there */
+/* Forces one engine for every set (-1 restores the per-set choices);
+ * GMC_GEMM_SPARSE applies to the encapsulation syndrome only (the
+ * decapsulation front end keeps its per-set GEMM engine).
  * gmc_get_gemm_engine returns the override or -1. */
 int gmc_set_gemm_engine(int engine);
 int gmc_get_gemm_engine(void);
 
 /* ---- autotuner --------------------------------------------------------------
- * Per parameter set: the GEMM engine of the encapsulation syndrome and of the
- * decapsulation front end, and the sampler block size (32/64/128). Defaults:
- * tcgen05, tcgen05, 64. gmc_autotune times every candidate on this GPU with a
+ * Per parameter set: the engine of the encapsulation syndrome (sparse or a
+ * GEMM engine) and the GEMM engine of the decapsulation front end, and the
+ * sampler block size (32/64/128). Defaults: sparse, tcgen05, 64. gmc_autotune times every candidate on this GPU with a
  * batch of n requests (median of 5), keeps the fastest and, when cache_path is
  * given, writes the choices of all tuned sets to that JSON file;
  * gmc_autotune_load applies such a file (returns the number of sets loaded).

@@ -20,11 +20,11 @@ from . import build as _build
 __all__ = [
     "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "Plan", "Server", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
     "set_gemm_engine", "get_gemm_engine", "set_randombytes", "autotune", "autotune_load", "tune_get",
-    "tune_set", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC",
+    "tune_set", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC", "GEMM_SPARSE",
 ]
 
 SETS = ("348864", "460896", "6688128", "6960119", "8192128")
-GEMM_POPC, GEMM_B1MMA, GEMM_TC = 0, 1, 2
+GEMM_POPC, GEMM_B1MMA, GEMM_TC, GEMM_SPARSE = 0, 1, 2, 3
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad key"}
 
 _lib = None
@@ -364,14 +364,14 @@ def tune_get(set_name):
     sid = set_name if isinstance(set_name, int) else set_id(set_name)
     a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     tuned = _check(lib().gmc_tune_get(sid, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "gmc_tune_get")
-    names = {GEMM_POPC: "popc", GEMM_B1MMA: "b1mma", GEMM_TC: "tc"}
+    names = {GEMM_POPC: "popc", GEMM_B1MMA: "b1mma", GEMM_TC: "tc", GEMM_SPARSE: "sparse"}
     return {"enc_engine": names[a.value], "dec_engine": names[b.value], "sample_threads": c.value,
             "tuned": bool(tuned)}
 
 
 def tune_set(set_name, enc_engine, dec_engine, sample_threads):
     sid = set_name if isinstance(set_name, int) else set_id(set_name)
-    ids = {"popc": GEMM_POPC, "b1mma": GEMM_B1MMA, "tc": GEMM_TC}
+    ids = {"popc": GEMM_POPC, "b1mma": GEMM_B1MMA, "tc": GEMM_TC, "sparse": GEMM_SPARSE}
     _check(lib().gmc_tune_set(sid, ids[enc_engine], ids[dec_engine], int(sample_threads)), "gmc_tune_set")
 
 

@@ -54,8 +54,10 @@ void gmc::set_last_error(const char *msg) { g_last_error = msg; }
 static SetTune g_tune[GMC_NSETS];
 static int g_engine_override = -1;
 static std::mutex g_tune_mu;
+// op 0: encapsulation syndrome, 1: decapsulation front end (no sparse form:
+// c is dense), where a GEMM_SPARSE override leaves the per-set engine.
 static int engine_for(int set, int op) {
-  if (g_engine_override >= 0) return g_engine_override;
+  if (g_engine_override >= 0 && !(op && g_engine_override == GEMM_SPARSE)) return g_engine_override;
   return op ? g_tune[set].dec_engine : g_tune[set].enc_engine;
 }
 SetTune gmc::tune_get(int set) {
@@ -249,11 +251,21 @@ extern "C" int gmc_pk_load(gmc_key **out, int set, const unsigned char *pk) {
   k->set = set;
   k->kind = 0;
   cudaGetDevice(&k->device);
-  k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad;
+  k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad; k->ldtt = h.ldtt;
+  const gmc_setinfo &S = set_info(set);
+  const size_t tt_bytes = (size_t)(S.k + 1) * h.ldtt * 4;
   cudaError_t e = cudaMalloc(&k->T, h.T.size() * 4);
-  if (e != cudaSuccess) { delete k->a8_mu; delete k; return cuda_fail(e, "gmc_pk_load: cudaMalloc"); }
-  e = cudaMemcpy(k->T, h.T.data(), h.T.size() * 4, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) { cudaFree(k->T); delete k->a8_mu; delete k; return cuda_fail(e, "gmc_pk_load: copy"); }
+  if (e == cudaSuccess) e = cudaMalloc(&k->TT, tt_bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(k->T, h.T.data(), h.T.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(k->TT, 0, tt_bytes);
+  if (e == cudaSuccess) e = launch_transpose_pk(k->T, k->lda, S.mt, S.k, k->TT, k->ldtt, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (e != cudaSuccess) {
+    cudaFree(k->T); cudaFree(k->TT);
+    delete k->a8_mu;
+    delete k;
+    return cuda_fail(e, "gmc_pk_load");
+  }
   *out = k;
   return GMC_OK;
 }
@@ -304,6 +316,7 @@ extern "C" void gmc_key_free(gmc_key *key) {
   cudaFree(key->a8);
   delete key->a8_mu;
   cudaFree(key->T);
+  cudaFree(key->TT);
   cudaFree(key->F);
   cudaFree(key->tabs);
   cudaFree(key->s);
@@ -313,7 +326,7 @@ extern "C" void gmc_key_free(gmc_key *key) {
 extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set : GMC_EINVAL; }
 
 extern "C" int gmc_set_gemm_engine(int engine) {
-  if (engine < -1 || engine > GEMM_TC) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
+  if (engine < -1 || engine > GEMM_SPARSE) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
   g_engine_override = engine;
   return GMC_OK;
 }
@@ -358,6 +371,8 @@ static cudaError_t gemm_keys(const gmc_key *const *keys, int nkeys, int engine, 
   *err = nullptr;
   for (int i = 0; i < nkeys; i++) {
     gk->A[i] = keys[i]->kind == 0 ? keys[i]->T : keys[i]->F;
+    gk->TT[i] = keys[i]->TT;
+    gk->ldtt = keys[i]->ldtt;
     if (engine == GEMM_TC) {
       cudaError_t e = key_a8(keys[i], st, &gk->A8[i]);
       if (e != cudaSuccess) return e;
@@ -374,8 +389,14 @@ static cudaError_t enc_sample_gemm_seg(const Segs &segs, const gmc_key *ref, con
                                        const EncDims &d, cudaStream_t st) {
   using p = P<SET>;
   prof_mark(nullptr, st);
-  cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, tune_get(SET).sample_threads,
-                                     reinterpret_cast<unsigned int *>(S), st);
+  if (engine == GEMM_SPARSE) {  // the sampler writes S itself; Ens lends its first word as the work counter
+    cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, &gk, S, d.lds, tune_get(SET).sample_threads,
+                                       reinterpret_cast<unsigned int *>(Ens), st);
+    prof_mark("enc_sample_syndrome", st);
+    return e;
+  }
+  cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, nullptr, S, d.lds,
+                                     tune_get(SET).sample_threads, reinterpret_cast<unsigned int *>(S), st);
   if (e != cudaSuccess) return e;
   prof_mark("enc_sample", st);
   e = launch_gf2_gemm_seg(engine, gk, segs, ref->lda, ref->rows_pad, Ens, d.ldx, ref->kw_pad, S, d.lds, p::mw, err,
@@ -651,7 +672,8 @@ extern "C" int gmc_enc_stages_dev(const gmc_key *pk, const unsigned char *seeds,
 extern "C" int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int rows_pad, const unsigned int *X,
                                 int ldx, long long n_pad, int kw_pad, unsigned int *out, int ldo, int out_words,
                                 long long n, void *stream) {
-  if (!A || !X || !out || n < 0 || lda < kw_pad || ldx < kw_pad || ldo < out_words)
+  if (!A || !X || !out || n < 0 || lda < kw_pad || ldx < kw_pad || ldo < out_words || engine < GEMM_POPC ||
+      engine > GEMM_TC)
     return fail(GMC_EINVAL, "gmc_gf2_gemm_dev: bad argument");
   cudaStream_t st = (cudaStream_t)stream;
   uint8_t *a8 = nullptr;

@@ -13,7 +13,8 @@ struct gmc_key {
   int device = 0;
   // public key
   uint32_t *T = nullptr;
-  int lda = 0, rows_pad = 0, kw_pad = 0, pad_bad = 0;
+  uint32_t *TT = nullptr;  // columns of T (sparse syndrome)
+  int lda = 0, rows_pad = 0, kw_pad = 0, pad_bad = 0, ldtt = 0;
   // secret key
   uint32_t *F = nullptr;
   int ldf = 0, frows_pad = 0, cw_pad = 0;
@@ -31,7 +32,7 @@ void set_last_error(const char *msg);
 
 // per-parameter-set launch configuration chosen by the autotuner
 struct SetTune {
-  int enc_engine = GEMM_TC;   // GF(2) GEMM engine of the encapsulation syndrome
+  int enc_engine = GEMM_SPARSE;  // engine of the encapsulation syndrome
   int dec_engine = GEMM_TC;   // GF(2) GEMM engine of the decapsulation front end
   int sample_threads = 64;    // sampler block size (32, 64 or 128)
   int tuned = 0;              // 1 when measured on this device

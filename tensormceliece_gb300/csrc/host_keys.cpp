@@ -196,6 +196,7 @@ void build_pk(int set, const uint8_t *pk, PkHost &out) {
     uint32_t *dst = &out.T[(size_t)r * out.lda];
     for (int b = 0; b < S.pk_row_bytes; b++) dst[b >> 2] |= (uint32_t)row[b] << (8 * (b & 3));
   }
+  out.ldtt = round_up((S.mt + 31) / 32, 32) < 64 ? 64 : round_up((S.mt + 31) / 32, 32);
   out.pad_bad = 0;
   if (S.k % 8) {
     uint8_t acc = 0;

@@ -44,8 +44,9 @@ FftTables build_fft_tables(int m, int d);
 
 // Public key -> row-major T words for the syndrome GEMM.
 struct PkHost {
-  std::vector<uint32_t> T;  // rows_pad x lda
+  std::vector<uint32_t> T;   // rows_pad x lda
   int lda = 0, rows_pad = 0, kw_pad = 0;
+  int ldtt = 0;              // row stride of the column image TT (built on the device)
   int pad_bad = 0;          // 6960119: nonzero pk padding bits
 };
 void build_pk(int set, const uint8_t *pk, PkHost &out);

@@ -43,7 +43,10 @@ __device__ inline bool seg_live(const Segs &S, long long row, int *seg) {
 #endif
 
 // GF(2) GEMM engines for Out[op] = parity(A[row] & X[op]) over KW words.
-enum GemmEngine { GEMM_POPC = 0, GEMM_B1MMA = 1, GEMM_TC = 2 };
+// GEMM_SPARSE is the encapsulation-only alternative: e has weight t, so
+// T e[mt:n] is the XOR of the <= t columns of T at e's positions, gathered by
+// the sampler from a column-major image of T (no GEMM launch).
+enum GemmEngine { GEMM_POPC = 0, GEMM_B1MMA = 1, GEMM_TC = 2, GEMM_SPARSE = 3 };
 
 // Tiling of every engine: A padded to a multiple of kGemmRowTile rows and X
 // to a multiple of kGemmOpTile requests, K to a multiple of kGemmKTile words.
@@ -63,9 +66,13 @@ constexpr int kTcStages = 4;
 
 // Key matrices of the segments of a GEMM launch (same shape for all: one set).
 // A8: the key matrix pre-expanded to FP8 stage images (GEMM_TC only).
+// TT: public keys only, the columns of T as rows of ldtt words (column k is
+// zero, the target of positions below mt), for GEMM_SPARSE.
 struct GemmKeys {
   const uint32_t *A[kMaxSegs];
   const uint8_t *A8[kMaxSegs];
+  const uint32_t *TT[kMaxSegs];
+  int ldtt;
 };
 // Out rows follow X rows (padded row space). err: device word set to 1 when a
 // tensor-core CTA gave up on a bounded wait.
@@ -87,12 +94,20 @@ Segs one_segment(long long n);
 // Encapsulation: seeds / C / K rows in padded row space; E, Ens, S have
 // seg_rows(segs) rows. pk_bad_mask bit s: segment s's public key has
 // nonzero padding bits (6960119), its c and K are zeroed.
+// TT (k + 1 rows of ldtt words, zeroed by the caller): row j = column j of T
+// (mt bits); row k stays zero.
+cudaError_t launch_transpose_pk(const uint32_t *T, int lda, int mt, int k, uint32_t *TT, int ldtt, cudaStream_t st);
+
+// Dense mode (sparse == nullptr): writes E and Ens (e[mt:n] at bit 0, the
+// GEMM operand). Sparse mode: writes E and S = T e[mt:n] (lds words per row)
+// from sparse->TT, and not Ens.
 // counter: 4 bytes of device scratch (zeroed here, on st) that nothing else
 // touches until the sampler ends; the pipelines lend the first word of the
-// syndrome buffer, which only the following GEMM writes.
+// buffer the sampler does not write (S in dense mode, Ens in sparse mode).
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
-                          int threads, unsigned int *counter, cudaStream_t st);
+                          const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
+                          cudaStream_t st);
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
                             const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st);

@@ -35,11 +35,12 @@ struct SampleLayout {
 
 __device__ __forceinline__ int cand_slot(int c, int l) { return c * 32 + (l ^ ((c & 15) << 1)); }
 
-template <int SET>
+template <int SET, bool SPARSE>
 __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t *__restrict__ seeds, const Segs segs,
                                                                 uint32_t *__restrict__ E, int lde,
                                                                 uint32_t *__restrict__ Ens, int ldx,
-                                                                unsigned int *__restrict__ counter) {
+                                                                const GemmKeys keys, uint32_t *__restrict__ S,
+                                                                int lds, unsigned int *__restrict__ counter) {
   using p = P<SET>;
   using LY = SampleLayout<SET>;
   constexpr int NCW = (p::t + 31) / 32;
@@ -52,6 +53,7 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
   const long long N = seg_rows(segs);
   bool has = false, exhausted = false;
   long long op = 0;
+  int myseg = 0;
   uint64_t st[4] = {0, 0, 0, 0};
   constexpr int ncand = p::cand_bytes / 2;  // 16-bit candidates per attempt
   constexpr int nlanes = (ncand + 3) / 4;   // output lanes holding them
@@ -71,9 +73,8 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
         if (idx >= N) {
           exhausted = true;
         } else {
-          int seg;
           op = idx;
-          has = seg_live(segs, idx, &seg);
+          has = seg_live(segs, idx, &myseg);
           if (has) {
             const uint8_t *sd = seeds + 32 * idx;
 #pragma unroll
@@ -156,11 +157,55 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
         okmask |= 1u << r;
         uint32_t *erow = E + opr * lde;
         for (int w = lane; w < p::ew; w += 32) erow[w] = bm[w];
-        uint32_t *xrow = Ens + opr * ldx;
-        for (int w = lane; w < p::kw; w += 32) {
-          const uint32_t lo = bm[w0 + w];
-          const uint32_t hi = (w0 + w + 1 < p::ew) ? bm[w0 + w + 1] : 0u;
-          xrow[w] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
+        if (SPARSE) {
+          // S = T e[mt:n]: XOR of the columns at this request's positions >= mt.
+          // Lane l XORs the columns of positions l, l+32, ... (16-byte loads,
+          // all in flight at once; positions < mt read the zero column k),
+          // then one XOR reduction per syndrome word.
+          const uint32_t *TT = keys.TT[__shfl_sync(0xffffffffu, myseg, r)];
+          constexpr int MW4 = (p::mw + 3) / 4;
+          uint4 acc[MW4];
+#pragma unroll
+          for (int w = 0; w < MW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
+#pragma unroll
+          for (int i = 0; i < NCW; i++) {
+            const int c = lane + 32 * i;
+            const int pos = c < p::t ? cand[cand_slot(c, r)] : 0;
+            const uint4 *col =
+                reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * keys.ldtt);
+#pragma unroll
+            for (int w = 0; w < MW4; w++) {
+              const uint4 v = col[w];
+              acc[w].x ^= v.x;
+              acc[w].y ^= v.y;
+              acc[w].z ^= v.z;
+              acc[w].w ^= v.w;
+            }
+          }
+          uint32_t my0 = 0, my1 = 0;
+#pragma unroll
+          for (int w = 0; w < MW4; w++) {
+            const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
+#pragma unroll
+            for (int e2 = 0; e2 < 4; e2++) {
+              const int word = 4 * w + e2;
+              if (word < p::mw) {
+                const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
+                if (word < 32) my0 = (lane == word) ? v : my0;
+                else my1 = (lane == word - 32) ? v : my1;
+              }
+            }
+          }
+          uint32_t *srow = S + opr * lds;
+          if (lane < p::mw) srow[lane] = my0;
+          if (p::mw > 32 && lane + 32 < p::mw) srow[lane + 32] = my1;
+        } else {
+          uint32_t *xrow = Ens + opr * ldx;
+          for (int w = lane; w < p::kw; w += 32) {
+            const uint32_t lo = bm[w0 + w];
+            const uint32_t hi = (w0 + w + 1 < p::ew) ? bm[w0 + w + 1] : 0u;
+            xrow[w] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
+          }
         }
       }
       __syncwarp();
@@ -218,22 +263,49 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
     for (int b = 0; b < 8; b++) k[8 * i + b] = pk_bad ? 0 : (uint8_t)(h[i] >> (8 * b));
 }
 
+// ---------------------------------------------------------------- column image of T
+// One warp per (32 rows, 32 columns) block: lane b holds row 32w + b's word of
+// the block, ballot j gives column 32jw + j's bits of those rows.
+__global__ void transpose_pk_kernel(const uint32_t *__restrict__ T, int lda, int mt, int k, uint32_t *__restrict__ TT,
+                                    int ldtt) {
+  const int lane = threadIdx.x & 31;
+  const long long task = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int mw = (mt + 31) / 32, kw = (k + 31) / 32;
+  if (task >= (long long)mw * kw) return;  // warp-uniform
+  const int w = (int)(task % mw), jw = (int)(task / mw);
+  const int row = 32 * w + lane;
+  const uint32_t x = row < mt ? T[(size_t)row * lda + jw] : 0u;
+  uint32_t mine = 0;
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    const uint32_t v = __ballot_sync(0xffffffffu, (x >> j) & 1u);
+    mine = (lane == j) ? v : mine;
+  }
+  const int col = 32 * jw + lane;
+  if (col < k) TT[(size_t)col * ldtt + w] = mine;
+}
+
+cudaError_t launch_transpose_pk(const uint32_t *T, int lda, int mt, int k, uint32_t *TT, int ldtt, cudaStream_t st) {
+  const long long warps = (long long)((mt + 31) / 32) * ((k + 31) / 32);
+  transpose_pk_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(T, lda, mt, k, TT, ldtt);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- launchers
-template <int SET>
-cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
-                          int threads, unsigned int *counter, cudaStream_t st) {
+template <int SET, bool SPARSE>
+static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens,
+                                     int ldx, const GemmKeys &keys, uint32_t *S, int lds, int threads,
+                                     unsigned int *counter, cudaStream_t st) {
   const long long N = seg_rows(segs);
-  if (N <= 0) return cudaSuccess;
-  if ((threads != 32 && threads != 64 && threads != 128) || !counter) return cudaErrorInvalidValue;
   const int smem = (threads / 32) * SampleLayout<SET>::warp_bytes;
-  cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (kSampleThreadsMax / 32) * SampleLayout<SET>::warp_bytes);
   if (err != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st)) != cudaSuccess) return err;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sample_kernel<SET>, threads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sample_kernel<SET, SPARSE>, threads, smem);
   if (per_sm < 1) per_sm = 1;
   // fewer lanes than requests: a lane that finishes early takes further
   // requests, so the last slow chains hold few warps (kSampleWarpsPerSM)
@@ -243,8 +315,25 @@ cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, i
   const long long need = (N + threads - 1) / threads;
   const long long resident = (long long)sms * per_sm_target;
   const long long blocks = need < resident ? need : resident;
-  sample_kernel<SET><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx, counter);
+  sample_kernel<SET, SPARSE><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx, keys, S, lds,
+                                                                      counter);
   return cudaGetLastError();
+}
+
+template <int SET>
+cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
+                          const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
+                          cudaStream_t st) {
+  const long long N = seg_rows(segs);
+  if (N <= 0) return cudaSuccess;
+  if ((threads != 32 && threads != 64 && threads != 128) || !counter) return cudaErrorInvalidValue;
+  if (sparse) {
+    if (!S || lds < P<SET>::mw || sparse->ldtt < 64) return cudaErrorInvalidValue;
+    for (int i = 0; i < segs.nseg; i++)
+      if (!sparse->TT[i]) return cudaErrorInvalidValue;
+    return launch_sample_mode<SET, true>(seeds, segs, E, lde, Ens, ldx, *sparse, S, lds, threads, counter, st);
+  }
+  return launch_sample_mode<SET, false>(seeds, segs, E, lde, Ens, ldx, GemmKeys{}, S, lds, threads, counter, st);
 }
 
 template <int SET>
@@ -258,8 +347,8 @@ cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int l
 }
 
 #define GMC_INST_ENC(SET)                                                                                        \
-  template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int, int,  \
-                                          unsigned int *, cudaStream_t);                                         \
+  template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int,       \
+                                          const GemmKeys *, uint32_t *, int, int, unsigned int *, cudaStream_t); \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
                                             const Segs &, uint32_t, cudaStream_t);
 GMC_INST_ENC(0)

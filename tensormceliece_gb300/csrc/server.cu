@@ -130,11 +130,15 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp) {
   uint8_t *work = sl.dev + pp.work_off;
   const gmc_key *ref = pp.keys[0];
   const SetTune tune = tune_get(SET);
-  const int engine = gmc_get_gemm_engine() >= 0 ? gmc_get_gemm_engine() : (pp.kind ? tune.dec_engine : tune.enc_engine);
+  const int ov = gmc_get_gemm_engine();
+  // a sparse override applies to encapsulation only (c is dense)
+  const int engine = (ov >= 0 && !(pp.kind && ov == GEMM_SPARSE)) ? ov : (pp.kind ? tune.dec_engine : tune.enc_engine);
   GemmKeys gk{};
   for (size_t i = 0; i < pp.keys.size(); i++) {
     gk.A[i] = pp.kind == 0 ? pp.keys[i]->T : pp.keys[i]->F;
     gk.A8[i] = pp.keys[i]->a8;
+    gk.TT[i] = pp.keys[i]->TT;
+    gk.ldtt = pp.keys[i]->ldtt;
     if (engine == GEMM_TC && !gk.A8[i]) return cudaErrorInvalidValue;  // registered keys carry their images
   }
   const gmc_setinfo &S = set_info(SET);
@@ -147,11 +151,17 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp) {
     uint32_t bad = 0;
     for (size_t i = 0; i < pp.keys.size(); i++)
       if (pp.keys[i]->pad_bad) bad |= 1u << i;
-    cudaError_t e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, tune.sample_threads,
-                                       reinterpret_cast<unsigned int *>(Sy), sl.st);
-    if (e == cudaSuccess)
-      e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->lda, ref->rows_pad, Ens, kw, ref->kw_pad, Sy, mw, p::mw,
-                              tc_err_word_ptr(), sl.st);
+    cudaError_t e;
+    if (engine == GEMM_SPARSE) {
+      e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, &gk, Sy, mw, tune.sample_threads,
+                             reinterpret_cast<unsigned int *>(Ens), sl.st);
+    } else {
+      e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, nullptr, Sy, mw, tune.sample_threads,
+                             reinterpret_cast<unsigned int *>(Sy), sl.st);
+      if (e == cudaSuccess)
+        e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->lda, ref->rows_pad, Ens, kw, ref->kw_pad, Sy, mw, p::mw,
+                                tc_err_word_ptr(), sl.st);
+    }
     if (e == cudaSuccess)
       e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, sl.st);
     return e;

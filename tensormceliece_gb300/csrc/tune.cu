@@ -3,9 +3,10 @@
 // the fastest, and persists the choices in a JSON cache that later processes
 // load with gmc_autotune_load.
 //
-// Candidates: the GF(2) GEMM engine of the encapsulation syndrome (CUDA-core
-// popcount or tcgen05) crossed with the sampler's block size (32, 64, 128),
-// and the GEMM engine of the decapsulation front end. Timing: CUDA events
+// Candidates: the engine of the encapsulation syndrome (sparse column gather
+// in the sampler, or the tcgen05 GEMM) crossed with the sampler's block size
+// (32, 64, 128), and the GEMM engine of the decapsulation front end (CUDA-core
+// popcount or tcgen05). Timing: CUDA events
 // around whole batched calls (median of 5 after 2 warm-ups).
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -26,8 +27,12 @@ using namespace gmc;
 
 namespace {
 
-const char *engine_name(int e) { return e == GEMM_TC ? "tc" : e == GEMM_B1MMA ? "b1mma" : "popc"; }
-int engine_id(const std::string &s) { return s == "tc" ? GEMM_TC : s == "b1mma" ? GEMM_B1MMA : GEMM_POPC; }
+const char *engine_name(int e) {
+  return e == GEMM_SPARSE ? "sparse" : e == GEMM_TC ? "tc" : e == GEMM_B1MMA ? "b1mma" : "popc";
+}
+int engine_id(const std::string &s) {
+  return s == "sparse" ? GEMM_SPARSE : s == "tc" ? GEMM_TC : s == "b1mma" ? GEMM_B1MMA : GEMM_POPC;
+}
 
 int tune_error(int code, const std::string &msg) {
   set_last_error(msg.c_str());
@@ -136,7 +141,7 @@ int write_cache(const char *path) {
 }  // namespace
 
 extern "C" int gmc_tune_set(int set, int enc_engine, int dec_engine, int sample_threads) {
-  if (set < 0 || set >= GMC_NSETS || enc_engine < 0 || enc_engine > GEMM_TC || dec_engine < 0 ||
+  if (set < 0 || set >= GMC_NSETS || enc_engine < 0 || enc_engine > GEMM_SPARSE || dec_engine < 0 ||
       dec_engine > GEMM_TC || (sample_threads != 32 && sample_threads != 64 && sample_threads != 128))
     return tune_error(GMC_EINVAL, "gmc_tune_set: bad argument");
   SetTune t = tune_get(set);
@@ -186,19 +191,20 @@ extern "C" int gmc_autotune(int set, long long n, const char *cache_path) {
   if (e == cudaSuccess) {
     fill_bytes_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(seeds, n * 32, 0x1234u + set);
     float best_enc = 1e30f, best_dec = 1e30f;
+    const int enc_engines[2] = {GEMM_SPARSE, GEMM_TC};
     const int engines[2] = {GEMM_POPC, GEMM_TC};
     const int threads[3] = {32, 64, 128};
     for (int ei = 0; ei < 2; ei++)
       for (int ti = 0; ti < 3; ti++) {
         SetTune t = best;
-        t.enc_engine = engines[ei];
+        t.enc_engine = enc_engines[ei];
         t.sample_threads = threads[ti];
         tune_put(set, t);
         const float ms =
             time_median([&] { return gmc_enc_batch_dev(P, ct, key, seeds, n, nullptr, st); }, st, a, b, &rc);
         if (ms < best_enc) {
           best_enc = ms;
-          best.enc_engine = engines[ei];
+          best.enc_engine = enc_engines[ei];
           best.sample_threads = threads[ti];
         }
       }
@@ -249,6 +255,7 @@ extern "C" int gmc_autotune_load(const char *cache_path) {
     SetTune t = tune_get(s);
     t.enc_engine = engine_id(field(o, "enc_engine"));
     t.dec_engine = engine_id(field(o, "dec_engine"));
+    if (t.dec_engine == GEMM_SPARSE) t.dec_engine = GEMM_TC;  // no sparse form for the front end
     const int th = atoi(field(o, "sample_threads").c_str());
     t.sample_threads = (th == 32 || th == 64 || th == 128) ? th : 64;
     t.n = atoll(field(o, "n").c_str());

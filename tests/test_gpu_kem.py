@@ -216,12 +216,12 @@ def test_full_size_roundtrip(gmc, keys, sid):
     assert len({bytes(x) for x in k[:4096]}) == 4096
 
 
-@pytest.mark.parametrize("engine", ["tc", "b1mma"])
+@pytest.mark.parametrize("engine", ["tc", "b1mma", "popc", "sparse"])
 @pytest.mark.parametrize("sid", range(5), ids=SETS)
 def test_kem_parity_per_gemm_engine(gmc, keys, sid, engine):
-    """Encapsulation and decapsulation byte-exact with the tensor-core and legacy 1-bit GEMM engines."""
+    """Encapsulation and decapsulation byte-exact with every syndrome engine (sparse: encapsulation only)."""
     pk, sk = keys(sid)
-    eng = {"tc": gmc.GEMM_TC, "b1mma": gmc.GEMM_B1MMA}[engine]
+    eng = {"tc": gmc.GEMM_TC, "b1mma": gmc.GEMM_B1MMA, "popc": gmc.GEMM_POPC, "sparse": gmc.GEMM_SPARSE}[engine]
     prev = gmc.get_gemm_engine()  # -1: no override
     gmc.set_gemm_engine(eng)
     try:
