@@ -17,6 +17,7 @@
 #include <sys/random.h>
 
 #include <map>
+#include <set>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -333,12 +334,31 @@ extern "C" int gmc_set_gemm_engine(int engine) {
 extern "C" int gmc_get_gemm_engine(void) { return g_engine_override; }
 
 // ---------------------------------------------------------------- workspace
+// The default memory pool of the current device keeps freed blocks for reuse
+// (release threshold raised once per device, for this process): without it
+// the pool unmaps the batch scratch at every synchronization and the next
+// batch maps it again.
+static void keep_pool_warm() {
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done.count(dev)) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done.insert(dev);
+}
+
 // Stream-ordered scratch: allocated from the device's default memory pool on
 // the caller's stream and released on it after the last kernel.
 struct Scratch {
   cudaStream_t st;
   std::vector<void *> ptrs;
-  explicit Scratch(cudaStream_t s) : st(s) {}
+  explicit Scratch(cudaStream_t s) : st(s) { keep_pool_warm(); }
   cudaError_t get(void **p, size_t bytes) {
     cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, st);
     if (e == cudaSuccess) ptrs.push_back(*p);
@@ -568,6 +588,7 @@ extern "C" int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char 
   if (n < 0 || (n && (!c || !k || !seeds))) return fail(GMC_EINVAL, "gmc_enc_batch: bad argument");
   if (!n) return GMC_OK;
   const gmc_setinfo &S = set_info(pk->set);
+  keep_pool_warm();
   cudaStream_t st;
   GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   uint8_t *d_seeds = nullptr, *d_c = nullptr, *d_k = nullptr;
@@ -602,6 +623,7 @@ extern "C" int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned
   if (n < 0 || (n && (!c || !k))) return fail(GMC_EINVAL, "gmc_dec_batch: bad argument");
   if (!n) return GMC_OK;
   const gmc_setinfo &S = set_info(sk->set);
+  keep_pool_warm();
   cudaStream_t st;
   GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   uint8_t *d_c = nullptr, *d_k = nullptr;
