@@ -297,8 +297,10 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 2 * n, h.LW2.data(), n * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->tabs + 3 * n, h.invL.data(), q * 2, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(k->s, h.s.data(), S.e_bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&k->HT, h.HT.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(k->HT, h.HT.data(), h.HT.size() * 4, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
-    cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s);
+    cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s); cudaFree(k->HT);
     delete k->a8_mu;
     delete k;
     return cuda_fail(e, "gmc_sk_load");
@@ -308,6 +310,8 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   k->dk.LW2 = k->tabs + 2 * n;
   k->dk.invL = k->tabs + 3 * n;
   k->dk.s = k->s;
+  k->dk.HT = k->HT;
+  k->dk.ldh = h.ldh;
   *out = k;
   return GMC_OK;
 }
@@ -321,6 +325,7 @@ extern "C" void gmc_key_free(gmc_key *key) {
   cudaFree(key->F);
   cudaFree(key->tabs);
   cudaFree(key->s);
+  cudaFree(key->HT);
   delete key;
 }
 

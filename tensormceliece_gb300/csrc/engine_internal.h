@@ -22,6 +22,7 @@ struct gmc_key {
   uint8_t *a8 = nullptr;     // FP8 stage images of T (public) or F (secret) for the tensor-core engine
   std::mutex *a8_mu = nullptr;
   uint8_t *s = nullptr;
+  uint32_t *HT = nullptr;  // first t syndromes per code position (re-encryption check)
   gmc::DecKeyDev dk{};
 };
 

@@ -263,6 +263,17 @@ int build_sk(int set, const uint8_t *sk, SkHost &out) {
   out.ldf = out.cw_pad;
   out.frows_pad = round_up(2 * t * m, kGemmRowTile);
   out.F.assign((size_t)out.frows_pad * out.ldf, 0u);
+  out.ldh = round_up((t * m + 31) / 32, 32);
+  out.HT.assign((size_t)n * out.ldh, 0u);
+  for (int i = 0; i < n; i++) {
+    uint16_t v = w2[i];
+    uint32_t *row = &out.HT[(size_t)i * out.ldh];
+    for (int j = 0; j < t; j++) {
+      for (int b = 0; b < m; b++)
+        if ((v >> b) & 1) row[(j * m + b) >> 5] |= 1u << ((j * m + b) & 31);
+      v = F.mul(v, out.L[i]);
+    }
+  }
   const int ncols = std::min(n, 8 * S.synd_bytes);
   for (int i = 0; i < ncols; i++) {
     uint16_t v = w2[i];

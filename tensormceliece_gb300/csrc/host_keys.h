@@ -58,6 +58,10 @@ struct SkHost {
   std::vector<uint8_t> s;                   // [n/8]
   std::vector<uint32_t> F;                  // frows_pad x ldf
   int ldf = 0, frows_pad = 0, cw_pad = 0;
+  // per code position i: the first t syndromes of the unit error at i,
+  // w2_i L_i^j (j < t), packed m bits each like the received syndromes
+  std::vector<uint32_t> HT;                 // n x ldh
+  int ldh = 0;
 };
 int build_sk(int set, const uint8_t *sk, SkHost &out);
 

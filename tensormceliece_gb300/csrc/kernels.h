@@ -119,6 +119,8 @@ struct DecKeyDev {
   const uint16_t *LW2;   // log of 1/g(L_i)^2 [n]
   const uint16_t *invL;  // code position of each field element, 0xFFFF off the support [2^m]
   const uint8_t *s;      // implicit-rejection string [n/8]
+  const uint32_t *HT;    // first t syndromes of each unit error [n][ldh] (m bits per syndrome)
+  int ldh;
 };
 
 // Per-field / per-set device tables (shared by all keys of a set).

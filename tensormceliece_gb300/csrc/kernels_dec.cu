@@ -559,62 +559,46 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     // locator would be a shorter LFSR), so the library's check fails as well.
     bool ok = (weight == T) && !long_lfsr;
     if (ok) {
+      // first t syndromes of the found error: XOR of the key's columns at the
+      // t positions (lane l takes roots l, l+32, ...; 16-byte loads), then one
+      // XOR reduction per word, compared with the received words
       constexpr int NSC = (T + 31) / 32;
-      // received syndromes j = lane + 32k < t (m bits each)
-      const uint32_t *srow = S2 + op * lds2;
-      uint32_t sr[NSC];
+      constexpr int TW = (T * M + 31) / 32;
+      constexpr int TW4 = (TW + 3) / 4;
+      uint4 acc[TW4];
 #pragma unroll
-      for (int k = 0; k < NSC; k++) {
-        const int j = lane + 32 * k;
-        sr[k] = 0;
-        if (j < T) {
-          const int b = j * M, w = b >> 5, sh = b & 31;
-          uint32_t v = srow[w] >> sh;
-          if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
-          sr[k] = v & (Q - 1);
-        }
-      }
-      // per root: log w2_i (key table, global) and log L_i, fetched by all
-      // lanes at once and stored back over the root list as lw << 16 | ll
-      // (ll = 0xFFFF for L_i = 0)
+      for (int w = 0; w < TW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int k = 0; k < NSC; k++) {
         const int r = lane + 32 * k;
         if (r < T) {
-          const uint32_t rv = roots[r];
-          const int elt = rv & 0xFFFF, pos = rv >> 16;
-          const uint32_t lw = key.LW2[pos];
-          roots[r] = (lw << 16) | (elt ? glog[elt] : 0xFFFFu);
-        }
-      }
-      __syncwarp();
-      // syndromes of the found error: sum over roots of w2_i L_i^j
-      uint32_t sc[NSC];
+          const uint4 *col = reinterpret_cast<const uint4 *>(key.HT + (size_t)(roots[r] >> 16) * key.ldh);
 #pragma unroll
-      for (int k = 0; k < NSC; k++) sc[k] = 0;
-#pragma unroll 4
-      for (int r = 0; r < T; r++) {
-        const uint32_t rv = roots[r];
-        const int lw = rv >> 16, ll = rv & 0xFFFF;
-        if (ll == 0xFFFF) {  // L_i = 0 contributes only to s_0
-          if (lane == 0) sc[0] ^= gexp[lw];
-        } else {
-          // log(w2_i L_i^j) for j = lane + 32k, stepping by 32 log L_i mod 2^m - 1
-          int idx = fold_mod<M>(lw + lane * ll);
-          const int step = fold_mod<M>(32 * ll);
-#pragma unroll
-          for (int k = 0; k < NSC; k++) {
-            sc[k] ^= gexp[idx];
-            idx += step;
-            idx = idx >= Q - 1 ? idx - (Q - 1) : idx;
+          for (int w = 0; w < TW4; w++) {
+            const uint4 v = col[w];
+            acc[w].x ^= v.x;
+            acc[w].y ^= v.y;
+            acc[w].z ^= v.z;
+            acc[w].w ^= v.w;
           }
         }
       }
-      bool mism = false;
+      const uint32_t *srow = S2 + op * lds2;
+      uint32_t mism = 0;
 #pragma unroll
-      for (int k = 0; k < NSC; k++)
-        if (lane + 32 * k < T && sc[k] != sr[k]) mism = true;
-      ok = !__any_sync(0xffffffffu, mism);
+      for (int w = 0; w < TW4; w++) {
+        const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
+#pragma unroll
+        for (int e2 = 0; e2 < 4; e2++) {
+          const int word = 4 * w + e2;
+          if (word < TW) {
+            const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
+            const uint32_t msk = (word == TW - 1 && (T * M) % 32) ? ((1u << ((T * M) % 32)) - 1u) : 0xFFFFFFFFu;
+            if ((word & 31) == lane) mism |= (v ^ srow[word]) & msk;
+          }
+        }
+      }
+      ok = !__any_sync(0xffffffffu, mism != 0);
     }
     uint32_t *erow = E + op * lde;
     for (int it = lane; it < NW; it += 32) erow[it] = esm[it];
