@@ -133,13 +133,20 @@ __device__ __forceinline__ uint32_t expand4(uint32_t v) {
 }
 
 // ---------------------------------------------------------------- tcgen05 engine
-constexpr int TC_EXP_WARPS = 4;                           // X expanders, then the epilogue
-constexpr int TC_THREADS = (TC_EXP_WARPS + 2) * 32;       // + A producer warp + MMA warp
+// Persistent: one CTA per SM walks the (m-tile, n-tile) list. The stage ring
+// runs on across tiles, and the FP32 accumulator is double-buffered in tensor
+// memory (2 x 256 columns), so the epilogue of one tile overlaps the MMAs of
+// the next. Warp roles: 0-3 expand X stages, 4 issues the A bulk copies, 5
+// issues the MMAs, 6-9 drain accumulators (warp w reads TMEM lanes
+// 32 (w % 4) .. +31).
+constexpr int TC_EXP_WARPS = 4;
+constexpr int TC_EPI_WARP0 = TC_EXP_WARPS + 2;
+constexpr int TC_THREADS = (TC_EXP_WARPS + 2 + 4) * 32;
 constexpr int TC_EXP_THREADS = TC_EXP_WARPS * 32;
 constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
 constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
-constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 256;
-constexpr uint32_t TC_TMEM_COLS = kTcN;    // FP32 accumulator: 128 lanes x kTcN columns
+constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 512;
+constexpr uint32_t TC_TMEM_COLS = 2 * kTcN;  // two FP32 accumulators of 128 lanes x kTcN columns
 static_assert(TC_EXP_THREADS == kTcM, "one expander thread per accumulator lane");
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
@@ -147,6 +154,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys, const Segs segs, int kstages,
+                                                              int mtiles, long long ntiles,
                                                               const uint32_t *__restrict__ X, int ldx,
                                                               uint32_t *__restrict__ Out, int ldo, int out_words,
                                                               int *__restrict__ err) {
@@ -156,18 +164,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   uint64_t *full_a = reinterpret_cast<uint64_t *>(Xs + kTcStages * TC_X_BYTES);
   uint64_t *full_x = full_a + kTcStages;
   uint64_t *empty = full_x + kTcStages;
-  uint64_t *done = empty + kTcStages;
+  uint64_t *acc_full = empty + kTcStages;  // [2]
+  uint64_t *acc_empty = acc_full + 2;      // [2]
+  uint64_t *done = acc_empty + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   int *last_copy = reinterpret_cast<int *>(tmem_slot + 2);  // [kTcStages]: last stage copied per buffer
-  int *issued_sh = last_copy + kTcStages;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long op0 = (long long)blockIdx.x * kTcN;
-  const int mtile = blockIdx.y;
-  const int seg = seg_find(segs, op0);  // a tile never straddles segments
-  const uint8_t *__restrict__ A8 = keys.A8[seg];
-  const long long live_end = segs.row0[seg] + segs.nreq[seg];
+  const long long ntile_all = (long long)mtiles * ntiles;
   if (tid == 0) {
     for (int i = 0; i < kTcStages; i++) {
       mbar_init(&full_a[i], 1);
@@ -175,9 +180,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
       mbar_init(&empty[i], 1);
       last_copy[i] = -1;
     }
+    for (int i = 0; i < 2; i++) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 4 * 32);
+    }
     mbar_init(done, 1);
     *abort_flag = 0;
-    *issued_sh = 0;
     fence_mbar_init();
   }
   if (warp == 0) {
@@ -191,100 +199,117 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   constexpr uint32_t idesc = idesc_f8f6f4_e4m3(kTcM, kTcN);
 
   if (warp < TC_EXP_WARPS) {
-    // X expanders: thread tid writes whole 128-bit stage rows r = tid + 128 j;
-    // the 16-byte loads of stage s+1 are in flight while stage s is expanded
+    // X expanders: thread tid writes whole 128-bit stage rows r = tid + 128 j
     constexpr int RPT = kTcN / TC_EXP_THREADS;
-    uint4 xnext[RPT];
-    const uint32_t *xrow0 = X + (size_t)(op0 + tid) * ldx;
+    long long g = 0;  // global stage counter of this CTA
+    for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x) {
+      const long long op0 = (tile / mtiles) * kTcN;
+      const uint32_t *xrow0 = X + (size_t)(op0 + tid) * ldx;
+      uint4 xnext[RPT];
 #pragma unroll
-    for (int j = 0; j < RPT; j++)
-      xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx);
-    for (int s = 0; s < kstages; s++) {
-      const int buf = s % kTcStages;
-      if (s >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(s / kTcStages - 1) & 1)) *abort_flag = 1;
-      if (*abort_flag) break;
-      uint4 xcur[RPT];
+      for (int j = 0; j < RPT; j++)
+        xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx);
+      for (int s = 0; s < kstages; s++, g++) {
+        const int buf = (int)(g % kTcStages);
+        if (g >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(g / kTcStages - 1) & 1)) *abort_flag = 1;
+        if (*abort_flag) break;
+        uint4 xcur[RPT];
 #pragma unroll
-      for (int j = 0; j < RPT; j++) xcur[j] = xnext[j];
-      if (s + 1 < kstages) {
+        for (int j = 0; j < RPT; j++) xcur[j] = xnext[j];
+        if (s + 1 < kstages) {
 #pragma unroll
-        for (int j = 0; j < RPT; j++)
-          xnext[j] =
-              *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx + 4 * (s + 1));
-      }
-      // request bits -> FP8 core matrices (row r, 16-bit chunk kc at
-      // ((r/8)*8 + kc)*128 + (r%8)*16)
-      uint8_t *xb = Xs + buf * TC_X_BYTES;
-#pragma unroll
-      for (int j = 0; j < RPT; j++) {
-        const int r = tid + j * TC_EXP_THREADS;
-        const uint32_t wv[4] = {xcur[j].x, xcur[j].y, xcur[j].z, xcur[j].w};
-        uint8_t *rb = xb + (r >> 3) * 1024 + (r & 7) * 16;
-#pragma unroll
-        for (int kc = 0; kc < 8; kc++) {
-          const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
-          uint4 v;
-          v.x = expand4(bits & 0xFu);
-          v.y = expand4((bits >> 4) & 0xFu);
-          v.z = expand4((bits >> 8) & 0xFu);
-          v.w = expand4((bits >> 12) & 0xFu);
-          *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
+          for (int j = 0; j < RPT; j++)
+            xnext[j] =
+                *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx + 4 * (s + 1));
         }
+        // request bits -> FP8 core matrices (row r, 16-bit chunk kc at
+        // ((r/8)*8 + kc)*128 + (r%8)*16)
+        uint8_t *xb = Xs + buf * TC_X_BYTES;
+#pragma unroll
+        for (int j = 0; j < RPT; j++) {
+          const int r = tid + j * TC_EXP_THREADS;
+          const uint32_t wv[4] = {xcur[j].x, xcur[j].y, xcur[j].z, xcur[j].w};
+          uint8_t *rb = xb + (r >> 3) * 1024 + (r & 7) * 16;
+#pragma unroll
+          for (int kc = 0; kc < 8; kc++) {
+            const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
+            uint4 v;
+            v.x = expand4(bits & 0xFu);
+            v.y = expand4((bits >> 4) & 0xFu);
+            v.z = expand4((bits >> 8) & 0xFu);
+            v.w = expand4((bits >> 12) & 0xFu);
+            *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
+          }
+        }
+        fence_proxy_async();  // generic-proxy writes visible to the tensor core
+        mbar_arrive(&full_x[buf]);
       }
-      fence_proxy_async();  // generic-proxy writes visible to the tensor core
-      mbar_arrive(&full_x[buf]);
     }
   } else if (warp == TC_EXP_WARPS) {
     if (lane == 0) {  // A producer: one bulk copy per stage into a free buffer
-      const uint8_t *Atile = A8 + (size_t)mtile * kstages * TC_A_BYTES;
-      for (int s = 0; s < kstages; s++) {
-        const int buf = s % kTcStages;
-        if (s >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(s / kTcStages - 1) & 1)) *abort_flag = 1;
-        if (*abort_flag) break;
-        mbar_expect_tx(&full_a[buf], TC_A_BYTES);
-        bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &full_a[buf]);
-        last_copy[buf] = s;
+      long long g = 0;
+      for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x) {
+        const int mtile = (int)(tile % mtiles);
+        const int seg = seg_find(segs, (tile / mtiles) * kTcN);  // a tile never straddles segments
+        const uint8_t *Atile = keys.A8[seg] + (size_t)mtile * kstages * TC_A_BYTES;
+        for (int s = 0; s < kstages; s++, g++) {
+          const int buf = (int)(g % kTcStages);
+          if (g >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(g / kTcStages - 1) & 1)) *abort_flag = 1;
+          if (*abort_flag) break;
+          mbar_expect_tx(&full_a[buf], TC_A_BYTES);
+          bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &full_a[buf]);
+          last_copy[buf] = (int)g;
+        }
       }
     }
-  } else {
+  } else if (warp == TC_EXP_WARPS + 1) {
     if (lane == 0) {  // MMA issuer
-      int issued = 0;
-      for (int s = 0; s < kstages; s++) {
-        const int buf = s % kTcStages;
-        const uint32_t par = (uint32_t)(s / kTcStages) & 1;
-        if (!mbar_wait(&full_a[buf], par) || !mbar_wait(&full_x[buf], par)) *abort_flag = 1;
+      long long g = 0;
+      int i = 0;  // local tile index
+      for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x, i++) {
+        const int ab = i & 1;
+        // the epilogue has drained this accumulator's previous tile
+        if (i >= 2 && !mbar_wait(&acc_empty[ab], (uint32_t)((i >> 1) - 1) & 1)) *abort_flag = 1;
         if (*abort_flag) break;
         tc_fence_after();
-        const uint32_t a0 = smem_u32(As + buf * TC_A_BYTES), x0 = smem_u32(Xs + buf * TC_X_BYTES);
+        const uint32_t dacc = tmem + (uint32_t)(ab * kTcN);
+        for (int s = 0; s < kstages; s++, g++) {
+          const int buf = (int)(g % kTcStages);
+          const uint32_t par = (uint32_t)(g / kTcStages) & 1;
+          if (!mbar_wait(&full_a[buf], par) || !mbar_wait(&full_x[buf], par)) *abort_flag = 1;
+          if (*abort_flag) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(As + buf * TC_A_BYTES), x0 = smem_u32(Xs + buf * TC_X_BYTES);
 #pragma unroll
-        for (int kk = 0; kk < kTcKB / 32; kk++) {
-          const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
-          const uint64_t bd = smem_desc(x0 + kk * 256, 128, 1024);
-          mma_f8(tmem, ad, bd, idesc, (s > 0 || kk > 0) ? 1u : 0u);
+          for (int kk = 0; kk < kTcKB / 32; kk++) {
+            const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
+            const uint64_t bd = smem_desc(x0 + kk * 256, 128, 1024);
+            mma_f8(dacc, ad, bd, idesc, (s > 0 || kk > 0) ? 1u : 0u);
+          }
+          mma_commit(&empty[buf]);
         }
-        mma_commit(&empty[buf]);
-        issued = s + 1;
+        if (*abort_flag) break;
+        mma_commit(&acc_full[ab]);  // arrives when this tile's MMAs have completed
       }
       mma_commit(done);  // arrives once every MMA issued above has completed
-      *issued_sh = issued;
     }
-  }
-  __syncthreads();
-  // drain: the MMAs (done barrier) and any A copy still landing
-  bool ok = mbar_wait(done, 0);
-  if (warp == TC_EXP_WARPS && lane == 0) {
-    for (int b = 0; b < kTcStages; b++)
-      if (last_copy[b] >= 0 && !mbar_wait(&full_a[b], (uint32_t)(last_copy[b] / kTcStages) & 1)) ok = false;
-  }
-  const int good = __syncthreads_and(ok && !*abort_flag && *issued_sh == kstages);
-  tc_fence_after();
-  if (good) {
-    if (warp < TC_EXP_WARPS) {
-      // epilogue: warp w owns accumulator lanes (rows) 32w..32w+31
+  } else {
+    // epilogue: accumulator lanes (rows) 32 (warp % 4) .. +31
+    const int quad = warp & 3;
+    int i = 0;
+    for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x, i++) {
+      const int ab = i & 1;
+      if (!mbar_wait(&acc_full[ab], (uint32_t)(i >> 1) & 1)) *abort_flag = 1;
+      if (*abort_flag) break;
+      tc_fence_after();
+      const int mtile = (int)(tile % mtiles);
+      const long long op0 = (tile / mtiles) * kTcN;
+      const int seg = seg_find(segs, op0);
+      const long long live_end = segs.row0[seg] + segs.nreq[seg];
 #pragma unroll 1
       for (int cb = 0; cb < kTcN / 32; cb++) {
         uint32_t r[32];
-        GMC_TMEM_LD32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * cb), r);
+        GMC_TMEM_LD32(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(ab * kTcN + 32 * cb), r);
         tmem_ld_wait();
         uint32_t mine = 0;
 #pragma unroll
@@ -294,13 +319,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
           if (lane == j) mine = word;
         }
         const long long op = op0 + 32 * cb + lane;
-        const int wd = mtile * (kTcM / 32) + warp;
+        const int wd = mtile * (kTcM / 32) + quad;
         if (op < live_end && wd < out_words) Out[op * ldo + wd] = mine;
       }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[ab]);
     }
-  } else if (tid == 0) {
-    atomicExch(err, 1);
   }
+  __syncthreads();
+  // drain: the MMAs (done barrier) and any A copy still landing
+  bool ok = mbar_wait(done, 0);
+  if (warp == TC_EXP_WARPS && lane == 0) {
+    for (int b = 0; b < kTcStages; b++)
+      if (last_copy[b] >= 0 && !mbar_wait(&full_a[b], (uint32_t)(last_copy[b] / kTcStages) & 1)) ok = false;
+  }
+  const int good = __syncthreads_and(ok && !*abort_flag);
+  if (!good && tid == 0) atomicExch(err, 1);
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, TC_TMEM_COLS);
@@ -347,8 +381,14 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
     if (!keys.A8[i]) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(gf2_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)(rows / kTcN), rows_pad / kTcM);
-  gf2_gemm_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(keys, segs, kw_pad / (kTcKB / 32), X, ldx, Out, ldo, out_words, err);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int mtiles = rows_pad / kTcM;
+  const long long ntiles = rows / kTcN, tiles = ntiles * mtiles;
+  const int grid = (int)(tiles < sms ? tiles : sms);  // persistent: one CTA per SM (smem and TMEM bound)
+  gf2_gemm_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(keys, segs, kw_pad / (kTcKB / 32), mtiles, ntiles, X, ldx, Out, ldo,
+                                                 out_words, err);
   return cudaGetLastError();
 }
 
