@@ -140,8 +140,7 @@ __device__ __forceinline__ uint32_t expand4(uint32_t v) {
 // issues the MMAs, 6-9 drain accumulators (warp w reads TMEM lanes
 // 32 (w % 4) .. +31).
 constexpr int TC_EXP_WARPS = 4;
-constexpr int TC_EPI_WARP0 = TC_EXP_WARPS + 2;
-constexpr int TC_THREADS = (TC_EXP_WARPS + 2 + 4) * 32;
+constexpr int TC_THREADS = (TC_EXP_WARPS + 2 + 4) * 32;  // expanders, producer, MMA, 4 epilogue warps
 constexpr int TC_EXP_THREADS = TC_EXP_WARPS * 32;
 constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
 constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
