@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="seconds per serving load level (60 = the "
                     "full serving configuration)")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the N = 256..65536 throughput sweep")
+    ap.add_argument("--no-engines", action="store_true", help="skip the syndrome-engine comparison")
     return ap.parse_args()
 
 
@@ -306,6 +308,122 @@ def grouped_mix(gmc, torch, dev, total, steps, warmup):
     }
 
 
+def n_sweep(gmc, torch, dev, set_name, ns, steps, flip=0.10):
+    """KEM ops/s (enc + dec of N requests, device-timed, L2 flushed between steps) for each batch size N."""
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+    sid = gmc.set_id(set_name)
+    z = gmc.set_sizes(sid)
+    pk, sk = gmc.keypair(sid, bytes([0x5A]) * 32)
+    P, S = gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(99)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device=dev)
+    out = {}
+    for n in ns:
+        seeds = torch.randint(0, 256, (n, 32), dtype=torch.uint8, device=dev, generator=gen)
+        seeds2 = torch.randint(0, 256, (n, 32), dtype=torch.uint8, device=dev, generator=gen)
+        c = torch.empty((n, z["ct_bytes"]), dtype=torch.uint8, device=dev)
+        k = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+        cts = torch.empty((n, z["ct_bytes"]), dtype=torch.uint8, device=dev)
+        kd = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+        P.enc_batch_dev(cts.data_ptr(), kd.data_ptr(), seeds2.data_ptr(), n, 0, st)
+        nflip = int(flip * n)
+        if nflip:
+            rng = np.random.default_rng(n)
+            idx = torch.from_numpy(rng.choice(n, nflip, replace=False)).to(dev)
+            bits = torch.from_numpy(rng.integers(0, z["mt"], nflip)).to(dev)
+            cts[idx, bits // 8] ^= (1 << (bits % 8)).to(torch.uint8)
+
+        def step():
+            P.enc_batch_dev(c.data_ptr(), k.data_ptr(), seeds.data_ptr(), n, 0, st)
+            S.dec_batch_dev(kd.data_ptr(), cts.data_ptr(), n, 0, st)
+
+        for _ in range(3):
+            step()
+        ms = []
+        for i in range(steps):
+            flush.fill_(i)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        m = sum(ms) / len(ms)
+        out[str(n)] = {"ops_s": 2 * n / (m / 1e3), "ms_per_step": m}
+    return out
+
+
+def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops):
+    """The encapsulation syndrome c[0:mt] = e[0:mt] ^ T e[mt:n] of n requests with each engine, from the
+    engine's per-kernel events: the GF(2) GEMM (mt x k bits times k x n) for the CUDA-core, legacy b1 mma and
+    tcgen05 engines, and for the sparse engine the sampler time it adds over the sampler alone.
+    Work = mt*k bit-MACs per request; the tensor-core figures also as a fraction of the measured dense bf16
+    peak (the tcgen05 FP8 kind used here has twice the nominal rate of bf16)."""
+    import ctypes
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+    sid = gmc.set_id(set_name)
+    z = gmc.set_sizes(sid)
+    pk, _ = gmc.keypair(sid, bytes([0x33]) * 32)
+    P = gmc.PublicKey(sid, pk)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    seeds = torch.randint(0, 256, (n, 32), dtype=torch.uint8, device=dev, generator=gen)
+    c = torch.empty((n, z["ct_bytes"]), dtype=torch.uint8, device=dev)
+    k = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    macs = z["mt"] * z["k"] * n
+    prev = gmc.get_gemm_engine()
+    times = {}
+    for name, eng in (("popc", gmc.GEMM_POPC), ("b1mma", gmc.GEMM_B1MMA), ("tc", gmc.GEMM_TC),
+                      ("sparse", gmc.GEMM_SPARSE)):
+        gmc.set_gemm_engine(eng)
+        for _ in range(2):
+            P.enc_batch_dev(c.data_ptr(), k.data_ptr(), seeds.data_ptr(), n, 0, st)
+        torch.cuda.synchronize()
+        L.gmc_prof_enable(1)
+        reps = 2 if name == "b1mma" else steps
+        for _ in range(reps):
+            P.enc_batch_dev(c.data_ptr(), k.data_ptr(), seeds.data_ptr(), n, 0, st)
+        torch.cuda.synchronize()
+        buf = ctypes.create_string_buffer(4096)
+        L.gmc_prof_report(buf, 4096)
+        L.gmc_prof_enable(0)
+        ks = {}
+        for ln in buf.value.decode().strip().splitlines():
+            nm, cnt, ms = ln.split()
+            ks[nm] = float(ms) / reps
+        times[name] = ks
+    gmc.set_gemm_engine(prev)
+    sample_only = times["tc"].get("enc_sample", 0.0)
+    out = {"set": set_name, "n": n, "bit_macs": macs, "engines": {}}
+    for name in ("popc", "b1mma", "tc"):
+        ms = times[name]["enc_syndrome_gemm"]
+        e = {"ms": ms, "bit_macs_per_s": macs / (ms / 1e3)}
+        if name == "tc":
+            tf = 2.0 * macs / (ms / 1e3) / 1e12
+            e["fp8_equivalent_tflops"] = tf
+            e["frac_of_measured_bf16_peak"] = tf / tc_peak_tflops
+            e["frac_of_fp8_nominal_2x_bf16"] = tf / (2 * tc_peak_tflops)
+        out["engines"][name] = e
+    sp = times["sparse"]["enc_sample_syndrome"]
+    out["engines"]["sparse"] = {"ms_sampler_with_syndrome": sp, "ms_added_over_sampler": sp - sample_only,
+                                "note": "XOR of <= t public-key columns per request inside the sampler"}
+    return out
+
+
+def keccak_rates(z, n, kernels):
+    """Keccak-f[1600] permutations per second of the two session-key hash kernels (each request hashes the
+    1 + n/8 + ct-byte preimage: ceil((len + 1) / 136) permutations)."""
+    perms = (1 + z["n"] // 8 + z["ct_bytes"] + 1 + 135) // 136
+    out = {"perms_per_hash": perms}
+    for kname in ("enc_finalize_hash", "dec_tail_hash"):
+        if kname in kernels:
+            out[kname] = {"perms_per_s": n * perms / (kernels[kname]["ms"] / 1e3)}
+    return out
+
+
 def serving(gmc, torch, seconds):
     """16 device-resident key pairs over the five sets, 50/50 enc/dec, Poisson arrivals at 10/50/90% of the
     measured peak; p50/p99 latency (arrival to completion) against sequential one-request calls."""
@@ -480,6 +598,13 @@ def main():
         "wall_s_timed_loop": wall,
     }
 
+    line["keccak"] = keccak_rates(z, N, kernels)
+    if rank == 0 and not args.no_sweep:
+        line["n_sweep"] = {"set": args.set, "flip": args.flip,
+                           "ops_s": n_sweep(gmc, torch, dev, args.set, [256, 1024, 4096, 16384, 65536], 5, args.flip)}
+    if rank == 0 and not args.no_engines:
+        line["syndrome_engines"] = [syndrome_engines(gmc, torch, dev, L, s_, 65536, 5, tc_peak)
+                                    for s_ in dict.fromkeys(("348864", args.set))]
     if rank == 0 and not args.no_grouped:
         line["grouped"] = grouped_mix(gmc, torch, dev, N, max(5, args.steps // 2), args.warmup)
     if rank == 0 and not args.no_serving:

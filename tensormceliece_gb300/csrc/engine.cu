@@ -158,7 +158,7 @@ static int get_field(int set, FieldDev *out) {
     return at;
   };
   const size_t o_exp = put(F.exp), o_log = put(F.log), o_twist = put(ft.twist_log), o_frlo = put(ft.frob_lo),
-               o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs);
+               o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs), o_zech = put(ft.zech);
   FieldEntry e;
   GMC_CUDA(cudaMalloc(&e.buf, all.size() * 2));
   GMC_CUDA(cudaMemcpy(e.buf, all.data(), all.size() * 2, cudaMemcpyHostToDevice));
@@ -168,6 +168,7 @@ static int get_field(int set, FieldDev *out) {
   e.fd.frob_lo = e.buf + o_frlo;
   e.fd.fft_alpha_bs = reinterpret_cast<const uint32_t *>(e.buf + o_abs);
   e.fd.frob_hi_bs = reinterpret_cast<const uint32_t *>(e.buf + o_fhbs);
+  e.fd.zech = e.buf + o_zech;
   g_fields[key] = e;
   *out = e.fd;
   return GMC_OK;

@@ -154,6 +154,10 @@ FftTables build_fft_tables(int m, int d) {
   t.frob_hi.resize(1 << (m - d));
   for (int c = 0; c < (1 << (m - d)); c++) t.frob_hi[c] = frob((uint16_t)(c << d));
 
+  t.zech.assign(1 << m, 0);
+  t.zech[0] = (uint16_t)(3 << m);
+  for (int k = 1; k < (1 << m) - 1; k++) t.zech[k] = F.log[1 ^ F.exp[k]];
+
   // bit-sliced forms: 32 chunks per word
   const int H = (1 << (m - d)) / 32;
   auto put_word = [](std::vector<uint16_t> &v, size_t w, uint32_t x) {

@@ -39,6 +39,10 @@ struct FftTables {
   //   frob_hi_bs[h * m + b]: frob_hi[c]
   std::vector<uint16_t> alpha_bs;
   std::vector<uint16_t> frob_hi_bs;
+  // Zech logarithms: zech[k] = log(1 + g^k) for 0 < k < q-1; zech[0] (1 + 1 = 0)
+  // is 3q, a log at or above the zero sentinel 2q-2 that stays below 2^16
+  // after adding any log < q-1 and reducing once by q-1.
+  std::vector<uint16_t> zech;
 };
 FftTables build_fft_tables(int m, int d);
 

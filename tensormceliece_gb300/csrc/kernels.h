@@ -10,6 +10,8 @@ constexpr int kSampleWarpsPerSM = 8;     // sampler: resident warps per SM (lane
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
 constexpr int kBMWarps = 8;     // Berlekamp-Massey kernel: warps per block (32 requests per warp)
+constexpr int kBMLatWarps = 24;  // Berlekamp-Massey latency form: warps per block (one request per warp)
+constexpr long long kBMBitslicedMinRows = 24576;  // smaller batches take the latency form
 constexpr int kRootWarps = 8;  // root-finding kernel: warps per block
 
 // ---------------------------------------------------------------- segments
@@ -132,6 +134,7 @@ struct FieldDev {
   // bit-sliced over 32 chunks per word (bit k: chunk 32 h + k), plane b = bit b
   const uint32_t *fft_alpha_bs;   // [(2^d - 2^(d-l) + xh) * H + h][m]: alpha_{l, (c << (d-1-l)) + xh}
   const uint32_t *frob_hi_bs;     // [h][m]: (c 2^d)^(2^d)
+  const uint16_t *zech;           // [q]: log(1 + g^k), zech[0] = 3q (zero)
 };
 
 // Per-key decapsulation tables of the segments of a launch.

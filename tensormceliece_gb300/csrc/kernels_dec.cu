@@ -281,6 +281,159 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
   }
 }
 
+// ---------------------------------------------------------------- BM, latency form
+// Used for small batches (fewer requests than the bit-sliced form needs to
+// fill the GPU): per-request latency is one warp walking 2t iterations of
+// ~100 instructions instead of a group of 32 walking ~1500.
+// One warp per request (persistent grid). Coefficient i of C (connection
+// polynomial) lives in lane i%32, slot i/32, as its log only: the update
+// C_i += f B_i is done in the log domain with Zech logarithms,
+// log(a + b) = log a + zech(log b - log a), one table lookup instead of an
+// antilog and a log. Any log at or above the zero sentinel 2q-2 means 0.
+// B = x^s B' is kept unshifted: B' (the connection polynomial before the last
+// length change, as logs) sits in a per-warp shared array behind a guard of
+// 2t zero logs, so B_i is the entry at i - s and the per-iteration shift is
+// s += 1. The syndrome logs sit behind a 32-entry zero guard, so the
+// discrepancy reads s_{n-i} for every lane of an active slot without a
+// per-lane test (C_i = 0 above deg C). Coefficients above t are never
+// updated, as in the library's fixed-size arrays.
+// Degree bounds used to skip empty slots (exact, also for undecodable input):
+// before iteration n, deg C <= L and deg B <= n+1-L, so the discrepancy needs
+// coefficients i <= min(L, t) and the update i <= min(max(L, n+1-L), t).
+template <int SET>
+struct BMLatLayout {
+  using p = P<SET>;
+  static constexpr int Q = p::q, T = p::t;
+  static constexpr int NS = (T + 1 + 31) / 32;
+  static constexpr int exp_off = 0, log_off = 2 * Q, zech_off = 3 * Q;
+  static constexpr int shared_u16 = 4 * Q;
+  static constexpr int sguard = 32, bguard = 2 * T;
+  static constexpr int s_off = 0, s_len = sguard + 2 * T;          // per warp, u16
+  static constexpr int b_off = s_len, b_len = bguard + 32 * NS;
+  static constexpr int warp_u16 = (s_len + b_len + 1) & ~1;
+  static constexpr int bytes(int warps) { return shared_u16 * 2 + warps * warp_u16 * 2; }
+};
+
+template <int SET>
+__global__ void __launch_bounds__(kBMLatWarps * 32, 2) dec_bm_lat_kernel(const uint32_t *__restrict__ S2, int lds2,
+                                                                  FieldDev fd, const Segs segs,
+                                                                  uint16_t *__restrict__ Sig) {
+  using p = P<SET>;
+  using LY = BMLatLayout<SET>;
+  constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
+  constexpr int ZL = GFLog<M>::zero_log;
+  constexpr int NS = LY::NS;
+  constexpr int NSY = (2 * T + 31) / 32;
+  constexpr int SIG = 1 << D;
+  extern __shared__ __align__(16) uint16_t lsm[];
+  uint16_t *gexp = lsm + LY::exp_off;
+  uint16_t *glog = lsm + LY::log_off;
+  uint16_t *zech = lsm + LY::zech_off;
+  for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) {
+    glog[i] = fd.glog[i];
+    zech[i] = fd.zech[i];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint16_t *wsm = lsm + LY::shared_u16 + warp * LY::warp_u16;
+  uint16_t *slog = wsm + LY::s_off + LY::sguard;  // slog[-32 .. -1] = zero logs
+  uint16_t *blog = wsm + LY::b_off + LY::bguard;  // blog[-2t .. -1] = zero logs
+  for (int i = lane; i < LY::sguard; i += 32) wsm[LY::s_off + i] = (uint16_t)ZL;
+  for (int i = lane; i < LY::bguard; i += 32) wsm[LY::b_off + i] = (uint16_t)ZL;
+  __syncthreads();
+  const long long N = seg_rows(segs);
+  const long long nwarps = (long long)gridDim.x * kBMLatWarps;
+  for (long long op = (long long)blockIdx.x * kBMLatWarps + warp; op < N; op += nwarps) {
+    int seg;
+    if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
+    const uint32_t *srow = S2 + op * lds2;
+#pragma unroll
+    for (int k = 0; k < NSY; k++) {
+      const int j = lane + 32 * k;
+      if (j < 2 * T) {
+        const int b = j * M, w = b >> 5, sh = b & 31;
+        uint32_t v = srow[w] >> sh;
+        if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
+        slog[j] = glog[v & (Q - 1)];
+      }
+    }
+    // B' = 1, s = 1 (B = x)
+#pragma unroll
+    for (int k = 0; k < NS; k++) blog[lane + 32 * k] = (lane + 32 * k == 0) ? 0 : (uint16_t)ZL;
+    __syncwarp();
+    uint32_t lC[NS];
+#pragma unroll
+    for (int k = 0; k < NS; k++) lC[k] = (lane + 32 * k == 0) ? 0 : ZL;
+    int L = 0, sft = 1;
+    uint32_t lb = 0;  // log b, b = 1
+#pragma unroll 1
+    for (int n = 0; n < 2 * T; n++) {
+      const int bd = L < T ? L : T;                       // discrepancy: i <= min(L, t) (L <= n)
+      int bu = (L > n + 1 - L) ? L : n + 1 - L;           // update: i <= min(max(L, n+1-L), t)
+      bu = bu < T ? bu : T;
+      uint32_t dp = 0;
+      const uint16_t *sn = slog + n - lane;
+#pragma unroll
+      for (int k = 0; k < NS; k++)
+        if (32 * k <= bd) dp ^= gf_mul_log<M>(gexp, lC[k], sn[-32 * k]);
+      const uint32_t d = __reduce_xor_sync(0xffffffffu, dp);
+      if (d) {
+        const bool upd = (n >= 2 * L);
+        const int ld = glog[d];
+        int lf = ld - (int)lb;
+        if (lf < 0) lf += Q - 1;
+        const uint16_t *bs = blog + lane - sft;
+        uint32_t lco[NS];
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+          lco[k] = lC[k];
+          if (32 * k <= bu) {
+            // log(C_i + f B_i): p = log(f B_i); zero B_i keeps C_i, zero C_i takes p
+            constexpr uint32_t Q1 = Q - 1;
+            const uint32_t lbi = bs[32 * k], lc = lC[k];
+            uint32_t pl = (uint32_t)lf + lbi;
+            pl = min(pl, pl - Q1);                      // < q-1 when B_i != 0
+            uint32_t kk = pl - lc;                      // log(f B_i / C_i) mod q-1
+            kk = min(kk + Q1, kk);
+            const uint32_t z = zech[min(kk, Q1 - 1)];   // index clamped for the zero cases
+            uint32_t nl = lc + z;
+            nl = min(nl, nl - Q1);                      // >= 2q-2 when the sum is 0
+            nl = (lc >= (uint32_t)ZL) ? pl : nl;
+            nl = (lbi >= (uint32_t)ZL) ? lc : nl;
+            const bool in = (k < NS - 1) || (lane + 32 * k <= T);  // coefficients above t stay zero
+            if (in) lC[k] = nl;
+          }
+        }
+        if (upd) {
+          __syncwarp();  // every lane has read B' before it is replaced
+#pragma unroll
+          for (int k = 0; k < NS; k++)
+            if (32 * k <= bu) blog[lane + 32 * k] = (uint16_t)lco[k];
+          __syncwarp();
+          L = n + 1 - L;
+          lb = ld;
+          sft = 0;
+        }
+      }
+      sft++;
+    }
+    // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d);
+    // coefficients are < 2^m <= 2^13, so bit 15 is free for the length flag
+    uint16_t *sig = Sig + op * SIG;
+    for (int x = lane; x < SIG; x += 32)
+      if (x > T) sig[x] = 0;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+      const int i = lane + 32 * k;
+      const int deg = T - i;
+      // bit 15 of the constant coefficient flags a final length L > t
+      const uint32_t c = gexp[min(lC[k], (uint32_t)ZL)];
+      if (i <= T && deg < SIG) sig[deg] = (uint16_t)(c | ((deg == 0 && L > T) ? 0x8000u : 0u));
+    }
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------- root finding
 // One warp per request: additive FFT of sigma over all 2^m field elements
 // (Gao-Mateer, basis beta_i = 2^i so point c is the element c), the error
@@ -672,6 +825,15 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
                           cudaStream_t st) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
+  if (N < kBMBitslicedMinRows) {  // small batch: warp per request (lower latency per request)
+    const int smem_l = BMLatLayout<SET>::bytes(kBMLatWarps);
+    cudaError_t err =
+        cudaFuncSetAttribute(dec_bm_lat_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_l);
+    if (err != cudaSuccess) return err;
+    const int gl = persistent_blocks(dec_bm_lat_kernel<SET>, kBMLatWarps * 32, smem_l, N, kBMLatWarps);
+    dec_bm_lat_kernel<SET><<<gl, kBMLatWarps * 32, smem_l, st>>>(S2, lds2, fd, segs, Sig);
+    return cudaGetLastError();
+  }
   const int smem_bm = BMLayout<SET>::bytes(kBMWarps);
   cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bm);
   if (err != cudaSuccess) return err;

@@ -70,8 +70,8 @@ constexpr size_t kScratchBytes =
          DecScratch<4>::total(kMaxRequests));
 
 // per-set field/FFT tables (u16 entries): exp (2q-1) | log (q) | twist (2^(d+1)) | frob_lo (2^d) |
-// bit-sliced alpha (2 (2^d - 1) 2 m) | bit-sliced frob_hi (2 * 2 m), u32 tables at even offsets
-constexpr int kFieldSlot = 2 * 8192 + 8192 + 256 + 128 + 2 * 127 * 2 * 13 + 2 * 2 * 13 + 16;
+// bit-sliced alpha (2 (2^d - 1) 2 m) | bit-sliced frob_hi (2 * 2 m) | zech (q), u32 tables at even offsets
+constexpr int kFieldSlot = 2 * 8192 + 8192 + 256 + 128 + 2 * 127 * 2 * 13 + 2 * 2 * 13 + 8192 + 16;
 static_assert(kFieldSlot % 2 == 0, "per-set slots must keep the u32 tables 4-byte aligned");
 
 }  // namespace
@@ -128,7 +128,7 @@ int device_setup(const DeviceSetup **out) {
       return at;
     };
     const size_t o_exp = put(F.exp), o_log = put(F.log), o_twist = put(ft.twist_log), o_flo = put(ft.frob_lo),
-                 o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs);
+                 o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs), o_zech = put(ft.zech);
     if (!fits) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: field table slot too small");
     uint16_t *base = su.fields + (size_t)set * kFieldSlot;
     if (cudaMemcpy(base, all.data(), all.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -139,6 +139,7 @@ int device_setup(const DeviceSetup **out) {
     su.fd[set].frob_lo = base + o_flo;
     su.fd[set].fft_alpha_bs = reinterpret_cast<const uint32_t *>(base + o_abs);
     su.fd[set].frob_hi_bs = reinterpret_cast<const uint32_t *>(base + o_fhbs);
+    su.fd[set].zech = base + o_zech;
   }
   g_setups.push_back({dev, su});
   *out = &g_setups.back().second;

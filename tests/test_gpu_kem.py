@@ -216,6 +216,28 @@ def test_full_size_roundtrip(gmc, keys, sid):
     assert len({bytes(x) for x in k[:4096]}) == 4096
 
 
+@pytest.mark.parametrize("sid", range(5), ids=SETS)
+def test_bm_forms_agree_on_corrupted_batches(gmc, keys, sid):
+    """A batch large enough for the bit-sliced Berlekamp-Massey (>= 24576 rows) and the same ciphertexts in
+    small batches (warp-per-request form) give identical keys and return codes, on valid, single-bit-flipped
+    and random ciphertexts; an oracle sample of each kind agrees."""
+    pk, sk = keys(sid)
+    n = 32768
+    rng = np.random.default_rng(7 + sid)
+    seeds = rng.integers(0, 256, size=(n, 32), dtype=np.uint8)
+    c, _, _ = gmc.PublicKey(sid, pk).enc_batch(seeds)
+    cts, flipped = flipped_and_random(sid, c, frac=0.1, nrand=256, seed=3)
+    key = gmc.SecretKey(sid, sk)
+    k_big, rc_big = key.dec_batch(cts)
+    parts = [key.dec_batch(cts[i:i + 4096]) for i in range(0, len(cts), 4096)]
+    k_small = np.concatenate([p[0] for p in parts])
+    rc_small = np.concatenate([p[1] for p in parts])
+    assert (k_big == k_small).all() and (rc_big == rc_small).all()
+    sample = np.concatenate([rng.choice(n, 16, replace=False), flipped[:16], np.arange(n, n + 16)])
+    ok2, orc2 = O.dec_batch(sid, sk, cts[sample], threads=THREADS)
+    assert (k_big[sample] == ok2).all() and (rc_big[sample] == orc2).all()
+
+
 @pytest.mark.parametrize("engine", ["tc", "b1mma", "popc", "sparse"])
 @pytest.mark.parametrize("sid", range(5), ids=SETS)
 def test_kem_parity_per_gemm_engine(gmc, keys, sid, engine):
