@@ -10,7 +10,9 @@
 // the free device memory measured at start-up: admission by free HBM).
 // A batch runs as: gather inputs into pinned staging -> one host-to-device
 // copy -> per (parameter set, enc/dec) the segment-aware kernels over all its
-// keys -> one device-to-host copy -> a host callback that scatters results,
+// keys, each pipeline on its own stream (forked from and joined back to the
+// slot's stream, so they overlap) -> one device-to-host copy -> a host
+// callback that scatters results,
 // marks the requests done and records their latency (arrival to completion)
 // in a log-bucket histogram (p50 / p99). Several slots keep several batches in
 // flight, so their work overlaps on the device.
@@ -24,7 +26,6 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
-#include <map>
 #include <mutex>
 #include <random>
 #include <set>
@@ -76,20 +77,48 @@ struct Pipe {
   size_t in_off, k_off, ct_off, rc_off, work_off;
 };
 
+constexpr int kPipes = 2 * GMC_NSETS;  // at most one pipeline per (set, op) in a batch
+
 struct Slot {
   cudaStream_t st = nullptr;
+  cudaStream_t pst[kPipes] = {};     // one stream per pipeline: the pipelines of a batch overlap
+  cudaEvent_t fork = nullptr, join[kPipes] = {};
   uint8_t *dev = nullptr;
   size_t dev_bytes = 0;
   uint8_t *h_in = nullptr, *h_out = nullptr;
   size_t h_in_bytes = 0, h_out_bytes = 0;
   std::vector<Piece> pieces;
   std::vector<Pipe> pipes;
+  std::vector<Req> incoming;  // requests moved out of the queue for the next batch
   size_t in_used = 0, out_used = 0;
   bool busy = false;
   struct gmc_server *srv = nullptr;
 };
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Runs fn(begin, end) over [0, n) in up to kHostThreads pieces (the calling
+// thread takes the first): the per-request gather and scatter of a batch of
+// tens of thousands of requests touch every request's own host buffers.
+constexpr int kHostThreads = 8;
+template <typename F>
+void parallel_for(size_t n, F fn) {
+  const size_t per = 4096;  // below this a piece is not worth a thread
+  const int parts = (int)std::min<size_t>(kHostThreads, (n + per - 1) / per);
+  if (parts <= 1) {
+    fn((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(parts - 1);
+  const size_t chunk = (n + parts - 1) / parts;
+  for (int i = 1; i < parts; i++) {
+    const size_t b = (size_t)i * chunk, e = std::min(n, b + chunk);
+    th.emplace_back([=] { fn(b, e); });
+  }
+  fn((size_t)0, std::min(n, chunk));
+  for (auto &t : th) t.join();
+}
 
 // device bytes of one pipeline's work buffers for `rows` padded rows
 size_t work_bytes(int set, int kind, long long rows) {
@@ -124,7 +153,7 @@ struct gmc_server {
 namespace {
 
 template <int SET>
-cudaError_t run_pipe(Slot &sl, Pipe &pp) {
+cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   const long long rows = seg_rows(pp.segs);
   uint8_t *in = sl.dev + pp.in_off, *kout = sl.dev + pp.k_off;
   uint8_t *work = sl.dev + pp.work_off;
@@ -154,16 +183,16 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp) {
     cudaError_t e;
     if (engine == GEMM_SPARSE) {
       e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, &gk, Sy, mw, tune.sample_threads,
-                             reinterpret_cast<unsigned int *>(Ens), sl.st);
+                             reinterpret_cast<unsigned int *>(Ens), pst);
     } else {
       e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, nullptr, Sy, mw, tune.sample_threads,
-                             reinterpret_cast<unsigned int *>(Sy), sl.st);
+                             reinterpret_cast<unsigned int *>(Sy), pst);
       if (e == cudaSuccess)
         e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->lda, ref->rows_pad, Ens, kw, ref->kw_pad, Sy, mw, p::mw,
-                                tc_err_word_ptr(), sl.st);
+                                tc_err_word_ptr(), pst);
     }
     if (e == cudaSuccess)
-      e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, sl.st);
+      e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, pst);
     return e;
   }
   const int cw = ref->cw_pad, s2 = round_up((2 * S.t * S.m + 31) / 32, 4);
@@ -181,14 +210,14 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp) {
   if (field_tables(SET, &fd) != GMC_OK) return cudaErrorUnknown;
   DecKeys dk{};
   for (size_t i = 0; i < pp.keys.size(); i++) dk.k[i] = pp.keys[i]->dk;
-  cudaError_t e = launch_pack_ct<SET>(in, pp.segs, X, cw, sl.st);
+  cudaError_t e = launch_pack_ct<SET>(in, pp.segs, X, cw, pst);
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->ldf, ref->frows_pad, X, cw, ref->cw_pad, S2, s2, p::s2w,
-                            tc_err_word_ptr(), sl.st);
-  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, sl.st);
-  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, sl.st);
+                            tc_err_word_ptr(), pst);
+  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst);
+  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst);
   if (e == cudaSuccess)
-    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, sl.st);
+    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, pst);
   return e;
 }
 
@@ -196,21 +225,34 @@ void CUDART_CB on_batch_done(void *arg) {
   Slot *sl = (Slot *)arg;
   gmc_server *srv = sl->srv;
   const double t = now_s();
-  for (auto &pc : sl->pieces) {
-    const gmc_setinfo &S = set_info(pc.r.key->set);
-    memcpy(pc.r.k, sl->h_out + pc.out_k, 32);
-    if (pc.r.key->kind == 0) {
-      memcpy(pc.r.ct, sl->h_out + pc.out_ct, S.synd_bytes);
-      if (pc.r.rc) *pc.r.rc = pc.r.key->pad_bad ? -1 : 0;
-    } else if (pc.r.rc) {
-      memcpy(pc.r.rc, sl->h_out + pc.out_rc, 4);
+  // scatter results and bucket latencies (outside the lock), in parallel pieces
+  const int parts = kHostThreads;
+  std::vector<std::vector<long long>> local(parts, std::vector<long long>(kBuckets, 0));
+  std::atomic<int> next_part{0};
+  parallel_for(sl->pieces.size(), [&](size_t b, size_t e) {
+    std::vector<long long> &h = local[next_part.fetch_add(1) % parts];
+    double last_t = -1.0;
+    int last_b = 0;
+    for (size_t i = b; i < e; i++) {
+      Piece &pc = sl->pieces[i];
+      memcpy(pc.r.k, sl->h_out + pc.out_k, 32);
+      if (pc.r.key->kind == 0) {
+        memcpy(pc.r.ct, sl->h_out + pc.out_ct, set_info(pc.r.key->set).synd_bytes);
+        if (pc.r.rc) *pc.r.rc = pc.r.key->pad_bad ? -1 : 0;
+      } else if (pc.r.rc) {
+        memcpy(pc.r.rc, sl->h_out + pc.out_rc, 4);
+      }
+      if (pc.r.t_arrive != last_t) {  // requests of a batch often share their bucket
+        last_t = pc.r.t_arrive;
+        last_b = bucket_of((t - last_t) * 1e3);
+      }
+      h[last_b]++;
+      if (pc.r.done) pc.r.done->store(1, std::memory_order_release);
     }
-  }
+  });
   std::lock_guard<std::mutex> lk(srv->mu);
-  for (auto &pc : sl->pieces) {
-    srv->hist[bucket_of((t - pc.r.t_arrive) * 1e3)]++;
-    if (pc.r.done) pc.r.done->store(1, std::memory_order_release);
-  }
+  for (auto &h : local)
+    for (int b = 0; b < kBuckets; b++) srv->hist[b] += h[b];
   srv->completed += (long long)sl->pieces.size();
   srv->t_last = t;
   sl->busy = false;
@@ -241,65 +283,92 @@ size_t out_bytes(int set, int kind, long long rows) {
 // the largest padding a batch can carry: 5 sets x {enc, dec} pipelines of kMaxSegs keys
 constexpr long long kPadRows = 10LL * kMaxSegs * kGemmOpPad;
 
-// lays out the next batch in a free slot; returns false when nothing was taken
+// Lays out the next batch in a free slot from sl.incoming (moved out of the
+// queue by the dispatcher). Requests are taken in order while they fit the
+// slot's arena and staging (admission by device memory); the rest go back to
+// the queue front. Per request the work is O(1): sizes change only when a
+// key's row count crosses a multiple of kGemmOpPad or a key joins a pipeline.
+// Returns false when nothing was taken.
 bool form_batch(gmc_server *srv, Slot &sl) {
   sl.pieces.clear();
   sl.pipes.clear();
-  // take requests FIFO while they fit the slot's arena and staging (admission by device memory)
+  struct KeyAcc {
+    const gmc_key *key;
+    std::vector<int> members;
+  };
   struct Acc {
-    std::map<const gmc_key *, std::vector<int>> keys;
+    std::vector<KeyAcc> keys;
+    int last = -1;
     long long rows = 0;
   };
-  std::map<std::pair<int, int>, Acc> by;
+  Acc by[GMC_NSETS][2];
   size_t in_b = 0, out_b = 0, dev_need = 0;
-  long long taken = 0;
-  while (!srv->queue.empty() && taken < srv->max_batch) {
-    const Req &r = srv->queue.front();
-    const gmc_setinfo &S = set_info(r.key->set);
-    (void)S;
+  size_t taken = 0;
+  for (; taken < sl.incoming.size(); taken++) {
+    const Req &r = sl.incoming[taken];
     const int kind = r.key->kind, set = r.key->set;
-    Acc &acc = by[{set, kind}];
-    auto it = acc.keys.find(r.key);
-    const size_t cnt = it == acc.keys.end() ? 0 : it->second.size();
-    if (it == acc.keys.end() && acc.keys.size() >= (size_t)kMaxSegs) break;  // one pipeline per (set, op)
-    const long long rows_new = acc.rows - padded(cnt) + padded(cnt + 1);
-    const size_t dev_new = dev_need - pipe_bytes(set, kind, acc.rows) + pipe_bytes(set, kind, rows_new);
-    const size_t in_new = in_b - in_bytes(set, kind, acc.rows) + in_bytes(set, kind, rows_new);
-    const size_t out_new = out_b - out_bytes(set, kind, acc.rows) + out_bytes(set, kind, rows_new);
-    if (in_new > sl.h_in_bytes || out_new > sl.h_out_bytes || dev_new > sl.dev_bytes) break;
-    acc.keys[r.key].push_back((int)sl.pieces.size());
-    acc.rows = rows_new;
-    dev_need = dev_new;
-    in_b = in_new;
-    out_b = out_new;
+    Acc &acc = by[set][kind];
+    int ki = acc.last;
+    if (ki < 0 || acc.keys[ki].key != r.key) {
+      ki = -1;
+      for (size_t i = 0; i < acc.keys.size(); i++)
+        if (acc.keys[i].key == r.key) {
+          ki = (int)i;
+          break;
+        }
+    }
+    const size_t cnt = ki < 0 ? 0 : acc.keys[ki].members.size();
+    if (cnt % kGemmOpPad == 0) {  // a new padded block of rows (or a new key): re-check the admission
+      if (ki < 0 && acc.keys.size() >= (size_t)kMaxSegs) break;  // one pipeline per (set, op)
+      const long long rows_new = acc.rows + kGemmOpPad;
+      const size_t dev_new = dev_need - pipe_bytes(set, kind, acc.rows) + pipe_bytes(set, kind, rows_new);
+      const size_t in_new = in_b - in_bytes(set, kind, acc.rows) + in_bytes(set, kind, rows_new);
+      const size_t out_new = out_b - out_bytes(set, kind, acc.rows) + out_bytes(set, kind, rows_new);
+      if (in_new > sl.h_in_bytes || out_new > sl.h_out_bytes || dev_new > sl.dev_bytes) break;
+      acc.rows = rows_new;
+      dev_need = dev_new;
+      in_b = in_new;
+      out_b = out_new;
+      if (ki < 0) {
+        acc.keys.push_back({r.key, {}});
+        ki = (int)acc.keys.size() - 1;
+      }
+    }
+    acc.last = ki;
+    acc.keys[ki].members.push_back((int)sl.pieces.size());
     sl.pieces.push_back({r, 0, 0, 0});
-    taken++;
-    srv->queue.pop_front();
   }
+  if (taken < sl.incoming.size()) {  // what did not fit waits for the next batch, in order
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (size_t i = sl.incoming.size(); i-- > taken;) srv->queue.push_front(sl.incoming[i]);
+  }
+  sl.incoming.clear();
   if (sl.pieces.empty()) return false;
   // device layout: [inputs of all pipes][outputs of all pipes][work of each pipe]
   size_t off = 0;
-  for (auto &kv : by) {
-    if (kv.second.keys.empty()) continue;
-    Pipe pp{};
-    pp.set = kv.first.first;
-    pp.kind = kv.first.second;
-    pp.segs = Segs{};
-    long long row = 0;
-    for (auto &kk : kv.second.keys) {
+  for (int set = 0; set < GMC_NSETS; set++)
+    for (int kind = 0; kind < 2; kind++) {
+      Acc &acc = by[set][kind];
+      if (acc.keys.empty()) continue;
+      Pipe pp{};
+      pp.set = set;
+      pp.kind = kind;
+      pp.segs = Segs{};
+      long long row = 0;
+      for (auto &kk : acc.keys) {
+        pp.segs.row0[pp.keys.size()] = row;
+        pp.segs.nreq[pp.keys.size()] = (long long)kk.members.size();
+        row += (long long)((kk.members.size() + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad;
+        pp.keys.push_back(kk.key);
+        pp.members.push_back(std::move(kk.members));
+      }
+      pp.segs.nseg = (int)pp.keys.size();
       pp.segs.row0[pp.keys.size()] = row;
-      pp.segs.nreq[pp.keys.size()] = (long long)kk.second.size();
-      row += (long long)((kk.second.size() + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad;
-      pp.keys.push_back(kk.first);
-      pp.members.push_back(kk.second);
+      const gmc_setinfo &S = set_info(pp.set);
+      pp.in_off = off;
+      off += align256(row * (pp.kind == 0 ? 32 : S.synd_bytes));
+      sl.pipes.push_back(std::move(pp));
     }
-    pp.segs.nseg = (int)pp.keys.size();
-    pp.segs.row0[pp.keys.size()] = row;
-    const gmc_setinfo &S = set_info(pp.set);
-    pp.in_off = off;
-    off += align256(row * (pp.kind == 0 ? 32 : S.synd_bytes));
-    sl.pipes.push_back(pp);
-  }
   sl.in_used = off;
   for (auto &pp : sl.pipes) {
     const gmc_setinfo &S = set_info(pp.set);
@@ -318,7 +387,8 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   }
   if (sl.in_used > sl.h_in_bytes || sl.out_used > sl.h_out_bytes || off > sl.dev_bytes) {
     // cannot happen when the admission above holds; never write past the buffers
-    for (auto &pc : sl.pieces) srv->queue.push_front(pc.r);
+    std::lock_guard<std::mutex> lk(srv->mu);
+    for (size_t i = sl.pieces.size(); i-- > 0;) srv->queue.push_front(sl.pieces[i].r);
     sl.pieces.clear();
     return false;
   }
@@ -326,15 +396,19 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   for (auto &pp : sl.pipes) {
     const gmc_setinfo &S = set_info(pp.set);
     const size_t inb = pp.kind == 0 ? 32 : S.synd_bytes;
-    for (size_t s = 0; s < pp.keys.size(); s++)
-      for (size_t j = 0; j < pp.members[s].size(); j++) {
-        Piece &pc = sl.pieces[pp.members[s][j]];
-        const long long row = pp.segs.row0[s] + (long long)j;
-        memcpy(sl.h_in + pp.in_off + row * inb, pc.r.in, inb);
-        pc.out_k = pp.k_off - sl.in_used + row * 32;
-        pc.out_ct = pp.ct_off - sl.in_used + row * S.synd_bytes;
-        pc.out_rc = pp.rc_off - sl.in_used + row * 4;
-      }
+    for (size_t sg = 0; sg < pp.keys.size(); sg++) {
+      const std::vector<int> &mem = pp.members[sg];
+      parallel_for(mem.size(), [&](size_t b, size_t e) {
+        for (size_t j = b; j < e; j++) {
+          Piece &pc = sl.pieces[mem[j]];
+          const long long row = pp.segs.row0[sg] + (long long)j;
+          memcpy(sl.h_in + pp.in_off + row * inb, pc.r.in, inb);
+          pc.out_k = pp.k_off - sl.in_used + row * 32;
+          pc.out_ct = pp.ct_off - sl.in_used + row * S.synd_bytes;
+          pc.out_rc = pp.rc_off - sl.in_used + row * 4;
+        }
+      });
+    }
   }
   return true;
 }
@@ -356,30 +430,44 @@ void dispatcher_main(gmc_server *srv) {
     });
     if (srv->stop) break;
     Slot &sl = *free_slot;
-    if (!form_batch(srv, sl)) {  // the head request does not fit an empty slot: reject it
-      srv->errors++;
-      srv->last_error = "request does not fit a slot";
-      Req r = srv->queue.front();
-      srv->queue.pop_front();
-      if (r.done) r.done->store(-1);
+    sl.busy = true;  // reserved while its batch is formed outside the lock
+    const size_t take = std::min(srv->queue.size(), (size_t)srv->max_batch);
+    sl.incoming.assign(srv->queue.begin(), srv->queue.begin() + (long)take);
+    srv->queue.erase(srv->queue.begin(), srv->queue.begin() + (long)take);
+    lk.unlock();
+    const bool formed = form_batch(srv, sl);
+    lk.lock();
+    if (!formed) {  // the head request does not fit an empty slot: reject it
+      sl.busy = false;
+      if (!srv->queue.empty()) {
+        srv->errors++;
+        srv->last_error = "request does not fit a slot";
+        Req r = srv->queue.front();
+        srv->queue.pop_front();
+        if (r.done) r.done->store(-1);
+      }
       continue;
     }
-    sl.busy = true;
     srv->batches++;
     srv->batched_requests += (long long)sl.pieces.size();
     lk.unlock();
     const char *step = "input copy";
     cudaError_t e = cudaMemcpyAsync(sl.dev, sl.h_in, sl.in_used, cudaMemcpyHostToDevice, sl.st);
-    for (auto &pp : sl.pipes) {
-      if (e != cudaSuccess) break;
+    if (e == cudaSuccess) e = cudaEventRecord(sl.fork, sl.st);
+    for (size_t i = 0; i < sl.pipes.size() && e == cudaSuccess; i++) {
+      Pipe &pp = sl.pipes[i];
       step = pp.kind == 0 ? "encapsulation kernels" : "decapsulation kernels";
+      e = cudaStreamWaitEvent(sl.pst[i], sl.fork, 0);
+      if (e != cudaSuccess) break;
       switch (pp.set) {
-        case 0: e = run_pipe<0>(sl, pp); break;
-        case 1: e = run_pipe<1>(sl, pp); break;
-        case 2: e = run_pipe<2>(sl, pp); break;
-        case 3: e = run_pipe<3>(sl, pp); break;
-        default: e = run_pipe<4>(sl, pp); break;
+        case 0: e = run_pipe<0>(sl, pp, sl.pst[i]); break;
+        case 1: e = run_pipe<1>(sl, pp, sl.pst[i]); break;
+        case 2: e = run_pipe<2>(sl, pp, sl.pst[i]); break;
+        case 3: e = run_pipe<3>(sl, pp, sl.pst[i]); break;
+        default: e = run_pipe<4>(sl, pp, sl.pst[i]); break;
       }
+      if (e == cudaSuccess) e = cudaEventRecord(sl.join[i], sl.pst[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(sl.st, sl.join[i], 0);
     }
     if (e == cudaSuccess) {
       step = "output copy";
@@ -415,6 +503,14 @@ void server_release(gmc_server *s) {
       cudaStreamSynchronize(sl.st);
       cudaStreamDestroy(sl.st);
     }
+    for (int i = 0; i < kPipes; i++) {
+      if (sl.pst[i]) {
+        cudaStreamSynchronize(sl.pst[i]);
+        cudaStreamDestroy(sl.pst[i]);
+      }
+      if (sl.join[i]) cudaEventDestroy(sl.join[i]);
+    }
+    if (sl.fork) cudaEventDestroy(sl.fork);
     cudaFree(sl.dev);
     cudaFreeHost(sl.h_in);
     cudaFreeHost(sl.h_out);
@@ -454,6 +550,11 @@ extern "C" int gmc_server_create(gmc_server **out, long long max_batch, int slot
     sl.h_in_bytes = (size_t)(max_batch + kPadRows) * 208 + 10 * 256;
     sl.h_out_bytes = (size_t)(max_batch + kPadRows) * (208 + 32 + 4) + 30 * 256;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
+    for (int i = 0; i < kPipes && e == cudaSuccess; i++) {
+      e = cudaStreamCreateWithFlags(&sl.pst[i], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.join[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&sl.dev, sl.dev_bytes);
     if (e == cudaSuccess) e = cudaMallocHost(&sl.h_in, sl.h_in_bytes);
     if (e == cudaSuccess) e = cudaMallocHost(&sl.h_out, sl.h_out_bytes);
@@ -575,22 +676,37 @@ extern "C" int gmc_server_loadgen(gmc_server *s, const gmc_key *const *pks, cons
   std::vector<uint8_t> sink_ct(ring * 208), sink_k(ring * 32);
   std::vector<int> sink_rc(ring);
   gmc_server_reset_stats(s);
-  std::exponential_distribution<double> gap(rate);
-  std::uniform_real_distribution<double> uni(0.0, 1.0);
+  // splitmix64 draws: the generator must outpace the server it loads
+  uint64_t sm = seed ^ 0x9E3779B97F4A7C15ull;
+  auto next64 = [&]() {
+    uint64_t z = (sm += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  auto unit = [&]() { return (double)(next64() >> 11) * (1.0 / 9007199254740992.0); };  // [0, 1)
   const double t0 = now_s();
   double t_next = t0;
   size_t idx = 0;
   long long submitted = 0;
   std::vector<Req> due;
+  const size_t queue_cap = (size_t)4 * (size_t)s->max_batch * s->slots.size();  // bounds host memory under overload
   while (true) {
     const double t = now_s();
     if (t - t0 > seconds) break;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (s->queue.size() > queue_cap) {
+        t_next = std::max(t_next, t);  // arrivals while the queue is over its cap are not offered
+      }
+    }
     due.clear();
-    while (t_next <= t) {
-      const int pair = (int)(uni(rng) * npairs) % npairs;
-      const bool enc = uni(rng) < enc_fraction;
+    while (t_next <= t && due.size() < (1u << 20)) {
+      const uint64_t x = next64();
+      const int pair = (int)(((x & 0xFFFFFFFFull) * (uint64_t)npairs) >> 32);
+      const bool enc = (double)(x >> 40) * (1.0 / 16777216.0) < enc_fraction;
       const size_t slot = idx++ % ring;
-      const int pi = (int)(rng() % pool_n);
+      const int pi = (int)((x >> 32) & 0xFF) % pool_n;
       Req r{};
       r.key = enc ? pks[pair] : sks[pair];
       r.in = enc ? seeds.data() + (size_t)pi * 32 : cts[pair].data() + (size_t)pi * set_info(sks[pair]->set).synd_bytes;
@@ -600,7 +716,7 @@ extern "C" int gmc_server_loadgen(gmc_server *s, const gmc_key *const *pks, cons
       r.t_arrive = t_next;
       r.done = nullptr;
       due.push_back(r);
-      t_next += gap(rng);
+      t_next += -log1p(-unit()) / rate;  // exponential inter-arrival gap
     }
     if (!due.empty()) {
       {
