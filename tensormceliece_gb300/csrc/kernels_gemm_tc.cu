@@ -11,13 +11,13 @@
 //   X (request bits) is expanded to FP8 by the CUDA cores into the same
 //   canonical layout (no-swizzle K-major: 8-row x 16-byte core matrices,
 //   K-adjacent core matrices 128 B apart, row groups 1024 B apart).
-//   Warp roles: four expander warps write the X stages, one warp's lane 0
+//   Warp roles: expander warps write the X stages, one warp's lane 0
 //   issues the A copies, another's lane 0 issues 4 MMAs (K = 32 each) per
 //   128-bit K stage. Stages hand over through mbarriers only: A full (copy
-//   bytes landed), X full (128 expander arrivals), empty (the MMA commit that
-//   releases both buffers), so expansion, copies and MMAs of different stages
-//   overlap. The expander warps then read the accumulators with tcgen05.ld
-//   and pack 32 parities per ballot.
+//   bytes landed), X full (one arrival per expander thread), empty (the MMA
+//   commit that releases both buffers), so expansion, copies and MMAs of
+//   different stages overlap. Epilogue warps read the accumulators with
+//   tcgen05.ld and pack 32 parities per ballot.
 //   Every wait is bounded (about 2 s of globaltimer); on expiry the CTA sets
 //   the error word, stops issuing, waits (bounded) for its own copies and
 //   MMAs, frees its tensor memory and returns.
@@ -136,17 +136,17 @@ __device__ __forceinline__ uint32_t expand4(uint32_t v) {
 // Persistent: one CTA per SM walks the (m-tile, n-tile) list. The stage ring
 // runs on across tiles, and the FP32 accumulator is double-buffered in tensor
 // memory (2 x 256 columns), so the epilogue of one tile overlaps the MMAs of
-// the next. Warp roles: 0-3 expand X stages, 4 issues the A bulk copies, 5
-// issues the MMAs, 6-9 drain accumulators (warp w reads TMEM lanes
-// 32 (w % 4) .. +31).
-constexpr int TC_EXP_WARPS = 4;
+// the next. Warp roles: the first TC_EXP_WARPS expand X stages, the next
+// issues the A bulk copies, the next issues the MMAs, the last four drain
+// accumulators (warp w reads TMEM lanes 32 (w % 4) .. +31).
+constexpr int TC_EXP_WARPS = 8;
 constexpr int TC_THREADS = (TC_EXP_WARPS + 2 + 4) * 32;  // expanders, producer, MMA, 4 epilogue warps
 constexpr int TC_EXP_THREADS = TC_EXP_WARPS * 32;
 constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
 constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
 constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 512;
 constexpr uint32_t TC_TMEM_COLS = 2 * kTcN;  // two FP32 accumulators of 128 lanes x kTcN columns
-static_assert(TC_EXP_THREADS == kTcM, "one expander thread per accumulator lane");
+static_assert(kTcN % TC_EXP_THREADS == 0, "whole X rows per expander thread");
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
