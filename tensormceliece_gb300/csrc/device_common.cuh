@@ -149,6 +149,84 @@ __device__ __forceinline__ uint64_t kem_preimage_lane(int i, uint32_t b, EWord e
   return v;
 }
 
+// SHAKE256 (first 32 output bytes) of the KEM preimage b || e || c of PRE
+// bytes, e of EB bytes, for the 32 requests of a warp (one per lane; every
+// lane of the warp must call). erow is this lane's e as 32-bit words (zero
+// past EB up to the next word); cword gives c as words (zero past c).
+// The e words of each 136-byte absorb block are loaded for the whole warp as
+// 35 independent loads per lane (word j of every request, and words 32..34 of
+// the lane's own request), issued before the previous block is permuted so
+// they land under the permutation, and handed over through shared memory
+// (stage: 32 x 35 words, odd stride: no bank conflicts; rows: 32 pointers).
+// Lanes outside e (the first, the e/c boundary, c) use kem_preimage_lane.
+constexpr int kStageStride = 35;
+template <int EB, int PRE, typename CWord>
+__device__ __forceinline__ void kem_hash_staged(uint64_t out[4], uint32_t b, const uint32_t *erow, CWord cword,
+                                                uint32_t *stage, const uint32_t **rows) {
+  constexpr int EW = (EB + 3) / 4;
+  constexpr int NB = PRE / 136 + 1;  // full blocks and the final (padded) one
+  const int lane = threadIdx.x & 31;
+  auto eword = [&](int w) -> uint32_t { return erow[w]; };
+  rows[lane] = erow;
+  __syncwarp();
+  auto w_lo_of = [](int blk) { return blk > 0 ? (136 * blk - 1) >> 2 : 0; };
+  uint32_t pf[32], pf2[3];
+  auto prefetch = [&](int blk) {
+    const int w_lo = w_lo_of(blk);
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+      const int w = w_lo + lane;
+      pf[r] = w < EW ? rows[r][w] : 0u;
+    }
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+      const int w = w_lo + 32 + e;
+      pf2[e] = w < EW ? erow[w] : 0u;
+    }
+  };
+  prefetch(0);
+  uint64_t s[25];
+#pragma unroll
+  for (int i = 0; i < 25; i++) s[i] = 0;
+#pragma unroll 1
+  for (int blk = 0; blk < NB; blk++) {
+    const int x0 = 136 * blk;
+    const int w_lo = w_lo_of(blk);
+    const bool in_e = x0 - 1 < EB;
+    if (in_e) {
+#pragma unroll
+      for (int r = 0; r < 32; r++) stage[r * kStageStride + lane] = pf[r];
+#pragma unroll
+      for (int e = 0; e < 3; e++) stage[lane * kStageStride + 32 + e] = pf2[e];
+      __syncwarp();
+      if (blk + 1 < NB && 136 * (blk + 1) - 1 < EB) prefetch(blk + 1);
+    }
+    const int rem = (blk == NB - 1) ? PRE % 136 : 136;  // preimage bytes in this block
+    const uint32_t *mine = stage + lane * kStageStride;
+#pragma unroll
+    for (int i = 0; i < 17; i++) {
+      const int L = 17 * blk + i, o = 8 * L;
+      uint64_t v = 0;
+      if (8 * i < rem) {
+        if (o > 0 && o + 7 <= EB) {
+          const int rel = (o - 1) - 4 * w_lo, q = rel >> 2, sh = 8 * (rel & 3);
+          v = (uint64_t)mine[q] | ((uint64_t)mine[q + 1] << 32);
+          if (sh) v = (v >> sh) | ((uint64_t)mine[q + 2] << (64 - sh));
+        } else {
+          v = kem_preimage_lane<EB>(L, b, eword, cword);
+        }
+      }
+      if (blk == NB - 1 && i == rem / 8) v ^= 0x1Full << (8 * (rem % 8));
+      s[i] ^= v;
+    }
+    if (blk == NB - 1) s[16] ^= 0x8000000000000000ull;
+    keccak_f1600(s);
+    __syncwarp();  // every lane has read the staged words before they are replaced
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) out[i] = s[i];
+}
+
 // ---------------------------------------------------------------- GF(2^m)
 // Log/antilog representation: log[0] = 2q-2 (sentinel), exp has 2q-1 entries
 // with exp[2q-2] = 0, so a*b = exp[min(log a + log b, 2q-2)] without branches.

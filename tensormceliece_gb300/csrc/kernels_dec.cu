@@ -768,16 +768,18 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
                                                                 uint8_t *__restrict__ K, int *__restrict__ rc,
                                                                 const Segs segs) {
   using p = P<SET>;
+  __shared__ uint32_t stage[kTailThreads / 32][32 * kStageStride];
+  __shared__ const uint32_t *rows[kTailThreads / 32][32];
+  const long long N = seg_rows(segs);
   const long long op = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long opc = op < N ? op : N - 1;  // every lane of a warp takes part in the staged hash
   int seg;
-  if (!seg_live(segs, op, &seg)) return;
-  const DecKeyDev &key = keys.k[seg];
-  const bool ok = okin[op] != 0;
-  const uint32_t *e = E + op * lde;
-  const uint8_t *c = Cin + op * p::synd_bytes;
+  const bool live = seg_live(segs, op, &seg);
+  const DecKeyDev &key = keys.k[seg_find(segs, opc)];
+  const bool ok = okin[opc] != 0;
+  const uint8_t *c = Cin + opc * p::synd_bytes;
   // b || (e or s) || c; s is the key's n/8 bytes, stored zero-padded to whole words
-  const uint32_t *sw = reinterpret_cast<const uint32_t *>(key.s);
-  auto eword = [&](int w) -> uint32_t { return ok ? e[w] : sw[w]; };
+  const uint32_t *erow = ok ? E + opc * lde : reinterpret_cast<const uint32_t *>(key.s);
   auto cword = [&](int w) -> uint32_t {  // ciphertext rows need not be 4-byte aligned
     uint32_t v = 0;
 #pragma unroll
@@ -785,9 +787,10 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
       if (4 * w + k < p::synd_bytes) v |= (uint32_t)c[4 * w + k] << (8 * k);
     return v;
   };
-  auto lane = [&](int i) -> uint64_t { return kem_preimage_lane<p::e_bytes>(i, ok ? 1u : 0u, eword, cword); };
   uint64_t h[4];
-  shake256_32<p::pre_bytes>(h, lane);
+  kem_hash_staged<p::e_bytes, p::pre_bytes>(h, ok ? 1u : 0u, erow, cword, stage[threadIdx.x >> 5],
+                                            rows[threadIdx.x >> 5]);
+  if (!live) return;
   bool pad_bad = false;
   if (p::mt % 8) pad_bad = (c[p::synd_bytes - 1] >> (p::mt % 8)) != 0;
   uint8_t *k = K + op * 32;

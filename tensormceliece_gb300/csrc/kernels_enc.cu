@@ -237,12 +237,15 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
                                                                 uint8_t *__restrict__ C, uint8_t *__restrict__ K,
                                                                 const Segs segs, uint32_t pk_bad_mask) {
   using p = P<SET>;
+  __shared__ uint32_t stage[kTailThreads / 32][32 * kStageStride];
+  __shared__ const uint32_t *rows[kTailThreads / 32][32];
+  const long long N = seg_rows(segs);
   const long long op = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long opc = op < N ? op : N - 1;  // every lane of a warp takes part in the staged hash
   int seg;
-  if (!seg_live(segs, op, &seg)) return;
-  const bool pk_bad = (pk_bad_mask >> seg) & 1u;
-  const uint32_t *e = E + op * lde;
-  const uint32_t *sy = S + op * lds;
+  const bool live = seg_live(segs, op, &seg);
+  const uint32_t *e = E + opc * lde;
+  const uint32_t *sy = S + opc * lds;
   // c word w: e[0:mt] xor the syndrome, bits from mt on cleared (zero past c)
   auto cword = [&](int w) -> uint32_t {
     if (w >= p::mw) return 0u;
@@ -250,10 +253,10 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
     if (w == p::mt / 32 && (p::mt % 32)) v &= (1u << (p::mt % 32)) - 1u;
     return v;
   };
-  auto eword = [&](int w) -> uint32_t { return e[w]; };
-  auto lane = [&](int i) -> uint64_t { return kem_preimage_lane<p::e_bytes>(i, 1u, eword, cword); };
   uint64_t h[4];
-  shake256_32<p::pre_bytes>(h, lane);
+  kem_hash_staged<p::e_bytes, p::pre_bytes>(h, 1u, e, cword, stage[threadIdx.x >> 5], rows[threadIdx.x >> 5]);
+  if (!live) return;
+  const bool pk_bad = (pk_bad_mask >> seg) & 1u;
   uint8_t *c = C + op * p::synd_bytes;
   uint8_t *k = K + op * 32;
   for (int x = 0; x < p::synd_bytes; x++) c[x] = pk_bad ? 0 : (uint8_t)(cword(x >> 2) >> (8 * (x & 3)));
