@@ -182,7 +182,7 @@ int gmc_get_gemm_engine(void);
 /* ---- autotuner --------------------------------------------------------------
  * Per parameter set: the engine of the encapsulation syndrome (sparse or a
  * GEMM engine) and the GEMM engine of the decapsulation front end, and the
- * sampler block size (32/64/128). Defaults: sparse, tcgen05, 64. gmc_autotune times every candidate on this GPU with a
+ * sampler block size (32/64/128). Defaults: sparse, tcgen05, 128. gmc_autotune times every candidate on this GPU with a
  * batch of n requests (median of 5), keeps the fastest and, when cache_path is
  * given, writes the choices of all tuned sets to that JSON file;
  * gmc_autotune_load applies such a file (returns the number of sets loaded).

@@ -35,7 +35,7 @@ void set_last_error(const char *msg);
 struct SetTune {
   int enc_engine = GEMM_SPARSE;  // engine of the encapsulation syndrome
   int dec_engine = GEMM_TC;   // GF(2) GEMM engine of the decapsulation front end
-  int sample_threads = 64;    // sampler block size (32, 64 or 128)
+  int sample_threads = 128;   // sampler block size (32, 64 or 128)
   int tuned = 0;              // 1 when measured on this device
   double enc_ms = 0, dec_ms = 0;
   long long n = 0;

@@ -780,7 +780,10 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
   const uint8_t *c = Cin + opc * p::synd_bytes;
   // b || (e or s) || c; s is the key's n/8 bytes, stored zero-padded to whole words
   const uint32_t *erow = ok ? E + opc * lde : reinterpret_cast<const uint32_t *>(key.s);
-  auto cword = [&](int w) -> uint32_t {  // ciphertext rows need not be 4-byte aligned
+  // word loads when every ciphertext row is 4-byte aligned (the buffer and the row length), else bytes
+  const bool c_words = (p::synd_bytes % 4 == 0) && ((reinterpret_cast<uintptr_t>(Cin) & 3) == 0);
+  auto cword = [&](int w) -> uint32_t {
+    if (c_words) return 4 * w < p::synd_bytes ? reinterpret_cast<const uint32_t *>(c)[w] : 0u;
     uint32_t v = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++)

@@ -268,8 +268,6 @@ size_t pipe_bytes(int set, int kind, long long rows) {
          work_bytes(set, kind, rows);
 }
 
-long long padded(size_t n) { return (long long)((n + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad; }
-
 // staging bytes of one pipeline (padded rows, same layout as on the device)
 size_t in_bytes(int set, int kind, long long rows) {
   if (rows <= 0) return 0;

@@ -257,7 +257,7 @@ extern "C" int gmc_autotune_load(const char *cache_path) {
     t.dec_engine = engine_id(field(o, "dec_engine"));
     if (t.dec_engine == GEMM_SPARSE) t.dec_engine = GEMM_TC;  // no sparse form for the front end
     const int th = atoi(field(o, "sample_threads").c_str());
-    t.sample_threads = (th == 32 || th == 64 || th == 128) ? th : 64;
+    t.sample_threads = (th == 32 || th == 64 || th == 128) ? th : 128;
     t.n = atoll(field(o, "n").c_str());
     t.enc_ms = atof(field(o, "enc_ms").c_str());
     t.dec_ms = atof(field(o, "dec_ms").c_str());
