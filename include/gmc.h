@@ -79,6 +79,17 @@ int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned char *c, l
  * generation is outside the batched enc/dec path). */
 int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32);
 
+/* Batched key generation on the device: nkeys keypairs, key i from the
+ * 32-byte seed seeds + 32 i (the single randombytes draw of libmceliece's
+ * keypair, mc:crypto_kem/<set>/vec/kem_keypair.c:36), written to
+ * pk + i * pk_bytes and sk + i * sk_bytes (host memory). Every key is
+ * byte-identical to gmc_keypair_seed's for the same seed. Each key walks the
+ * library's seed chain until an attempt gives an irreducible Goppa
+ * polynomial, a repetition-free support and a systematic public key; the
+ * attempts run on the GPU (seed expansion, minimal polynomial, support sort,
+ * Gaussian elimination, Benes control bits). */
+int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seeds, long long nkeys);
+
 /* ---- grouped launches over many keys and parameter sets -------------------
  * A group is one key's batch: a public key with n seeds (encapsulation) or a
  * secret key with n ciphertexts (decapsulation), device buffers. A plan

@@ -18,7 +18,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = [
-    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "Plan", "Server", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
+    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "keypair_batch", "Plan", "Server", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
     "set_gemm_engine", "get_gemm_engine", "set_randombytes", "autotune", "autotune_load", "tune_get",
     "tune_set", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC", "GEMM_SPARSE",
 ]
@@ -70,6 +70,7 @@ def lib():
             for op in ("enc", "dec"):
                 getattr(L, f"gmc_kem_{s}_{op}").argtypes = [c_u8p, c_u8p, c_u8p]
         L.gmc_keypair_seed.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p]
+        L.gmc_keypair_batch.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p, ctypes.c_longlong]
         for s in SETS:
             getattr(L, f"gmc_kem_{s}_keypair").argtypes = [c_u8p, c_u8p]
             getattr(L, f"gmc_kem_{s}_keypair").restype = None
@@ -320,6 +321,20 @@ def keypair(set_name, seed32=None):
     else:
         seed = _u8(bytes(seed32), 32)
         _check(lib().gmc_keypair_seed(sid, _ptr(pk), _ptr(sk), _ptr(seed)), "gmc_keypair_seed")
+    return pk, sk
+
+
+def keypair_batch(set_name, seeds):
+    """Keys generated on the GPU, one per 32-byte seed: (pk, sk) uint8 arrays of shape
+    (nkeys, pk_bytes) and (nkeys, sk_bytes), each row identical to keypair(set_name, seed)."""
+    sid = set_name if isinstance(set_name, int) else set_id(set_name)
+    sz = set_sizes(sid)
+    seeds = np.ascontiguousarray(np.frombuffer(bytes(seeds), np.uint8) if not isinstance(seeds, np.ndarray) else seeds,
+                                 dtype=np.uint8).reshape(-1, 32)
+    n = seeds.shape[0]
+    pk = np.zeros((n, sz["pk_bytes"]), np.uint8)
+    sk = np.zeros((n, sz["sk_bytes"]), np.uint8)
+    _check(lib().gmc_keypair_batch(sid, _ptr(pk), _ptr(sk), _ptr(seeds), n), "gmc_keypair_batch")
     return pk, sk
 
 

@@ -1,0 +1,935 @@
+// Batched key generation on the device, byte-identical to libmceliece's
+// keypair (mc:crypto_kem/<set>/vec/kem_keypair.c:20-100) for the same 32-byte
+// randombytes draw of each key.
+//
+// Per key the library walks a seed chain: attempt a expands its seed with
+// r = SHAKE256({64} || seed, n/8 + 4q + 2t + 32), the next seed is r's last
+// 32 bytes, and the attempt succeeds when
+//   (1) f = r[-32-2t:-32] has a minimal polynomial g of degree t (sk_gen.c:29),
+//   (2) the 2^m 32-bit values r[n/8 : n/8+4q] are distinct (pk_gen.c:82), and
+//   (3) the left mt x mt block A_L of the parity-check matrix
+//       [A_L | A_R] built from g and the support is invertible (pk_gen.c:150).
+// The key is then pk = T = A_L^-1 A_R (the unique reduced form), the Benes
+// control bits of the support permutation, and sk = seed | pivots | g |
+// control bits | r[0:n/8].
+//
+// Device pipeline of one round (each pending key gets k chained attempts):
+//   kg_expand    one thread per key   k chained SHAKE256 expansions
+//   kg_minpoly   one CTA per attempt  powers of f in GF((2^m)^t), Gauss-Jordan
+//   kg_support   one CTA per attempt  bitonic sort of (value, index) pairs
+//   kg_build     CTAs per attempt     columns of A_L (the rank test's matrix)
+//   kg_elim      one CTA per attempt  blocked Gauss-Jordan of A_L (rank test)
+// and for the first successful attempt of each key (the winner):
+//   kg_build + kg_elim on the full mt x n matrix (row order of [I | T])
+//   kg_cbits     one CTA per winner   control bits, checked by re-applying them
+//   kg_assemble  pk and sk bytes
+// Only the rank test runs on the ~70% of attempts whose A_L is singular; the
+// full elimination (4-5x the rank test's work for 8192128) runs once per key.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <climits>
+#include <string>
+#include <vector>
+
+#include "../../include/gmc.h"
+#include "device_common.cuh"
+#include "engine_internal.h"
+#include "host_keys.h"
+
+namespace gmc {
+
+// ---------------------------------------------------------------- constants
+// GF((2^m)^t) reduction y^t = sum_k c_k y^pos_k, c_k in {1, z} (z = the field
+// element 2): mc:crypto_kem/<set>/vec/gf_2mt_mul.c.
+template <int SET> struct ExtPoly;
+#define GMC_EXT_POLY(SET, N, MAXPOS, P0, P1, P2, P3, Z0, Z1, Z2, Z3)                                   \
+  template <> struct ExtPoly<SET> {                                                                 \
+    static constexpr int n = N, maxpos = MAXPOS;                                                    \
+    __device__ static constexpr int pos(int i) { return i == 0 ? P0 : i == 1 ? P1 : i == 2 ? P2 : P3; } \
+    __device__ static constexpr int z(int i) { return i == 0 ? Z0 : i == 1 ? Z1 : i == 2 ? Z2 : Z3; }   \
+  };
+GMC_EXT_POLY(0, 3, 3, 3, 1, 0, 0, 0, 0, 1, 0)
+GMC_EXT_POLY(1, 4, 10, 10, 9, 6, 0, 0, 0, 0, 0)
+GMC_EXT_POLY(2, 4, 7, 7, 2, 1, 0, 0, 0, 0, 0)
+GMC_EXT_POLY(3, 2, 8, 8, 0, 0, 0, 0, 0, 0, 0)
+GMC_EXT_POLY(4, 4, 7, 7, 2, 1, 0, 0, 0, 0, 0)
+#undef GMC_EXT_POLY
+
+template <int SET> struct KG {
+  using Q = P<SET>;
+  static constexpr int m = Q::m, n = Q::n, t = Q::t, mt = Q::mt, k = Q::k, q = Q::q;
+  static constexpr int rlen = Q::e_bytes + 4 * q + 2 * t + 32;    // SHAKE output bytes per attempt
+  static constexpr int rblocks = (rlen + 135) / 136;
+  static constexpr int rstride = rblocks * 136;                   // per-attempt r bytes (whole blocks)
+  static constexpr int rw = (((n + 31) / 32) + 31) / 32 * 32;     // u32 words per full row
+  static constexpr int rwl = (((mt + 31) / 32) + 31) / 32 * 32;   // u32 words per A_L row
+  static constexpr int npanel = (mt + 31) / 32;
+  static constexpr int gstride = (t + 2) & ~1;                    // u16 per g (t+1 coefficients)
+  static constexpr int cond_bytes = (q / 16) * (2 * m - 1);
+  static constexpr int pk_row_bytes = (k + 7) / 8;
+  static constexpr long long pk_bytes = (long long)mt * pk_row_bytes;
+  static constexpr long long sk_bytes = 40 + 2 * t + cond_bytes + n / 8;
+  static constexpr int zl = 2 * q - 2;                            // log of 0
+  static constexpr int exp_n = 2 * q - 1;
+};
+
+// status bits per attempt
+constexpr uint8_t kKgMinpoly = 1, kKgDistinct = 2, kKgRank = 4, kKgAll = 7;
+
+// ---------------------------------------------------------------- expansion
+// Thread per pending key: k chained expansions r_a = SHAKE256({64} || seed_a),
+// seed_{a+1} = r_a[rlen-32 : rlen]. Attempt a of key j is j * k + a.
+template <int SET>
+__global__ void __launch_bounds__(32) kg_expand_kernel(const uint8_t *__restrict__ seed_in, uint8_t *__restrict__ seed_out,
+                                                       int nkeys, int k, uint8_t *__restrict__ rbuf,
+                                                       uint8_t *__restrict__ delta, uint8_t *__restrict__ status) {
+  using C = KG<SET>;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nkeys) return;
+  uint8_t seed[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) seed[i] = seed_in[32 * j + i];
+  for (int a = 0; a < k; a++) {
+    const long long att = (long long)j * k + a;
+    uint8_t *r = rbuf + att * C::rstride;
+    uint64_t s[25];
+#pragma unroll
+    for (int i = 0; i < 25; i++) s[i] = 0;
+    // absorb {64} || seed || 0x1F, final bit of the 136-byte block
+    uint8_t in[40];
+    in[0] = 64;
+#pragma unroll
+    for (int i = 0; i < 32; i++) in[1 + i] = seed[i];
+    in[33] = 0x1F;
+#pragma unroll
+    for (int i = 34; i < 40; i++) in[i] = 0;
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+      uint64_t w = 0;
+#pragma unroll
+      for (int b = 0; b < 8; b++) w |= (uint64_t)in[8 * l + b] << (8 * b);
+      s[l] = w;
+    }
+    s[16] ^= 0x8000000000000000ull;
+#pragma unroll
+    for (int i = 0; i < 32; i++) delta[att * 32 + i] = seed[i];
+    uint64_t *out = reinterpret_cast<uint64_t *>(r);
+#pragma unroll 1
+    for (int b = 0; b < C::rblocks; b++) {
+      keccak_f1600(s);
+#pragma unroll
+      for (int i = 0; i < 17; i++) out[17 * b + i] = s[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 32; i++) seed[i] = r[C::rlen - 32 + i];
+    status[att] = 0;
+  }
+#pragma unroll
+  for (int i = 0; i < 32; i++) seed_out[32 * j + i] = seed[i];
+}
+
+// ---------------------------------------------------------------- minimal polynomial
+// CTA per attempt. Columns col[c] = f^c (c <= t) in GF((2^m)^t); solve
+// sum_{c<t} g_c f^c = f^t by Gauss-Jordan (the solution is unique when it
+// exists, so the pivot order does not change g). mc:crypto_kem/<set>/vec/sk_gen.c:29-75.
+constexpr int kMinpolyThreads = 256;
+template <int SET> struct MinpolySmem {
+  using C = KG<SET>;
+  static constexpr int ex = 0;                                   // exp_n u16
+  static constexpr int lg = ex + ((C::exp_n + 1) & ~1);          // q u16
+  static constexpr int col = lg + C::q;                          // (t+1) * t u16
+  static constexpr int la = col + (C::t + 1) * C::t;             // t
+  static constexpr int lf = la + C::t;                           // t
+  static constexpr int prod = lf + C::t;                         // 2t
+  static constexpr int r1 = prod + 2 * C::t;                     // t + 16
+  static constexpr int lrow = r1 + C::t + 16;                    // t + 1
+  static constexpr int lcoef = lrow + C::t + 2;                  // t
+  static constexpr int total_u16 = (lcoef + C::t + 2 + 7) & ~7;  // flags (int) follow, aligned
+  static constexpr int bytes = total_u16 * 2 + 16;
+};
+
+template <int SET>
+__global__ void __launch_bounds__(kMinpolyThreads) kg_minpoly_kernel(const uint8_t *__restrict__ rbuf, int natt,
+                                                                     const uint16_t *__restrict__ gexp,
+                                                                     const uint16_t *__restrict__ glog,
+                                                                     uint16_t *__restrict__ gout,
+                                                                     uint8_t *__restrict__ status) {
+  using C = KG<SET>;
+  using L = MinpolySmem<SET>;
+  using X = ExtPoly<SET>;
+  constexpr int T = C::t, q = C::q, ZL = C::zl;
+  extern __shared__ __align__(16) uint16_t kgsm_mp[];
+  uint16_t *ex = kgsm_mp + L::ex, *lg = kgsm_mp + L::lg, *col = kgsm_mp + L::col, *la = kgsm_mp + L::la,
+           *lf = kgsm_mp + L::lf, *prod = kgsm_mp + L::prod, *r1 = kgsm_mp + L::r1, *lrow = kgsm_mp + L::lrow,
+           *lcoef = kgsm_mp + L::lcoef;
+  int *flags = reinterpret_cast<int *>(kgsm_mp + L::total_u16);
+  const int att = blockIdx.x;
+  if (att >= natt) return;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < C::exp_n; i += kMinpolyThreads) ex[i] = gexp[i];
+  for (int i = tid; i < q; i += kMinpolyThreads) lg[i] = glog[i];
+  const uint8_t *rp = rbuf + (long long)att * C::rstride + C::rlen - 32 - 2 * T;
+  if (tid < T) {
+    const uint16_t f = (uint16_t)((rp[2 * tid] | (rp[2 * tid + 1] << 8)) & (q - 1));
+    col[0 * T + tid] = tid == 0 ? 1 : 0;
+    col[1 * T + tid] = f;
+  }
+  if (tid == 0) flags[0] = 0;
+  __syncthreads();
+  if (tid < T) lf[tid] = lg[col[T + tid]];
+  const int log2 = lg[2];
+  auto mulz = [&](uint16_t x) -> uint16_t { return ex[min((int)lg[x] + log2, ZL)]; };
+  // powers f^c = f^(c-1) * f
+  for (int c = 2; c <= T; c++) {
+    const uint16_t *prev = col + (c - 1) * T;
+    if (tid < T) la[tid] = lg[prev[tid]];
+    __syncthreads();
+    if (tid < 2 * T - 1) {
+      const int lo = max(0, tid - T + 1), hi = min(tid, T - 1);
+      uint16_t acc = 0;
+      for (int i = lo; i <= hi; i++) acc ^= ex[min((int)la[i] + (int)lf[tid - i], ZL)];
+      prod[tid] = acc;
+    }
+    __syncthreads();
+    // fold the high half H (degrees t .. 2t-2) once: R1 = low + sum_k c_k H y^pos_k
+    if (tid < T - 1 + X::maxpos) {
+      uint16_t v = tid < T ? prod[tid] : 0;
+#pragma unroll
+      for (int kk = 0; kk < X::n; kk++) {
+        const int h = tid - X::pos(kk);
+        if (h >= 0 && h <= T - 2) {
+          const uint16_t x = prod[T + h];
+          v ^= X::z(kk) ? mulz(x) : x;
+        }
+      }
+      r1[tid] = v;
+    }
+    __syncthreads();
+    // fold R1's degrees t .. t+maxpos-2 once more (they land below degree 2 maxpos)
+    if (tid < T) {
+      uint16_t v = r1[tid];
+#pragma unroll
+      for (int kk = 0; kk < X::n; kk++) {
+        const int h = tid - X::pos(kk);
+        if (h >= 0 && h <= X::maxpos - 2) {
+          const uint16_t x = r1[T + h];
+          v ^= X::z(kk) ? mulz(x) : x;
+        }
+      }
+      col[c * T + tid] = v;
+    }
+    __syncthreads();
+  }
+  // Gauss-Jordan on rows r < t of the columns c <= t
+  for (int j = 0; j < T; j++) {
+    if (tid == 0) {
+      int kk = -1;
+      if (col[j * T + j] == 0) {
+        for (int r = j + 1; r < T; r++)
+          if (col[j * T + r]) { kk = r; break; }
+        if (kk < 0) flags[0] = 1;
+      }
+      flags[1] = kk;
+    }
+    __syncthreads();
+    if (flags[0]) break;
+    const int kk = flags[1];
+    if (kk >= 0)
+      for (int c = j + tid; c <= T; c += kMinpolyThreads) col[c * T + j] ^= col[c * T + kk];
+    __syncthreads();
+    const int lp = lg[col[j * T + j]];
+    const int linv = (q - 1 - lp) % (q - 1);
+    for (int c = j + tid; c <= T; c += kMinpolyThreads) {
+      const uint16_t v = ex[min((int)lg[col[c * T + j]] + linv, ZL)];
+      col[c * T + j] = v;
+      lrow[c] = lg[v];
+    }
+    if (tid < T) lcoef[tid] = tid == j ? ZL : lg[col[j * T + tid]];
+    __syncthreads();
+    const int width = T + 1 - j;
+    for (int idx = tid; idx < width * T; idx += kMinpolyThreads) {
+      const int c = j + idx / T, r = idx - (idx / T) * T;
+      col[c * T + r] ^= ex[min((int)lrow[c] + (int)lcoef[r], ZL)];
+    }
+    __syncthreads();
+  }
+  if (flags[0]) return;
+  uint16_t *g = gout + (long long)att * C::gstride;
+  if (tid < T) g[tid] = col[T * T + tid];
+  if (tid == 0) {
+    g[T] = 1;
+    status[att] |= kKgMinpoly;
+  }
+}
+
+// ---------------------------------------------------------------- support
+// CTA per attempt: sort the 2^m pairs (value_i << 31 | i) (pk_gen.c:82-96),
+// reject a repeated value, keep pi_i = the index part of the i-th smallest.
+constexpr int kSupportThreads = 1024;
+template <int SET>
+__global__ void __launch_bounds__(kSupportThreads) kg_support_kernel(const uint8_t *__restrict__ rbuf, int natt,
+                                                                     uint16_t *__restrict__ pi_out,
+                                                                     uint8_t *__restrict__ status) {
+  using C = KG<SET>;
+  constexpr int q = C::q;
+  extern __shared__ __align__(16) uint64_t kgsm_sup[];
+  const int att = blockIdx.x;
+  if (att >= natt || !(status[att] & kKgMinpoly)) return;
+  const int tid = threadIdx.x;
+  const uint8_t *pv = rbuf + (long long)att * C::rstride + C::n / 8;
+  for (int i = tid; i < q; i += kSupportThreads) {
+    const uint32_t v = (uint32_t)pv[4 * i] | ((uint32_t)pv[4 * i + 1] << 8) | ((uint32_t)pv[4 * i + 2] << 16) |
+                       ((uint32_t)pv[4 * i + 3] << 24);
+    kgsm_sup[i] = ((uint64_t)v << 31) | (uint64_t)i;
+  }
+  __syncthreads();
+  for (int size = 2; size <= q; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int p = tid; p < q / 2; p += kSupportThreads) {
+        const int i = 2 * p - (p & (stride - 1)), j = i + stride;
+        const bool up = (i & size) == 0;
+        const uint64_t a = kgsm_sup[i], b = kgsm_sup[j];
+        if ((a > b) == up) {
+          kgsm_sup[i] = b;
+          kgsm_sup[j] = a;
+        }
+      }
+      __syncthreads();
+    }
+  int tie = 0;
+  for (int i = tid + 1; i < q; i += kSupportThreads)
+    if ((kgsm_sup[i - 1] >> 31) == (kgsm_sup[i] >> 31)) tie = 1;
+  tie = __syncthreads_or(tie);
+  if (tie) return;
+  uint16_t *pi = pi_out + (long long)att * q;
+  for (int i = tid; i < q; i += kSupportThreads) pi[i] = (uint16_t)(kgsm_sup[i] & (q - 1));
+  if (tid == 0) status[att] |= kKgDistinct;
+}
+
+// ---------------------------------------------------------------- matrix
+// Block (b, slot): columns 256 b .. 256 b + 255 (one warp per 32-column word)
+// of the attempt's parity-check matrix, rows i*m + bit for i < t:
+// bit of L_j^i / g(L_j), L_j = bitrev_m(pi_j) (pk_gen.c:98-140). Columns at
+// or past n are zero. Words [0, nwords) of each row of stride ld are written.
+constexpr int kBuildThreads = 256;
+template <int SET> struct BuildSmem {
+  using C = KG<SET>;
+  static constexpr int ex = 0, lg = ex + ((C::exp_n + 1) & ~1), g = lg + C::q, tile_u16 = g + C::gstride;
+  static constexpr int bytes = tile_u16 * 2 + C::mt * 8 * 4;
+};
+template <int SET>
+__global__ void __launch_bounds__(kBuildThreads) kg_build_kernel(const uint16_t *__restrict__ gall,
+                                                                 const uint16_t *__restrict__ piall,
+                                                                 const int *__restrict__ att_of, const uint8_t *__restrict__ status,
+                                                                 uint32_t *__restrict__ mat, int ld, int nwords,
+                                                                 const uint16_t *__restrict__ gexp,
+                                                                 const uint16_t *__restrict__ glog) {
+  using C = KG<SET>;
+  using L = BuildSmem<SET>;
+  constexpr int q = C::q, T = C::t, M = C::m, ZL = C::zl;
+  extern __shared__ __align__(16) uint16_t kgsm_bd[];
+  uint16_t *ex = kgsm_bd + L::ex, *lg = kgsm_bd + L::lg, *gs = kgsm_bd + L::g;
+  uint32_t *tile = reinterpret_cast<uint32_t *>(kgsm_bd + L::tile_u16);
+  const int slot = blockIdx.y;
+  const int att = att_of ? att_of[slot] : slot;
+  if ((status[att] & (kKgMinpoly | kKgDistinct)) != (kKgMinpoly | kKgDistinct)) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < C::exp_n; i += kBuildThreads) ex[i] = gexp[i];
+  for (int i = tid; i < q; i += kBuildThreads) lg[i] = glog[i];
+  for (int i = tid; i <= T; i += kBuildThreads) gs[i] = gall[(long long)att * C::gstride + i];
+  __syncthreads();
+  const int col = (blockIdx.x * 8 + warp) * 32 + lane;
+  uint16_t inv = 0;
+  int lL = ZL;
+  if (col < C::n) {
+    const uint16_t p = piall[(long long)att * q + col];
+    const uint16_t Lj = (uint16_t)(__brev((uint32_t)p) >> (32 - M));
+    lL = lg[Lj];
+    uint16_t v = gs[T];
+    for (int i = T - 1; i >= 0; i--) v = ex[min((int)lg[v] + lL, ZL)] ^ gs[i];
+    const int lv = lg[v];
+    inv = lv < q - 1 ? ex[q - 1 - lv] : 0;
+  }
+  for (int i = 0; i < T; i++) {
+#pragma unroll
+    for (int b = 0; b < M; b++) {
+      const uint32_t bal = __ballot_sync(0xffffffffu, (inv >> b) & 1);
+      if (lane == 0) tile[(i * M + b) * 8 + warp] = bal;
+    }
+    inv = ex[min((int)lg[inv] + lL, ZL)];
+  }
+  __syncthreads();
+  uint32_t *dst = mat + (long long)slot * C::mt * ld;
+  for (int idx = tid; idx < C::mt * 8; idx += kBuildThreads) {
+    const int row = idx >> 3, w = blockIdx.x * 8 + (idx & 7);
+    if (w < nwords) dst[(long long)row * ld + w] = tile[idx];
+  }
+}
+
+// ---------------------------------------------------------------- elimination
+// CTA per matrix (mt rows of ld words; words [0, nwords) take part). Blocked
+// Gauss-Jordan with 32-column panels: per panel the CTA finds pivot rows for
+// the panel's columns (forward elimination on the panel word only), inverts
+// their 32 x 32 panel block B, replaces the pivot rows P by P' = B^-1 P and
+// clears the panel from every other row r with r ^= c_r P', c_r = r's panel
+// word. The last update is a Four-Russians product: per 32-word group four
+// 256-entry tables of XOR combinations of P' rows (8 rows each) in shared
+// memory, four lookups per row word. Singular A_L: no pivot for some column,
+// the attempt fails (pk_gen.c:150-156 rejects the same matrices).
+constexpr int kElimThreads = 1024;
+template <int SET> struct ElimSmem {
+  using C = KG<SET>;
+  static constexpr int tab = 0;                       // 4 * 256 * 32 u32
+  static constexpr int pw = tab + 4 * 256 * 32;       // 32 * 32 u32
+  static constexpr int colw = pw + 32 * 32;           // mt u32
+  static constexpr int wk = colw + C::mt;             // mt u32
+  static constexpr int binv = wk + C::mt;             // 32 u32
+  static constexpr int misc = binv + 32;              // 4 ints
+  static constexpr int rowid_u32 = misc + 4;          // mt u16
+  static constexpr int bytes = rowid_u32 * 4 + C::mt * 2 + 16;
+};
+template <int SET>
+__global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__restrict__ mat, int ld, int nwords,
+                                                                  const int *__restrict__ att_of,
+                                                                  uint8_t *__restrict__ status, int need, int set_bit,
+                                                                  uint16_t *__restrict__ rowid_out) {
+  using C = KG<SET>;
+  using L = ElimSmem<SET>;
+  constexpr int MT = C::mt;
+  extern __shared__ __align__(16) uint32_t kgsm_el[];
+  uint32_t *tab = kgsm_el + L::tab, *Pw = kgsm_el + L::pw, *colw = kgsm_el + L::colw, *wk = kgsm_el + L::wk,
+           *binv = kgsm_el + L::binv;
+  int *misc = reinterpret_cast<int *>(kgsm_el + L::misc);
+  uint16_t *rowid = reinterpret_cast<uint16_t *>(kgsm_el + L::rowid_u32);
+  const int slot = blockIdx.x;
+  const int att = att_of ? att_of[slot] : slot;
+  if ((status[att] & need) != need) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint32_t *A = mat + (long long)slot * MT * ld;
+  for (int i = tid; i < MT; i += kElimThreads) rowid[i] = (uint16_t)i;
+  const int ngroups = nwords / 32;
+  for (int p = 0; p < C::npanel; p++) {
+    const int base = 32 * p, np = min(32, MT - base);
+    const uint32_t npmask = np == 32 ? 0xffffffffu : ((1u << np) - 1);
+    if (tid == 0) {
+      misc[0] = INT_MAX;
+      misc[1] = 0;
+    }
+    __syncthreads();
+    // panel words; search for column 0's pivot
+    {
+      int cand = INT_MAX;
+      for (int pos = tid; pos < MT; pos += kElimThreads) {
+        const uint32_t v = A[(long long)rowid[pos] * ld + p];
+        colw[pos] = v;
+        wk[pos] = v;
+        if (pos >= base && (v & 1)) cand = min(cand, pos);
+      }
+      cand = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+      if (lane == 0 && cand != INT_MAX) atomicMin(&misc[0], cand);
+    }
+    __syncthreads();
+    for (int j = 0; j < np; j++) {
+      if (tid == 0) {
+        const int piv = misc[0];
+        misc[0] = INT_MAX;
+        if (piv == INT_MAX) {
+          misc[1] = 1;
+        } else if (piv != base + j) {
+          const int at = base + j;
+          uint32_t t0 = wk[piv]; wk[piv] = wk[at]; wk[at] = t0;
+          t0 = colw[piv]; colw[piv] = colw[at]; colw[at] = t0;
+          const uint16_t r0 = rowid[piv]; rowid[piv] = rowid[at]; rowid[at] = r0;
+        }
+      }
+      __syncthreads();
+      if (misc[1]) return;  // no pivot: A_L is singular
+      const uint32_t pwd = wk[base + j], bit = 1u << j;
+      int cand = INT_MAX;
+      for (int pos = base + j + 1 + tid; pos < MT; pos += kElimThreads) {
+        uint32_t x = wk[pos];
+        if (x & bit) {
+          x ^= pwd;
+          wk[pos] = x;
+        }
+        if (j + 1 < np && ((x >> (j + 1)) & 1)) cand = min(cand, pos);
+      }
+      cand = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+      if (lane == 0 && cand != INT_MAX) atomicMin(&misc[0], cand);
+      __syncthreads();
+    }
+    // B^-1 for the pivot rows' original panel words (warp 0, lane = row)
+    if (warp == 0) {
+      uint32_t b = lane < np ? (colw[base + lane] & npmask) : 0;
+      uint32_t e = lane < np ? (1u << lane) : 0;
+      for (int i = 0; i < np; i++) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, lane >= i && lane < np && ((b >> i) & 1));
+        const int pl = __ffs(bal) - 1;  // exists: the pivot rows are independent on the panel
+        const uint32_t bp = __shfl_sync(0xffffffffu, b, pl), ep = __shfl_sync(0xffffffffu, e, pl);
+        const uint32_t bi = __shfl_sync(0xffffffffu, b, i), ei = __shfl_sync(0xffffffffu, e, i);
+        if (lane == i) { b = bp; e = ep; }
+        else if (lane == pl) { b = bi; e = ei; }
+        if (lane != i && ((b >> i) & 1)) {
+          b ^= bp;
+          e ^= ep;
+        }
+      }
+      binv[lane] = e;
+    }
+    __syncthreads();
+    for (int g = p >> 5; g < ngroups; g++) {
+      const int w0 = 32 * g;
+      {
+        const int b = tid >> 5;
+        Pw[tid] = b < np ? A[(long long)rowid[base + b] * ld + w0 + lane] : 0;
+      }
+      __syncthreads();
+      uint32_t v = 0;
+      {
+        uint32_t e = binv[warp];
+        while (e) {
+          const int b = __ffs(e) - 1;
+          e &= e - 1;
+          v ^= Pw[b * 32 + lane];
+        }
+      }
+      __syncthreads();
+      Pw[tid] = v;
+      if (warp < np) A[(long long)rowid[base + warp] * ld + w0 + lane] = v;
+      __syncthreads();
+      {
+        const int kq = tid >> 8, vhi = (tid >> 5) & 7;
+        const uint32_t *pr = Pw + 8 * kq * 32 + lane;
+        uint32_t h = 0;
+        if (vhi & 1) h ^= pr[5 * 32];
+        if (vhi & 2) h ^= pr[6 * 32];
+        if (vhi & 4) h ^= pr[7 * 32];
+        const uint32_t p0 = pr[0], p1 = pr[32], p2 = pr[64], p3 = pr[96], p4 = pr[128];
+        uint32_t *tp = tab + ((kq * 256 + vhi * 32) * 32) + lane;
+        uint32_t r[32];
+        r[0] = h;
+#pragma unroll
+        for (int vl = 1; vl < 32; vl++) {
+          const int low = __ffs(vl) - 1;
+          const uint32_t pb = low == 0 ? p0 : low == 1 ? p1 : low == 2 ? p2 : low == 3 ? p3 : p4;
+          r[vl] = r[vl & (vl - 1)] ^ pb;
+        }
+#pragma unroll
+        for (int vl = 0; vl < 32; vl++) tp[vl * 32] = r[vl];
+      }
+      __syncthreads();
+      for (int pos0 = warp; pos0 < MT; pos0 += 4 * 32) {
+        uint32_t x[4], c[4];
+        uint32_t *ad[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int pos = pos0 + 32 * u;
+          const bool live = pos < MT && (unsigned)(pos - base) >= (unsigned)np;
+          c[u] = live ? (colw[pos] & npmask) : 0;
+          ad[u] = A + (long long)rowid[live ? pos : 0] * ld + w0 + lane;
+          x[u] = c[u] ? *ad[u] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (!c[u]) continue;
+          const uint32_t cc = c[u];
+          x[u] ^= tab[((cc & 255) << 5) + lane] ^ tab[((256 + ((cc >> 8) & 255)) << 5) + lane] ^
+                  tab[((512 + ((cc >> 16) & 255)) << 5) + lane] ^ tab[((768 + (cc >> 24)) << 5) + lane];
+          *ad[u] = x[u];
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (rowid_out)
+    for (int i = tid; i < MT; i += kElimThreads) rowid_out[(long long)slot * MT + i] = rowid[i];
+  if (tid == 0) status[att] |= (uint8_t)set_bit;
+}
+
+// ---------------------------------------------------------------- control bits
+// CTA per winner. The library's recursion (controlbits.c:29-150, restated in
+// host_keygen.cpp) processes a permutation of 2^w entries and recurses into
+// two halves with doubled bit stride; here every depth d runs all 2^d
+// sub-permutations at once, each a segment of 2^(w-d) entries, with each of
+// the recursion's sorts a segmented bitonic sort. Segment s at depth d writes
+// layer d and layer 2w-2-d at bits offset_s + 2^d j, offset_s = bitrev_d(s).
+// The bits are checked by applying the 2w-1 layers to the identity.
+constexpr int kCbitsThreads = 1024;
+template <int SET> struct CbitsSmem {
+  using C = KG<SET>;
+  static constexpr int a = 0, b = a + C::q, cb = b + C::q, pi_u32 = cb + C::cond_bytes / 4;
+  static constexpr int bytes = pi_u32 * 4 + C::q * 2 + 16;
+};
+
+template <int Q>
+__device__ __forceinline__ void seg_sort(uint32_t *arr, int nn) {
+  __syncthreads();
+  for (int size = 2; size <= nn; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int p = threadIdx.x; p < Q / 2; p += kCbitsThreads) {
+        const int i = 2 * p - (p & (stride - 1)), j = i + stride;
+        const bool up = size == nn || (i & size) == 0;
+        const uint32_t a = arr[i], b = arr[j];
+        if ((a > b) == up) {
+          arr[i] = b;
+          arr[j] = a;
+        }
+      }
+      __syncthreads();
+    }
+}
+
+template <int SET>
+__global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t *__restrict__ piall,
+                                                                 const int *__restrict__ att_of, int nwin,
+                                                                 uint8_t *__restrict__ cond_out,
+                                                                 uint8_t *__restrict__ cb_ok) {
+  using C = KG<SET>;
+  using L = CbitsSmem<SET>;
+  constexpr int q = C::q, W = C::m, H = q / 2;
+  extern __shared__ __align__(16) uint32_t kgsm_cb[];
+  uint32_t *A = kgsm_cb + L::a, *B = kgsm_cb + L::b, *CB = kgsm_cb + L::cb;
+  uint16_t *PI = reinterpret_cast<uint16_t *>(kgsm_cb + L::pi_u32);
+  const int w = blockIdx.x;
+  if (w >= nwin) return;
+  const int tid = threadIdx.x;
+  const uint16_t *pi0 = piall + (long long)att_of[w] * q;
+  for (int i = tid; i < q; i += kCbitsThreads) PI[i] = pi0[i];
+  for (int i = tid; i < C::cond_bytes / 4; i += kCbitsThreads) CB[i] = 0;
+  __syncthreads();
+  auto setbit = [&](int bit) { atomicOr(&CB[bit >> 5], 1u << (bit & 31)); };
+  for (int d = 0; d < W; d++) {
+    const int ww = W - d, nn = 1 << ww;
+    auto offs = [&](int s) { return d == 0 ? 0 : (int)(__brev((uint32_t)s) >> (32 - d)); };
+    if (ww == 1) {
+      for (int s = tid; s < H; s += kCbitsThreads)
+        if (PI[2 * s] & 1) setbit((W - 1) * H + offs(s));
+      break;
+    }
+    for (int X = tid; X < q; X += kCbitsThreads) A[X] = ((uint32_t)(PI[X] ^ 1) << 16) | (uint32_t)PI[X ^ 1];
+    seg_sort<q>(A, nn);
+    for (int X = tid; X < q; X += kCbitsThreads) {
+      const uint32_t x = (uint32_t)(X & (nn - 1)), a = A[X], px = a & 0xffff;
+      B[X] = (px << 16) | min(px, x);
+      A[X] = (a << 16) | x;
+    }
+    seg_sort<q>(A, nn);
+    for (int X = tid; X < q; X += kCbitsThreads) A[X] = (A[X] << 16) + (B[X] >> 16);
+    seg_sort<q>(A, nn);
+    if (ww <= 10) {
+      for (int X = tid; X < q; X += kCbitsThreads) B[X] = ((A[X] & 0xffff) << 10) | (B[X] & 0x3ff);
+      for (int i = 1; i < ww - 1; i++) {
+        for (int X = tid; X < q; X += kCbitsThreads) A[X] = ((B[X] & ~0x3ffu) << 6) | (uint32_t)(X & (nn - 1));
+        seg_sort<q>(A, nn);
+        for (int X = tid; X < q; X += kCbitsThreads) A[X] = (A[X] << 20) | B[X];
+        seg_sort<q>(A, nn);
+        for (int X = tid; X < q; X += kCbitsThreads) {
+          const uint32_t ppcp = A[X] & 0xfffff, ppc = (A[X] & 0xffc00) | (B[X] & 0x3ff);
+          B[X] = min(ppc, ppcp);
+        }
+      }
+      for (int X = tid; X < q; X += kCbitsThreads) B[X] &= 0x3ff;
+    } else {
+      for (int X = tid; X < q; X += kCbitsThreads) B[X] = (A[X] << 16) | (B[X] & 0xffff);
+      for (int i = 1; i < ww - 1; i++) {
+        for (int X = tid; X < q; X += kCbitsThreads) A[X] = (B[X] & ~0xffffu) | (uint32_t)(X & (nn - 1));
+        seg_sort<q>(A, nn);
+        for (int X = tid; X < q; X += kCbitsThreads) A[X] = (A[X] << 16) | (B[X] & 0xffff);
+        if (i < ww - 2) {
+          for (int X = tid; X < q; X += kCbitsThreads) B[X] = (A[X] & ~0xffffu) | (B[X] >> 16);
+          seg_sort<q>(B, nn);
+          for (int X = tid; X < q; X += kCbitsThreads) B[X] = (B[X] << 16) | (A[X] & 0xffff);
+        }
+        seg_sort<q>(A, nn);
+        for (int X = tid; X < q; X += kCbitsThreads) {
+          const uint32_t cp = (B[X] & ~0xffffu) | (A[X] & 0xffff);
+          B[X] = min(B[X], cp);
+        }
+      }
+      for (int X = tid; X < q; X += kCbitsThreads) B[X] &= 0xffff;
+    }
+    for (int X = tid; X < q; X += kCbitsThreads) A[X] = ((uint32_t)PI[X] << 16) + (uint32_t)(X & (nn - 1));
+    seg_sort<q>(A, nn);
+    for (int pr = tid; pr < H; pr += kCbitsThreads) {
+      const int X = 2 * pr, z = X & (nn - 1), s = X >> ww;
+      const uint32_t fj = B[X] & 1, Fz = (uint32_t)z + fj, Fz1 = Fz ^ 1;
+      if (fj) setbit(d * H + offs(s) + ((z >> 1) << d));
+      B[X] = (A[X] << 16) | Fz;
+      B[X + 1] = (A[X + 1] << 16) | Fz1;
+    }
+    seg_sort<q>(B, nn);
+    for (int pr = tid; pr < H; pr += kCbitsThreads) {
+      const int X = 2 * pr, y = X & (nn - 1), s = X >> ww;
+      const uint32_t lk = B[X] & 1, Ly = (uint32_t)y + lk, Ly1 = Ly ^ 1;
+      if (lk) setbit((2 * W - 2 - d) * H + offs(s) + ((y >> 1) << d));
+      A[X] = (Ly << 16) | (B[X] & 0xffff);
+      A[X + 1] = (Ly1 << 16) | (B[X + 1] & 0xffff);
+    }
+    seg_sort<q>(A, nn);
+    for (int pr = tid; pr < H; pr += kCbitsThreads) {
+      const int X = 2 * pr, base = X & ~(nn - 1), j = (X & (nn - 1)) >> 1;
+      PI[base + j] = (uint16_t)((A[X] & 0xffff) >> 1);
+      PI[base + nn / 2 + j] = (uint16_t)((A[X + 1] & 0xffff) >> 1);
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  // check: the layers applied to the identity give pi
+  for (int i = tid; i < q; i += kCbitsThreads) A[i] = (uint32_t)i;
+  __syncthreads();
+  for (int l = 0; l < 2 * W - 1; l++) {
+    const int s = l < W ? l : 2 * W - 2 - l, stride = 1 << s;
+    for (int idx = tid; idx < H; idx += kCbitsThreads) {
+      const int bit = l * H + idx;
+      if ((CB[bit >> 5] >> (bit & 31)) & 1) {
+        const int i0 = (idx >> s) * 2 * stride + (idx & (stride - 1)), i1 = i0 + stride;
+        const uint32_t t0 = A[i0];
+        A[i0] = A[i1];
+        A[i1] = t0;
+      }
+    }
+    __syncthreads();
+  }
+  int bad = 0;
+  for (int i = tid; i < q; i += kCbitsThreads) bad |= A[i] != (uint32_t)pi0[i];
+  bad = __syncthreads_or(bad);
+  uint32_t *co = reinterpret_cast<uint32_t *>(cond_out + (long long)w * C::cond_bytes);
+  for (int i = tid; i < C::cond_bytes / 4; i += kCbitsThreads) co[i] = CB[i];
+  if (tid == 0) cb_ok[w] = bad ? 0 : 1;
+}
+
+// ---------------------------------------------------------------- assembly
+// pk row i = bits [mt, n) of the reduced row at position i; sk = seed |
+// ff ff ff ff 00 00 00 00 | g_0..g_{t-1} (LE u16) | control bits | r[0:n/8].
+template <int SET>
+__global__ void kg_assemble_kernel(const int *__restrict__ att_of, int nwin, const uint8_t *__restrict__ rbuf,
+                                   const uint8_t *__restrict__ delta, const uint16_t *__restrict__ gall,
+                                   const uint8_t *__restrict__ cond, const uint32_t *__restrict__ matF,
+                                   const uint16_t *__restrict__ rowid, uint8_t *__restrict__ pk_out,
+                                   uint8_t *__restrict__ sk_out) {
+  using C = KG<SET>;
+  const int w = blockIdx.y;
+  if (w >= nwin) return;
+  const int att = att_of[w];
+  const long long pkb = C::pk_bytes, skb = C::sk_bytes;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < pkb + skb; i += stride) {
+    if (i < pkb) {
+      const int row = (int)(i / C::pk_row_bytes), byte = (int)(i - (long long)row * C::pk_row_bytes);
+      const uint32_t *src = matF + ((long long)w * C::mt + rowid[(long long)w * C::mt + row]) * C::rw;
+      const int bp = C::mt + 8 * byte, wd = bp >> 5, sh = bp & 31;
+      uint32_t v = src[wd] >> sh;
+      if (sh > 24) v |= src[wd + 1] << (32 - sh);
+      pk_out[(long long)w * pkb + i] = (uint8_t)v;
+    } else {
+      const int o = (int)(i - pkb);
+      uint8_t v;
+      if (o < 32) v = delta[(long long)att * 32 + o];
+      else if (o < 36) v = 0xff;
+      else if (o < 40) v = 0;
+      else if (o < 40 + 2 * C::t) {
+        const uint16_t gv = gall[(long long)att * C::gstride + ((o - 40) >> 1)];
+        v = (uint8_t)(((o - 40) & 1) ? gv >> 8 : gv);
+      } else if (o < 40 + 2 * C::t + C::cond_bytes) v = cond[(long long)w * C::cond_bytes + (o - 40 - 2 * C::t)];
+      else v = rbuf[(long long)att * C::rstride + (o - 40 - 2 * C::t - C::cond_bytes)];
+      sk_out[(long long)w * skb + o] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- host side
+namespace {
+int kg_fail(int code, const std::string &msg) {
+  set_last_error(msg.c_str());
+  return code;
+}
+#define KG_CUDA(call)                                                                    \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess) {                                                             \
+      rc = kg_fail(GMC_ECUDA, std::string(#call) + ": " + cudaGetErrorString(_e));       \
+      goto done;                                                                         \
+    }                                                                                    \
+  } while (0)
+
+template <typename F>
+cudaError_t smem_attr(F *fn, int bytes) {
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <int SET>
+cudaError_t kg_attrs() {
+  static cudaError_t once = [] {
+    cudaError_t e = smem_attr(kg_minpoly_kernel<SET>, MinpolySmem<SET>::bytes);
+    if (e == cudaSuccess) e = smem_attr(kg_support_kernel<SET>, KG<SET>::q * 8);
+    if (e == cudaSuccess) e = smem_attr(kg_build_kernel<SET>, BuildSmem<SET>::bytes);
+    if (e == cudaSuccess) e = smem_attr(kg_elim_kernel<SET>, ElimSmem<SET>::bytes);
+    if (e == cudaSuccess) e = smem_attr(kg_cbits_kernel<SET>, CbitsSmem<SET>::bytes);
+    return e;
+  }();
+  return once;
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count, cudaStream_t st) {
+  return cudaMallocAsync(reinterpret_cast<void **>(p), std::max<size_t>(count, 1) * sizeof(T), st);
+}
+
+constexpr long long kMaxAttemptsPerKey = 100000;
+
+template <int SET>
+int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, cudaStream_t st) {
+  using C = KG<SET>;
+  int rc = GMC_OK;
+  FieldDev fd{};
+  int dev = 0, sms = 0;
+  uint8_t *d_seed_in = nullptr, *d_seed_out = nullptr, *d_r = nullptr, *d_delta = nullptr, *d_status = nullptr,
+          *d_cond = nullptr, *d_cbok = nullptr, *d_pk = nullptr, *d_sk = nullptr;
+  uint16_t *d_g = nullptr, *d_pi = nullptr, *d_rowid = nullptr;
+  uint32_t *d_matL = nullptr, *d_matF = nullptr;
+  int *d_win = nullptr;
+  std::vector<long long> pending, next;
+  std::vector<uint8_t> cur, h_status, h_seed, h_cbok;
+  std::vector<long long> tries;
+  std::vector<int> win_att;
+  std::vector<long long> win_key;
+  int cap = 0, wcap = 0;
+  if (field_tables(SET, &fd) != GMC_OK) return GMC_ECUDA;
+  KG_CUDA(cudaGetDevice(&dev));
+  KG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  KG_CUDA(kg_attrs<SET>());
+  cap = 2 * sms;                                      // attempts per round
+  wcap = (int)std::min<long long>(nkeys, cap);        // winners per round
+  KG_CUDA(dalloc(&d_seed_in, (size_t)cap * 32, st));
+  KG_CUDA(dalloc(&d_seed_out, (size_t)cap * 32, st));
+  KG_CUDA(dalloc(&d_r, (size_t)cap * C::rstride, st));
+  KG_CUDA(dalloc(&d_delta, (size_t)cap * 32, st));
+  KG_CUDA(dalloc(&d_status, (size_t)cap, st));
+  KG_CUDA(dalloc(&d_g, (size_t)cap * C::gstride, st));
+  KG_CUDA(dalloc(&d_pi, (size_t)cap * C::q, st));
+  KG_CUDA(dalloc(&d_matL, (size_t)cap * C::mt * C::rwl, st));
+  KG_CUDA(dalloc(&d_win, (size_t)wcap, st));
+  KG_CUDA(dalloc(&d_matF, (size_t)wcap * C::mt * C::rw, st));
+  KG_CUDA(dalloc(&d_rowid, (size_t)wcap * C::mt, st));
+  KG_CUDA(dalloc(&d_cond, (size_t)wcap * C::cond_bytes, st));
+  KG_CUDA(dalloc(&d_cbok, (size_t)wcap, st));
+  KG_CUDA(dalloc(&d_pk, (size_t)wcap * C::pk_bytes, st));
+  KG_CUDA(dalloc(&d_sk, (size_t)wcap * C::sk_bytes, st));
+  cur.assign(seeds, seeds + 32 * nkeys);
+  tries.assign(nkeys, 0);
+  for (long long i = 0; i < nkeys; i++) pending.push_back(i);
+  while (!pending.empty()) {
+    const int nr = (int)std::min<long long>((long long)pending.size(), cap);
+    const int k = std::max(1, std::min(64, cap / nr));
+    const int natt = nr * k;
+    h_seed.resize((size_t)nr * 32);
+    for (int j = 0; j < nr; j++) memcpy(&h_seed[32 * j], &cur[32 * pending[j]], 32);
+    KG_CUDA(cudaMemcpyAsync(d_seed_in, h_seed.data(), (size_t)nr * 32, cudaMemcpyHostToDevice, st));
+    kg_expand_kernel<SET><<<(nr + 31) / 32, 32, 0, st>>>(d_seed_in, d_seed_out, nr, k, d_r, d_delta, d_status);
+    kg_minpoly_kernel<SET><<<natt, kMinpolyThreads, MinpolySmem<SET>::bytes, st>>>(d_r, natt, fd.gexp, fd.glog, d_g,
+                                                                                 d_status);
+    kg_support_kernel<SET><<<natt, kSupportThreads, C::q * 8, st>>>(d_r, natt, d_pi, d_status);
+    kg_build_kernel<SET><<<dim3(C::rwl / 8, natt), kBuildThreads, BuildSmem<SET>::bytes, st>>>(
+        d_g, d_pi, nullptr, d_status, d_matL, C::rwl, C::rwl, fd.gexp, fd.glog);
+    kg_elim_kernel<SET><<<natt, kElimThreads, ElimSmem<SET>::bytes, st>>>(
+        d_matL, C::rwl, C::rwl, nullptr, d_status, kKgMinpoly | kKgDistinct, kKgRank, nullptr);
+    KG_CUDA(cudaGetLastError());
+    h_status.resize(natt);
+    h_seed.resize((size_t)nr * 32);
+    KG_CUDA(cudaMemcpyAsync(h_status.data(), d_status, natt, cudaMemcpyDeviceToHost, st));
+    KG_CUDA(cudaMemcpyAsync(h_seed.data(), d_seed_out, (size_t)nr * 32, cudaMemcpyDeviceToHost, st));
+    KG_CUDA(cudaStreamSynchronize(st));
+    win_att.clear();
+    win_key.clear();
+    next.clear();
+    for (int j = 0; j < nr; j++) {
+      const long long key = pending[j];
+      int a = 0;
+      while (a < k && h_status[(size_t)j * k + a] != kKgAll) a++;
+      if (a < k) {
+        win_att.push_back(j * k + a);
+        win_key.push_back(key);
+      } else {
+        tries[key] += k;
+        if (tries[key] >= kMaxAttemptsPerKey) {
+          rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: no systematic key within the attempt limit");
+          goto done;
+        }
+        memcpy(&cur[32 * key], &h_seed[32 * j], 32);
+        next.push_back(key);
+      }
+    }
+    for (size_t j = nr; j < pending.size(); j++) next.push_back(pending[j]);
+    if (!win_att.empty()) {
+      const int nw = (int)win_att.size();
+      KG_CUDA(cudaMemcpyAsync(d_win, win_att.data(), nw * sizeof(int), cudaMemcpyHostToDevice, st));
+      kg_build_kernel<SET><<<dim3(C::rw / 8, nw), kBuildThreads, BuildSmem<SET>::bytes, st>>>(
+          d_g, d_pi, d_win, d_status, d_matF, C::rw, C::rw, fd.gexp, fd.glog);
+      // the winners' status already has every bit: the full elimination re-derives the same pivots
+      kg_elim_kernel<SET><<<nw, kElimThreads, ElimSmem<SET>::bytes, st>>>(d_matF, C::rw, C::rw, d_win, d_status,
+                                                                        kKgAll, kKgAll, d_rowid);
+      kg_cbits_kernel<SET><<<nw, kCbitsThreads, CbitsSmem<SET>::bytes, st>>>(d_pi, d_win, nw, d_cond, d_cbok);
+      kg_assemble_kernel<SET><<<dim3(256, nw), 256, 0, st>>>(d_win, nw, d_r, d_delta, d_g, d_cond, d_matF, d_rowid,
+                                                              d_pk, d_sk);
+      KG_CUDA(cudaGetLastError());
+      for (int w = 0; w < nw; w++) {
+        KG_CUDA(cudaMemcpyAsync(pk + win_key[w] * C::pk_bytes, d_pk + (long long)w * C::pk_bytes, C::pk_bytes,
+                                cudaMemcpyDeviceToHost, st));
+        KG_CUDA(cudaMemcpyAsync(sk + win_key[w] * C::sk_bytes, d_sk + (long long)w * C::sk_bytes, C::sk_bytes,
+                                cudaMemcpyDeviceToHost, st));
+      }
+      h_cbok.resize(nw);
+      KG_CUDA(cudaMemcpyAsync(h_cbok.data(), d_cbok, nw, cudaMemcpyDeviceToHost, st));
+      KG_CUDA(cudaStreamSynchronize(st));
+      for (int w = 0; w < nw; w++)
+        if (!h_cbok[w]) {
+          rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: control bits do not encode the support permutation");
+          goto done;
+        }
+    }
+    pending.swap(next);
+  }
+done:
+  for (void *p : {(void *)d_seed_in, (void *)d_seed_out, (void *)d_r, (void *)d_delta, (void *)d_status, (void *)d_g,
+                  (void *)d_pi, (void *)d_matL, (void *)d_win, (void *)d_matF, (void *)d_rowid, (void *)d_cond,
+                  (void *)d_cbok, (void *)d_pk, (void *)d_sk})
+    if (p) cudaFreeAsync(p, st);
+  if (rc == GMC_OK) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
+  } else {
+    cudaStreamSynchronize(st);
+  }
+  return rc;
+}
+#undef KG_CUDA
+}  // namespace
+
+}  // namespace gmc
+
+// Batched key generation (host buffers): key i from seeds[32 i .. 32 i + 31],
+// the single randombytes draw of libmceliece's keypair; identical bytes to
+// gmc_keypair_seed for every key.
+extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seeds,
+                                 long long nkeys) {
+  using namespace gmc;
+  if (set < 0 || set >= GMC_NSETS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
+    return kg_fail(GMC_EINVAL, "gmc_keypair_batch: bad argument");
+  if (nkeys == 0) return GMC_OK;
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
+  int rc = GMC_EINVAL;
+  switch (set) {
+    case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, st); break;
+    case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, st); break;
+    case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, st); break;
+    case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, st); break;
+    case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, st); break;
+  }
+  cudaStreamDestroy(st);
+  return rc;
+}
