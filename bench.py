@@ -59,6 +59,8 @@ def parse():
                     "full serving configuration)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the N = 256..65536 throughput sweep")
     ap.add_argument("--no-engines", action="store_true", help="skip the syndrome-engine comparison")
+    ap.add_argument("--no-keygen", action="store_true", help="skip the batched key-generation measurement")
+    ap.add_argument("--keygen-keys", type=int, default=608, help="keys per batched key-generation call")
     return ap.parse_args()
 
 
@@ -424,6 +426,44 @@ def keccak_rates(z, n, kernels):
     return out
 
 
+def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True):
+    """Batched key generation (gmc_keypair_batch, host buffers in and out) per parameter set: keys/s
+    over nkeys seeds, beside the oracle's keypair on the host threads (a bounded sample whose
+    keys are also compared byte for byte with the GPU's)."""
+    import hashlib
+    out = {"nkeys": nkeys, "sets": {}}
+    if with_cpu:
+        from concurrent.futures import ThreadPoolExecutor
+        from oracle import pyoracle as O
+        O.lib()
+    for name in gmc.SETS:
+        sid = gmc.set_id(name)
+        seeds = np.frombuffer(b"".join(hashlib.sha256(b"bench-kg" + bytes([sid]) + i.to_bytes(4, "little")).digest()
+                                       for i in range(nkeys)), np.uint8).reshape(nkeys, 32)
+        gmc.keypair_batch(sid, seeds[:8])  # warm-up (tables, pool)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            pk, sk = gmc.keypair_batch(sid, seeds)
+            ts.append(time.perf_counter() - t0)
+        e = {"keys_s": nkeys / min(ts), "s_per_call": min(ts)}
+        if with_cpu:
+            ns = cpu_threads
+            t0 = time.perf_counter()
+            with ThreadPoolExecutor(cpu_threads) as ex:
+                ref = list(ex.map(lambda s_: O.keypair(sid, bytes(s_)), seeds[:ns]))
+            t_cpu = time.perf_counter() - t0
+            bad = sum(int(not (np.array_equal(pk[i], np.asarray(ref[i][0])) and
+                               np.array_equal(sk[i], np.asarray(ref[i][1])))) for i in range(ns))
+            e["cpu_baseline"] = {"value": ns / t_cpu, "unit": "keys/s", "cores": cpu_threads, "kind": "port",
+                                 "sample": f"{ns} keypairs of the same seeds, {cpu_threads} threads"}
+            e["checked_keys"] = ns
+            e["mismatches"] = bad
+        out["sets"][name] = e
+    return out
+
+
 def serving(gmc, torch, seconds):
     """16 device-resident key pairs over the five sets, 50/50 enc/dec, Poisson arrivals at 10/50/90% of the
     measured peak; p50/p99 latency (arrival to completion) against sequential one-request calls."""
@@ -609,6 +649,9 @@ def main():
         line["grouped"] = grouped_mix(gmc, torch, dev, N, max(5, args.steps // 2), args.warmup)
     if rank == 0 and not args.no_serving:
         line["serving"] = serving(gmc, torch, args.serve_seconds)
+    if rank == 0 and not args.no_keygen:
+        line["keygen"] = keygen_rates(gmc, torch, args.keygen_keys, os.cpu_count() or 1,
+                                      with_cpu=not args.no_cpu and world == 1)
 
     if rank == 0 and not args.no_e2e:
         # end to end through the host-pointer C ABI (pinned host buffers)

@@ -13,13 +13,16 @@
 // control bits of the support permutation, and sk = seed | pivots | g |
 // control bits | r[0:n/8].
 //
-// Device pipeline of one round (each pending key gets k chained attempts):
+// Device pipeline of one round (each pending key gets k <= 8 chained attempts,
+// k filling 4 x SMs attempts; stream 1):
 //   kg_expand    one thread per key   k chained SHAKE256 expansions
 //   kg_minpoly   one CTA per attempt  powers of f in GF((2^m)^t), Gauss-Jordan
 //   kg_support   one CTA per attempt  bitonic sort of (value, index) pairs
 //   kg_build     CTAs per attempt     columns of A_L (the rank test's matrix)
-//   kg_elim      one CTA per attempt  blocked Gauss-Jordan of A_L (rank test)
-// and for the first successful attempt of each key (the winner):
+//   kg_elim      one CTA per attempt  blocked forward elimination of A_L (rank test)
+// and for the first successful attempt of each key (the winner; stream 2,
+// overlapping the next round, whose attempt buffers are the other half of a
+// double buffer):
 //   kg_build + kg_elim on the full mt x n matrix (row order of [I | T])
 //   kg_cbits     one CTA per winner   control bits, checked by re-applying them
 //   kg_assemble  pk and sk bytes
@@ -75,6 +78,12 @@ template <int SET> struct KG {
   static constexpr int zl = 2 * q - 2;                            // log of 0
   static constexpr int exp_n = 2 * q - 1;
 };
+
+// barrier over every thread of the CTA's cluster; release/acquire order the
+// global writes before it against the reads after it
+__device__ __forceinline__ void kg_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 // status bits per attempt
 constexpr uint8_t kKgMinpoly = 1, kKgDistinct = 2, kKgRank = 4, kKgAll = 7;
@@ -380,6 +389,8 @@ __global__ void __launch_bounds__(kBuildThreads) kg_build_kernel(const uint16_t 
 // memory, four lookups per row word. Singular A_L: no pivot for some column,
 // the attempt fails (pk_gen.c:150-156 rejects the same matrices).
 constexpr int kElimThreads = 1024;
+constexpr int kElimRows = 4;      // rows in flight per warp in the panel update
+constexpr int kElimCluster = 4;   // CTAs per matrix in the full elimination
 template <int SET> struct ElimSmem {
   using C = KG<SET>;
   static constexpr int tab = 0;                       // 4 * 256 * 32 u32
@@ -387,7 +398,7 @@ template <int SET> struct ElimSmem {
   static constexpr int colw = pw + 32 * 32;           // mt u32
   static constexpr int wk = colw + C::mt;             // mt u32
   static constexpr int binv = wk + C::mt;             // 32 u32
-  static constexpr int misc = binv + 32;              // 4 ints
+  static constexpr int misc = binv + 32;              // 4 ints: candidate, failure, search mode
   static constexpr int rowid_u32 = misc + 4;          // mt u16
   static constexpr int bytes = rowid_u32 * 4 + C::mt * 2 + 16;
 };
@@ -395,7 +406,7 @@ template <int SET>
 __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__restrict__ mat, int ld, int nwords,
                                                                   const int *__restrict__ att_of,
                                                                   uint8_t *__restrict__ status, int need, int set_bit,
-                                                                  uint16_t *__restrict__ rowid_out) {
+                                                                  int forward, int cl, uint16_t *__restrict__ rowid_out) {
   using C = KG<SET>;
   using L = ElimSmem<SET>;
   constexpr int MT = C::mt;
@@ -404,7 +415,9 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
            *binv = kgsm_el + L::binv;
   int *misc = reinterpret_cast<int *>(kgsm_el + L::misc);
   uint16_t *rowid = reinterpret_cast<uint16_t *>(kgsm_el + L::rowid_u32);
-  const int slot = blockIdx.x;
+  // cl CTAs (a cluster) per matrix: each repeats the panel factorization
+  // (same inputs, same decisions) and updates the 32-word groups g = crank mod cl
+  const int slot = blockIdx.x / cl, crank = blockIdx.x - slot * cl;
   const int att = att_of ? att_of[slot] : slot;
   if ((status[att] & need) != need) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -414,52 +427,97 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
   for (int p = 0; p < C::npanel; p++) {
     const int base = 32 * p, np = min(32, MT - base);
     const uint32_t npmask = np == 32 ? 0xffffffffu : ((1u << np) - 1);
-    if (tid == 0) {
-      misc[0] = INT_MAX;
-      misc[1] = 0;
-    }
+    for (int pos = tid; pos < MT; pos += kElimThreads) colw[pos] = A[(long long)rowid[pos] * ld + p];
     __syncthreads();
-    // panel words; search for column 0's pivot
-    {
-      int cand = INT_MAX;
-      for (int pos = tid; pos < MT; pos += kElimThreads) {
-        const uint32_t v = A[(long long)rowid[pos] * ld + p];
-        colw[pos] = v;
-        wk[pos] = v;
-        if (pos >= base && (v & 1)) cand = min(cand, pos);
+    // Pivot search, first in the window of positions base .. base+63 (warp 0,
+    // slots in registers: forward elimination on the panel word, slot tags
+    // follow the swaps). A window without a pivot for some column either
+    // covers every remaining row (A_L is singular) or falls back to the
+    // CTA-wide search below.
+    if (warp == 0) {
+      const bool in0 = base + lane < MT, in1 = base + 32 + lane < MT;
+      uint32_t w0 = in0 ? colw[base + lane] : 0, w1 = in1 ? colw[base + 32 + lane] : 0;
+      int t0 = lane, t1 = 32 + lane;
+      int mode = 0;
+      for (int j = 0; j < np; j++) {
+        const uint32_t bit = 1u << j;
+        const uint32_t b0 = __ballot_sync(0xffffffffu, lane >= j && (w0 & bit));
+        const uint32_t b1 = __ballot_sync(0xffffffffu, (w1 & bit) != 0);
+        if (!b0 && !b1) {
+          mode = base + 64 >= MT ? 2 : 1;
+          break;
+        }
+        const bool lo = b0 != 0;
+        const int pl = __ffs(lo ? b0 : b1) - 1;
+        const uint32_t wj = __shfl_sync(0xffffffffu, w0, j), tj = __shfl_sync(0xffffffffu, t0, j);
+        const uint32_t wp = __shfl_sync(0xffffffffu, lo ? w0 : w1, pl);
+        const int tp = __shfl_sync(0xffffffffu, lo ? t0 : t1, pl);
+        if (lane == pl) {
+          if (lo) { w0 = wj; t0 = tj; }
+          else { w1 = wj; t1 = tj; }
+        }
+        if (lane == j) { w0 = wp; t0 = tp; }
+        if (lane > j && (w0 & bit)) w0 ^= wp;
+        if (w1 & bit) w1 ^= wp;
       }
-      cand = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
-      if (lane == 0 && cand != INT_MAX) atomicMin(&misc[0], cand);
-    }
-    __syncthreads();
-    for (int j = 0; j < np; j++) {
-      if (tid == 0) {
-        const int piv = misc[0];
+      if (mode == 0) {
+        // commit the window's permutation: position base + slot <- base + tag
+        const uint16_t r0 = in0 ? rowid[base + t0] : 0, r1 = in1 ? rowid[base + t1] : 0;
+        const uint32_t c0 = in0 ? colw[base + t0] : 0, c1 = in1 ? colw[base + t1] : 0;
+        __syncwarp();
+        if (in0) { rowid[base + lane] = r0; colw[base + lane] = c0; }
+        if (in1) { rowid[base + 32 + lane] = r1; colw[base + 32 + lane] = c1; }
+      }
+      if (lane == 0) {
         misc[0] = INT_MAX;
-        if (piv == INT_MAX) {
-          misc[1] = 1;
-        } else if (piv != base + j) {
-          const int at = base + j;
-          uint32_t t0 = wk[piv]; wk[piv] = wk[at]; wk[at] = t0;
-          t0 = colw[piv]; colw[piv] = colw[at]; colw[at] = t0;
-          const uint16_t r0 = rowid[piv]; rowid[piv] = rowid[at]; rowid[at] = r0;
+        misc[1] = 0;
+        misc[2] = mode;
+      }
+    }
+    __syncthreads();
+    if (misc[2] == 2) return;  // no pivot: A_L is singular
+    if (misc[2] == 1) {
+      // CTA-wide search: forward elimination of the panel word over all rows
+      {
+        int cand = INT_MAX;
+        for (int pos = base + tid; pos < MT; pos += kElimThreads) {
+          const uint32_t v = colw[pos];
+          wk[pos] = v;
+          if (v & 1) cand = min(cand, pos);
         }
+        cand = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+        if (lane == 0 && cand != INT_MAX) atomicMin(&misc[0], cand);
       }
       __syncthreads();
-      if (misc[1]) return;  // no pivot: A_L is singular
-      const uint32_t pwd = wk[base + j], bit = 1u << j;
-      int cand = INT_MAX;
-      for (int pos = base + j + 1 + tid; pos < MT; pos += kElimThreads) {
-        uint32_t x = wk[pos];
-        if (x & bit) {
-          x ^= pwd;
-          wk[pos] = x;
+      for (int j = 0; j < np; j++) {
+        if (tid == 0) {
+          const int piv = misc[0];
+          misc[0] = INT_MAX;
+          if (piv == INT_MAX) {
+            misc[1] = 1;
+          } else if (piv != base + j) {
+            const int at = base + j;
+            uint32_t x0 = wk[piv]; wk[piv] = wk[at]; wk[at] = x0;
+            x0 = colw[piv]; colw[piv] = colw[at]; colw[at] = x0;
+            const uint16_t r0 = rowid[piv]; rowid[piv] = rowid[at]; rowid[at] = r0;
+          }
         }
-        if (j + 1 < np && ((x >> (j + 1)) & 1)) cand = min(cand, pos);
+        __syncthreads();
+        if (misc[1]) return;  // no pivot: A_L is singular
+        const uint32_t pwd = wk[base + j], bit = 1u << j;
+        int cand = INT_MAX;
+        for (int pos = base + j + 1 + tid; pos < MT; pos += kElimThreads) {
+          uint32_t x = wk[pos];
+          if (x & bit) {
+            x ^= pwd;
+            wk[pos] = x;
+          }
+          if (j + 1 < np && ((x >> (j + 1)) & 1)) cand = min(cand, pos);
+        }
+        cand = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
+        if (lane == 0 && cand != INT_MAX) atomicMin(&misc[0], cand);
+        __syncthreads();
       }
-      cand = (int)__reduce_min_sync(0xffffffffu, (unsigned)cand);
-      if (lane == 0 && cand != INT_MAX) atomicMin(&misc[0], cand);
-      __syncthreads();
     }
     // B^-1 for the pivot rows' original panel words (warp 0, lane = row)
     if (warp == 0) {
@@ -479,8 +537,10 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
       }
       binv[lane] = e;
     }
-    __syncthreads();
-    for (int g = p >> 5; g < ngroups; g++) {
+    // every CTA of the cluster has read the panel words before any updates them
+    if (cl > 1) kg_cluster_sync();
+    else __syncthreads();
+    for (int g = (p >> 5) + ((crank - (p >> 5)) % cl + cl) % cl; g < ngroups; g += cl) {
       const int w0 = 32 * g;
       {
         const int b = tid >> 5;
@@ -521,11 +581,11 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
         for (int vl = 0; vl < 32; vl++) tp[vl * 32] = r[vl];
       }
       __syncthreads();
-      for (int pos0 = warp; pos0 < MT; pos0 += 4 * 32) {
-        uint32_t x[4], c[4];
-        uint32_t *ad[4];
+      for (int pos0 = (forward ? base + np : 0) + warp; pos0 < MT; pos0 += kElimRows * 32) {
+        uint32_t x[kElimRows], c[kElimRows];
+        uint32_t *ad[kElimRows];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < kElimRows; u++) {
           const int pos = pos0 + 32 * u;
           const bool live = pos < MT && (unsigned)(pos - base) >= (unsigned)np;
           c[u] = live ? (colw[pos] & npmask) : 0;
@@ -533,7 +593,7 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
           x[u] = c[u] ? *ad[u] : 0;
         }
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
+        for (int u = 0; u < kElimRows; u++) {
           if (!c[u]) continue;
           const uint32_t cc = c[u];
           x[u] ^= tab[((cc & 255) << 5) + lane] ^ tab[((256 + ((cc >> 8) & 255)) << 5) + lane] ^
@@ -543,7 +603,9 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
       }
       __syncthreads();
     }
+    if (cl > 1) kg_cluster_sync();  // the next panel word is final in every row
   }
+  if (crank) return;
   if (rowid_out)
     for (int i = tid; i < MT; i += kElimThreads) rowid_out[(long long)slot * MT + i] = rowid[i];
   if (tid == 0) status[att] |= (uint8_t)set_bit;
@@ -553,45 +615,32 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
 // CTA per winner. The library's recursion (controlbits.c:29-150, restated in
 // host_keygen.cpp) processes a permutation of 2^w entries and recurses into
 // two halves with doubled bit stride; here every depth d runs all 2^d
-// sub-permutations at once, each a segment of 2^(w-d) entries, with each of
-// the recursion's sorts a segmented bitonic sort. Segment s at depth d writes
-// layer d and layer 2w-2-d at bits offset_s + 2^d j, offset_s = bitrev_d(s).
-// The bits are checked by applying the 2w-1 layers to the identity.
+// sub-permutations at once, each a segment of 2^(w-d) entries. Segment s at
+// depth d writes layer d and layer 2w-2-d at bits offset_s + 2^d j,
+// offset_s = bitrev_d(s).
+// Every sort of the recursion orders packed words whose key field (bits 16+,
+// or 20+ in one step) is a permutation of the segment's local indices: the
+// sort's output at index i is the word whose key is i, so each sort is the
+// scatter out[key] = word (one pass, no comparisons). The bits are checked by
+// applying the 2w-1 layers to the identity.
 constexpr int kCbitsThreads = 1024;
 template <int SET> struct CbitsSmem {
   using C = KG<SET>;
-  static constexpr int a = 0, b = a + C::q, cb = b + C::q, pi_u32 = cb + C::cond_bytes / 4;
+  static constexpr int a = 0, b = a + C::q, t = b + C::q, cb = t + C::q, pi_u32 = cb + C::cond_bytes / 4;
   static constexpr int bytes = pi_u32 * 4 + C::q * 2 + 16;
 };
 
-template <int Q>
-__device__ __forceinline__ void seg_sort(uint32_t *arr, int nn) {
-  __syncthreads();
-  for (int size = 2; size <= nn; size <<= 1)
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int p = threadIdx.x; p < Q / 2; p += kCbitsThreads) {
-        const int i = 2 * p - (p & (stride - 1)), j = i + stride;
-        const bool up = size == nn || (i & size) == 0;
-        const uint32_t a = arr[i], b = arr[j];
-        if ((a > b) == up) {
-          arr[i] = b;
-          arr[j] = a;
-        }
-      }
-      __syncthreads();
-    }
-}
-
 template <int SET>
 __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t *__restrict__ piall,
-                                                                 const int *__restrict__ att_of, int nwin,
+                                                                 const int *__restrict__ att_of,
+                                                                 const int *__restrict__ out_of, int nwin,
                                                                  uint8_t *__restrict__ cond_out,
                                                                  uint8_t *__restrict__ cb_ok) {
   using C = KG<SET>;
   using L = CbitsSmem<SET>;
   constexpr int q = C::q, W = C::m, H = q / 2;
   extern __shared__ __align__(16) uint32_t kgsm_cb[];
-  uint32_t *A = kgsm_cb + L::a, *B = kgsm_cb + L::b, *CB = kgsm_cb + L::cb;
+  uint32_t *A = kgsm_cb + L::a, *B = kgsm_cb + L::b, *T = kgsm_cb + L::t, *CB = kgsm_cb + L::cb;
   uint16_t *PI = reinterpret_cast<uint16_t *>(kgsm_cb + L::pi_u32);
   const int w = blockIdx.x;
   if (w >= nwin) return;
@@ -604,28 +653,40 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
   for (int d = 0; d < W; d++) {
     const int ww = W - d, nn = 1 << ww;
     auto offs = [&](int s) { return d == 0 ? 0 : (int)(__brev((uint32_t)s) >> (32 - d)); };
+    // sort of arr by its key field (a permutation of each segment's indices)
+    auto scatter = [&](uint32_t *&arr, int shift) {
+      __syncthreads();
+      for (int X = tid; X < q; X += kCbitsThreads) {
+        const uint32_t v = arr[X];
+        T[(X & ~(nn - 1)) + ((v >> shift) & (nn - 1))] = v;
+      }
+      __syncthreads();
+      uint32_t *t = arr;
+      arr = T;
+      T = t;
+    };
     if (ww == 1) {
       for (int s = tid; s < H; s += kCbitsThreads)
         if (PI[2 * s] & 1) setbit((W - 1) * H + offs(s));
       break;
     }
     for (int X = tid; X < q; X += kCbitsThreads) A[X] = ((uint32_t)(PI[X] ^ 1) << 16) | (uint32_t)PI[X ^ 1];
-    seg_sort<q>(A, nn);
+    scatter(A, 16);
     for (int X = tid; X < q; X += kCbitsThreads) {
       const uint32_t x = (uint32_t)(X & (nn - 1)), a = A[X], px = a & 0xffff;
       B[X] = (px << 16) | min(px, x);
       A[X] = (a << 16) | x;
     }
-    seg_sort<q>(A, nn);
+    scatter(A, 16);
     for (int X = tid; X < q; X += kCbitsThreads) A[X] = (A[X] << 16) + (B[X] >> 16);
-    seg_sort<q>(A, nn);
+    scatter(A, 16);
     if (ww <= 10) {
       for (int X = tid; X < q; X += kCbitsThreads) B[X] = ((A[X] & 0xffff) << 10) | (B[X] & 0x3ff);
       for (int i = 1; i < ww - 1; i++) {
         for (int X = tid; X < q; X += kCbitsThreads) A[X] = ((B[X] & ~0x3ffu) << 6) | (uint32_t)(X & (nn - 1));
-        seg_sort<q>(A, nn);
+        scatter(A, 16);
         for (int X = tid; X < q; X += kCbitsThreads) A[X] = (A[X] << 20) | B[X];
-        seg_sort<q>(A, nn);
+        scatter(A, 20);
         for (int X = tid; X < q; X += kCbitsThreads) {
           const uint32_t ppcp = A[X] & 0xfffff, ppc = (A[X] & 0xffc00) | (B[X] & 0x3ff);
           B[X] = min(ppc, ppcp);
@@ -636,14 +697,14 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
       for (int X = tid; X < q; X += kCbitsThreads) B[X] = (A[X] << 16) | (B[X] & 0xffff);
       for (int i = 1; i < ww - 1; i++) {
         for (int X = tid; X < q; X += kCbitsThreads) A[X] = (B[X] & ~0xffffu) | (uint32_t)(X & (nn - 1));
-        seg_sort<q>(A, nn);
+        scatter(A, 16);
         for (int X = tid; X < q; X += kCbitsThreads) A[X] = (A[X] << 16) | (B[X] & 0xffff);
         if (i < ww - 2) {
           for (int X = tid; X < q; X += kCbitsThreads) B[X] = (A[X] & ~0xffffu) | (B[X] >> 16);
-          seg_sort<q>(B, nn);
+          scatter(B, 16);
           for (int X = tid; X < q; X += kCbitsThreads) B[X] = (B[X] << 16) | (A[X] & 0xffff);
         }
-        seg_sort<q>(A, nn);
+        scatter(A, 16);
         for (int X = tid; X < q; X += kCbitsThreads) {
           const uint32_t cp = (B[X] & ~0xffffu) | (A[X] & 0xffff);
           B[X] = min(B[X], cp);
@@ -652,7 +713,7 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
       for (int X = tid; X < q; X += kCbitsThreads) B[X] &= 0xffff;
     }
     for (int X = tid; X < q; X += kCbitsThreads) A[X] = ((uint32_t)PI[X] << 16) + (uint32_t)(X & (nn - 1));
-    seg_sort<q>(A, nn);
+    scatter(A, 16);
     for (int pr = tid; pr < H; pr += kCbitsThreads) {
       const int X = 2 * pr, z = X & (nn - 1), s = X >> ww;
       const uint32_t fj = B[X] & 1, Fz = (uint32_t)z + fj, Fz1 = Fz ^ 1;
@@ -660,7 +721,7 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
       B[X] = (A[X] << 16) | Fz;
       B[X + 1] = (A[X + 1] << 16) | Fz1;
     }
-    seg_sort<q>(B, nn);
+    scatter(B, 16);
     for (int pr = tid; pr < H; pr += kCbitsThreads) {
       const int X = 2 * pr, y = X & (nn - 1), s = X >> ww;
       const uint32_t lk = B[X] & 1, Ly = (uint32_t)y + lk, Ly1 = Ly ^ 1;
@@ -668,7 +729,7 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
       A[X] = (Ly << 16) | (B[X] & 0xffff);
       A[X + 1] = (Ly1 << 16) | (B[X + 1] & 0xffff);
     }
-    seg_sort<q>(A, nn);
+    scatter(A, 16);
     for (int pr = tid; pr < H; pr += kCbitsThreads) {
       const int X = 2 * pr, base = X & ~(nn - 1), j = (X & (nn - 1)) >> 1;
       PI[base + j] = (uint16_t)((A[X] & 0xffff) >> 1);
@@ -698,14 +759,15 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
   bad = __syncthreads_or(bad);
   uint32_t *co = reinterpret_cast<uint32_t *>(cond_out + (long long)w * C::cond_bytes);
   for (int i = tid; i < C::cond_bytes / 4; i += kCbitsThreads) co[i] = CB[i];
-  if (tid == 0) cb_ok[w] = bad ? 0 : 1;
+  if (tid == 0) cb_ok[out_of[w]] = bad ? 0 : 1;
 }
 
 // ---------------------------------------------------------------- assembly
 // pk row i = bits [mt, n) of the reduced row at position i; sk = seed |
 // ff ff ff ff 00 00 00 00 | g_0..g_{t-1} (LE u16) | control bits | r[0:n/8].
 template <int SET>
-__global__ void kg_assemble_kernel(const int *__restrict__ att_of, int nwin, const uint8_t *__restrict__ rbuf,
+__global__ void kg_assemble_kernel(const int *__restrict__ att_of, const int *__restrict__ out_of, int nwin,
+                                   const uint8_t *__restrict__ rbuf,
                                    const uint8_t *__restrict__ delta, const uint16_t *__restrict__ gall,
                                    const uint8_t *__restrict__ cond, const uint32_t *__restrict__ matF,
                                    const uint16_t *__restrict__ rowid, uint8_t *__restrict__ pk_out,
@@ -723,7 +785,7 @@ __global__ void kg_assemble_kernel(const int *__restrict__ att_of, int nwin, con
       const int bp = C::mt + 8 * byte, wd = bp >> 5, sh = bp & 31;
       uint32_t v = src[wd] >> sh;
       if (sh > 24) v |= src[wd + 1] << (32 - sh);
-      pk_out[(long long)w * pkb + i] = (uint8_t)v;
+      pk_out[(long long)out_of[w] * pkb + i] = (uint8_t)v;
     } else {
       const int o = (int)(i - pkb);
       uint8_t v;
@@ -735,7 +797,7 @@ __global__ void kg_assemble_kernel(const int *__restrict__ att_of, int nwin, con
         v = (uint8_t)(((o - 40) & 1) ? gv >> 8 : gv);
       } else if (o < 40 + 2 * C::t + C::cond_bytes) v = cond[(long long)w * C::cond_bytes + (o - 40 - 2 * C::t)];
       else v = rbuf[(long long)att * C::rstride + (o - 40 - 2 * C::t - C::cond_bytes)];
-      sk_out[(long long)w * skb + o] = v;
+      sk_out[(long long)out_of[w] * skb + o] = v;
     }
   }
 }
@@ -779,129 +841,173 @@ cudaError_t dalloc(T **p, size_t count, cudaStream_t st) {
 }
 
 constexpr long long kMaxAttemptsPerKey = 100000;
+constexpr int kMaxSpeculation = 8;        // chained attempts per key and round
+constexpr long long kChunkBytes = 2ll << 30;  // device-side pk + sk staging per chunk of keys
+
+// Round state, double-buffered: the winners of round r (second stream) read
+// round r's attempt buffers while round r+1 (first stream) fills the others.
+struct KgRound {
+  uint8_t *seed_in = nullptr, *seed_out = nullptr, *r = nullptr, *delta = nullptr, *status = nullptr;
+  uint16_t *g = nullptr, *pi = nullptr;
+  uint32_t *matL = nullptr;
+  int *win = nullptr;                                   // [2][wcap]: attempt, output slot
+  uint8_t *h_seed = nullptr, *h_status = nullptr;      // pinned
+  int *h_win = nullptr;
+  cudaEvent_t ranked = nullptr, done = nullptr;
+};
 
 template <int SET>
-int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, cudaStream_t st) {
+int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, cudaStream_t s1, cudaStream_t s2) {
   using C = KG<SET>;
   int rc = GMC_OK;
   FieldDev fd{};
-  int dev = 0, sms = 0;
-  uint8_t *d_seed_in = nullptr, *d_seed_out = nullptr, *d_r = nullptr, *d_delta = nullptr, *d_status = nullptr,
-          *d_cond = nullptr, *d_cbok = nullptr, *d_pk = nullptr, *d_sk = nullptr;
-  uint16_t *d_g = nullptr, *d_pi = nullptr, *d_rowid = nullptr;
-  uint32_t *d_matL = nullptr, *d_matF = nullptr;
-  int *d_win = nullptr;
-  std::vector<long long> pending, next;
-  std::vector<uint8_t> cur, h_status, h_seed, h_cbok;
-  std::vector<long long> tries;
-  std::vector<int> win_att;
-  std::vector<long long> win_key;
-  int cap = 0, wcap = 0;
+  int dev = 0, sms = 0, cap = 0, wcap = 0;
+  long long kc = 0;
+  KgRound R[2];
+  uint32_t *d_matF = nullptr;
+  uint16_t *d_rowid = nullptr;
+  uint8_t *d_cond = nullptr, *d_cbok = nullptr, *d_pk = nullptr, *d_sk = nullptr;
+  std::vector<long long> pending, next, tries;
+  std::vector<uint8_t> cur, h_cbok;
   if (field_tables(SET, &fd) != GMC_OK) return GMC_ECUDA;
   KG_CUDA(cudaGetDevice(&dev));
   KG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   KG_CUDA(kg_attrs<SET>());
-  cap = 2 * sms;                                      // attempts per round
-  wcap = (int)std::min<long long>(nkeys, cap);        // winners per round
-  KG_CUDA(dalloc(&d_seed_in, (size_t)cap * 32, st));
-  KG_CUDA(dalloc(&d_seed_out, (size_t)cap * 32, st));
-  KG_CUDA(dalloc(&d_r, (size_t)cap * C::rstride, st));
-  KG_CUDA(dalloc(&d_delta, (size_t)cap * 32, st));
-  KG_CUDA(dalloc(&d_status, (size_t)cap, st));
-  KG_CUDA(dalloc(&d_g, (size_t)cap * C::gstride, st));
-  KG_CUDA(dalloc(&d_pi, (size_t)cap * C::q, st));
-  KG_CUDA(dalloc(&d_matL, (size_t)cap * C::mt * C::rwl, st));
-  KG_CUDA(dalloc(&d_win, (size_t)wcap, st));
-  KG_CUDA(dalloc(&d_matF, (size_t)wcap * C::mt * C::rw, st));
-  KG_CUDA(dalloc(&d_rowid, (size_t)wcap * C::mt, st));
-  KG_CUDA(dalloc(&d_cond, (size_t)wcap * C::cond_bytes, st));
-  KG_CUDA(dalloc(&d_cbok, (size_t)wcap, st));
-  KG_CUDA(dalloc(&d_pk, (size_t)wcap * C::pk_bytes, st));
-  KG_CUDA(dalloc(&d_sk, (size_t)wcap * C::sk_bytes, st));
-  cur.assign(seeds, seeds + 32 * nkeys);
-  tries.assign(nkeys, 0);
-  for (long long i = 0; i < nkeys; i++) pending.push_back(i);
-  while (!pending.empty()) {
-    const int nr = (int)std::min<long long>((long long)pending.size(), cap);
-    const int k = std::max(1, std::min(64, cap / nr));
-    const int natt = nr * k;
-    h_seed.resize((size_t)nr * 32);
-    for (int j = 0; j < nr; j++) memcpy(&h_seed[32 * j], &cur[32 * pending[j]], 32);
-    KG_CUDA(cudaMemcpyAsync(d_seed_in, h_seed.data(), (size_t)nr * 32, cudaMemcpyHostToDevice, st));
-    kg_expand_kernel<SET><<<(nr + 31) / 32, 32, 0, st>>>(d_seed_in, d_seed_out, nr, k, d_r, d_delta, d_status);
-    kg_minpoly_kernel<SET><<<natt, kMinpolyThreads, MinpolySmem<SET>::bytes, st>>>(d_r, natt, fd.gexp, fd.glog, d_g,
-                                                                                 d_status);
-    kg_support_kernel<SET><<<natt, kSupportThreads, C::q * 8, st>>>(d_r, natt, d_pi, d_status);
-    kg_build_kernel<SET><<<dim3(C::rwl / 8, natt), kBuildThreads, BuildSmem<SET>::bytes, st>>>(
-        d_g, d_pi, nullptr, d_status, d_matL, C::rwl, C::rwl, fd.gexp, fd.glog);
-    kg_elim_kernel<SET><<<natt, kElimThreads, ElimSmem<SET>::bytes, st>>>(
-        d_matL, C::rwl, C::rwl, nullptr, d_status, kKgMinpoly | kKgDistinct, kKgRank, nullptr);
-    KG_CUDA(cudaGetLastError());
-    h_status.resize(natt);
-    h_seed.resize((size_t)nr * 32);
-    KG_CUDA(cudaMemcpyAsync(h_status.data(), d_status, natt, cudaMemcpyDeviceToHost, st));
-    KG_CUDA(cudaMemcpyAsync(h_seed.data(), d_seed_out, (size_t)nr * 32, cudaMemcpyDeviceToHost, st));
-    KG_CUDA(cudaStreamSynchronize(st));
-    win_att.clear();
-    win_key.clear();
-    next.clear();
-    for (int j = 0; j < nr; j++) {
-      const long long key = pending[j];
-      int a = 0;
-      while (a < k && h_status[(size_t)j * k + a] != kKgAll) a++;
-      if (a < k) {
-        win_att.push_back(j * k + a);
-        win_key.push_back(key);
-      } else {
-        tries[key] += k;
-        if (tries[key] >= kMaxAttemptsPerKey) {
-          rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: no systematic key within the attempt limit");
-          goto done;
-        }
-        memcpy(&cur[32 * key], &h_seed[32 * j], 32);
-        next.push_back(key);
-      }
-    }
-    for (size_t j = nr; j < pending.size(); j++) next.push_back(pending[j]);
-    if (!win_att.empty()) {
-      const int nw = (int)win_att.size();
-      KG_CUDA(cudaMemcpyAsync(d_win, win_att.data(), nw * sizeof(int), cudaMemcpyHostToDevice, st));
-      kg_build_kernel<SET><<<dim3(C::rw / 8, nw), kBuildThreads, BuildSmem<SET>::bytes, st>>>(
-          d_g, d_pi, d_win, d_status, d_matF, C::rw, C::rw, fd.gexp, fd.glog);
-      // the winners' status already has every bit: the full elimination re-derives the same pivots
-      kg_elim_kernel<SET><<<nw, kElimThreads, ElimSmem<SET>::bytes, st>>>(d_matF, C::rw, C::rw, d_win, d_status,
-                                                                        kKgAll, kKgAll, d_rowid);
-      kg_cbits_kernel<SET><<<nw, kCbitsThreads, CbitsSmem<SET>::bytes, st>>>(d_pi, d_win, nw, d_cond, d_cbok);
-      kg_assemble_kernel<SET><<<dim3(256, nw), 256, 0, st>>>(d_win, nw, d_r, d_delta, d_g, d_cond, d_matF, d_rowid,
-                                                              d_pk, d_sk);
+  cap = 4 * sms;
+  kc = std::max<long long>(1, std::min<long long>(nkeys, kChunkBytes / (C::pk_bytes + C::sk_bytes)));
+  wcap = (int)std::min<long long>(kc, cap);
+  for (KgRound &b : R) {
+    KG_CUDA(dalloc(&b.seed_in, (size_t)cap * 32, s1));
+    KG_CUDA(dalloc(&b.seed_out, (size_t)cap * 32, s1));
+    KG_CUDA(dalloc(&b.r, (size_t)cap * C::rstride, s1));
+    KG_CUDA(dalloc(&b.delta, (size_t)cap * 32, s1));
+    KG_CUDA(dalloc(&b.status, (size_t)cap, s1));
+    KG_CUDA(dalloc(&b.g, (size_t)cap * C::gstride, s1));
+    KG_CUDA(dalloc(&b.pi, (size_t)cap * C::q, s1));
+    KG_CUDA(dalloc(&b.matL, (size_t)cap * C::mt * C::rwl, s1));
+    KG_CUDA(dalloc(&b.win, (size_t)2 * wcap, s1));
+    KG_CUDA(cudaMallocHost(&b.h_seed, (size_t)cap * 32 * 2));
+    KG_CUDA(cudaMallocHost(&b.h_status, (size_t)cap));
+    KG_CUDA(cudaMallocHost(&b.h_win, (size_t)2 * wcap * sizeof(int)));
+    KG_CUDA(cudaEventCreateWithFlags(&b.ranked, cudaEventDisableTiming));
+    KG_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
+  }
+  KG_CUDA(dalloc(&d_matF, (size_t)wcap * C::mt * C::rw, s1));
+  KG_CUDA(dalloc(&d_rowid, (size_t)wcap * C::mt, s1));
+  KG_CUDA(dalloc(&d_cond, (size_t)wcap * C::cond_bytes, s1));
+  KG_CUDA(dalloc(&d_cbok, (size_t)kc, s1));
+  KG_CUDA(dalloc(&d_pk, (size_t)kc * C::pk_bytes, s1));
+  KG_CUDA(dalloc(&d_sk, (size_t)kc * C::sk_bytes, s1));
+  KG_CUDA(cudaStreamSynchronize(s1));
+  for (long long k0 = 0; k0 < nkeys; k0 += kc) {
+    const long long nk = std::min(kc, nkeys - k0);
+    cur.assign(seeds + 32 * k0, seeds + 32 * (k0 + nk));
+    tries.assign(nk, 0);
+    pending.clear();
+    for (long long i = 0; i < nk; i++) pending.push_back(i);
+    KG_CUDA(cudaMemsetAsync(d_cbok, 0, (size_t)nk, s2));
+    for (int round = 0; !pending.empty(); round++) {
+      KgRound &b = R[round & 1];
+      if (round >= 2) KG_CUDA(cudaEventSynchronize(b.done));  // round-2's winners released these buffers
+      const int nr = (int)std::min<long long>((long long)pending.size(), cap);
+      const int k = std::max(1, std::min(kMaxSpeculation, cap / nr));
+      const int natt = nr * k;
+      for (int j = 0; j < nr; j++) memcpy(b.h_seed + 32 * j, &cur[32 * pending[j]], 32);
+      KG_CUDA(cudaMemcpyAsync(b.seed_in, b.h_seed, (size_t)nr * 32, cudaMemcpyHostToDevice, s1));
+      kg_expand_kernel<SET><<<(nr + 31) / 32, 32, 0, s1>>>(b.seed_in, b.seed_out, nr, k, b.r, b.delta, b.status);
+      kg_minpoly_kernel<SET><<<natt, kMinpolyThreads, MinpolySmem<SET>::bytes, s1>>>(b.r, natt, fd.gexp, fd.glog,
+                                                                                   b.g, b.status);
+      kg_support_kernel<SET><<<natt, kSupportThreads, C::q * 8, s1>>>(b.r, natt, b.pi, b.status);
+      kg_build_kernel<SET><<<dim3(C::rwl / 8, natt), kBuildThreads, BuildSmem<SET>::bytes, s1>>>(
+          b.g, b.pi, nullptr, b.status, b.matL, C::rwl, C::rwl, fd.gexp, fd.glog);
+      kg_elim_kernel<SET><<<natt, kElimThreads, ElimSmem<SET>::bytes, s1>>>(
+          b.matL, C::rwl, C::rwl, nullptr, b.status, kKgMinpoly | kKgDistinct, kKgRank, 1, 1, nullptr);
       KG_CUDA(cudaGetLastError());
-      for (int w = 0; w < nw; w++) {
-        KG_CUDA(cudaMemcpyAsync(pk + win_key[w] * C::pk_bytes, d_pk + (long long)w * C::pk_bytes, C::pk_bytes,
-                                cudaMemcpyDeviceToHost, st));
-        KG_CUDA(cudaMemcpyAsync(sk + win_key[w] * C::sk_bytes, d_sk + (long long)w * C::sk_bytes, C::sk_bytes,
-                                cudaMemcpyDeviceToHost, st));
-      }
-      h_cbok.resize(nw);
-      KG_CUDA(cudaMemcpyAsync(h_cbok.data(), d_cbok, nw, cudaMemcpyDeviceToHost, st));
-      KG_CUDA(cudaStreamSynchronize(st));
-      for (int w = 0; w < nw; w++)
-        if (!h_cbok[w]) {
-          rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: control bits do not encode the support permutation");
-          goto done;
+      KG_CUDA(cudaMemcpyAsync(b.h_status, b.status, natt, cudaMemcpyDeviceToHost, s1));
+      KG_CUDA(cudaMemcpyAsync(b.h_seed + (size_t)cap * 32, b.seed_out, (size_t)nr * 32, cudaMemcpyDeviceToHost, s1));
+      KG_CUDA(cudaEventRecord(b.ranked, s1));
+      KG_CUDA(cudaStreamSynchronize(s1));
+      int nw = 0;
+      next.clear();
+      for (int j = 0; j < nr; j++) {
+        const long long key = pending[j];
+        int a = 0;
+        while (a < k && b.h_status[(size_t)j * k + a] != kKgAll) a++;
+        if (a < k) {
+          b.h_win[nw] = j * k + a;
+          b.h_win[wcap + nw] = (int)key;
+          nw++;
+        } else {
+          tries[key] += k;
+          if (tries[key] >= kMaxAttemptsPerKey) {
+            rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: no systematic key within the attempt limit");
+            goto done;
+          }
+          memcpy(&cur[32 * key], b.h_seed + (size_t)cap * 32 + 32 * j, 32);
+          next.push_back(key);
         }
+      }
+      for (size_t j = nr; j < pending.size(); j++) next.push_back(pending[j]);
+      if (nw) {
+        int *watt = b.win, *wout = b.win + wcap;
+        KG_CUDA(cudaStreamWaitEvent(s2, b.ranked, 0));
+        KG_CUDA(cudaMemcpyAsync(b.win, b.h_win, (size_t)2 * wcap * sizeof(int), cudaMemcpyHostToDevice, s2));
+        kg_build_kernel<SET><<<dim3(C::rw / 8, nw), kBuildThreads, BuildSmem<SET>::bytes, s2>>>(
+            b.g, b.pi, watt, b.status, d_matF, C::rw, C::rw, fd.gexp, fd.glog);
+        // the winners' status has every bit: the full elimination re-derives the same pivots
+        {
+          cudaLaunchConfig_t lc = {};
+          cudaLaunchAttribute at[1];
+          at[0].id = cudaLaunchAttributeClusterDimension;
+          at[0].val.clusterDim.x = kElimCluster;
+          at[0].val.clusterDim.y = 1;
+          at[0].val.clusterDim.z = 1;
+          lc.gridDim = dim3(nw * kElimCluster);
+          lc.blockDim = dim3(kElimThreads);
+          lc.dynamicSmemBytes = ElimSmem<SET>::bytes;
+          lc.stream = s2;
+          lc.attrs = at;
+          lc.numAttrs = 1;
+          KG_CUDA(cudaLaunchKernelEx(&lc, kg_elim_kernel<SET>, d_matF, (int)C::rw, (int)C::rw, (const int *)watt,
+                                     b.status, (int)kKgAll, (int)kKgAll, 0, kElimCluster, d_rowid));
+        }
+        kg_cbits_kernel<SET><<<nw, kCbitsThreads, CbitsSmem<SET>::bytes, s2>>>(b.pi, watt, wout, nw, d_cond, d_cbok);
+        kg_assemble_kernel<SET><<<dim3(256, nw), 256, 0, s2>>>(watt, wout, nw, b.r, b.delta, b.g, d_cond, d_matF,
+                                                                d_rowid, d_pk, d_sk);
+        KG_CUDA(cudaGetLastError());
+      }
+      KG_CUDA(cudaEventRecord(b.done, s2));
+      pending.swap(next);
     }
-    pending.swap(next);
+    KG_CUDA(cudaStreamSynchronize(s2));
+    h_cbok.resize(nk);
+    KG_CUDA(cudaMemcpy(h_cbok.data(), d_cbok, (size_t)nk, cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < nk; i++)
+      if (!h_cbok[i]) {
+        rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: control bits do not encode the support permutation");
+        goto done;
+      }
+    KG_CUDA(cudaMemcpy(pk + k0 * C::pk_bytes, d_pk, (size_t)nk * C::pk_bytes, cudaMemcpyDeviceToHost));
+    KG_CUDA(cudaMemcpy(sk + k0 * C::sk_bytes, d_sk, (size_t)nk * C::sk_bytes, cudaMemcpyDeviceToHost));
   }
 done:
-  for (void *p : {(void *)d_seed_in, (void *)d_seed_out, (void *)d_r, (void *)d_delta, (void *)d_status, (void *)d_g,
-                  (void *)d_pi, (void *)d_matL, (void *)d_win, (void *)d_matF, (void *)d_rowid, (void *)d_cond,
-                  (void *)d_cbok, (void *)d_pk, (void *)d_sk})
-    if (p) cudaFreeAsync(p, st);
-  if (rc == GMC_OK) {
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
-  } else {
-    cudaStreamSynchronize(st);
+  cudaStreamSynchronize(s1);
+  cudaStreamSynchronize(s2);
+  for (KgRound &b : R) {
+    for (void *p : {(void *)b.seed_in, (void *)b.seed_out, (void *)b.r, (void *)b.delta, (void *)b.status,
+                    (void *)b.g, (void *)b.pi, (void *)b.matL, (void *)b.win})
+      if (p) cudaFreeAsync(p, s1);
+    if (b.h_seed) cudaFreeHost(b.h_seed);
+    if (b.h_status) cudaFreeHost(b.h_status);
+    if (b.h_win) cudaFreeHost(b.h_win);
+    if (b.ranked) cudaEventDestroy(b.ranked);
+    if (b.done) cudaEventDestroy(b.done);
+  }
+  for (void *p : {(void *)d_matF, (void *)d_rowid, (void *)d_cond, (void *)d_cbok, (void *)d_pk, (void *)d_sk})
+    if (p) cudaFreeAsync(p, s1);
+  {
+    cudaError_t e = cudaStreamSynchronize(s1);
+    if (rc == GMC_OK && e != cudaSuccess) rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
   }
   return rc;
 }
@@ -919,17 +1025,22 @@ extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, 
   if (set < 0 || set >= GMC_NSETS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
     return kg_fail(GMC_EINVAL, "gmc_keypair_batch: bad argument");
   if (nkeys == 0) return GMC_OK;
-  cudaStream_t st = nullptr;
-  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-  if (e != cudaSuccess) return kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
+  cudaStream_t s1 = nullptr, s2 = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
   int rc = GMC_EINVAL;
-  switch (set) {
-    case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, st); break;
-    case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, st); break;
-    case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, st); break;
-    case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, st); break;
-    case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, st); break;
+  if (e != cudaSuccess) {
+    rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
+  } else {
+    switch (set) {
+      case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, s1, s2); break;
+      case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, s1, s2); break;
+      case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, s1, s2); break;
+      case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, s1, s2); break;
+      case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, s1, s2); break;
+    }
   }
-  cudaStreamDestroy(st);
+  if (s1) cudaStreamDestroy(s1);
+  if (s2) cudaStreamDestroy(s2);
   return rc;
 }

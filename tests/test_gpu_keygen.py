@@ -67,7 +67,7 @@ def test_keygen_many_rounds(gmc):
     """More keys than one round's attempts for the small set: several rounds, with
     1 and more speculative attempts per key."""
     sid = 0
-    cap = 2 * torch.cuda.get_device_properties(0).multi_processor_count
+    cap = 4 * torch.cuda.get_device_properties(0).multi_processor_count  # attempts per round
     seeds = seeds_for(sid, cap + 37, tag=b"kg-many")
     pk, sk = gmc.keypair_batch(sid, seeds)
     check(sid, seeds, pk, sk, oracle_keys(sid, seeds))
