@@ -61,6 +61,11 @@ def parse():
     ap.add_argument("--no-engines", action="store_true", help="skip the syndrome-engine comparison")
     ap.add_argument("--no-keygen", action="store_true", help="skip the batched key-generation measurement")
     ap.add_argument("--keygen-keys", type=int, default=608, help="keys per batched key-generation call")
+    ap.add_argument("--keygen-only", action="store_true",
+                    help="measure only batched key generation (--keygen-sets, default all five) and print its JSON")
+    ap.add_argument("--keygen-sets", default=None, help="comma-separated sets for the key-generation section")
+    ap.add_argument("--keygen-calls", type=int, default=2, help="timed key-generation calls per set (best is kept)")
+    ap.add_argument("--no-keygen-warmup", action="store_true", help="no 8-key warm-up call before the timed ones")
     return ap.parse_args()
 
 
@@ -426,7 +431,7 @@ def keccak_rates(z, n, kernels):
     return out
 
 
-def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True):
+def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True, sets=None, calls=2, warmup=True):
     """Batched key generation (gmc_keypair_batch, host buffers in and out) per parameter set: keys/s
     over nkeys seeds, beside the oracle's keypair on the host threads (a bounded sample whose
     keys are also compared byte for byte with the GPU's)."""
@@ -436,14 +441,15 @@ def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True):
         from concurrent.futures import ThreadPoolExecutor
         from oracle import pyoracle as O
         O.lib()
-    for name in gmc.SETS:
+    for name in (sets or gmc.SETS):
         sid = gmc.set_id(name)
         seeds = np.frombuffer(b"".join(hashlib.sha256(b"bench-kg" + bytes([sid]) + i.to_bytes(4, "little")).digest()
                                        for i in range(nkeys)), np.uint8).reshape(nkeys, 32)
-        gmc.keypair_batch(sid, seeds[:8])  # warm-up (tables, pool)
+        if warmup:
+            gmc.keypair_batch(sid, seeds[:8])  # warm-up (tables, pool)
         torch.cuda.synchronize()
         ts = []
-        for _ in range(2):
+        for _ in range(max(1, calls)):
             t0 = time.perf_counter()
             pk, sk = gmc.keypair_batch(sid, seeds)
             ts.append(time.perf_counter() - t0)
@@ -519,6 +525,13 @@ def main():
     import ctypes
 
     torch.cuda.set_device(local_rank)
+    if args.keygen_only:
+        if rank == 0:
+            sets = args.keygen_sets.split(",") if args.keygen_sets else None
+            print(json.dumps({"keygen": keygen_rates(gmc, torch, args.keygen_keys, os.cpu_count() or 1,
+                                                     with_cpu=not args.no_cpu, sets=sets, calls=args.keygen_calls,
+                                                     warmup=not args.no_keygen_warmup)}))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -651,7 +664,8 @@ def main():
         line["serving"] = serving(gmc, torch, args.serve_seconds)
     if rank == 0 and not args.no_keygen:
         line["keygen"] = keygen_rates(gmc, torch, args.keygen_keys, os.cpu_count() or 1,
-                                      with_cpu=not args.no_cpu and world == 1)
+                                      with_cpu=not args.no_cpu and world == 1,
+                                      sets=args.keygen_sets.split(",") if args.keygen_sets else None)
 
     if rank == 0 and not args.no_e2e:
         # end to end through the host-pointer C ABI (pinned host buffers)

@@ -520,6 +520,13 @@ static int controlbits(uint8_t *out, const int16_t *pi, int w) {
   return bad ? -1 : 0;
 }
 
+/* Control bits of a permutation of 2^w entries (the recursion above, as keygen
+ * runs it); 0, or -1 when the bits do not re-encode pi. */
+int gmo_controlbits(uint8_t *out, const int16_t *pi, int w) {
+  if (w < 1 || w > 13) return -1;
+  return controlbits(out, pi, w);
+}
+
 /* Key generation (mc:crypto_kem/348864/vec/kem_keypair.c:20, identical for
  * all five sets): one 32-byte randombytes draw, then the seed-expansion loop. */
 int gmo_keypair_rng(int set, uint8_t *pk, uint8_t *sk, gmo_rng_fn rng, void *ctx) {

@@ -50,6 +50,8 @@ int gmo_decrypt_stages(int set, const uint8_t *sk, const uint8_t *c, uint16_t *s
 /* support L[n] and 1/g(L_i)^2 [n] (w2 may be NULL) */
 int gmo_support(int set, const uint8_t *sk, uint16_t *L_out, uint16_t *w2_out);
 int gmo_gf_mul(int m, int a, int b);
+/* Benes control bits of pi (2^w entries), the keygen recursion */
+int gmo_controlbits(uint8_t *out, const int16_t *pi, int w);
 
 /* threaded batches (CPU baseline and fixture generation) */
 int gmo_enc_batch(int set, long long count, uint8_t *c, uint8_t *key, const uint8_t *pk, const uint8_t *seeds,

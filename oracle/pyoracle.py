@@ -31,6 +31,7 @@ def lib():
         vp = ctypes.c_void_p
         L.gmo_sizes.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
         L.gmo_keypair.argtypes = [ctypes.c_int, vp, vp, vp]
+        L.gmo_controlbits.argtypes = [vp, vp, ctypes.c_int]
         L.gmo_enc.argtypes = [ctypes.c_int, vp, vp, vp, vp]
         L.gmo_dec.argtypes = [ctypes.c_int, vp, vp, vp]
         L.gmo_gen_e.argtypes = [ctypes.c_int, vp, vp]
@@ -67,6 +68,16 @@ def keypair(s, seed32):
     rc = lib().gmo_keypair(sid(s), _p(pk), _p(sk), _p(seed))
     assert rc == 0, rc
     return pk, sk
+
+
+def controlbits(pi):
+    """Benes control bits of the permutation pi (2^w int entries), as key generation computes them."""
+    pi = np.ascontiguousarray(pi, dtype=np.int16)
+    w = int(pi.size).bit_length() - 1
+    out = np.zeros(((2 * w - 1) * pi.size // 2 + 7) // 8, np.uint8)
+    rc = lib().gmo_controlbits(_p(out), _p(pi), w)
+    assert rc == 0, rc
+    return out
 
 
 def enc(s, pk, seed32):

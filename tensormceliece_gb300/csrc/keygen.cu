@@ -13,9 +13,13 @@
 // control bits of the support permutation, and sk = seed | pivots | g |
 // control bits | r[0:n/8].
 //
-// Device pipeline of one round (each pending key gets k <= 8 chained attempts,
-// k filling 4 x SMs attempts; stream 1):
-//   kg_expand    one thread per key   k chained SHAKE256 expansions
+// Seed chains (stream 0): kg_expand, one thread per key and chain link,
+// expands 16 links of every key ahead of the rounds into an expansion store
+// (more for the rare key that needs them); a chain link costs 251 sequential
+// Keccak-f permutations for 8192128, so expanding ahead keeps the chain
+// latency off the rounds.
+// Device pipeline of one round (each pending key gets k <= 8 attempts, k
+// filling 4 x SMs attempts; stream 1):
 //   kg_minpoly   one CTA per attempt  powers of f in GF((2^m)^t), Gauss-Jordan
 //   kg_support   one CTA per attempt  bitonic sort of (value, index) pairs
 //   kg_build     CTAs per attempt     columns of A_L (the rank test's matrix)
@@ -33,7 +37,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -66,7 +74,8 @@ template <int SET> struct KG {
   static constexpr int m = Q::m, n = Q::n, t = Q::t, mt = Q::mt, k = Q::k, q = Q::q;
   static constexpr int rlen = Q::e_bytes + 4 * q + 2 * t + 32;    // SHAKE output bytes per attempt
   static constexpr int rblocks = (rlen + 135) / 136;
-  static constexpr int rstride = rblocks * 136;                   // per-attempt r bytes (whole blocks)
+  static constexpr int dofs = rblocks * 136;                      // the attempt's seed follows its r blocks
+  static constexpr int rstride = dofs + 32;                       // per-attempt bytes: r (whole blocks), seed
   static constexpr int rw = (((n + 31) / 32) + 31) / 32 * 32;     // u32 words per full row
   static constexpr int rwl = (((mt + 31) / 32) + 31) / 32 * 32;   // u32 words per A_L row
   static constexpr int npanel = (mt + 31) / 32;
@@ -89,55 +98,49 @@ __device__ __forceinline__ void kg_cluster_sync() {
 constexpr uint8_t kKgMinpoly = 1, kKgDistinct = 2, kKgRank = 4, kKgAll = 7;
 
 // ---------------------------------------------------------------- expansion
-// Thread per pending key: k chained expansions r_a = SHAKE256({64} || seed_a),
-// seed_{a+1} = r_a[rlen-32 : rlen]. Attempt a of key j is j * k + a.
+// One link of every listed key's seed chain: thread i takes key = keys[i]
+// (or i), expands r = SHAKE256({64} || seed) into slot (a, i) of a block of
+// nb keys, stores the seed after r's blocks, and advances the key's chain
+// to seed' = r[rlen-32 : rlen].
 template <int SET>
-__global__ void __launch_bounds__(32) kg_expand_kernel(const uint8_t *__restrict__ seed_in, uint8_t *__restrict__ seed_out,
-                                                       int nkeys, int k, uint8_t *__restrict__ rbuf,
-                                                       uint8_t *__restrict__ delta, uint8_t *__restrict__ status) {
+__global__ void __launch_bounds__(32) kg_expand_kernel(uint8_t *__restrict__ seedc, const int *__restrict__ keys,
+                                                       int nb, int a, uint8_t *__restrict__ out) {
   using C = KG<SET>;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nkeys) return;
-  uint8_t seed[32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const int key = keys ? keys[i] : i;
+  uint8_t *r = out + ((long long)a * nb + i) * C::rstride;
+  uint8_t in[40];
+  in[0] = 64;
 #pragma unroll
-  for (int i = 0; i < 32; i++) seed[i] = seed_in[32 * j + i];
-  for (int a = 0; a < k; a++) {
-    const long long att = (long long)j * k + a;
-    uint8_t *r = rbuf + att * C::rstride;
-    uint64_t s[25];
+  for (int j = 0; j < 32; j++) in[1 + j] = seedc[32 * key + j];
+  in[33] = 0x1F;
 #pragma unroll
-    for (int i = 0; i < 25; i++) s[i] = 0;
-    // absorb {64} || seed || 0x1F, final bit of the 136-byte block
-    uint8_t in[40];
-    in[0] = 64;
+  for (int j = 34; j < 40; j++) in[j] = 0;
+  uint64_t s[25];
 #pragma unroll
-    for (int i = 0; i < 32; i++) in[1 + i] = seed[i];
-    in[33] = 0x1F;
+  for (int j = 0; j < 25; j++) s[j] = 0;
+  // absorb {64} || seed || 0x1F, final bit of the 136-byte block
 #pragma unroll
-    for (int i = 34; i < 40; i++) in[i] = 0;
+  for (int l = 0; l < 5; l++) {
+    uint64_t w = 0;
 #pragma unroll
-    for (int l = 0; l < 5; l++) {
-      uint64_t w = 0;
-#pragma unroll
-      for (int b = 0; b < 8; b++) w |= (uint64_t)in[8 * l + b] << (8 * b);
-      s[l] = w;
-    }
-    s[16] ^= 0x8000000000000000ull;
-#pragma unroll
-    for (int i = 0; i < 32; i++) delta[att * 32 + i] = seed[i];
-    uint64_t *out = reinterpret_cast<uint64_t *>(r);
+    for (int b = 0; b < 8; b++) w |= (uint64_t)in[8 * l + b] << (8 * b);
+    s[l] = w;
+  }
+  s[16] ^= 0x8000000000000000ull;
+  uint64_t *o = reinterpret_cast<uint64_t *>(r);
 #pragma unroll 1
-    for (int b = 0; b < C::rblocks; b++) {
-      keccak_f1600(s);
+  for (int b = 0; b < C::rblocks; b++) {
+    keccak_f1600(s);
 #pragma unroll
-      for (int i = 0; i < 17; i++) out[17 * b + i] = s[i];
-    }
-#pragma unroll
-    for (int i = 0; i < 32; i++) seed[i] = r[C::rlen - 32 + i];
-    status[att] = 0;
+    for (int j = 0; j < 17; j++) o[17 * b + j] = s[j];
   }
 #pragma unroll
-  for (int i = 0; i < 32; i++) seed_out[32 * j + i] = seed[i];
+  for (int j = 0; j < 32; j++) {
+    r[C::dofs + j] = in[1 + j];
+    seedc[32 * key + j] = r[C::rlen - 32 + j];
+  }
 }
 
 // ---------------------------------------------------------------- minimal polynomial
@@ -161,7 +164,7 @@ template <int SET> struct MinpolySmem {
 };
 
 template <int SET>
-__global__ void __launch_bounds__(kMinpolyThreads) kg_minpoly_kernel(const uint8_t *__restrict__ rbuf, int natt,
+__global__ void __launch_bounds__(kMinpolyThreads) kg_minpoly_kernel(const uint8_t *const *__restrict__ rptr, int natt,
                                                                      const uint16_t *__restrict__ gexp,
                                                                      const uint16_t *__restrict__ glog,
                                                                      uint16_t *__restrict__ gout,
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(kMinpolyThreads) kg_minpoly_kernel(const uint8
   const int tid = threadIdx.x;
   for (int i = tid; i < C::exp_n; i += kMinpolyThreads) ex[i] = gexp[i];
   for (int i = tid; i < q; i += kMinpolyThreads) lg[i] = glog[i];
-  const uint8_t *rp = rbuf + (long long)att * C::rstride + C::rlen - 32 - 2 * T;
+  const uint8_t *rp = rptr[att] + C::rlen - 32 - 2 * T;
   if (tid < T) {
     const uint16_t f = (uint16_t)((rp[2 * tid] | (rp[2 * tid + 1] << 8)) & (q - 1));
     col[0 * T + tid] = tid == 0 ? 1 : 0;
@@ -279,7 +282,7 @@ __global__ void __launch_bounds__(kMinpolyThreads) kg_minpoly_kernel(const uint8
 // reject a repeated value, keep pi_i = the index part of the i-th smallest.
 constexpr int kSupportThreads = 1024;
 template <int SET>
-__global__ void __launch_bounds__(kSupportThreads) kg_support_kernel(const uint8_t *__restrict__ rbuf, int natt,
+__global__ void __launch_bounds__(kSupportThreads) kg_support_kernel(const uint8_t *const *__restrict__ rptr, int natt,
                                                                      uint16_t *__restrict__ pi_out,
                                                                      uint8_t *__restrict__ status) {
   using C = KG<SET>;
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(kSupportThreads) kg_support_kernel(const uint8
   const int att = blockIdx.x;
   if (att >= natt || !(status[att] & kKgMinpoly)) return;
   const int tid = threadIdx.x;
-  const uint8_t *pv = rbuf + (long long)att * C::rstride + C::n / 8;
+  const uint8_t *pv = rptr[att] + C::n / 8;
   for (int i = tid; i < q; i += kSupportThreads) {
     const uint32_t v = (uint32_t)pv[4 * i] | ((uint32_t)pv[4 * i + 1] << 8) | ((uint32_t)pv[4 * i + 2] << 16) |
                        ((uint32_t)pv[4 * i + 3] << 24);
@@ -767,8 +770,7 @@ __global__ void __launch_bounds__(kCbitsThreads) kg_cbits_kernel(const uint16_t 
 // ff ff ff ff 00 00 00 00 | g_0..g_{t-1} (LE u16) | control bits | r[0:n/8].
 template <int SET>
 __global__ void kg_assemble_kernel(const int *__restrict__ att_of, const int *__restrict__ out_of, int nwin,
-                                   const uint8_t *__restrict__ rbuf,
-                                   const uint8_t *__restrict__ delta, const uint16_t *__restrict__ gall,
+                                   const uint8_t *const *__restrict__ rptr, const uint16_t *__restrict__ gall,
                                    const uint8_t *__restrict__ cond, const uint32_t *__restrict__ matF,
                                    const uint16_t *__restrict__ rowid, uint8_t *__restrict__ pk_out,
                                    uint8_t *__restrict__ sk_out) {
@@ -789,14 +791,14 @@ __global__ void kg_assemble_kernel(const int *__restrict__ att_of, const int *__
     } else {
       const int o = (int)(i - pkb);
       uint8_t v;
-      if (o < 32) v = delta[(long long)att * 32 + o];
+      if (o < 32) v = rptr[att][C::dofs + o];
       else if (o < 36) v = 0xff;
       else if (o < 40) v = 0;
       else if (o < 40 + 2 * C::t) {
         const uint16_t gv = gall[(long long)att * C::gstride + ((o - 40) >> 1)];
         v = (uint8_t)(((o - 40) & 1) ? gv >> 8 : gv);
       } else if (o < 40 + 2 * C::t + C::cond_bytes) v = cond[(long long)w * C::cond_bytes + (o - 40 - 2 * C::t)];
-      else v = rbuf[(long long)att * C::rstride + (o - 40 - 2 * C::t - C::cond_bytes)];
+      else v = rptr[att][o - 40 - 2 * C::t - C::cond_bytes];
       sk_out[(long long)out_of[w] * skb + o] = v;
     }
   }
@@ -841,34 +843,60 @@ cudaError_t dalloc(T **p, size_t count, cudaStream_t st) {
 }
 
 constexpr long long kMaxAttemptsPerKey = 100000;
-constexpr int kMaxSpeculation = 8;        // chained attempts per key and round
+constexpr int kMaxSpeculation = 8;        // attempts per key and round
+constexpr int kExpandBlock = 16;          // twice the minimum chain links per key of an extension block
 constexpr long long kChunkBytes = 2ll << 30;  // device-side pk + sk staging per chunk of keys
 
-// Round state, double-buffered: the winners of round r (second stream) read
-// round r's attempt buffers while round r+1 (first stream) fills the others.
+// Round state, double-buffered: the winners of round r (stream 2) read round
+// r's buffers while round r+1 (stream 1) fills the others.
 struct KgRound {
-  uint8_t *seed_in = nullptr, *seed_out = nullptr, *r = nullptr, *delta = nullptr, *status = nullptr;
+  uint8_t *status = nullptr;
   uint16_t *g = nullptr, *pi = nullptr;
   uint32_t *matL = nullptr;
+  const uint8_t **rptr = nullptr;                       // per attempt: its r in the expansion store
   int *win = nullptr;                                   // [2][wcap]: attempt, output slot
-  uint8_t *h_seed = nullptr, *h_status = nullptr;      // pinned
+  const uint8_t **h_rptr = nullptr;                     // pinned
+  uint8_t *h_status = nullptr;
   int *h_win = nullptr;
   cudaEvent_t ranked = nullptr, done = nullptr;
 };
 
+// Expansion store block: kExpandBlock chained attempts for each of nb keys,
+// expanded on stream 0 ahead of the rounds; attempt a of the block's i-th key
+// at base + (a * nb + i) * rstride.
+struct KgBlock {
+  uint8_t *base = nullptr;
+  int *keys = nullptr;    // device list (null: keys 0..nb-1)
+  int *h_keys = nullptr;  // pinned source of the list
+  int nb = 0;
+  int seq0 = 0;         // launch sequence number of the block's first link
+  int a0 = 0, nlinks = 0;  // attempts a0 .. a0 + nlinks - 1 of each of its keys
+  std::vector<int> slot;  // key -> index in the block, -1 if absent
+};
+
 template <int SET>
-int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, cudaStream_t s1, cudaStream_t s2) {
+int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, cudaStream_t s0, cudaStream_t s1,
+                  cudaStream_t s2) {
   using C = KG<SET>;
   int rc = GMC_OK;
   FieldDev fd{};
   int dev = 0, sms = 0, cap = 0, wcap = 0;
   long long kc = 0;
   KgRound R[2];
+  std::vector<KgBlock> blocks;
+  std::vector<cudaEvent_t> links;  // one per expansion launch, in stream-0 order
+  std::vector<std::vector<int>> kblocks;  // per key: its store blocks, in chain order
+  uint8_t *d_seedc = nullptr;
   uint32_t *d_matF = nullptr;
   uint16_t *d_rowid = nullptr;
   uint8_t *d_cond = nullptr, *d_cbok = nullptr, *d_pk = nullptr, *d_sk = nullptr;
-  std::vector<long long> pending, next, tries;
-  std::vector<uint8_t> cur, h_cbok;
+  std::vector<long long> pending, next;
+  std::vector<int> na;
+  std::vector<uint8_t> h_cbok;
+  // GMC_KG_TRACE=1: one stderr line per round (host clock, ms since the call)
+  static const bool trace = getenv("GMC_KG_TRACE") && getenv("GMC_KG_TRACE")[0] == '1';
+  const auto t_start = std::chrono::steady_clock::now();
+  auto ms_now = [&] { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count(); };
   if (field_tables(SET, &fd) != GMC_OK) return GMC_ECUDA;
   KG_CUDA(cudaGetDevice(&dev));
   KG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -877,21 +905,19 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
   kc = std::max<long long>(1, std::min<long long>(nkeys, kChunkBytes / (C::pk_bytes + C::sk_bytes)));
   wcap = (int)std::min<long long>(kc, cap);
   for (KgRound &b : R) {
-    KG_CUDA(dalloc(&b.seed_in, (size_t)cap * 32, s1));
-    KG_CUDA(dalloc(&b.seed_out, (size_t)cap * 32, s1));
-    KG_CUDA(dalloc(&b.r, (size_t)cap * C::rstride, s1));
-    KG_CUDA(dalloc(&b.delta, (size_t)cap * 32, s1));
     KG_CUDA(dalloc(&b.status, (size_t)cap, s1));
     KG_CUDA(dalloc(&b.g, (size_t)cap * C::gstride, s1));
     KG_CUDA(dalloc(&b.pi, (size_t)cap * C::q, s1));
     KG_CUDA(dalloc(&b.matL, (size_t)cap * C::mt * C::rwl, s1));
+    KG_CUDA(dalloc(&b.rptr, (size_t)cap, s1));
     KG_CUDA(dalloc(&b.win, (size_t)2 * wcap, s1));
-    KG_CUDA(cudaMallocHost(&b.h_seed, (size_t)cap * 32 * 2));
+    KG_CUDA(cudaMallocHost(&b.h_rptr, (size_t)cap * sizeof(void *)));
     KG_CUDA(cudaMallocHost(&b.h_status, (size_t)cap));
     KG_CUDA(cudaMallocHost(&b.h_win, (size_t)2 * wcap * sizeof(int)));
     KG_CUDA(cudaEventCreateWithFlags(&b.ranked, cudaEventDisableTiming));
     KG_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
   }
+  KG_CUDA(dalloc(&d_seedc, (size_t)kc * 32, s1));
   KG_CUDA(dalloc(&d_matF, (size_t)wcap * C::mt * C::rw, s1));
   KG_CUDA(dalloc(&d_rowid, (size_t)wcap * C::mt, s1));
   KG_CUDA(dalloc(&d_cond, (size_t)wcap * C::cond_bytes, s1));
@@ -901,10 +927,50 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
   KG_CUDA(cudaStreamSynchronize(s1));
   for (long long k0 = 0; k0 < nkeys; k0 += kc) {
     const long long nk = std::min(kc, nkeys - k0);
-    cur.assign(seeds + 32 * k0, seeds + 32 * (k0 + nk));
-    tries.assign(nk, 0);
+    // chain heads, then the first store block for every key (stream 0 runs ahead of the rounds)
+    KG_CUDA(cudaMemcpyAsync(d_seedc, seeds + 32 * k0, (size_t)nk * 32, cudaMemcpyHostToDevice, s0));
+    kblocks.assign(nk, {});
+    na.assign(nk, 0);
     pending.clear();
     for (long long i = 0; i < nk; i++) pending.push_back(i);
+    auto add_block = [&](const std::vector<long long> *keys, int a0, int nlinks) -> cudaError_t {
+      blocks.emplace_back();  // owned by the list from here on (freed with it on any exit)
+      const int bid = (int)blocks.size() - 1;
+      KgBlock &blk = blocks.back();
+      blk.nb = keys ? (int)keys->size() : (int)nk;
+      blk.a0 = a0;
+      blk.nlinks = nlinks;
+      blk.slot.assign(nk, -1);
+      cudaError_t e = dalloc(&blk.base, (size_t)blk.nb * nlinks * C::rstride, s0);
+      if (e != cudaSuccess) return e;
+      if (keys) {
+        if ((e = cudaMallocHost(&blk.h_keys, (size_t)blk.nb * sizeof(int))) != cudaSuccess) return e;
+        for (int i = 0; i < blk.nb; i++) blk.h_keys[i] = (int)(*keys)[i];
+        if ((e = dalloc(&blk.keys, (size_t)blk.nb, s0)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(blk.keys, blk.h_keys, (size_t)blk.nb * sizeof(int), cudaMemcpyHostToDevice,
+                                 s0)) != cudaSuccess)
+          return e;
+      }
+      for (int i = 0; i < blk.nb; i++) {
+        const int key = keys ? (int)(*keys)[i] : i;
+        blk.slot[key] = i;
+        kblocks[key].push_back(bid);
+      }
+      blk.seq0 = (int)links.size();
+      for (int a = 0; a < nlinks; a++) {
+        kg_expand_kernel<SET><<<(blk.nb + 31) / 32, 32, 0, s0>>>(d_seedc, blk.keys, blk.nb, a, blk.base);
+        cudaEvent_t ev;
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+        links.push_back(ev);
+        if ((e = cudaEventRecord(ev, s0)) != cudaSuccess) return e;
+      }
+      return cudaGetLastError();
+    };
+    // links ahead: a key needs more than L attempts with probability ~0.71^L
+    // (29% of attempts succeed for every set), so ln(nk)/0.34 + 8 links cover
+    // the whole chunk but in ~6% of calls
+    const int ahead = std::min(64, std::max(12, (int)std::ceil(std::log((double)nk) / 0.3425) + 8));
+    KG_CUDA(add_block(nullptr, 0, ahead));
     KG_CUDA(cudaMemsetAsync(d_cbok, 0, (size_t)nk, s2));
     for (int round = 0; !pending.empty(); round++) {
       KgRound &b = R[round & 1];
@@ -912,19 +978,41 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
       const int nr = (int)std::min<long long>((long long)pending.size(), cap);
       const int k = std::max(1, std::min(kMaxSpeculation, cap / nr));
       const int natt = nr * k;
-      for (int j = 0; j < nr; j++) memcpy(b.h_seed + 32 * j, &cur[32 * pending[j]], 32);
-      KG_CUDA(cudaMemcpyAsync(b.seed_in, b.h_seed, (size_t)nr * 32, cudaMemcpyHostToDevice, s1));
-      kg_expand_kernel<SET><<<(nr + 31) / 32, 32, 0, s1>>>(b.seed_in, b.seed_out, nr, k, b.r, b.delta, b.status);
-      kg_minpoly_kernel<SET><<<natt, kMinpolyThreads, MinpolySmem<SET>::bytes, s1>>>(b.r, natt, fd.gexp, fd.glog,
-                                                                                   b.g, b.status);
-      kg_support_kernel<SET><<<natt, kSupportThreads, C::q * 8, s1>>>(b.r, natt, b.pi, b.status);
+      // chains that run past their store: one more block for every pending key
+      // (every pending key has been in every block so far: the same attempts)
+      {
+        const KgBlock &last = blocks[kblocks[pending[0]].back()];
+        const int end = last.a0 + last.nlinks;
+        int need = end;
+        for (int j = 0; j < nr; j++) need = std::max(need, na[pending[j]] + k);
+        // as many links as this round needs, at least one extension block's worth
+        if (need > end) KG_CUDA(add_block(&pending, end, std::max(need - end, kExpandBlock / 2)));
+      }
+      int wait_seq = 0;
+      for (int j = 0; j < nr; j++) {
+        const long long key = pending[j];
+        for (int a = 0; a < k; a++) {
+          const int A = na[key] + a;
+          int bi = 0;
+          while (A >= blocks[kblocks[key][bi]].a0 + blocks[kblocks[key][bi]].nlinks) bi++;
+          const KgBlock &blk = blocks[kblocks[key][bi]];
+          const int al = A - blk.a0;
+          b.h_rptr[j * k + a] = blk.base + ((long long)al * blk.nb + blk.slot[key]) * C::rstride;
+          wait_seq = std::max(wait_seq, blk.seq0 + al);
+        }
+      }
+      KG_CUDA(cudaStreamWaitEvent(s1, links[wait_seq], 0));
+      KG_CUDA(cudaMemcpyAsync(b.rptr, b.h_rptr, (size_t)natt * sizeof(void *), cudaMemcpyHostToDevice, s1));
+      KG_CUDA(cudaMemsetAsync(b.status, 0, (size_t)natt, s1));
+      kg_minpoly_kernel<SET><<<natt, kMinpolyThreads, MinpolySmem<SET>::bytes, s1>>>(b.rptr, natt, fd.gexp,
+                                                                                   fd.glog, b.g, b.status);
+      kg_support_kernel<SET><<<natt, kSupportThreads, C::q * 8, s1>>>(b.rptr, natt, b.pi, b.status);
       kg_build_kernel<SET><<<dim3(C::rwl / 8, natt), kBuildThreads, BuildSmem<SET>::bytes, s1>>>(
           b.g, b.pi, nullptr, b.status, b.matL, C::rwl, C::rwl, fd.gexp, fd.glog);
       kg_elim_kernel<SET><<<natt, kElimThreads, ElimSmem<SET>::bytes, s1>>>(
           b.matL, C::rwl, C::rwl, nullptr, b.status, kKgMinpoly | kKgDistinct, kKgRank, 1, 1, nullptr);
       KG_CUDA(cudaGetLastError());
       KG_CUDA(cudaMemcpyAsync(b.h_status, b.status, natt, cudaMemcpyDeviceToHost, s1));
-      KG_CUDA(cudaMemcpyAsync(b.h_seed + (size_t)cap * 32, b.seed_out, (size_t)nr * 32, cudaMemcpyDeviceToHost, s1));
       KG_CUDA(cudaEventRecord(b.ranked, s1));
       KG_CUDA(cudaStreamSynchronize(s1));
       int nw = 0;
@@ -938,12 +1026,11 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
           b.h_win[wcap + nw] = (int)key;
           nw++;
         } else {
-          tries[key] += k;
-          if (tries[key] >= kMaxAttemptsPerKey) {
+          na[key] += k;
+          if (na[key] >= kMaxAttemptsPerKey) {
             rc = kg_fail(GMC_EKEY, "gmc_keypair_batch: no systematic key within the attempt limit");
             goto done;
           }
-          memcpy(&cur[32 * key], b.h_seed + (size_t)cap * 32 + 32 * j, 32);
           next.push_back(key);
         }
       }
@@ -954,8 +1041,8 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
         KG_CUDA(cudaMemcpyAsync(b.win, b.h_win, (size_t)2 * wcap * sizeof(int), cudaMemcpyHostToDevice, s2));
         kg_build_kernel<SET><<<dim3(C::rw / 8, nw), kBuildThreads, BuildSmem<SET>::bytes, s2>>>(
             b.g, b.pi, watt, b.status, d_matF, C::rw, C::rw, fd.gexp, fd.glog);
-        // the winners' status has every bit: the full elimination re-derives the same pivots
         {
+          // the winners' status has every bit: the full elimination re-derives the same pivots
           cudaLaunchConfig_t lc = {};
           cudaLaunchAttribute at[1];
           at[0].id = cudaLaunchAttributeClusterDimension;
@@ -972,14 +1059,20 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
                                      b.status, (int)kKgAll, (int)kKgAll, 0, kElimCluster, d_rowid));
         }
         kg_cbits_kernel<SET><<<nw, kCbitsThreads, CbitsSmem<SET>::bytes, s2>>>(b.pi, watt, wout, nw, d_cond, d_cbok);
-        kg_assemble_kernel<SET><<<dim3(256, nw), 256, 0, s2>>>(watt, wout, nw, b.r, b.delta, b.g, d_cond, d_matF,
-                                                                d_rowid, d_pk, d_sk);
+        kg_assemble_kernel<SET><<<dim3(256, nw), 256, 0, s2>>>(watt, wout, nw, (const uint8_t *const *)b.rptr, b.g,
+                                                                d_cond, d_matF, d_rowid, d_pk, d_sk);
         KG_CUDA(cudaGetLastError());
       }
       KG_CUDA(cudaEventRecord(b.done, s2));
+      if (trace)
+        fprintf(stderr, "[keygen] set %d round %d: %d keys x %d attempts (link <= %d, %zu blocks), %d winners, "
+                        "ranked at %.2f ms\n", SET, round, nr, k, wait_seq, blocks.size(), nw, ms_now());
       pending.swap(next);
     }
     KG_CUDA(cudaStreamSynchronize(s2));
+    if (trace) fprintf(stderr, "[keygen] winners done at %.2f ms\n", ms_now());
+    KG_CUDA(cudaStreamSynchronize(s0));
+    if (trace) fprintf(stderr, "[keygen] expansion done at %.2f ms\n", ms_now());
     h_cbok.resize(nk);
     KG_CUDA(cudaMemcpy(h_cbok.data(), d_cbok, (size_t)nk, cudaMemcpyDeviceToHost));
     for (long long i = 0; i < nk; i++)
@@ -989,21 +1082,36 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
       }
     KG_CUDA(cudaMemcpy(pk + k0 * C::pk_bytes, d_pk, (size_t)nk * C::pk_bytes, cudaMemcpyDeviceToHost));
     KG_CUDA(cudaMemcpy(sk + k0 * C::sk_bytes, d_sk, (size_t)nk * C::sk_bytes, cudaMemcpyDeviceToHost));
+    for (KgBlock &blk : blocks) {
+      cudaFreeAsync(blk.base, s1);
+      if (blk.keys) cudaFreeAsync(blk.keys, s1);
+      if (blk.h_keys) cudaFreeHost(blk.h_keys);
+    }
+    blocks.clear();
+    for (cudaEvent_t ev : links) cudaEventDestroy(ev);
+    links.clear();
   }
 done:
+  cudaStreamSynchronize(s0);
   cudaStreamSynchronize(s1);
   cudaStreamSynchronize(s2);
+  for (KgBlock &blk : blocks) {
+    if (blk.base) cudaFreeAsync(blk.base, s1);
+    if (blk.keys) cudaFreeAsync(blk.keys, s1);
+    if (blk.h_keys) cudaFreeHost(blk.h_keys);
+  }
+  for (cudaEvent_t ev : links) cudaEventDestroy(ev);
   for (KgRound &b : R) {
-    for (void *p : {(void *)b.seed_in, (void *)b.seed_out, (void *)b.r, (void *)b.delta, (void *)b.status,
-                    (void *)b.g, (void *)b.pi, (void *)b.matL, (void *)b.win})
+    for (void *p : {(void *)b.status, (void *)b.g, (void *)b.pi, (void *)b.matL, (void *)b.rptr, (void *)b.win})
       if (p) cudaFreeAsync(p, s1);
-    if (b.h_seed) cudaFreeHost(b.h_seed);
+    if (b.h_rptr) cudaFreeHost(b.h_rptr);
     if (b.h_status) cudaFreeHost(b.h_status);
     if (b.h_win) cudaFreeHost(b.h_win);
     if (b.ranked) cudaEventDestroy(b.ranked);
     if (b.done) cudaEventDestroy(b.done);
   }
-  for (void *p : {(void *)d_matF, (void *)d_rowid, (void *)d_cond, (void *)d_cbok, (void *)d_pk, (void *)d_sk})
+  for (void *p : {(void *)d_seedc, (void *)d_matF, (void *)d_rowid, (void *)d_cond, (void *)d_cbok, (void *)d_pk,
+                  (void *)d_sk})
     if (p) cudaFreeAsync(p, s1);
   {
     cudaError_t e = cudaStreamSynchronize(s1);
@@ -1025,21 +1133,23 @@ extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, 
   if (set < 0 || set >= GMC_NSETS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
     return kg_fail(GMC_EINVAL, "gmc_keypair_batch: bad argument");
   if (nkeys == 0) return GMC_OK;
-  cudaStream_t s1 = nullptr, s2 = nullptr;
-  cudaError_t e = cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
+  cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
   int rc = GMC_EINVAL;
   if (e != cudaSuccess) {
     rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
   } else {
     switch (set) {
-      case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, s1, s2); break;
-      case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, s1, s2); break;
-      case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, s1, s2); break;
-      case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, s1, s2); break;
-      case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, s1, s2); break;
+      case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, s0, s1, s2); break;
+      case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, s0, s1, s2); break;
+      case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, s0, s1, s2); break;
+      case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, s0, s1, s2); break;
+      case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, s0, s1, s2); break;
     }
   }
+  if (s0) cudaStreamDestroy(s0);
   if (s1) cudaStreamDestroy(s1);
   if (s2) cudaStreamDestroy(s2);
   return rc;
