@@ -391,13 +391,22 @@ __global__ void __launch_bounds__(kBuildThreads) kg_build_kernel(const uint16_t 
 // 256-entry tables of XOR combinations of P' rows (8 rows each) in shared
 // memory, four lookups per row word. Singular A_L: no pivot for some column,
 // the attempt fails (pk_gen.c:150-156 rejects the same matrices).
-constexpr int kElimThreads = 1024;
+// Table width: TB = 8 (four 256-entry tables per 32-word group, 128 KB,
+// 1024 threads, one CTA per SM) or TB = 4 (eight 16-entry tables, 16 KB,
+// 512 threads, three CTAs per SM, so one CTA's serial panel steps overlap the
+// others' updates).
+template <int TB> struct ElimCfg {
+  static constexpr int nt = TB == 8 ? 1024 : 512, ntab = 32 / TB, nent = 1 << TB, minb = TB == 8 ? 1 : 3;
+};
 constexpr int kElimRows = 4;      // rows in flight per warp in the panel update
 constexpr int kElimCluster = 4;   // CTAs per matrix in the full elimination
-template <int SET> struct ElimSmem {
+// measured: 4-bit tables (more resident CTAs) pay off only for 348864, whose
+// A_L rows are one 24-word group; the larger sets are instruction-bound
+template <int SET> constexpr int kg_table_bits() { return SET == 0 ? 4 : 8; }
+template <int SET, int TB> struct ElimSmem {
   using C = KG<SET>;
-  static constexpr int tab = 0;                       // 4 * 256 * 32 u32
-  static constexpr int pw = tab + 4 * 256 * 32;       // 32 * 32 u32
+  static constexpr int tab = 0;                                        // ntab * nent * 32 u32
+  static constexpr int pw = tab + ElimCfg<TB>::ntab * ElimCfg<TB>::nent * 32;  // 32 * 32 u32
   static constexpr int colw = pw + 32 * 32;           // mt u32
   static constexpr int wk = colw + C::mt;             // mt u32
   static constexpr int binv = wk + C::mt;             // 32 u32
@@ -405,14 +414,14 @@ template <int SET> struct ElimSmem {
   static constexpr int rowid_u32 = misc + 4;          // mt u16
   static constexpr int bytes = rowid_u32 * 4 + C::mt * 2 + 16;
 };
-template <int SET>
-__global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__restrict__ mat, int ld, int nwords,
+template <int SET, int TB>
+__global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_kernel(uint32_t *__restrict__ mat, int ld, int nwords,
                                                                   const int *__restrict__ att_of,
                                                                   uint8_t *__restrict__ status, int need, int set_bit,
                                                                   int forward, int cl, uint16_t *__restrict__ rowid_out) {
   using C = KG<SET>;
-  using L = ElimSmem<SET>;
-  constexpr int MT = C::mt;
+  using L = ElimSmem<SET, TB>;
+  constexpr int MT = C::mt, NT = ElimCfg<TB>::nt;
   extern __shared__ __align__(16) uint32_t kgsm_el[];
   uint32_t *tab = kgsm_el + L::tab, *Pw = kgsm_el + L::pw, *colw = kgsm_el + L::colw, *wk = kgsm_el + L::wk,
            *binv = kgsm_el + L::binv;
@@ -425,12 +434,12 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
   if ((status[att] & need) != need) return;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   uint32_t *A = mat + (long long)slot * MT * ld;
-  for (int i = tid; i < MT; i += kElimThreads) rowid[i] = (uint16_t)i;
+  for (int i = tid; i < MT; i += NT) rowid[i] = (uint16_t)i;
   const int ngroups = nwords / 32;
   for (int p = 0; p < C::npanel; p++) {
     const int base = 32 * p, np = min(32, MT - base);
     const uint32_t npmask = np == 32 ? 0xffffffffu : ((1u << np) - 1);
-    for (int pos = tid; pos < MT; pos += kElimThreads) colw[pos] = A[(long long)rowid[pos] * ld + p];
+    for (int pos = tid; pos < MT; pos += NT) colw[pos] = A[(long long)rowid[pos] * ld + p];
     __syncthreads();
     // Pivot search, first in the window of positions base .. base+63 (warp 0,
     // slots in registers: forward elimination on the panel word, slot tags
@@ -483,7 +492,7 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
       // CTA-wide search: forward elimination of the panel word over all rows
       {
         int cand = INT_MAX;
-        for (int pos = base + tid; pos < MT; pos += kElimThreads) {
+        for (int pos = base + tid; pos < MT; pos += NT) {
           const uint32_t v = colw[pos];
           wk[pos] = v;
           if (v & 1) cand = min(cand, pos);
@@ -509,7 +518,7 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
         if (misc[1]) return;  // no pivot: A_L is singular
         const uint32_t pwd = wk[base + j], bit = 1u << j;
         int cand = INT_MAX;
-        for (int pos = base + j + 1 + tid; pos < MT; pos += kElimThreads) {
+        for (int pos = base + j + 1 + tid; pos < MT; pos += NT) {
           uint32_t x = wk[pos];
           if (x & bit) {
             x ^= pwd;
@@ -545,25 +554,32 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
     else __syncthreads();
     for (int g = (p >> 5) + ((crank - (p >> 5)) % cl + cl) % cl; g < ngroups; g += cl) {
       const int w0 = 32 * g;
-      {
-        const int b = tid >> 5;
-        Pw[tid] = b < np ? A[(long long)rowid[base + b] * ld + w0 + lane] : 0;
+      for (int i = tid; i < 1024; i += NT) {
+        const int b = i >> 5;
+        Pw[i] = b < np ? A[(long long)rowid[base + b] * ld + w0 + lane] : 0;
       }
       __syncthreads();
-      uint32_t v = 0;
-      {
-        uint32_t e = binv[warp];
+      uint32_t v[1024 / NT];
+#pragma unroll
+      for (int u = 0; u < 1024 / NT; u++) {
+        uint32_t e = binv[(tid + u * NT) >> 5], acc = 0;
         while (e) {
           const int b = __ffs(e) - 1;
           e &= e - 1;
-          v ^= Pw[b * 32 + lane];
+          acc ^= Pw[b * 32 + lane];
         }
+        v[u] = acc;
       }
       __syncthreads();
-      Pw[tid] = v;
-      if (warp < np) A[(long long)rowid[base + warp] * ld + w0 + lane] = v;
+#pragma unroll
+      for (int u = 0; u < 1024 / NT; u++) {
+        const int j = (tid + u * NT) >> 5;
+        Pw[tid + u * NT] = v[u];
+        if (j < np) A[(long long)rowid[base + j] * ld + w0 + lane] = v[u];
+      }
       __syncthreads();
-      {
+      if constexpr (TB == 8) {
+        // four 256-entry tables: thread (kq, vhi, lane) writes entries vhi*32 .. vhi*32+31 of table kq
         const int kq = tid >> 8, vhi = (tid >> 5) & 7;
         const uint32_t *pr = Pw + 8 * kq * 32 + lane;
         uint32_t h = 0;
@@ -582,14 +598,29 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
         }
 #pragma unroll
         for (int vl = 0; vl < 32; vl++) tp[vl * 32] = r[vl];
+      } else {
+        // eight 16-entry tables: thread (kq, half, lane) writes entries half*8 .. half*8+7 of table kq
+        const int kq = tid >> 6, half = (tid >> 5) & 1;
+        const uint32_t *pr = Pw + 4 * kq * 32 + lane;
+        const uint32_t p0 = pr[0], p1 = pr[32], p2 = pr[64], h = half ? pr[96] : 0;
+        uint32_t *tp = tab + ((kq * 16 + half * 8) * 32) + lane;
+        tp[0] = h;
+        tp[32] = h ^ p0;
+        tp[64] = h ^ p1;
+        tp[96] = h ^ p1 ^ p0;
+        tp[128] = h ^ p2;
+        tp[160] = h ^ p2 ^ p0;
+        tp[192] = h ^ p2 ^ p1;
+        tp[224] = h ^ p2 ^ p1 ^ p0;
       }
       __syncthreads();
-      for (int pos0 = (forward ? base + np : 0) + warp; pos0 < MT; pos0 += kElimRows * 32) {
+      constexpr int NW = NT / 32;
+      for (int pos0 = (forward ? base + np : 0) + warp; pos0 < MT; pos0 += kElimRows * NW) {
         uint32_t x[kElimRows], c[kElimRows];
         uint32_t *ad[kElimRows];
 #pragma unroll
         for (int u = 0; u < kElimRows; u++) {
-          const int pos = pos0 + 32 * u;
+          const int pos = pos0 + NW * u;
           const bool live = pos < MT && (unsigned)(pos - base) >= (unsigned)np;
           c[u] = live ? (colw[pos] & npmask) : 0;
           ad[u] = A + (long long)rowid[live ? pos : 0] * ld + w0 + lane;
@@ -599,8 +630,13 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
         for (int u = 0; u < kElimRows; u++) {
           if (!c[u]) continue;
           const uint32_t cc = c[u];
-          x[u] ^= tab[((cc & 255) << 5) + lane] ^ tab[((256 + ((cc >> 8) & 255)) << 5) + lane] ^
-                  tab[((512 + ((cc >> 16) & 255)) << 5) + lane] ^ tab[((768 + (cc >> 24)) << 5) + lane];
+          if constexpr (TB == 8) {
+            x[u] ^= tab[((cc & 255) << 5) + lane] ^ tab[((256 + ((cc >> 8) & 255)) << 5) + lane] ^
+                    tab[((512 + ((cc >> 16) & 255)) << 5) + lane] ^ tab[((768 + (cc >> 24)) << 5) + lane];
+          } else {
+#pragma unroll
+            for (int kq = 0; kq < 8; kq++) x[u] ^= tab[((kq * 16 + ((cc >> (4 * kq)) & 15)) << 5) + lane];
+          }
           *ad[u] = x[u];
         }
       }
@@ -610,7 +646,7 @@ __global__ void __launch_bounds__(kElimThreads, 1) kg_elim_kernel(uint32_t *__re
   }
   if (crank) return;
   if (rowid_out)
-    for (int i = tid; i < MT; i += kElimThreads) rowid_out[(long long)slot * MT + i] = rowid[i];
+    for (int i = tid; i < MT; i += NT) rowid_out[(long long)slot * MT + i] = rowid[i];
   if (tid == 0) status[att] |= (uint8_t)set_bit;
 }
 
@@ -830,7 +866,8 @@ cudaError_t kg_attrs() {
     cudaError_t e = smem_attr(kg_minpoly_kernel<SET>, MinpolySmem<SET>::bytes);
     if (e == cudaSuccess) e = smem_attr(kg_support_kernel<SET>, KG<SET>::q * 8);
     if (e == cudaSuccess) e = smem_attr(kg_build_kernel<SET>, BuildSmem<SET>::bytes);
-    if (e == cudaSuccess) e = smem_attr(kg_elim_kernel<SET>, ElimSmem<SET>::bytes);
+    if (e == cudaSuccess) e = smem_attr(kg_elim_kernel<SET, kg_table_bits<SET>()>, ElimSmem<SET, kg_table_bits<SET>()>::bytes);
+    if (e == cudaSuccess) e = smem_attr(kg_elim_kernel<SET, kg_table_bits<SET>()>, ElimSmem<SET, kg_table_bits<SET>()>::bytes);
     if (e == cudaSuccess) e = smem_attr(kg_cbits_kernel<SET>, CbitsSmem<SET>::bytes);
     return e;
   }();
@@ -1009,7 +1046,7 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
       kg_support_kernel<SET><<<natt, kSupportThreads, C::q * 8, s1>>>(b.rptr, natt, b.pi, b.status);
       kg_build_kernel<SET><<<dim3(C::rwl / 8, natt), kBuildThreads, BuildSmem<SET>::bytes, s1>>>(
           b.g, b.pi, nullptr, b.status, b.matL, C::rwl, C::rwl, fd.gexp, fd.glog);
-      kg_elim_kernel<SET><<<natt, kElimThreads, ElimSmem<SET>::bytes, s1>>>(
+      kg_elim_kernel<SET, kg_table_bits<SET>()><<<natt, ElimCfg<kg_table_bits<SET>()>::nt, ElimSmem<SET, kg_table_bits<SET>()>::bytes, s1>>>(
           b.matL, C::rwl, C::rwl, nullptr, b.status, kKgMinpoly | kKgDistinct, kKgRank, 1, 1, nullptr);
       KG_CUDA(cudaGetLastError());
       KG_CUDA(cudaMemcpyAsync(b.h_status, b.status, natt, cudaMemcpyDeviceToHost, s1));
@@ -1050,12 +1087,12 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
           at[0].val.clusterDim.y = 1;
           at[0].val.clusterDim.z = 1;
           lc.gridDim = dim3(nw * kElimCluster);
-          lc.blockDim = dim3(kElimThreads);
-          lc.dynamicSmemBytes = ElimSmem<SET>::bytes;
+          lc.blockDim = dim3(ElimCfg<kg_table_bits<SET>()>::nt);
+          lc.dynamicSmemBytes = ElimSmem<SET, kg_table_bits<SET>()>::bytes;
           lc.stream = s2;
           lc.attrs = at;
           lc.numAttrs = 1;
-          KG_CUDA(cudaLaunchKernelEx(&lc, kg_elim_kernel<SET>, d_matF, (int)C::rw, (int)C::rw, (const int *)watt,
+          KG_CUDA(cudaLaunchKernelEx(&lc, kg_elim_kernel<SET, kg_table_bits<SET>()>, d_matF, (int)C::rw, (int)C::rw, (const int *)watt,
                                      b.status, (int)kKgAll, (int)kKgAll, 0, kElimCluster, d_rowid));
         }
         kg_cbits_kernel<SET><<<nw, kCbitsThreads, CbitsSmem<SET>::bytes, s2>>>(b.pi, watt, wout, nw, d_cond, d_cbok);
@@ -1133,10 +1170,14 @@ extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, 
   if (set < 0 || set >= GMC_NSETS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
     return kg_fail(GMC_EINVAL, "gmc_keypair_batch: bad argument");
   if (nkeys == 0) return GMC_OK;
+  // chain links and rounds are on the critical path (the host waits for each
+  // round's ranks); the winners' work only has to finish by the end
   cudaStream_t s0 = nullptr, s1 = nullptr, s2 = nullptr;
-  cudaError_t e = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+  int prio_low = 0, prio_high = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s0, cudaStreamNonBlocking, prio_high);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s1, cudaStreamNonBlocking, prio_high);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s2, cudaStreamNonBlocking, prio_low);
   int rc = GMC_EINVAL;
   if (e != cudaSuccess) {
     rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
