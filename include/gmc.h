@@ -27,10 +27,18 @@ extern "C" {
 
 typedef struct gmc_key gmc_key;
 
-/* ---- parameter sets -------------------------------------------------- */
+/* ---- parameter sets --------------------------------------------------
+ * Set ids 0..4: 348864, 460896, 6688128, 6960119, 8192128 (gmc_set_count()
+ * = 5). Ids 5..9 (GMC_NVARIANTS = 10): the plaintext-confirmation ("pc")
+ * variants of the same five sets (mc:crypto_kem/<set>pc): identical keys,
+ * ciphertexts C0 || C1 with C1 = SHAKE256(2 || e, 32) (32 bytes longer), the
+ * session key hashed over C0 || C1, and decapsulation also rejecting when C1
+ * does not match the decoded e. Every entry point taking a set id or a key
+ * accepts both, except the serving loop (gmc_server_*), which serves ids 0..4. */
+#define GMC_NVARIANTS 10
 int gmc_set_count(void);
 const char *gmc_set_name(int set);
-/* looks up "348864", "mceliece348864", ...; returns the id or GMC_EINVAL */
+/* looks up "348864", "mceliece348864", "8192128pc", ...; returns the id or GMC_EINVAL */
 int gmc_set_id(const char *name);
 /* out[8] = m, n, t, mt, k, public-key bytes, secret-key bytes, ciphertext bytes */
 int gmc_set_sizes(int set, long long *out);
@@ -170,6 +178,22 @@ int gmc_kem_6960119_dec(unsigned char *k, const unsigned char *c, const unsigned
 void gmc_kem_8192128_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_8192128_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_8192128_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+/* plaintext-confirmation variants (mc:crypto_kem/<set>pc/vec/wrap_{keypair,enc,dec}.c) */
+void gmc_kem_348864pc_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_348864pc_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_348864pc_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_460896pc_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_460896pc_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_460896pc_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6688128pc_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_6688128pc_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6688128pc_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6960119pc_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_6960119pc_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6960119pc_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_8192128pc_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_8192128pc_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_8192128pc_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
 
 /* randombytes source of the one-request enc entry points
  * (librandombytes' randombytes(), rb:include/randombytes.h:10). NULL restores

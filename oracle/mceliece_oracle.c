@@ -55,11 +55,16 @@ typedef struct {
   int m, n, t, mt, k, q; /* q = 2^m */
   int pk_row_bytes, synd_bytes, cond_bytes, irr_bytes, e_bytes;
   long pk_bytes, sk_bytes;
+  int pc;       /* plaintext-confirmation variant (ids GMO_NSETS ..): c = C0 || C1 */
+  int ct_bytes; /* synd_bytes, + 32 with plaintext confirmation */
 } sizes;
 
+/* Set ids 0..4 are the five parameter sets, GMO_NSETS + s their "pc"
+ * variants (mc:crypto_kem/<set>pc): the same keys, ciphertexts C0 || C1 with
+ * C1 = SHAKE256(2 || e, 32). */
 static int get_sizes(int set, sizes *P) {
-  if (set < 0 || set >= GMO_NSETS) return -1;
-  const setdef *S = &SETS[set];
+  if (set < 0 || set >= GMO_NVARIANTS) return -1;
+  const setdef *S = &SETS[set % GMO_NSETS];
   P->m = S->m; P->n = S->n; P->t = S->t;
   P->mt = S->m * S->t;
   P->k = S->n - P->mt;
@@ -71,6 +76,8 @@ static int get_sizes(int set, sizes *P) {
   P->e_bytes = S->n / 8;
   P->pk_bytes = (long)P->mt * P->pk_row_bytes;
   P->sk_bytes = 40 + P->irr_bytes + P->cond_bytes + P->e_bytes;
+  P->pc = set >= GMO_NSETS;
+  P->ct_bytes = P->synd_bytes + (P->pc ? 32 : 0);
   return 0;
 }
 
@@ -78,7 +85,7 @@ int gmo_sizes(int set, long long *out /* [8] */) {
   sizes P;
   if (get_sizes(set, &P)) return -1;
   out[0] = P.m; out[1] = P.n; out[2] = P.t; out[3] = P.mt; out[4] = P.k;
-  out[5] = P.pk_bytes; out[6] = P.sk_bytes; out[7] = P.synd_bytes;
+  out[5] = P.pk_bytes; out[6] = P.sk_bytes; out[7] = P.ct_bytes;
   return 0;
 }
 
@@ -533,7 +540,7 @@ int gmo_keypair_rng(int set, uint8_t *pk, uint8_t *sk, gmo_rng_fn rng, void *ctx
   sizes P;
   if (get_sizes(set, &P)) return -1;
   ensure_init();
-  const setdef *S = &SETS[set];
+  const setdef *S = &SETS[set % GMO_NSETS];
   const field *F = &FIELD[P.m - 12];
   uint8_t seed[33];
   seed[0] = 64;
@@ -674,21 +681,27 @@ static int c_padding_bad(const sizes *P, const uint8_t *c) {
 
 /* KEM encapsulation (mc:crypto_kem/348864/vec/kem_enc.c:18; pk padding rule
  * of 6960119 at mc:crypto_kem/6960119/vec/kem_enc.c:21-66):
- * K = SHAKE256(1 || e || c, 32). */
+ * K = SHAKE256(1 || e || c, 32). Plaintext confirmation
+ * (mc:crypto_kem/348864pc/vec/kem_enc.c:24-35): c = C0 || SHAKE256(2 || e, 32). */
 int gmo_enc_rng(int set, uint8_t *c, uint8_t *key, const uint8_t *pk, gmo_rng_fn rng, void *ctx) {
   sizes P;
   if (get_sizes(set, &P)) return -1;
   uint8_t e[GMO_MAX_N / 8];
-  uint8_t pre[1 + GMO_MAX_N / 8 + GMO_MAX_MT / 8];
+  uint8_t pre[1 + GMO_MAX_N / 8 + GMO_MAX_MT / 8 + 32];
   int bad = pk_padding_bad(&P, pk);
   gmo_gen_e_rng(set, e, rng, ctx, NULL);
   gmo_syndrome(set, c, pk, e);
+  if (P.pc) {
+    pre[0] = 2;
+    memcpy(pre + 1, e, (size_t)P.e_bytes);
+    gmo_shake256(c + P.synd_bytes, 32, pre, 1 + P.e_bytes);
+  }
   pre[0] = 1;
   memcpy(pre + 1, e, (size_t)P.e_bytes);
-  memcpy(pre + 1 + P.e_bytes, c, (size_t)P.synd_bytes);
-  gmo_shake256(key, 32, pre, 1 + P.e_bytes + P.synd_bytes);
+  memcpy(pre + 1 + P.e_bytes, c, (size_t)P.ct_bytes);
+  gmo_shake256(key, 32, pre, 1 + P.e_bytes + P.ct_bytes);
   if (bad) {
-    memset(c, 0, (size_t)P.synd_bytes);
+    memset(c, 0, (size_t)P.ct_bytes);
     memset(key, 0, 32);
     return -1;
   }
@@ -803,15 +816,24 @@ static int decrypt_ctx(const keyctx *K, uint8_t *e, const uint8_t *c, gf *s_out,
  * c padding rule of 6960119 at mc:crypto_kem/6960119/vec/kem_dec.c:21-78). */
 static int dec_ctx(const keyctx *K, uint8_t *key, const uint8_t *c) {
   const sizes *P = &K->P;
-  uint8_t cc[GMO_MAX_MT / 8];
-  memcpy(cc, c, (size_t)P->synd_bytes); /* key may alias c */
+  uint8_t cc[GMO_MAX_MT / 8 + 32];
+  memcpy(cc, c, (size_t)P->ct_bytes); /* key may alias c */
   uint8_t e[GMO_MAX_N / 8];
-  uint8_t pre[1 + GMO_MAX_N / 8 + GMO_MAX_MT / 8];
+  uint8_t pre[1 + GMO_MAX_N / 8 + GMO_MAX_MT / 8 + 32];
   int fail = decrypt_ctx(K, e, cc, NULL, NULL);
+  if (P->pc) {
+    /* plaintext confirmation (mc:crypto_kem/348864pc/vec/kem_dec.c:43-48):
+     * reject unless SHAKE256(2 || e, 32) equals C1 */
+    uint8_t conf[32];
+    pre[0] = 2;
+    memcpy(pre + 1, e, (size_t)P->e_bytes);
+    gmo_shake256(conf, 32, pre, 1 + P->e_bytes);
+    fail |= memcmp(conf, cc + P->synd_bytes, 32) != 0;
+  }
   pre[0] = fail ? 0 : 1;
   memcpy(pre + 1, fail ? K->s : e, (size_t)P->e_bytes);
-  memcpy(pre + 1 + P->e_bytes, cc, (size_t)P->synd_bytes);
-  gmo_shake256(key, 32, pre, 1 + P->e_bytes + P->synd_bytes);
+  memcpy(pre + 1 + P->e_bytes, cc, (size_t)P->ct_bytes);
+  gmo_shake256(key, 32, pre, 1 + P->e_bytes + P->ct_bytes);
   if (c_padding_bad(P, cc)) { memset(key, 0xFF, 32); return -1; }
   return 0;
 }
@@ -871,9 +893,9 @@ static void *worker(void *arg) {
   for (long long i = J->lo; i < J->hi; i++) {
     int r;
     if (J->op == 0)
-      r = gmo_enc(J->set, J->out_c + i * P.synd_bytes, J->out_k + 32 * i, J->pk, J->seeds + 32 * i);
+      r = gmo_enc(J->set, J->out_c + i * P.ct_bytes, J->out_k + 32 * i, J->pk, J->seeds + 32 * i);
     else
-      r = dec_ctx(J->K, J->out_k + 32 * i, J->in_c + i * P.synd_bytes);
+      r = dec_ctx(J->K, J->out_k + 32 * i, J->in_c + i * P.ct_bytes);
     if (J->rc) J->rc[i] = r;
   }
   return NULL;

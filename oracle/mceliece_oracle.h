@@ -16,6 +16,7 @@ extern "C" {
 #endif
 
 #define GMO_NSETS 5
+#define GMO_NVARIANTS 10 /* ids GMO_NSETS + s: the plaintext-confirmation ("pc") variant of set s */
 #define GMO_MAX_N 8192
 #define GMO_MAX_T 128
 #define GMO_MAX_M 13

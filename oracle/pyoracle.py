@@ -13,6 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libmceliece_oracle.so")
 SETS = ("348864", "460896", "6688128", "6960119", "8192128")
+# plaintext-confirmation variants: ids 5..9, the same keys as the base set
+VARIANTS = SETS + tuple(s + "pc" for s in SETS)
 _lib = None
 
 
@@ -51,7 +53,7 @@ def _p(a):
 
 
 def sid(s):
-    return s if isinstance(s, int) else SETS.index(str(s).replace("mceliece", ""))
+    return s if isinstance(s, int) else VARIANTS.index(str(s).replace("mceliece", ""))
 
 
 def sizes(s):

@@ -18,12 +18,14 @@ import numpy as np
 from . import build as _build
 
 __all__ = [
-    "SETS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "keypair_batch", "Plan", "Server", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
+    "SETS", "VARIANTS", "GmcError", "lib", "set_id", "set_sizes", "keypair", "keypair_batch", "Plan", "Server", "PublicKey", "SecretKey", "kem_enc", "kem_dec",
     "set_gemm_engine", "get_gemm_engine", "set_randombytes", "autotune", "autotune_load", "tune_get",
     "tune_set", "GEMM_POPC", "GEMM_B1MMA", "GEMM_TC", "GEMM_SPARSE",
 ]
 
 SETS = ("348864", "460896", "6688128", "6960119", "8192128")
+# set ids 5..9: the plaintext-confirmation ("pc") variants of SETS (same keys, ciphertexts 32 bytes longer)
+VARIANTS = SETS + tuple(s + "pc" for s in SETS)
 GEMM_POPC, GEMM_B1MMA, GEMM_TC, GEMM_SPARSE = 0, 1, 2, 3
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad key"}
 
@@ -66,12 +68,12 @@ def lib():
         L.gmc_gf2_gemm_dev.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                        ctypes.c_int, ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p]
-        for s in SETS:
+        for s in VARIANTS:
             for op in ("enc", "dec"):
                 getattr(L, f"gmc_kem_{s}_{op}").argtypes = [c_u8p, c_u8p, c_u8p]
         L.gmc_keypair_seed.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p]
         L.gmc_keypair_batch.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p, ctypes.c_longlong]
-        for s in SETS:
+        for s in VARIANTS:
             getattr(L, f"gmc_kem_{s}_keypair").argtypes = [c_u8p, c_u8p]
             getattr(L, f"gmc_kem_{s}_keypair").restype = None
         L.gmc_plan_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p, ctypes.c_int]
@@ -114,9 +116,9 @@ def set_id(name):
     name = str(name)
     if name.startswith("mceliece"):
         name = name[len("mceliece"):]
-    if name not in SETS:
+    if name not in VARIANTS:
         raise GmcError(f"unknown parameter set {name!r}")
-    return SETS.index(name)
+    return VARIANTS.index(name)
 
 
 def set_sizes(s):
@@ -317,7 +319,7 @@ def keypair(set_name, seed32=None):
     pk = np.zeros(sz["pk_bytes"], np.uint8)
     sk = np.zeros(sz["sk_bytes"], np.uint8)
     if seed32 is None:
-        getattr(lib(), f"gmc_kem_{SETS[sid]}_keypair")(_ptr(pk), _ptr(sk))
+        getattr(lib(), f"gmc_kem_{VARIANTS[sid]}_keypair")(_ptr(pk), _ptr(sk))
     else:
         seed = _u8(bytes(seed32), 32)
         _check(lib().gmc_keypair_seed(sid, _ptr(pk), _ptr(sk), _ptr(seed)), "gmc_keypair_seed")
@@ -344,7 +346,7 @@ def kem_enc(set_name, pk):
     c = np.zeros(sz["ct_bytes"], np.uint8)
     k = np.zeros(32, np.uint8)
     p = _u8(pk, sz["pk_bytes"])
-    name = SETS[set_name] if isinstance(set_name, int) else SETS[set_id(set_name)]
+    name = VARIANTS[set_name] if isinstance(set_name, int) else VARIANTS[set_id(set_name)]
     rc = getattr(lib(), f"gmc_kem_{name}_enc")(_ptr(c), _ptr(k), _ptr(p))
     if rc < -1:
         _check(rc, f"gmc_kem_{name}_enc")
@@ -357,7 +359,7 @@ def kem_dec(set_name, ct, sk):
     c = _u8(ct, sz["ct_bytes"])
     s = _u8(sk, sz["sk_bytes"])
     k = np.zeros(32, np.uint8)
-    name = SETS[set_name] if isinstance(set_name, int) else SETS[set_id(set_name)]
+    name = VARIANTS[set_name] if isinstance(set_name, int) else VARIANTS[set_id(set_name)]
     rc = getattr(lib(), f"gmc_kem_{name}_dec")(_ptr(k), _ptr(c), _ptr(s))
     if rc < -1:
         _check(rc, f"gmc_kem_{name}_dec")

@@ -175,6 +175,12 @@ static int get_field(int set, FieldDev *out) {
 }
 
 static bool valid_set(int set) { return set >= 0 && set < GMC_NSETS; }
+// public set ids: 0..4 the parameter sets, GMC_NSETS + s the plaintext-confirmation variant of s
+static bool valid_id(int id) { return id >= 0 && id < GMC_NVARIANTS; }
+static int base_of(int id) { return id % GMC_NSETS; }
+static bool pc_of(int id) { return id >= GMC_NSETS; }
+static long long ct_bytes_of(int set, bool pc) { return set_info(set).synd_bytes + (pc ? 32 : 0); }
+static long long ct_bytes_of(const gmc_key *k) { return ct_bytes_of(k->set, k->pc != 0); }
 
 // Per-device error word of the tensor-core engine (a CTA that gave up on a
 // bounded wait sets it to 1); gmc_tc_status() reads and clears it.
@@ -227,30 +233,36 @@ static cudaError_t key_a8(const gmc_key *kc, cudaStream_t st, const uint8_t **ou
 
 
 extern "C" int gmc_set_count(void) { return GMC_NSETS; }
-extern "C" const char *gmc_set_name(int set) { return valid_set(set) ? set_info(set).name : nullptr; }
+static const char *const kPcNames[GMC_NSETS] = {"348864pc", "460896pc", "6688128pc", "6960119pc", "8192128pc"};
+extern "C" const char *gmc_set_name(int set) {
+  if (!valid_id(set)) return nullptr;
+  return pc_of(set) ? kPcNames[base_of(set)] : set_info(set).name;
+}
 extern "C" int gmc_set_id(const char *name) {
   if (!name) return GMC_EINVAL;
   if (!strncmp(name, "mceliece", 8)) name += 8;
-  for (int i = 0; i < GMC_NSETS; i++)
-    if (!strcmp(name, set_info(i).name)) return i;
+  for (int i = 0; i < GMC_NVARIANTS; i++)
+    if (!strcmp(name, gmc_set_name(i))) return i;
   return GMC_EINVAL;
 }
 extern "C" int gmc_set_sizes(int set, long long *out) {
-  if (!valid_set(set) || !out) return fail(GMC_EINVAL, "gmc_set_sizes: bad argument");
-  const gmc_setinfo &S = set_info(set);
+  if (!valid_id(set) || !out) return fail(GMC_EINVAL, "gmc_set_sizes: bad argument");
+  const gmc_setinfo &S = set_info(base_of(set));
   out[0] = S.m; out[1] = S.n; out[2] = S.t; out[3] = S.mt; out[4] = S.k;
-  out[5] = S.pk_bytes; out[6] = S.sk_bytes; out[7] = S.synd_bytes;
+  out[5] = S.pk_bytes; out[6] = S.sk_bytes; out[7] = ct_bytes_of(base_of(set), pc_of(set));
   return GMC_OK;
 }
 
-extern "C" int gmc_pk_load(gmc_key **out, int set, const unsigned char *pk) {
-  if (!out || !pk || !valid_set(set)) return fail(GMC_EINVAL, "gmc_pk_load: bad argument");
+extern "C" int gmc_pk_load(gmc_key **out, int id, const unsigned char *pk) {
+  if (!out || !pk || !valid_id(id)) return fail(GMC_EINVAL, "gmc_pk_load: bad argument");
+  const int set = base_of(id);
   *out = nullptr;
   PkHost h;
   build_pk(set, pk, h);
   gmc_key *k = new gmc_key();
   k->a8_mu = new std::mutex();
   k->set = set;
+  k->pc = pc_of(id);
   k->kind = 0;
   cudaGetDevice(&k->device);
   k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad; k->ldtt = h.ldtt;
@@ -272,8 +284,9 @@ extern "C" int gmc_pk_load(gmc_key **out, int set, const unsigned char *pk) {
   return GMC_OK;
 }
 
-extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
-  if (!out || !sk || !valid_set(set)) return fail(GMC_EINVAL, "gmc_sk_load: bad argument");
+extern "C" int gmc_sk_load(gmc_key **out, int id, const unsigned char *sk) {
+  if (!out || !sk || !valid_id(id)) return fail(GMC_EINVAL, "gmc_sk_load: bad argument");
+  const int set = base_of(id);
   *out = nullptr;
   SkHost h;
   if (build_sk(set, sk, h)) return fail(GMC_EKEY, "gmc_sk_load: Goppa polynomial vanishes on the support");
@@ -281,6 +294,7 @@ extern "C" int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk) {
   gmc_key *k = new gmc_key();
   k->a8_mu = new std::mutex();
   k->set = set;
+  k->pc = pc_of(id);
   k->kind = 1;
   cudaGetDevice(&k->device);
   k->ldf = h.ldf; k->frows_pad = h.frows_pad; k->cw_pad = h.cw_pad;
@@ -330,7 +344,7 @@ extern "C" void gmc_key_free(gmc_key *key) {
   delete key;
 }
 
-extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set : GMC_EINVAL; }
+extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set + (key->pc ? GMC_NSETS : 0) : GMC_EINVAL; }
 
 extern "C" int gmc_set_gemm_engine(int engine) {
   if (engine < -1 || engine > GEMM_SPARSE) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
@@ -452,7 +466,7 @@ static cudaError_t enc_run(const gmc_key *pk, uint8_t *c, uint8_t *k, const uint
   if ((e = scr.get((void **)&Ens, (size_t)d.n_pad * d.ldx * 4)) != cudaSuccess) return e;
   if ((e = scr.get((void **)&S, (size_t)d.n_pad * d.lds * 4)) != cudaSuccess) return e;
   if ((e = enc_sample_gemm<SET>(pk, seeds, n, E, Ens, S, d, st)) != cudaSuccess) return e;
-  e = launch_finalize<SET>(E, d.lde, S, d.lds, c, k, one_segment(n), pk->pad_bad ? 1u : 0u, st);
+  e = launch_finalize<SET>(E, d.lde, S, d.lds, c, k, one_segment(n), pk->pad_bad ? 1u : 0u, pk->pc != 0, st);
   prof_mark("enc_finalize_hash", st);
   return e;
 }
@@ -476,12 +490,13 @@ static DecDims dec_dims(const gmc_key *sk, long long n) { return dec_dims(sk->se
 template <int SET>
 static cudaError_t dec_front_decode_seg(const Segs &segs, const gmc_key *ref, const GemmKeys &gk, const DecKeys &dk,
                                         int engine, int *err, const uint8_t *c, uint32_t *X, uint32_t *S2,
-                                        uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st) {
+                                        uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st,
+                                        bool pc = false) {
   using p = P<SET>;
   FieldDev fd;
   if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
   prof_mark(nullptr, st);
-  cudaError_t e = launch_pack_ct<SET>(c, segs, X, d.ldx, st);
+  cudaError_t e = launch_pack_ct<SET>(c, segs, X, d.ldx, pc, st);
   if (e != cudaSuccess) return e;
   prof_mark("dec_pack_ct", st);
   e = launch_gf2_gemm_seg(engine, gk, segs, ref->ldf, ref->frows_pad, X, d.ldx, ref->cw_pad, S2, d.lds2, p::s2w, err,
@@ -506,7 +521,8 @@ static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long lo
   if (e != cudaSuccess) return e;
   DecKeys dk{};
   dk.k[0] = sk->dk;
-  return dec_front_decode_seg<SET>(one_segment(n), sk, gk, dk, engine, err, c, X, S2, Sig, E, ok, d, st);
+  return dec_front_decode_seg<SET>(one_segment(n), sk, gk, dk, engine, err, c, X, S2, Sig, E, ok, d, st,
+                                   sk->pc != 0);
 }
 
 template <int SET>
@@ -525,7 +541,7 @@ static cudaError_t dec_run(const gmc_key *sk, uint8_t *k, const uint8_t *c, long
   if ((e = dec_front_decode<SET>(sk, c, n, X, S2, Sig, E, ok, d, st)) != cudaSuccess) return e;
   DecKeys dk{};
   dk.k[0] = sk->dk;
-  e = launch_dec_tail<SET>(E, d.lde, ok, c, dk, k, rc, one_segment(n), st);
+  e = launch_dec_tail<SET>(E, d.lde, ok, c, dk, k, rc, one_segment(n), sk->pc != 0, st);
   prof_mark("dec_tail_hash", st);
   return e;
 }
@@ -593,14 +609,14 @@ extern "C" int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char 
   if (r) return r;
   if (n < 0 || (n && (!c || !k || !seeds))) return fail(GMC_EINVAL, "gmc_enc_batch: bad argument");
   if (!n) return GMC_OK;
-  const gmc_setinfo &S = set_info(pk->set);
+  const size_t cb = (size_t)ct_bytes_of(pk);
   keep_pool_warm();
   cudaStream_t st;
   GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   uint8_t *d_seeds = nullptr, *d_c = nullptr, *d_k = nullptr;
   int *d_rc = nullptr;
   cudaError_t e = cudaMallocAsync(&d_seeds, (size_t)n * 32, st);
-  if (e == cudaSuccess) e = cudaMallocAsync(&d_c, (size_t)n * S.synd_bytes, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_c, (size_t)n * cb, st);
   if (e == cudaSuccess) e = cudaMallocAsync(&d_k, (size_t)n * 32, st);
   if (e == cudaSuccess && rc) e = cudaMallocAsync(&d_rc, (size_t)n * 4, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_seeds, seeds, (size_t)n * 32, cudaMemcpyHostToDevice, st);
@@ -608,7 +624,7 @@ extern "C" int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char 
   if (e == cudaSuccess) {
     res = gmc_enc_batch_dev(pk, d_c, d_k, d_seeds, n, d_rc, st);
     if (res == GMC_OK) {
-      e = cudaMemcpyAsync(c, d_c, (size_t)n * S.synd_bytes, cudaMemcpyDeviceToHost, st);
+      e = cudaMemcpyAsync(c, d_c, (size_t)n * cb, cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaMemcpyAsync(k, d_k, (size_t)n * 32, cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess && rc) e = cudaMemcpyAsync(rc, d_rc, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
     }
@@ -628,16 +644,16 @@ extern "C" int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned
   if (r) return r;
   if (n < 0 || (n && (!c || !k))) return fail(GMC_EINVAL, "gmc_dec_batch: bad argument");
   if (!n) return GMC_OK;
-  const gmc_setinfo &S = set_info(sk->set);
+  const size_t cb = (size_t)ct_bytes_of(sk);
   keep_pool_warm();
   cudaStream_t st;
   GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   uint8_t *d_c = nullptr, *d_k = nullptr;
   int *d_rc = nullptr;
-  cudaError_t e = cudaMallocAsync(&d_c, (size_t)n * S.synd_bytes, st);
+  cudaError_t e = cudaMallocAsync(&d_c, (size_t)n * cb, st);
   if (e == cudaSuccess) e = cudaMallocAsync(&d_k, (size_t)n * 32, st);
   if (e == cudaSuccess && rc) e = cudaMallocAsync(&d_rc, (size_t)n * 4, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, (size_t)n * S.synd_bytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, (size_t)n * cb, cudaMemcpyHostToDevice, st);
   int res = GMC_OK;
   if (e == cudaSuccess) {
     res = gmc_dec_batch_dev(sk, d_k, d_c, n, d_rc, st);
@@ -673,6 +689,7 @@ extern "C" int gmc_dec_stages_dev(const gmc_key *sk, const unsigned char *c, lon
     e = scr.get((void **)&X, (size_t)d.n_pad * d.ldx * 4);
     if (e == cudaSuccess) e = scr.get((void **)&Sig, (size_t)d.n_pad * 256);
     if (e == cudaSuccess) GMC_DISPATCH(sk->set, e = dec_front_decode<S_>(sk, c, n, X, synd, Sig, ev, ok, d, st));
+    // (dec_front_decode packs C0 at the key's ciphertext stride: pc keys take C0 || C1 rows)
   }
   if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_stages_dev");
   return GMC_OK;
@@ -764,8 +781,7 @@ static int one_enc(int set, unsigned char *c, unsigned char *k, const unsigned c
 }
 
 static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsigned char *sk) {
-  const gmc_setinfo &S = set_info(set);
-  std::vector<uint8_t> cc(c, c + S.synd_bytes);  // k may alias c or sk
+  std::vector<uint8_t> cc(c, c + ct_bytes_of(base_of(set), pc_of(set)));  // k may alias c or sk
   gmc_key *h = nullptr;
   int r = gmc_sk_load(&h, set, sk);
   if (r) return r;
@@ -779,8 +795,9 @@ static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsi
 }
 
 extern "C" int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32) {
-  if (!valid_set(set) || !pk || !sk || !seed32) return fail(GMC_EINVAL, "gmc_keypair_seed: bad argument");
-  if (host_keypair(set, pk, sk, seed32)) return fail(GMC_EKEY, "gmc_keypair_seed: key generation failed");
+  if (!valid_id(set) || !pk || !sk || !seed32) return fail(GMC_EINVAL, "gmc_keypair_seed: bad argument");
+  // a plaintext-confirmation variant has the keys of its parameter set
+  if (host_keypair(base_of(set), pk, sk, seed32)) return fail(GMC_EKEY, "gmc_keypair_seed: key generation failed");
   return GMC_OK;
 }
 
@@ -806,6 +823,11 @@ GMC_ONE(460896, 1)
 GMC_ONE(6688128, 2)
 GMC_ONE(6960119, 3)
 GMC_ONE(8192128, 4)
+GMC_ONE(348864pc, 5)
+GMC_ONE(460896pc, 6)
+GMC_ONE(6688128pc, 7)
+GMC_ONE(6960119pc, 8)
+GMC_ONE(8192128pc, 9)
 
 // ---------------------------------------------------------------- host-only views
 // Per-key tables exactly as uploaded, for host-side checks (no GPU needed).
@@ -862,6 +884,7 @@ int gmc::key_prepare_resident(const gmc_key *key) {
 // with a single cudaGraphLaunch.
 struct PlanPipe {
   int set = 0, kind = 0;  // kind 0 enc, 1 dec
+  int pc = 0;             // plaintext-confirmation keys (ciphertexts C0 || C1)
   int engine = GEMM_TC;
   std::vector<int> groups;
   Segs segs{};
@@ -916,14 +939,15 @@ static cudaError_t plan_pipe_kernels(gmc_plan *p, PlanPipe &pp) {
     EncDims d = enc_dims(SET, ref->kw_pad, rows);
     e = enc_sample_gemm_seg<SET>(pp.segs, ref, gk, pp.engine, err, pp.in, pp.w0, pp.w1, pp.w2, d, pp.st);
     if (e == cudaSuccess)
-      e = launch_finalize<SET>(pp.w0, d.lde, pp.w2, d.lds, pp.ct, pp.k, pp.segs, pp.pk_bad_mask, pp.st);
+      e = launch_finalize<SET>(pp.w0, d.lde, pp.w2, d.lds, pp.ct, pp.k, pp.segs, pp.pk_bad_mask, pp.pc != 0, pp.st);
   } else {
     DecDims d = dec_dims(SET, ref->cw_pad, rows);
     DecKeys dk{};
     for (size_t i = 0; i < pp.groups.size(); i++) dk.k[i] = keys[i]->dk;
     e = dec_front_decode_seg<SET>(pp.segs, ref, gk, dk, pp.engine, err, pp.in, pp.w0, pp.w1, pp.sig, pp.w2, pp.ok, d,
-                                  pp.st);
-    if (e == cudaSuccess) e = launch_dec_tail<SET>(pp.w2, d.lde, pp.ok, pp.in, dk, pp.k, pp.rc, pp.segs, pp.st);
+                                  pp.st, pp.pc != 0);
+    if (e == cudaSuccess)
+      e = launch_dec_tail<SET>(pp.w2, d.lde, pp.ok, pp.in, dk, pp.k, pp.rc, pp.segs, pp.pc != 0, pp.st);
   }
   return e;
 }
@@ -945,17 +969,20 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
   gmc_plan *p = new gmc_plan();
   cudaGetDevice(&p->device);
   p->groups.assign(groups, groups + ngroups);
-  // bucket by (set, kind), at most kMaxSegs groups per pipeline
+  // bucket by (set, pc, kind), at most kMaxSegs groups per pipeline
   for (int i = 0; i < ngroups; i++) {
     const gmc_group &g = groups[i];
     if (!g.n) continue;
     PlanPipe *dst = nullptr;
     for (auto &pp : p->pipes)
-      if (pp.set == g.key->set && pp.kind == g.key->kind && pp.groups.size() < (size_t)kMaxSegs) dst = &pp;
+      if (pp.set == g.key->set && pp.pc == g.key->pc && pp.kind == g.key->kind &&
+          pp.groups.size() < (size_t)kMaxSegs)
+        dst = &pp;
     if (!dst) {
       p->pipes.emplace_back();
       dst = &p->pipes.back();
       dst->set = g.key->set;
+      dst->pc = g.key->pc;
       dst->kind = g.key->kind;
       dst->engine = engine_for(dst->set, dst->kind);
     }
@@ -976,12 +1003,13 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
     }
     pp.segs.row0[pp.groups.size()] = row;
     const gmc_key *ref = p->groups[pp.groups[0]].key;
-    const size_t in_b = pp.kind == 0 ? 32 : (size_t)S.synd_bytes;
+    const size_t cb = (size_t)ct_bytes_of(pp.set, pp.pc != 0);
+    const size_t in_b = pp.kind == 0 ? 32 : cb;
     if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.in, row * in_b);
     if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.k, row * 32);
     if (pp.kind == 0) {
       EncDims d = enc_dims(pp.set, ref->kw_pad, row);
-      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.ct, row * S.synd_bytes);
+      if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.ct, row * cb);
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w0, row * d.lde * 4);
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w1, row * d.ldx * 4);
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w2, row * d.lds * 4);
@@ -1017,8 +1045,8 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
   if (e == cudaSuccess) e = cudaEventRecord(p->fork, p->cap);
   for (auto &pp : p->pipes) {
     if (e != cudaSuccess) break;
-    const gmc_setinfo &S = set_info(pp.set);
-    const size_t in_b = pp.kind == 0 ? 32 : (size_t)S.synd_bytes;
+    const size_t cb = (size_t)ct_bytes_of(pp.set, pp.pc != 0);
+    const size_t in_b = pp.kind == 0 ? 32 : cb;
     e = cudaStreamWaitEvent(pp.st, p->fork, 0);
     for (size_t j = 0; j < pp.groups.size() && e == cudaSuccess; j++) {
       const gmc_group &g = p->groups[pp.groups[j]];
@@ -1030,7 +1058,7 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
       const long long r0 = pp.segs.row0[j];
       e = cudaMemcpyAsync(g.k, pp.k + r0 * 32, g.n * 32, cudaMemcpyDeviceToDevice, pp.st);
       if (e == cudaSuccess && pp.kind == 0)
-        e = cudaMemcpyAsync(g.ct, pp.ct + r0 * S.synd_bytes, g.n * S.synd_bytes, cudaMemcpyDeviceToDevice, pp.st);
+        e = cudaMemcpyAsync(g.ct, pp.ct + r0 * cb, g.n * cb, cudaMemcpyDeviceToDevice, pp.st);
       if (e == cudaSuccess && g.rc) {
         if (pp.kind == 0)
           e = cudaMemsetAsync(g.rc, g.key->pad_bad ? 0xFF : 0, g.n * 4, pp.st);  // -1 or 0

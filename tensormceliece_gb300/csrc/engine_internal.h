@@ -8,7 +8,8 @@
 #include "kernels.h"
 
 struct gmc_key {
-  int set = 0;
+  int set = 0;     // parameter set 0..4
+  int pc = 0;      // plaintext-confirmation variant: ciphertexts C0 || SHAKE256(2 || e, 32)
   int kind = 0;  // 0 public, 1 secret
   int device = 0;
   // public key

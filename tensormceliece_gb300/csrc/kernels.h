@@ -110,9 +110,11 @@ template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
                           cudaStream_t st);
+// C rows: synd_bytes, or synd_bytes + 32 with plaintext confirmation (pc):
+// C0 || SHAKE256(2 || e, 32), K = SHAKE256(1 || e || C0 || C1).
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
-                            const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st);
+                            const Segs &segs, uint32_t pk_bad_mask, bool pc, cudaStream_t st);
 
 // Per-key decapsulation state on the device (built once per secret key).
 struct DecKeyDev {
@@ -144,8 +146,9 @@ struct DecKeys {
 
 // Decapsulation: C / K / rc rows in padded row space; X, S2, Sig, E, ok have
 // seg_rows(segs) rows.
+// C rows of synd_bytes (+ 32 with pc); only C0 is packed.
 template <int SET>
-cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int ldx, cudaStream_t st);
+cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int ldx, bool pc, cudaStream_t st);
 // Berlekamp-Massey: S2 (2t packed syndromes) -> Sig [N][2^fft_d] u16, the
 // error locator's coefficients by degree (the leading x^t term is implicit
 // when t = 2^fft_d).
@@ -156,8 +159,10 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
 template <int SET>
 cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
                             const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st);
+// With pc the decoded e must also give SHAKE256(2 || e, 32) = C1 (else implicit
+// rejection), and the session-key preimage covers C0 || C1.
 template <int SET>
 cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, const DecKeys &keys,
-                            uint8_t *K, int *rc, const Segs &segs, cudaStream_t st);
+                            uint8_t *K, int *rc, const Segs &segs, bool pc, cudaStream_t st);
 
 }  // namespace gmc

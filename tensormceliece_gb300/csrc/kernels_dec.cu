@@ -28,9 +28,10 @@ __device__ __forceinline__ uint32_t warp_xor(uint32_t v) {
 }
 
 // ---------------------------------------------------------------- pack_ct
-template <int SET>
+template <int SET, bool PC>
 __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, uint32_t *__restrict__ X, int ldx) {
   using p = P<SET>;
+  constexpr int CB = p::synd_bytes + (PC ? 32 : 0);  // ciphertext row bytes
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long op = idx / ldx;
   const int w = (int)(idx % ldx);
@@ -38,7 +39,7 @@ __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, u
   int seg;
   uint32_t v = 0;  // rows past a segment's live requests stay zero
   if (seg_live(segs, op, &seg)) {
-    const uint8_t *c = C + op * p::synd_bytes;
+    const uint8_t *c = C + op * CB;
 #pragma unroll
     for (int b = 0; b < 4; b++) {
       int x = 4 * w + b;
@@ -761,13 +762,14 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
 }
 
 // ---------------------------------------------------------------- tail
-template <int SET>
+template <int SET, bool PC>
 __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *__restrict__ E, int lde,
                                                                 const int *__restrict__ okin,
                                                                 const uint8_t *__restrict__ Cin, const DecKeys keys,
                                                                 uint8_t *__restrict__ K, int *__restrict__ rc,
                                                                 const Segs segs) {
   using p = P<SET>;
+  constexpr int SB = p::synd_bytes, CB = SB + (PC ? 32 : 0);  // C0 bytes, ciphertext bytes
   __shared__ uint32_t stage[kTailThreads / 32][32 * kStageStride];
   __shared__ const uint32_t *rows[kTailThreads / 32][32];
   const long long N = seg_rows(segs);
@@ -776,26 +778,38 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
   int seg;
   const bool live = seg_live(segs, op, &seg);
   const DecKeyDev &key = keys.k[seg_find(segs, opc)];
-  const bool ok = okin[opc] != 0;
-  const uint8_t *c = Cin + opc * p::synd_bytes;
+  bool ok = okin[opc] != 0;
+  const uint8_t *c = Cin + opc * CB;
+  if constexpr (PC) {
+    // plaintext confirmation (mc:crypto_kem/348864pc/vec/kem_dec.c:43-48): SHAKE256(2 || e, 32) of the
+    // decoded e must equal C1 (its value when decoding failed does not change the outcome)
+    auto none = [](int) -> uint32_t { return 0u; };
+    uint64_t cf[4];
+    kem_hash_staged<p::e_bytes, 1 + p::e_bytes>(cf, 2u, E + opc * lde, none, stage[threadIdx.x >> 5],
+                                                rows[threadIdx.x >> 5]);
+    uint32_t diff = 0;
+#pragma unroll
+    for (int j = 0; j < 32; j++) diff |= (uint32_t)c[SB + j] ^ ((uint32_t)(cf[j >> 3] >> (8 * (j & 7))) & 0xFFu);
+    ok = ok && diff == 0;
+  }
   // b || (e or s) || c; s is the key's n/8 bytes, stored zero-padded to whole words
   const uint32_t *erow = ok ? E + opc * lde : reinterpret_cast<const uint32_t *>(key.s);
   // word loads when every ciphertext row is 4-byte aligned (the buffer and the row length), else bytes
-  const bool c_words = (p::synd_bytes % 4 == 0) && ((reinterpret_cast<uintptr_t>(Cin) & 3) == 0);
+  const bool c_words = (CB % 4 == 0) && ((reinterpret_cast<uintptr_t>(Cin) & 3) == 0);
   auto cword = [&](int w) -> uint32_t {
-    if (c_words) return 4 * w < p::synd_bytes ? reinterpret_cast<const uint32_t *>(c)[w] : 0u;
+    if (c_words) return 4 * w < CB ? reinterpret_cast<const uint32_t *>(c)[w] : 0u;
     uint32_t v = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++)
-      if (4 * w + k < p::synd_bytes) v |= (uint32_t)c[4 * w + k] << (8 * k);
+      if (4 * w + k < CB) v |= (uint32_t)c[4 * w + k] << (8 * k);
     return v;
   };
   uint64_t h[4];
-  kem_hash_staged<p::e_bytes, p::pre_bytes>(h, ok ? 1u : 0u, erow, cword, stage[threadIdx.x >> 5],
-                                            rows[threadIdx.x >> 5]);
+  kem_hash_staged<p::e_bytes, p::pre_bytes + (PC ? 32 : 0)>(h, ok ? 1u : 0u, erow, cword, stage[threadIdx.x >> 5],
+                                                             rows[threadIdx.x >> 5]);
   if (!live) return;
   bool pad_bad = false;
-  if (p::mt % 8) pad_bad = (c[p::synd_bytes - 1] >> (p::mt % 8)) != 0;
+  if (p::mt % 8) pad_bad = (c[SB - 1] >> (p::mt % 8)) != 0;
   uint8_t *k = K + op * 32;
 #pragma unroll
   for (int i = 0; i < 4; i++)
@@ -806,11 +820,14 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
 
 // ---------------------------------------------------------------- launchers
 template <int SET>
-cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int ldx, cudaStream_t st) {
+cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int ldx, bool pc, cudaStream_t st) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   const long long total = N * ldx;
-  pack_ct_kernel<SET><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, segs, X, ldx);
+  if (pc)
+    pack_ct_kernel<SET, true><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, segs, X, ldx);
+  else
+    pack_ct_kernel<SET, false><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(C, segs, X, ldx);
   return cudaGetLastError();
 }
 
@@ -863,22 +880,25 @@ cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, c
 
 template <int SET>
 cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, const DecKeys &keys,
-                            uint8_t *K, int *rc, const Segs &segs, cudaStream_t st) {
+                            uint8_t *K, int *rc, const Segs &segs, bool pc, cudaStream_t st) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
-  dec_tail_kernel<SET><<<(unsigned)((N + kTailThreads - 1) / kTailThreads), kTailThreads, 0, st>>>(
-      E, lde, ok, C, keys, K, rc, segs);
+  const unsigned blocks = (unsigned)((N + kTailThreads - 1) / kTailThreads);
+  if (pc)
+    dec_tail_kernel<SET, true><<<blocks, kTailThreads, 0, st>>>(E, lde, ok, C, keys, K, rc, segs);
+  else
+    dec_tail_kernel<SET, false><<<blocks, kTailThreads, 0, st>>>(E, lde, ok, C, keys, K, rc, segs);
   return cudaGetLastError();
 }
 
 #define GMC_INST_DEC(SET)                                                                                       \
-  template cudaError_t launch_pack_ct<SET>(const uint8_t *, const Segs &, uint32_t *, int, cudaStream_t);       \
+  template cudaError_t launch_pack_ct<SET>(const uint8_t *, const Segs &, uint32_t *, int, bool, cudaStream_t);       \
   template cudaError_t launch_dec_bm<SET>(const uint32_t *, int, FieldDev, const Segs &, uint16_t *,             \
                                          cudaStream_t);                                                          \
   template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, const DecKeys &, FieldDev,  \
                                             const Segs &, uint32_t *, int, int *, cudaStream_t);                 \
   template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, const DecKeys &, \
-                                            uint8_t *, int *, const Segs &, cudaStream_t);
+                                            uint8_t *, int *, const Segs &, bool, cudaStream_t);
 GMC_INST_DEC(0)
 GMC_INST_DEC(1)
 GMC_INST_DEC(2)

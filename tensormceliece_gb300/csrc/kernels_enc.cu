@@ -231,12 +231,13 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
 // c = e[0:mt] xor (T e[mt:n]); K = SHAKE256(1 || e || c). When the public
 // key's padding bits are set (6960119 only), c and K are zeroed
 // (mc:crypto_kem/6960119/vec/kem_enc.c:21-66).
-template <int SET>
+template <int SET, bool PC>
 __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *__restrict__ E, int lde,
                                                                 const uint32_t *__restrict__ S, int lds,
                                                                 uint8_t *__restrict__ C, uint8_t *__restrict__ K,
                                                                 const Segs segs, uint32_t pk_bad_mask) {
   using p = P<SET>;
+  constexpr int SB = p::synd_bytes, CB = SB + (PC ? 32 : 0);  // C0 bytes, ciphertext bytes
   __shared__ uint32_t stage[kTailThreads / 32][32 * kStageStride];
   __shared__ const uint32_t *rows[kTailThreads / 32][32];
   const long long N = seg_rows(segs);
@@ -246,20 +247,46 @@ __global__ void __launch_bounds__(kTailThreads) finalize_kernel(const uint32_t *
   const bool live = seg_live(segs, op, &seg);
   const uint32_t *e = E + opc * lde;
   const uint32_t *sy = S + opc * lds;
-  // c word w: e[0:mt] xor the syndrome, bits from mt on cleared (zero past c)
-  auto cword = [&](int w) -> uint32_t {
+  // C0 word w: e[0:mt] xor the syndrome, bits from mt on cleared (zero past C0)
+  auto c0word = [&](int w) -> uint32_t {
     if (w >= p::mw) return 0u;
     uint32_t v = e[w] ^ sy[w];
     if (w == p::mt / 32 && (p::mt % 32)) v &= (1u << (p::mt % 32)) - 1u;
     return v;
   };
+  // plaintext confirmation: C1 = SHAKE256(2 || e, 32) (mc:crypto_kem/348864pc/vec/kem_enc.c:32)
+  uint64_t h2[4] = {0, 0, 0, 0};
+  if constexpr (PC) {
+    auto none = [](int) -> uint32_t { return 0u; };
+    kem_hash_staged<p::e_bytes, 1 + p::e_bytes>(h2, 2u, e, none, stage[threadIdx.x >> 5], rows[threadIdx.x >> 5]);
+  }
+  auto c1byte = [&](int j) -> uint32_t {
+    const uint64_t v = j < 8 ? h2[0] : j < 16 ? h2[1] : j < 24 ? h2[2] : h2[3];
+    return (uint32_t)(v >> (8 * (j & 7))) & 0xFFu;
+  };
+  auto cbyte = [&](int x) -> uint32_t {
+    if (x < SB) return (c0word(x >> 2) >> (8 * (x & 3))) & 0xFFu;
+    return x < CB ? c1byte(x - SB) : 0u;
+  };
+  // word w of the ciphertext C0 || C1 (zero past it)
+  auto cword = [&](int w) -> uint32_t {
+    if (!PC || 4 * w + 4 <= SB) return c0word(w);
+    if (4 * w >= CB) return 0u;
+    if (SB % 4 == 0) {
+      const int j4 = w - SB / 4;
+      const uint64_t v = j4 < 2 ? h2[0] : j4 < 4 ? h2[1] : j4 < 6 ? h2[2] : h2[3];
+      return (uint32_t)(v >> (32 * (j4 & 1)));
+    }
+    return cbyte(4 * w) | (cbyte(4 * w + 1) << 8) | (cbyte(4 * w + 2) << 16) | (cbyte(4 * w + 3) << 24);
+  };
   uint64_t h[4];
-  kem_hash_staged<p::e_bytes, p::pre_bytes>(h, 1u, e, cword, stage[threadIdx.x >> 5], rows[threadIdx.x >> 5]);
+  kem_hash_staged<p::e_bytes, p::pre_bytes + (PC ? 32 : 0)>(h, 1u, e, cword, stage[threadIdx.x >> 5],
+                                                             rows[threadIdx.x >> 5]);
   if (!live) return;
   const bool pk_bad = (pk_bad_mask >> seg) & 1u;
-  uint8_t *c = C + op * p::synd_bytes;
+  uint8_t *c = C + op * CB;
   uint8_t *k = K + op * 32;
-  for (int x = 0; x < p::synd_bytes; x++) c[x] = pk_bad ? 0 : (uint8_t)(cword(x >> 2) >> (8 * (x & 3)));
+  for (int x = 0; x < CB; x++) c[x] = pk_bad ? 0 : (uint8_t)cbyte(x);
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -341,11 +368,14 @@ cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, i
 
 template <int SET>
 cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int lds, uint8_t *C, uint8_t *K,
-                            const Segs &segs, uint32_t pk_bad_mask, cudaStream_t st) {
+                            const Segs &segs, uint32_t pk_bad_mask, bool pc, cudaStream_t st) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   long long blocks = (N + kTailThreads - 1) / kTailThreads;
-  finalize_kernel<SET><<<(unsigned)blocks, kTailThreads, 0, st>>>(E, lde, S, lds, C, K, segs, pk_bad_mask);
+  if (pc)
+    finalize_kernel<SET, true><<<(unsigned)blocks, kTailThreads, 0, st>>>(E, lde, S, lds, C, K, segs, pk_bad_mask);
+  else
+    finalize_kernel<SET, false><<<(unsigned)blocks, kTailThreads, 0, st>>>(E, lde, S, lds, C, K, segs, pk_bad_mask);
   return cudaGetLastError();
 }
 
@@ -353,7 +383,7 @@ cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int l
   template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int,       \
                                           const GemmKeys *, uint32_t *, int, int, unsigned int *, cudaStream_t); \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
-                                            const Segs &, uint32_t, cudaStream_t);
+                                            const Segs &, uint32_t, bool, cudaStream_t);
 GMC_INST_ENC(0)
 GMC_INST_ENC(1)
 GMC_INST_ENC(2)

@@ -1167,8 +1167,9 @@ done:
 extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seeds,
                                  long long nkeys) {
   using namespace gmc;
-  if (set < 0 || set >= GMC_NSETS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
+  if (set < 0 || set >= GMC_NVARIANTS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
     return kg_fail(GMC_EINVAL, "gmc_keypair_batch: bad argument");
+  set %= GMC_NSETS;  // a plaintext-confirmation variant has the keys of its parameter set
   if (nkeys == 0) return GMC_OK;
   // chain links and rounds are on the critical path (the host waits for each
   // round's ranks); the winners' work only has to finish by the end

@@ -192,7 +192,7 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
                                 tc_err_word_ptr(), pst);
     }
     if (e == cudaSuccess)
-      e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, pst);
+      e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, false, pst);
     return e;
   }
   const int cw = ref->cw_pad, s2 = round_up((2 * S.t * S.m + 31) / 32, 4);
@@ -210,14 +210,14 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   if (field_tables(SET, &fd) != GMC_OK) return cudaErrorUnknown;
   DecKeys dk{};
   for (size_t i = 0; i < pp.keys.size(); i++) dk.k[i] = pp.keys[i]->dk;
-  cudaError_t e = launch_pack_ct<SET>(in, pp.segs, X, cw, pst);
+  cudaError_t e = launch_pack_ct<SET>(in, pp.segs, X, cw, false, pst);
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->ldf, ref->frows_pad, X, cw, ref->cw_pad, S2, s2, p::s2w,
                             tc_err_word_ptr(), pst);
   if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst);
   if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst);
   if (e == cudaSuccess)
-    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, pst);
+    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, false, pst);
   return e;
 }
 
@@ -568,6 +568,9 @@ extern "C" int gmc_server_create(gmc_server **out, long long max_batch, int slot
 
 extern "C" int gmc_server_add_key(gmc_server *s, const gmc_key *key) {
   if (!s || !key) return srv_fail(GMC_EINVAL, "gmc_server_add_key: bad argument");
+  // the serving loop lays out rows of the five sets' ciphertexts; plaintext-confirmation keys take the
+  // per-key batch calls or grouped plans
+  if (key->pc) return srv_fail(GMC_EINVAL, "gmc_server_add_key: plaintext-confirmation (pc) keys are not served");
   // resident state needed by every engine choice is built now, outside the request path
   int r = key_prepare_resident(key);
   if (r) return r;

@@ -40,6 +40,14 @@ def test_set_table():
         assert gmc.lib().gmc_set_id(name.encode()) == sid
         assert gmc.lib().gmc_set_id(("mceliece" + name).encode()) == sid
     assert gmc.lib().gmc_set_id(b"nope") == -1
+    # plaintext-confirmation variants: ids 5..9, same keys, 32 more ciphertext bytes
+    for i, name in enumerate(SETS):
+        sid = 5 + i
+        assert gmc.lib().gmc_set_id((name + "pc").encode()) == sid
+        assert gmc.lib().gmc_set_name(sid) == (name + "pc").encode()
+        z = gmc.set_sizes(sid)
+        assert z == O.sizes(sid) and z["ct_bytes"] == gmc.set_sizes(i)["ct_bytes"] + 32
+    assert gmc.lib().gmc_set_name(10) is None
 
 
 def test_no_gpu_fails_loudly():

@@ -20,6 +20,17 @@ KAT = {
                 "15c6727d4f4867487a54bbb208c06c1142a56a7937d7b598c05f63801cbdd277"),
     "8192128": ("debad73db5027e8239b7e97d04c5a98b7521caba8ea4e58581c90efb50dd4b9e",
                 "5e64e0aeb5ab566a1efbb2b1127dcbf909ee1b395945f066cd5f097a85f2e135"),
+    # plaintext-confirmation variants (kem_<set>pc_checksums, e.g. :5021 for 348864pc, :3205 for 8192128pc)
+    "348864pc": ("ddfa65df30bee9c97e153089d24cce158a7979aa01ebdbb7bf374da13bd81feb",
+                 "9866af598e967b1b3903d9e125bf756a92aed474f750678238b2bb52129cd213"),
+    "460896pc": ("e27bb3f53c37eaaef460488d21750a80baf3874b0b26b23e510325e45c31c560",
+                 "99fe694290b1e02673ad7f1b69ce51aa94406ba23cdf77e69012f0b2fbcebaba"),
+    "6688128pc": ("f6d44759e9e52330923b5dc2957cd080c10b31990a96e0540c52ba42017fa849",
+                  "53e96db3d38fe59717c537c269eddb0474e0548e964d2fbfbc1082ef03e68857"),
+    "6960119pc": ("f164d7a16ea6175870f34056b211d4d45a2bc95085759e2f688721f3fbf326c8",
+                  "7f2438a79d20ae3b056f2d13bca43ea7c1ba2a2e0535cc35f7016188910a4720"),
+    "8192128pc": ("a9d56a17b9b870e832cddde5c5787b55ada2189992d03eb75e23e710bcb98ccd",
+                  "ac060fe5c1bdb9bd96bfa21ad4875cacb61f8e4eed791511020db06c65909811"),
 }
 
 
