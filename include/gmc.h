@@ -28,17 +28,24 @@ extern "C" {
 typedef struct gmc_key gmc_key;
 
 /* ---- parameter sets --------------------------------------------------
- * Set ids 0..4: 348864, 460896, 6688128, 6960119, 8192128 (gmc_set_count()
- * = 5). Ids 5..9 (GMC_NVARIANTS = 10): the plaintext-confirmation ("pc")
- * variants of the same five sets (mc:crypto_kem/<set>pc): identical keys,
- * ciphertexts C0 || C1 with C1 = SHAKE256(2 || e, 32) (32 bytes longer), the
- * session key hashed over C0 || C1, and decapsulation also rejecting when C1
- * does not match the decoded e. Every entry point taking a set id or a key
- * accepts both, except the serving loop (gmc_server_*), which serves ids 0..4. */
-#define GMC_NVARIANTS 10
+ * Set id = s + 5 v for parameter set s (0 = 348864, 1 = 460896, 2 = 6688128,
+ * 3 = 6960119, 4 = 8192128; gmc_set_count() = 5) and variant v
+ * (GMC_NVARIANTS = 20 ids), as libmceliece's crypto_kem/<set><variant>:
+ *   v = 0  the set itself;
+ *   v = 1  "pc", plaintext confirmation: the same keys; ciphertexts
+ *          C0 || C1 with C1 = SHAKE256(2 || e, 32) (32 bytes longer), the
+ *          session key hashed over C0 || C1, decapsulation also rejecting
+ *          when C1 does not match the decoded e;
+ *   v = 2  "f": semi-systematic key generation (different keys, the same
+ *          encapsulation and decapsulation as the set);
+ *   v = 3  "pcf": both.
+ * Every entry point taking a set id or a key accepts all of them, except the
+ * serving loop (gmc_server_*), which serves keys without plaintext
+ * confirmation. */
+#define GMC_NVARIANTS 20
 int gmc_set_count(void);
 const char *gmc_set_name(int set);
-/* looks up "348864", "mceliece348864", "8192128pc", ...; returns the id or GMC_EINVAL */
+/* looks up "348864", "mceliece348864", "8192128pc", "6960119pcf", ...; returns the id or GMC_EINVAL */
 int gmc_set_id(const char *name);
 /* out[8] = m, n, t, mt, k, public-key bytes, secret-key bytes, ciphertext bytes */
 int gmc_set_sizes(int set, long long *out);
@@ -194,6 +201,37 @@ int gmc_kem_6960119pc_dec(unsigned char *k, const unsigned char *c, const unsign
 void gmc_kem_8192128pc_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_8192128pc_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_8192128pc_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+/* semi-systematic key generation (mc:crypto_kem/<set>f, <set>pcf) */
+void gmc_kem_348864f_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_348864f_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_348864f_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_460896f_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_460896f_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_460896f_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6688128f_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_6688128f_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6688128f_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6960119f_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_6960119f_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6960119f_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_8192128f_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_8192128f_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_8192128f_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_348864pcf_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_348864pcf_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_348864pcf_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_460896pcf_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_460896pcf_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_460896pcf_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6688128pcf_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_6688128pcf_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6688128pcf_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_6960119pcf_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_6960119pcf_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_6960119pcf_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
+void gmc_kem_8192128pcf_keypair(unsigned char *pk, unsigned char *sk);
+int gmc_kem_8192128pcf_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
+int gmc_kem_8192128pcf_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
 
 /* randombytes source of the one-request enc entry points
  * (librandombytes' randombytes(), rb:include/randombytes.h:10). NULL restores

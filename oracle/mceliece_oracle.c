@@ -55,13 +55,15 @@ typedef struct {
   int m, n, t, mt, k, q; /* q = 2^m */
   int pk_row_bytes, synd_bytes, cond_bytes, irr_bytes, e_bytes;
   long pk_bytes, sk_bytes;
-  int pc;       /* plaintext-confirmation variant (ids GMO_NSETS ..): c = C0 || C1 */
+  int pc;       /* plaintext-confirmation variant: c = C0 || C1 */
+  int f;        /* semi-systematic key generation ("f" variants) */
   int ct_bytes; /* synd_bytes, + 32 with plaintext confirmation */
 } sizes;
 
-/* Set ids 0..4 are the five parameter sets, GMO_NSETS + s their "pc"
- * variants (mc:crypto_kem/<set>pc): the same keys, ciphertexts C0 || C1 with
- * C1 = SHAKE256(2 || e, 32). */
+/* Set id = s + GMO_NSETS * v for parameter set s and variant v: 0 the set
+ * itself, 1 "pc" (mc:crypto_kem/<set>pc: the same keys, ciphertexts C0 || C1
+ * with C1 = SHAKE256(2 || e, 32)), 2 "f" (mc:crypto_kem/<set>f: semi-systematic
+ * key generation, the same enc/dec), 3 "pcf" (both). */
 static int get_sizes(int set, sizes *P) {
   if (set < 0 || set >= GMO_NVARIANTS) return -1;
   const setdef *S = &SETS[set % GMO_NSETS];
@@ -76,7 +78,8 @@ static int get_sizes(int set, sizes *P) {
   P->e_bytes = S->n / 8;
   P->pk_bytes = (long)P->mt * P->pk_row_bytes;
   P->sk_bytes = 40 + P->irr_bytes + P->cond_bytes + P->e_bytes;
-  P->pc = set >= GMO_NSETS;
+  P->pc = (set / GMO_NSETS) & 1;
+  P->f = (set / GMO_NSETS) >> 1;
   P->ct_bytes = P->synd_bytes + (P->pc ? 32 : 0);
   return 0;
 }
@@ -343,11 +346,58 @@ static int genpoly(const setdef *S, const field *F, gf *g, const gf *f) {
   return 0;
 }
 
+static int mat_bit(const uint64_t *row, int c) { return (int)((row[c / 64] >> (c % 64)) & 1); }
+static void mat_swap_cols(uint64_t *row, int a, int b) {
+  if (mat_bit(row, a) != mat_bit(row, b)) {
+    row[a / 64] ^= 1ULL << (a % 64);
+    row[b / 64] ^= 1ULL << (b % 64);
+  }
+}
+
+/* Semi-systematic step of the "f" variants (mc:crypto_kem/348864f/vec/pk_gen.c,
+ * mov_columns; 6960119f at an unaligned row): with the first R = mt - 32
+ * columns reduced, the last 32 rows' 32 x 64 block at columns R .. R+63
+ * gives pivot columns c_0 < ... < c_31 (leftmost, by elimination on that
+ * block; fail when its rank is below 32); pivots = sum 2^c_j; for j = 0..31
+ * in turn, columns R+j and R+c_j of every row and pi[R+j], pi[R+c_j] are
+ * swapped. */
+static int mov_columns(const sizes *P, uint64_t *mat, int rw, int16_t *pi, uint64_t *pivots) {
+  const int R = P->mt - 32;
+  uint64_t buf[32];
+  int ctz[32];
+  for (int i = 0; i < 32; i++) {
+    buf[i] = 0;
+    for (int c = 0; c < 64; c++)
+      if (R + c < P->n && mat_bit(&mat[(size_t)(R + i) * rw], R + c)) buf[i] |= 1ULL << c;
+  }
+  *pivots = 0;
+  for (int i = 0; i < 32; i++) {
+    uint64_t t = 0;
+    for (int j = i; j < 32; j++) t |= buf[j];
+    if (!t) return -1;
+    int s = __builtin_ctzll(t);
+    ctz[i] = s;
+    *pivots |= 1ULL << s;
+    for (int j = i + 1; j < 32; j++)
+      if (!((buf[i] >> s) & 1)) buf[i] ^= buf[j];
+    for (int j = i + 1; j < 32; j++)
+      if ((buf[j] >> s) & 1) buf[j] ^= buf[i];
+  }
+  for (int j = 0; j < 32; j++) {
+    if (ctz[j] == j) continue;
+    int16_t tmp = pi[R + j]; pi[R + j] = pi[R + ctz[j]]; pi[R + ctz[j]] = tmp;
+    for (int r = 0; r < P->mt; r++) mat_swap_cols(&mat[(size_t)r * rw], R + j, R + ctz[j]);
+  }
+  return 0;
+}
+
 /* Public key: systematic form [I_mt | T] of the parity-check matrix with rows
  * (i*m+b) = bit b of L_j^i / g(L_j); pk stores T row-major, PK_ROW_BYTES per
  * row, little-endian bit order.  Same output as pk_gen,
- * mc:crypto_kem/348864/vec/pk_gen.c:82 (the RREF is unique). */
-static int pk_gen(const sizes *P, const field *F, uint8_t *pk, const gf *g, const uint32_t *perm, int16_t *pi) {
+ * mc:crypto_kem/348864/vec/pk_gen.c:82 (the RREF is unique). The f variants
+ * insert mov_columns before the last 32 rows (pivots != 0 then). */
+static int pk_gen(const sizes *P, const field *F, uint8_t *pk, const gf *g, const uint32_t *perm, int16_t *pi,
+                  uint64_t *pivots) {
   int m = P->m, n = P->n, t = P->t, mt = P->mt, q = P->q;
   int rw = (n + 63) / 64;
   uint64_t *buf = malloc(sizeof(uint64_t) * (size_t)q);
@@ -374,6 +424,7 @@ static int pk_gen(const sizes *P, const field *F, uint8_t *pk, const gf *g, cons
   free(L); free(inv);
 
   for (int row = 0; row < mt; row++) {
+    if (P->f && row == mt - 32 && mov_columns(P, mat, rw, pi, pivots)) { free(mat); return -1; }
     int w = row / 64; uint64_t bit = 1ULL << (row % 64);
     int piv = -1;
     for (int r = row; r < mt; r++) if (mat[(size_t)r * rw + w] & bit) { piv = r; break; }
@@ -565,13 +616,13 @@ int gmo_keypair_rng(int set, uint8_t *pk, uint8_t *sk, gmo_rng_fn rng, void *ctx
     gf g[GMO_MAX_T + 1];
     memcpy(g, irr, sizeof(gf) * (size_t)P.t);
     g[P.t] = 1;
-    if (pk_gen(&P, F, pk, g, perm, pi)) continue;
+    uint64_t pivots = 0xFFFFFFFFULL;
+    if (pk_gen(&P, F, pk, g, perm, pi, &pivots)) continue;
     if (controlbits(skp, pi, P.m)) { free(r); free(perm); free(pi); return -2; }
     skp += P.cond_bytes;
     memcpy(skp, r, (size_t)P.e_bytes);
-    /* pivot word: store8(sk + 32, 0xFFFFFFFF) */
-    sk[32] = sk[33] = sk[34] = sk[35] = 0xFF;
-    sk[36] = sk[37] = sk[38] = sk[39] = 0;
+    /* pivot word: store8(sk + 32, pivots), 0xFFFFFFFF without the semi-systematic step */
+    for (int i = 0; i < 8; i++) sk[32 + i] = (uint8_t)(pivots >> (8 * i));
     break;
   }
   free(r); free(perm); free(pi);

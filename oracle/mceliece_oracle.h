@@ -16,7 +16,7 @@ extern "C" {
 #endif
 
 #define GMO_NSETS 5
-#define GMO_NVARIANTS 10 /* ids GMO_NSETS + s: the plaintext-confirmation ("pc") variant of set s */
+#define GMO_NVARIANTS 20 /* id s + GMO_NSETS v: set s, variant v = 0 plain, 1 pc, 2 f, 3 pcf */
 #define GMO_MAX_N 8192
 #define GMO_MAX_T 128
 #define GMO_MAX_M 13

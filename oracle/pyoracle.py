@@ -13,8 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libmceliece_oracle.so")
 SETS = ("348864", "460896", "6688128", "6960119", "8192128")
-# plaintext-confirmation variants: ids 5..9, the same keys as the base set
-VARIANTS = SETS + tuple(s + "pc" for s in SETS)
+# variants: id = set + 5 v, v = 0 plain, 1 pc (same keys), 2 f (semi-systematic keys), 3 pcf
+VARIANTS = tuple(s + v for v in ("", "pc", "f", "pcf") for s in SETS)
 _lib = None
 
 

@@ -24,8 +24,9 @@ __all__ = [
 ]
 
 SETS = ("348864", "460896", "6688128", "6960119", "8192128")
-# set ids 5..9: the plaintext-confirmation ("pc") variants of SETS (same keys, ciphertexts 32 bytes longer)
-VARIANTS = SETS + tuple(s + "pc" for s in SETS)
+# set id = set + 5 v: v = 0 the set, 1 "pc" (plaintext confirmation: same keys, ciphertexts 32 bytes longer),
+# 2 "f" (semi-systematic keys, same enc/dec), 3 "pcf"
+VARIANTS = tuple(s + v for v in ("", "pc", "f", "pcf") for s in SETS)
 GEMM_POPC, GEMM_B1MMA, GEMM_TC, GEMM_SPARSE = 0, 1, 2, 3
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of device memory", -4: "bad key"}
 

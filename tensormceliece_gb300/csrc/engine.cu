@@ -175,10 +175,13 @@ static int get_field(int set, FieldDev *out) {
 }
 
 static bool valid_set(int set) { return set >= 0 && set < GMC_NSETS; }
-// public set ids: 0..4 the parameter sets, GMC_NSETS + s the plaintext-confirmation variant of s
+// public set ids: s + GMC_NSETS v for parameter set s and variant v = 0 (the set), 1 pc
+// (plaintext confirmation), 2 f (semi-systematic keys), 3 pcf
 static bool valid_id(int id) { return id >= 0 && id < GMC_NVARIANTS; }
 static int base_of(int id) { return id % GMC_NSETS; }
-static bool pc_of(int id) { return id >= GMC_NSETS; }
+static int variant_of(int id) { return id / GMC_NSETS; }
+static bool pc_of(int id) { return (variant_of(id) & 1) != 0; }
+static bool semi_of(int id) { return (variant_of(id) & 2) != 0; }
 static long long ct_bytes_of(int set, bool pc) { return set_info(set).synd_bytes + (pc ? 32 : 0); }
 static long long ct_bytes_of(const gmc_key *k) { return ct_bytes_of(k->set, k->pc != 0); }
 
@@ -233,11 +236,11 @@ static cudaError_t key_a8(const gmc_key *kc, cudaStream_t st, const uint8_t **ou
 
 
 extern "C" int gmc_set_count(void) { return GMC_NSETS; }
-static const char *const kPcNames[GMC_NSETS] = {"348864pc", "460896pc", "6688128pc", "6960119pc", "8192128pc"};
-extern "C" const char *gmc_set_name(int set) {
-  if (!valid_id(set)) return nullptr;
-  return pc_of(set) ? kPcNames[base_of(set)] : set_info(set).name;
-}
+static const char *const kVariantNames[GMC_NVARIANTS] = {
+    "348864",    "460896",    "6688128",    "6960119",    "8192128",    "348864pc",  "460896pc",
+    "6688128pc", "6960119pc", "8192128pc",  "348864f",    "460896f",    "6688128f",  "6960119f",
+    "8192128f",  "348864pcf", "460896pcf",  "6688128pcf", "6960119pcf", "8192128pcf"};
+extern "C" const char *gmc_set_name(int set) { return valid_id(set) ? kVariantNames[set] : nullptr; }
 extern "C" int gmc_set_id(const char *name) {
   if (!name) return GMC_EINVAL;
   if (!strncmp(name, "mceliece", 8)) name += 8;
@@ -263,6 +266,7 @@ extern "C" int gmc_pk_load(gmc_key **out, int id, const unsigned char *pk) {
   k->a8_mu = new std::mutex();
   k->set = set;
   k->pc = pc_of(id);
+  k->variant = variant_of(id);
   k->kind = 0;
   cudaGetDevice(&k->device);
   k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad; k->ldtt = h.ldtt;
@@ -295,6 +299,7 @@ extern "C" int gmc_sk_load(gmc_key **out, int id, const unsigned char *sk) {
   k->a8_mu = new std::mutex();
   k->set = set;
   k->pc = pc_of(id);
+  k->variant = variant_of(id);
   k->kind = 1;
   cudaGetDevice(&k->device);
   k->ldf = h.ldf; k->frows_pad = h.frows_pad; k->cw_pad = h.cw_pad;
@@ -344,7 +349,7 @@ extern "C" void gmc_key_free(gmc_key *key) {
   delete key;
 }
 
-extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set + (key->pc ? GMC_NSETS : 0) : GMC_EINVAL; }
+extern "C" int gmc_key_set(const gmc_key *key) { return key ? key->set + GMC_NSETS * key->variant : GMC_EINVAL; }
 
 extern "C" int gmc_set_gemm_engine(int engine) {
   if (engine < -1 || engine > GEMM_SPARSE) return fail(GMC_EINVAL, "gmc_set_gemm_engine: unknown engine");
@@ -796,8 +801,9 @@ static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsi
 
 extern "C" int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32) {
   if (!valid_id(set) || !pk || !sk || !seed32) return fail(GMC_EINVAL, "gmc_keypair_seed: bad argument");
-  // a plaintext-confirmation variant has the keys of its parameter set
-  if (host_keypair(base_of(set), pk, sk, seed32)) return fail(GMC_EKEY, "gmc_keypair_seed: key generation failed");
+  // a plaintext-confirmation variant has the keys of its parameter set; f variants the semi-systematic form
+  if (host_keypair(base_of(set), pk, sk, seed32, semi_of(set)))
+    return fail(GMC_EKEY, "gmc_keypair_seed: key generation failed");
   return GMC_OK;
 }
 
@@ -828,6 +834,16 @@ GMC_ONE(460896pc, 6)
 GMC_ONE(6688128pc, 7)
 GMC_ONE(6960119pc, 8)
 GMC_ONE(8192128pc, 9)
+GMC_ONE(348864f, 10)
+GMC_ONE(460896f, 11)
+GMC_ONE(6688128f, 12)
+GMC_ONE(6960119f, 13)
+GMC_ONE(8192128f, 14)
+GMC_ONE(348864pcf, 15)
+GMC_ONE(460896pcf, 16)
+GMC_ONE(6688128pcf, 17)
+GMC_ONE(6960119pcf, 18)
+GMC_ONE(8192128pcf, 19)
 
 // ---------------------------------------------------------------- host-only views
 // Per-key tables exactly as uploaded, for host-side checks (no GPU needed).

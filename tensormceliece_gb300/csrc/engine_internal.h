@@ -10,6 +10,7 @@
 struct gmc_key {
   int set = 0;     // parameter set 0..4
   int pc = 0;      // plaintext-confirmation variant: ciphertexts C0 || SHAKE256(2 || e, 32)
+  int variant = 0; // public id = set + GMC_NSETS * variant (0 plain, 1 pc, 2 f, 3 pcf)
   int kind = 0;  // 0 public, 1 secret
   int device = 0;
   // public key

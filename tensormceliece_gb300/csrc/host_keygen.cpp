@@ -157,8 +157,51 @@ static uint16_t bitrev_m(uint16_t a, int m) {
   return r;
 }
 
+// Semi-systematic step of the "f" variants (mc:crypto_kem/348864f/vec/pk_gen.c,
+// mov_columns): with the first R = mt - 32 columns reduced, the last 32 rows'
+// 32 x 64 block at columns R .. R+63 gives leftmost pivot columns c_0 < ... <
+// c_31 (rejection below rank 32); pivots = sum 2^c_j, and for j = 0..31 in
+// turn columns R+j, R+c_j of every row and pi[R+j], pi[R+c_j] trade places.
+static bool move_pivot_columns(const gmc_setinfo &S, std::vector<uint64_t> &mat, int rw, std::vector<int16_t> &pi,
+                               uint64_t *pivots) {
+  const int R = S.mt - 32;
+  auto bit = [&](int r, int c) { return (int)((mat[(size_t)r * rw + c / 64] >> (c % 64)) & 1); };
+  uint64_t buf[32];
+  int c_of[32];
+  for (int i = 0; i < 32; i++) {
+    buf[i] = 0;
+    for (int c = 0; c < 64; c++)
+      if (bit(R + i, R + c)) buf[i] |= 1ull << c;
+  }
+  *pivots = 0;
+  for (int i = 0; i < 32; i++) {
+    uint64_t t = 0;
+    for (int j = i; j < 32; j++) t |= buf[j];
+    if (!t) return false;
+    const int s = __builtin_ctzll(t);
+    c_of[i] = s;
+    *pivots |= 1ull << s;
+    int piv = i;
+    while (!((buf[piv] >> s) & 1)) piv++;
+    std::swap(buf[i], buf[piv]);
+    for (int j = i + 1; j < 32; j++)
+      if ((buf[j] >> s) & 1) buf[j] ^= buf[i];
+  }
+  for (int j = 0; j < 32; j++) {
+    const int a = R + j, b = R + c_of[j];
+    if (a == b) continue;
+    std::swap(pi[a], pi[b]);
+    for (int r = 0; r < S.mt; r++)
+      if (bit(r, a) != bit(r, b)) {
+        mat[(size_t)r * rw + a / 64] ^= 1ull << (a % 64);
+        mat[(size_t)r * rw + b / 64] ^= 1ull << (b % 64);
+      }
+  }
+  return true;
+}
+
 static bool public_key(const gmc_setinfo &S, const HostField &F, const uint16_t *g, const uint32_t *perm,
-                       std::vector<int16_t> &pi, uint8_t *pk) {
+                       std::vector<int16_t> &pi, uint8_t *pk, bool semi, uint64_t *pivots) {
   const int m = S.m, n = S.n, t = S.t, mt = S.mt, q = S.q;
   std::vector<uint64_t> buf(q);
   for (int i = 0; i < q; i++) buf[i] = ((uint64_t)perm[i] << 31) | (uint64_t)i;
@@ -183,6 +226,7 @@ static bool public_key(const gmc_setinfo &S, const HostField &F, const uint16_t 
     for (int j = 0; j < n; j++) inv[j] = F.mul(inv[j], L[j]);
   }
   for (int row = 0; row < mt; row++) {
+    if (semi && row == mt - 32 && !move_pivot_columns(S, mat, rw, pi, pivots)) return false;
     const int w = row / 64;
     const uint64_t bit = 1ull << (row % 64);
     int piv = -1;
@@ -317,7 +361,7 @@ static bool control_bits(uint8_t *out, const std::vector<int16_t> &pi, int w) {
   return true;
 }
 
-int host_keypair(int set, uint8_t *pk, uint8_t *sk, const uint8_t delta32[32]) {
+int host_keypair(int set, uint8_t *pk, uint8_t *sk, const uint8_t delta32[32], bool semi) {
   const gmc_setinfo &S = set_info(set);
   const HostField &F = host_field(S.m);
   uint8_t seed[33];
@@ -346,12 +390,12 @@ int host_keypair(int set, uint8_t *pk, uint8_t *sk, const uint8_t delta32[32]) {
     for (int i = 0; i < S.q; i++)
       perm[i] = (uint32_t)rp[4 * i] | ((uint32_t)rp[4 * i + 1] << 8) | ((uint32_t)rp[4 * i + 2] << 16) |
                 ((uint32_t)rp[4 * i + 3] << 24);
-    if (!public_key(S, F, g.data(), perm.data(), pi, pk)) continue;
+    uint64_t pivots = 0xFFFFFFFFull;
+    if (!public_key(S, F, g.data(), perm.data(), pi, pk, semi, &pivots)) continue;
     if (!control_bits(skp, pi, S.m)) return -1;
     skp += S.cond_bytes;
     memcpy(skp, r.data(), S.e_bytes);
-    sk[32] = sk[33] = sk[34] = sk[35] = 0xFF;
-    sk[36] = sk[37] = sk[38] = sk[39] = 0;
+    for (int i = 0; i < 8; i++) sk[32 + i] = (uint8_t)(pivots >> (8 * i));  // 0xFFFFFFFF unless semi-systematic
     return 0;
   }
   return -1;

@@ -410,15 +410,17 @@ template <int SET, int TB> struct ElimSmem {
   static constexpr int colw = pw + 32 * 32;           // mt u32
   static constexpr int wk = colw + C::mt;             // mt u32
   static constexpr int binv = wk + C::mt;             // 32 u32
-  static constexpr int misc = binv + 32;              // 4 ints: candidate, failure, search mode
-  static constexpr int rowid_u32 = misc + 4;          // mt u16
+  static constexpr int misc = binv + 32;              // 4 ints: candidate, failure, search mode; 32: pivot columns
+  static constexpr int rowid_u32 = misc + 36;         // mt u16
   static constexpr int bytes = rowid_u32 * 4 + C::mt * 2 + 16;
 };
 template <int SET, int TB>
 __global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_kernel(uint32_t *__restrict__ mat, int ld, int nwords,
                                                                   const int *__restrict__ att_of,
                                                                   uint8_t *__restrict__ status, int need, int set_bit,
-                                                                  int forward, int cl, uint16_t *__restrict__ rowid_out) {
+                                                                  int forward, int cl, uint16_t *__restrict__ rowid_out,
+                                                                  int semi, uint8_t *__restrict__ clist_out,
+                                                                  uint16_t *__restrict__ pi_all) {
   using C = KG<SET>;
   using L = ElimSmem<SET, TB>;
   constexpr int MT = C::mt, NT = ElimCfg<TB>::nt;
@@ -436,10 +438,62 @@ __global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_ke
   uint32_t *A = mat + (long long)slot * MT * ld;
   for (int i = tid; i < MT; i += NT) rowid[i] = (uint16_t)i;
   const int ngroups = nwords / 32;
-  for (int p = 0; p < C::npanel; p++) {
-    const int base = 32 * p, np = min(32, MT - base);
+  // Panels of up to 32 columns from column (= pivot row position) base. The
+  // semi-systematic form ("f" variants) ends the regular panels at R = mt - 32
+  // and takes the last 32 pivots as the leftmost independent columns of the
+  // 64-column window from R (mc:crypto_kem/348864f/vec/pk_gen.c, mov_columns).
+  const int R = semi ? MT - 32 : MT;
+  int *clist = misc + 4;  // the window's pivot columns (offsets from R)
+  for (int base = 0; base < MT;) {
+    const bool fpanel = semi && base == R;
+    const int np = fpanel ? 32 : min(32, (base < R ? R : MT) - base);
     const uint32_t npmask = np == 32 ? 0xffffffffu : ((1u << np) - 1);
-    for (int pos = tid; pos < MT; pos += NT) colw[pos] = A[(long long)rowid[pos] * ld + p];
+    const int pw0 = base >> 5, psh = base & 31;
+    // 32 bits of a row from column base + 32 h (a funnel of two words when base is unaligned)
+    auto bits32 = [&](const uint32_t *row, int h) -> uint32_t {
+      uint32_t v = row[pw0 + h] >> psh;
+      if (psh) v |= row[pw0 + h + 1] << (32 - psh);
+      return v;
+    };
+    if (fpanel) {
+      // the 32 remaining rows' window (warp 0, lane = row): leftmost pivot columns
+      if (warp == 0) {
+        const uint32_t *row = A + (long long)rowid[base + lane] * ld;
+        uint64_t w = (uint64_t)bits32(row, 0) | ((uint64_t)bits32(row, 1) << 32);
+        int mode = 0;
+        for (int i = 0; i < 32; i++) {
+          const uint64_t live = lane >= i ? w : 0;
+          const uint32_t lo = __reduce_or_sync(0xffffffffu, (uint32_t)live);
+          const uint32_t hi = __reduce_or_sync(0xffffffffu, (uint32_t)(live >> 32));
+          if (!lo && !hi) {
+            mode = 2;  // rank below 32: the library rejects the attempt
+            break;
+          }
+          const int sidx = lo ? __ffs(lo) - 1 : 32 + __ffs(hi) - 1;
+          if (lane == 0) clist[i] = sidx;
+          const uint32_t bal = __ballot_sync(0xffffffffu, lane >= i && ((w >> sidx) & 1));
+          const int pl = __ffs(bal) - 1;
+          const uint64_t wp = __shfl_sync(0xffffffffu, w, pl), wi = __shfl_sync(0xffffffffu, w, i);
+          if (lane == i) w = wp;
+          else if (lane == pl) w = wi;
+          if (lane > i && ((w >> sidx) & 1)) w ^= wp;
+        }
+        if (lane == 0) misc[2] = mode;
+      }
+      __syncthreads();
+      if (misc[2] == 2) return;
+      // every row's coefficients: its bits at the 32 pivot columns
+      for (int pos = tid; pos < MT; pos += NT) {
+        const uint32_t *row = A + (long long)rowid[pos] * ld;
+        const uint64_t w = (uint64_t)bits32(row, 0) | ((uint64_t)bits32(row, 1) << 32);
+        uint32_t v = 0;
+#pragma unroll 8
+        for (int j = 0; j < 32; j++) v |= (uint32_t)((w >> clist[j]) & 1) << j;
+        colw[pos] = v;
+      }
+      __syncthreads();
+    } else {
+    for (int pos = tid; pos < MT; pos += NT) colw[pos] = bits32(A + (long long)rowid[pos] * ld, 0);
     __syncthreads();
     // Pivot search, first in the window of positions base .. base+63 (warp 0,
     // slots in registers: forward elimination on the panel word, slot tags
@@ -531,6 +585,7 @@ __global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_ke
         __syncthreads();
       }
     }
+    }  // regular panel
     // B^-1 for the pivot rows' original panel words (warp 0, lane = row)
     if (warp == 0) {
       uint32_t b = lane < np ? (colw[base + lane] & npmask) : 0;
@@ -552,7 +607,7 @@ __global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_ke
     // every CTA of the cluster has read the panel words before any updates them
     if (cl > 1) kg_cluster_sync();
     else __syncthreads();
-    for (int g = (p >> 5) + ((crank - (p >> 5)) % cl + cl) % cl; g < ngroups; g += cl) {
+    for (int g = (pw0 >> 5) + ((crank - (pw0 >> 5)) % cl + cl) % cl; g < ngroups; g += cl) {
       const int w0 = 32 * g;
       for (int i = tid; i < 1024; i += NT) {
         const int b = i >> 5;
@@ -643,10 +698,24 @@ __global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_ke
       __syncthreads();
     }
     if (cl > 1) kg_cluster_sync();  // the next panel word is final in every row
+    base += np;
   }
   if (crank) return;
   if (rowid_out)
     for (int i = tid; i < MT; i += NT) rowid_out[(long long)slot * MT + i] = rowid[i];
+  if (semi && tid == 0) {
+    if (clist_out)
+      for (int j = 0; j < 32; j++) clist_out[(long long)slot * 32 + j] = (uint8_t)clist[j];
+    // the support follows the library's column swaps: pi[R + j] <-> pi[R + c_j], j = 0..31 in turn
+    if (pi_all) {
+      uint16_t *pi = pi_all + (long long)att * C::q;
+      for (int j = 0; j < 32; j++) {
+        const uint16_t x = pi[R + j];
+        pi[R + j] = pi[R + clist[j]];
+        pi[R + clist[j]] = x;
+      }
+    }
+  }
   if (tid == 0) status[att] |= (uint8_t)set_bit;
 }
 
@@ -808,12 +877,31 @@ template <int SET>
 __global__ void kg_assemble_kernel(const int *__restrict__ att_of, const int *__restrict__ out_of, int nwin,
                                    const uint8_t *const *__restrict__ rptr, const uint16_t *__restrict__ gall,
                                    const uint8_t *__restrict__ cond, const uint32_t *__restrict__ matF,
-                                   const uint16_t *__restrict__ rowid, uint8_t *__restrict__ pk_out,
-                                   uint8_t *__restrict__ sk_out) {
+                                   const uint16_t *__restrict__ rowid, const uint8_t *__restrict__ clist,
+                                   uint8_t *__restrict__ pk_out, uint8_t *__restrict__ sk_out) {
   using C = KG<SET>;
+  constexpr int R = C::mt - 32;
+  __shared__ uint8_t src_of[64];  // semi-systematic form: original column offset (from R) at each window position
+  __shared__ uint64_t pivots;
   const int w = blockIdx.y;
   if (w >= nwin) return;
   const int att = att_of[w];
+  if (threadIdx.x == 0) {
+    pivots = 0xFFFFFFFFull;
+    if (clist) {
+      // the library's swaps, positions R+j and R+c_j for j = 0..31 in turn
+      for (int j = 0; j < 64; j++) src_of[j] = (uint8_t)j;
+      pivots = 0;
+      for (int j = 0; j < 32; j++) {
+        const int c = clist[(long long)w * 32 + j];
+        const uint8_t x = src_of[j];
+        src_of[j] = src_of[c];
+        src_of[c] = x;
+        pivots |= 1ull << c;
+      }
+    }
+  }
+  __syncthreads();
   const long long pkb = C::pk_bytes, skb = C::sk_bytes;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < pkb + skb; i += stride) {
@@ -821,15 +909,24 @@ __global__ void kg_assemble_kernel(const int *__restrict__ att_of, const int *__
       const int row = (int)(i / C::pk_row_bytes), byte = (int)(i - (long long)row * C::pk_row_bytes);
       const uint32_t *src = matF + ((long long)w * C::mt + rowid[(long long)w * C::mt + row]) * C::rw;
       const int bp = C::mt + 8 * byte, wd = bp >> 5, sh = bp & 31;
-      uint32_t v = src[wd] >> sh;
-      if (sh > 24) v |= src[wd + 1] << (32 - sh);
+      uint32_t v;
+      if (clist && bp < R + 64) {
+        v = 0;
+        for (int u = 0; u < 8; u++) {
+          const int q = bp + u;
+          const int col = q < R + 64 ? R + src_of[q - R] : q;
+          if (q < C::n) v |= ((src[col >> 5] >> (col & 31)) & 1u) << u;
+        }
+      } else {
+        v = src[wd] >> sh;
+        if (sh > 24) v |= src[wd + 1] << (32 - sh);
+      }
       pk_out[(long long)out_of[w] * pkb + i] = (uint8_t)v;
     } else {
       const int o = (int)(i - pkb);
       uint8_t v;
       if (o < 32) v = rptr[att][C::dofs + o];
-      else if (o < 36) v = 0xff;
-      else if (o < 40) v = 0;
+      else if (o < 40) v = (uint8_t)(pivots >> (8 * (o - 32)));
       else if (o < 40 + 2 * C::t) {
         const uint16_t gv = gall[(long long)att * C::gstride + ((o - 40) >> 1)];
         v = (uint8_t)(((o - 40) & 1) ? gv >> 8 : gv);
@@ -912,8 +1009,8 @@ struct KgBlock {
 };
 
 template <int SET>
-int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, cudaStream_t s0, cudaStream_t s1,
-                  cudaStream_t s2) {
+int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkeys, bool semi, cudaStream_t s0,
+                  cudaStream_t s1, cudaStream_t s2) {
   using C = KG<SET>;
   int rc = GMC_OK;
   FieldDev fd{};
@@ -926,7 +1023,7 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
   uint8_t *d_seedc = nullptr;
   uint32_t *d_matF = nullptr;
   uint16_t *d_rowid = nullptr;
-  uint8_t *d_cond = nullptr, *d_cbok = nullptr, *d_pk = nullptr, *d_sk = nullptr;
+  uint8_t *d_cond = nullptr, *d_cbok = nullptr, *d_pk = nullptr, *d_sk = nullptr, *d_clist = nullptr;
   std::vector<long long> pending, next;
   std::vector<int> na;
   std::vector<uint8_t> h_cbok;
@@ -958,6 +1055,7 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
   KG_CUDA(dalloc(&d_matF, (size_t)wcap * C::mt * C::rw, s1));
   KG_CUDA(dalloc(&d_rowid, (size_t)wcap * C::mt, s1));
   KG_CUDA(dalloc(&d_cond, (size_t)wcap * C::cond_bytes, s1));
+  KG_CUDA(dalloc(&d_clist, (size_t)wcap * 32, s1));
   KG_CUDA(dalloc(&d_cbok, (size_t)kc, s1));
   KG_CUDA(dalloc(&d_pk, (size_t)kc * C::pk_bytes, s1));
   KG_CUDA(dalloc(&d_sk, (size_t)kc * C::sk_bytes, s1));
@@ -1047,7 +1145,8 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
       kg_build_kernel<SET><<<dim3(C::rwl / 8, natt), kBuildThreads, BuildSmem<SET>::bytes, s1>>>(
           b.g, b.pi, nullptr, b.status, b.matL, C::rwl, C::rwl, fd.gexp, fd.glog);
       kg_elim_kernel<SET, kg_table_bits<SET>()><<<natt, ElimCfg<kg_table_bits<SET>()>::nt, ElimSmem<SET, kg_table_bits<SET>()>::bytes, s1>>>(
-          b.matL, C::rwl, C::rwl, nullptr, b.status, kKgMinpoly | kKgDistinct, kKgRank, 1, 1, nullptr);
+          b.matL, C::rwl, C::rwl, nullptr, b.status, kKgMinpoly | kKgDistinct, kKgRank, 1, 1, nullptr, semi ? 1 : 0,
+          nullptr, nullptr);
       KG_CUDA(cudaGetLastError());
       KG_CUDA(cudaMemcpyAsync(b.h_status, b.status, natt, cudaMemcpyDeviceToHost, s1));
       KG_CUDA(cudaEventRecord(b.ranked, s1));
@@ -1093,11 +1192,13 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
           lc.attrs = at;
           lc.numAttrs = 1;
           KG_CUDA(cudaLaunchKernelEx(&lc, kg_elim_kernel<SET, kg_table_bits<SET>()>, d_matF, (int)C::rw, (int)C::rw, (const int *)watt,
-                                     b.status, (int)kKgAll, (int)kKgAll, 0, kElimCluster, d_rowid));
+                                     b.status, (int)kKgAll, (int)kKgAll, 0, kElimCluster, d_rowid, semi ? 1 : 0,
+                                     semi ? d_clist : (uint8_t *)nullptr, semi ? b.pi : (uint16_t *)nullptr));
         }
         kg_cbits_kernel<SET><<<nw, kCbitsThreads, CbitsSmem<SET>::bytes, s2>>>(b.pi, watt, wout, nw, d_cond, d_cbok);
         kg_assemble_kernel<SET><<<dim3(256, nw), 256, 0, s2>>>(watt, wout, nw, (const uint8_t *const *)b.rptr, b.g,
-                                                                d_cond, d_matF, d_rowid, d_pk, d_sk);
+                                                                d_cond, d_matF, d_rowid, semi ? d_clist : nullptr,
+                                                                d_pk, d_sk);
         KG_CUDA(cudaGetLastError());
       }
       KG_CUDA(cudaEventRecord(b.done, s2));
@@ -1148,7 +1249,7 @@ done:
     if (b.done) cudaEventDestroy(b.done);
   }
   for (void *p : {(void *)d_seedc, (void *)d_matF, (void *)d_rowid, (void *)d_cond, (void *)d_cbok, (void *)d_pk,
-                  (void *)d_sk})
+                  (void *)d_sk, (void *)d_clist})
     if (p) cudaFreeAsync(p, s1);
   {
     cudaError_t e = cudaStreamSynchronize(s1);
@@ -1169,7 +1270,9 @@ extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, 
   using namespace gmc;
   if (set < 0 || set >= GMC_NVARIANTS || nkeys < 0 || (nkeys > 0 && (!pk || !sk || !seeds)))
     return kg_fail(GMC_EINVAL, "gmc_keypair_batch: bad argument");
-  set %= GMC_NSETS;  // a plaintext-confirmation variant has the keys of its parameter set
+  // plaintext-confirmation variants have the keys of their set; f variants the semi-systematic form
+  const bool semi = ((set / GMC_NSETS) & 2) != 0;
+  set %= GMC_NSETS;
   if (nkeys == 0) return GMC_OK;
   // chain links and rounds are on the critical path (the host waits for each
   // round's ranks); the winners' work only has to finish by the end
@@ -1184,11 +1287,11 @@ extern "C" int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, 
     rc = kg_fail(GMC_ECUDA, std::string("gmc_keypair_batch: ") + cudaGetErrorString(e));
   } else {
     switch (set) {
-      case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, s0, s1, s2); break;
-      case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, s0, s1, s2); break;
-      case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, s0, s1, s2); break;
-      case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, s0, s1, s2); break;
-      case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, s0, s1, s2); break;
+      case 0: rc = keypair_batch<0>(pk, sk, seeds, nkeys, semi, s0, s1, s2); break;
+      case 1: rc = keypair_batch<1>(pk, sk, seeds, nkeys, semi, s0, s1, s2); break;
+      case 2: rc = keypair_batch<2>(pk, sk, seeds, nkeys, semi, s0, s1, s2); break;
+      case 3: rc = keypair_batch<3>(pk, sk, seeds, nkeys, semi, s0, s1, s2); break;
+      case 4: rc = keypair_batch<4>(pk, sk, seeds, nkeys, semi, s0, s1, s2); break;
     }
   }
   if (s0) cudaStreamDestroy(s0);

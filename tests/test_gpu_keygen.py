@@ -38,7 +38,7 @@ def oracle_keys(sid, seeds):
 
 
 def sk_fields(sid):
-    z = O.sizes(sid)
+    z = O.sizes(sid % 5)
     t, m = z["t"], z["m"]
     cond = (1 << (m - 4)) * (2 * m - 1)
     return [("seed", 0, 32), ("pivots", 32, 40), ("g", 40, 40 + 2 * t), ("cond", 40 + 2 * t, 40 + 2 * t + cond),
@@ -61,6 +61,18 @@ def test_keygen_parity(gmc, sid):
     seeds = np.concatenate([np.frombuffer(key_seed(sid), np.uint8)[None], seeds_for(sid, 3)])
     pk, sk = gmc.keypair_batch(sid, seeds)
     check(sid, seeds, pk, sk, oracle_keys(sid, seeds))
+
+
+@pytest.mark.parametrize("sid", range(10, 15), ids=[s + "f" for s in SETS])
+def test_keygen_semi_systematic_parity(gmc, sid):
+    """f variants (ids 10..14): the last 32 pivots from the 64-column window, the support swapped
+    accordingly, pivots in sk[32:40]."""
+    seeds = seeds_for(sid, 4, tag=b"kg-f")
+    pk, sk = gmc.keypair_batch(sid, seeds)
+    ref = oracle_keys(sid, seeds)
+    check(sid, seeds, pk, sk, ref)
+    pk2, sk2 = gmc.keypair_batch(sid + 5, seeds[:1])  # pcf: the same keys
+    assert np.array_equal(pk2[0], pk[0]) and np.array_equal(sk2[0], sk[0])
 
 
 def test_keygen_many_rounds(gmc):

@@ -41,7 +41,7 @@ def corrupted(sid, cts, seed=0):
         bit = int(rng.integers(0, z["mt"]))
         out[i, bit // 8] ^= np.uint8(1 << (bit % 8))
     sb = (z["mt"] + 7) // 8
-    for i in (c1 if sid >= 5 else []):
+    for i in (c1 if (sid // 5) & 1 else []):
         bit = int(rng.integers(0, 256))
         out[i, sb + bit // 8] ^= np.uint8(1 << (bit % 8))
     rnd = rng.integers(0, 256, size=(8, z["ct_bytes"]), dtype=np.uint8)
@@ -144,6 +144,22 @@ def test_pc_full_size_round_trip(gmc, keys):
     assert (rc == 0).all() and (rcd == 0).all() and (kd == k).all()
     oc, ok_, _ = O.enc_batch(sid, pk, seeds[:256], threads=THREADS)
     assert (c[:256] == oc).all() and (k[:256] == ok_).all()
+
+
+@pytest.mark.parametrize("sid", [13, 17, 19], ids=["6960119f", "6688128pcf", "8192128pcf"])
+def test_semi_systematic_keys_enc_dec_parity(gmc, sid):
+    """f / pcf variants: semi-systematic keys through the set's (or its pc form's) enc and dec."""
+    import hashlib
+    base = sid % 5
+    pk, sk = O.keypair(sid, hashlib.sha256(b"semi-enc" + bytes([sid])).digest())
+    seeds = request_seeds(base, 120, b"semi%d" % sid)
+    c, k, rc = gmc.PublicKey(sid, pk).enc_batch(seeds)
+    oc, ok_, orc = O.enc_batch(sid, pk, seeds, threads=THREADS)
+    assert (rc == orc).all() and (c == oc).all() and (k == ok_).all()
+    cts = corrupted(sid, c)
+    kd, rcd = gmc.SecretKey(sid, sk).dec_batch(cts)
+    okd, orcd = O.dec_batch(sid, sk, cts, threads=THREADS)
+    assert (rcd == orcd).all() and (kd == okd).all()
 
 
 def test_pc_keys_are_not_served(gmc, keys):

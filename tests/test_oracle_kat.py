@@ -31,6 +31,28 @@ KAT = {
                   "7f2438a79d20ae3b056f2d13bca43ea7c1ba2a2e0535cc35f7016188910a4720"),
     "8192128pc": ("a9d56a17b9b870e832cddde5c5787b55ada2189992d03eb75e23e710bcb98ccd",
                   "ac060fe5c1bdb9bd96bfa21ad4875cacb61f8e4eed791511020db06c65909811"),
+    # semi-systematic key generation (kem_<set>f_checksums, e.g. :4794 for 348864f, :2978 for 8192128f)
+    "348864f": ("5ad76eff6b5ccaedc1615e9795880cfd79b44c4247db4b8a13684c507a5db437",
+                "471a096310df17d7650c5d1a2e798909598b3b16652c70eb722be84673cf2f8f"),
+    "460896f": ("1418b90ac6aa9d36bd3c42c7e8c4ba299eafa45e93a903a383041629fb47f043",
+                "863b850af9436f66906c5824c32165b512352f398f32b2933c424bac34dcdd23"),
+    "6688128f": ("daec95f7a2db91986d2d1ca7312d66314149b066db0f467935ecf027aa1f4403",
+                 "a371ae9485120c1ea108b85723470e5b317ca4428fa01a27b3b5f33f5d924d32"),
+    "6960119f": ("8d0f85c0ffa074aff7cf1c5d2f8a048174de4ee62a74556e04e8da326e8b640d",
+                 "d62841358b16796439c261003bae87733ef9889374061bce0a261f80b072861f"),
+    "8192128f": ("2d50dd3ea54c764b5f79505d181c08cefc2276a28c791681cce3a45888c687cc",
+                 "717835d0cdf7f4e9a36a53d93116028be3ba3eb7f57bf4913303f3c2e1830900"),
+    # both (kem_<set>pcf_checksums, e.g. :5248 for 348864pcf, :3432 for 8192128pcf)
+    "348864pcf": ("4dcfc56d5e162873f227befd1e7c51f2b317f9ccf811e931e86e2fcdeea6c10e",
+                  "48fffebf6cd92a688b4724d88cf989ab199066040c7c62202dab6f30ef188d68"),
+    "460896pcf": ("1980e3f38d8258eca9d8d4300ac8dd6a6cde2f2c10c5e7b589971972531c8505",
+                  "063a2ecf26e027499a9f6b4e8344800819c28bf094926af1e3ec45107175ce53"),
+    "6688128pcf": ("80e0655938457c4dcd6aa6323d60f2495efda8a2d4a13b1958e8ca8fd2e848b6",
+                   "a4451d736f136a43032cd4d1047b4b7494ee6d0c91d75deff011e596bdb1b3ec"),
+    "6960119pcf": ("873616887e3e83679d5a708b3fbd8eb2301d18ea21f0f7c238db87178596267a",
+                   "d709f666d84fe4450ec59759ef20982df8d614afe788db2b7d0f91b0c0e02254"),
+    "8192128pcf": ("fdf47ca26ac3e1a3ae8c2859619cce789420a4af8533ded9e1104d232bd62f5e",
+                   "182ec5f02250b7764c121a1b481ec6003c0897f7d772ae7d0bba226660bb99e4"),
 }
 
 
