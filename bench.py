@@ -628,7 +628,7 @@ def main():
         "algorithmic_bytes_per_launch": dom_bytes,
         "traffic_source": (f"profiles/dram_traffic_kem{args.set}_n{N}.txt (one ncu capture)" if traffic else None),
         "note": "the decapsulation kernels (bit-sliced Berlekamp-Massey, bit-sliced additive FFT) are bounded by "
-                "the integer ALU pipe (79% / 72% of its peak in profiles/kernels_kem8192128_n65536.md), not by "
+                "the integer ALU pipe (79% / 70% of its peak in profiles/kernels_kem8192128_n65536.md), not by "
                 "HBM: their HBM bytes per request are ~1-2 KB",
     }
 
