@@ -655,6 +655,9 @@ def main():
     if rank == 0 and not args.no_sweep:
         line["n_sweep"] = {"set": args.set, "flip": args.flip,
                            "ops_s": n_sweep(gmc, torch, dev, args.set, [256, 1024, 4096, 16384, 65536], 5, args.flip)}
+        # config 1: mceliece348864, one key, 256 encapsulations + 256 decapsulations per step
+        line["config1"] = {"set": "348864", "n": 256, "flip": args.flip,
+                           "ops_s": n_sweep(gmc, torch, dev, "348864", [256], 20, args.flip)["256"]}
     if rank == 0 and not args.no_engines:
         line["syndrome_engines"] = [syndrome_engines(gmc, torch, dev, L, s_, 65536, 5, tc_peak)
                                     for s_ in dict.fromkeys(("348864", args.set))]
