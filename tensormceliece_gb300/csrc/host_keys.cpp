@@ -11,7 +11,10 @@
 
 #include <algorithm>
 #include <cstring>
+#include <atomic>
+#include <functional>
 #include <mutex>
+#include <thread>
 
 namespace gmc {
 
@@ -242,20 +245,33 @@ int build_sk(int set, const uint8_t *sk, SkHost &out) {
   out.invL.assign(q, 0xFFFF);
   std::vector<uint16_t> w2(n);
   const int d = S.fft_d;
-  for (int i = 0; i < n; i++) {
-    const uint16_t a = bitrev((uint16_t)pi[i], m);
-    uint16_t v = g[t];
-    for (int j = t - 1; j >= 0; j--) v = (uint16_t)(F.mul(v, a) ^ g[j]);
-    if (!v) return -1;  // g has a root on the support: not a valid key
-    w2[i] = F.inv(F.mul(v, v));
-    out.L[i] = a;
-    out.invL[a] = (uint16_t)i;
-    out.LL[i] = F.log[a];
-    out.LW2[i] = F.log[w2[i]];
-    uint16_t pw = a;
-    for (int r = 0; r < d; r++) pw = F.sq(pw);
-    out.Lpow[i] = S.lead_term ? pw : 0;
-  }
+  // per-position work split over host threads (positions, or 32-position word blocks where
+  // threads would otherwise share a word)
+  const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  auto parallel = [&](int count, const std::function<void(int, int)> &fn) {
+    std::vector<std::thread> th;
+    const int per = (count + nthreads - 1) / nthreads;
+    for (int lo = 0; lo < count; lo += per) th.emplace_back(fn, lo, std::min(count, lo + per));
+    for (auto &x : th) x.join();
+  };
+  std::atomic<int> bad{0};
+  parallel(n, [&](int lo, int hi) {
+    for (int i = lo; i < hi; i++) {
+      const uint16_t a = bitrev((uint16_t)pi[i], m);
+      uint16_t v = g[t];
+      for (int j = t - 1; j >= 0; j--) v = (uint16_t)(F.mul(v, a) ^ g[j]);
+      if (!v) bad = 1;  // g has a root on the support: not a valid key
+      w2[i] = v ? F.inv(F.mul(v, v)) : 0;
+      out.L[i] = a;
+      out.LL[i] = F.log[a];
+      out.LW2[i] = F.log[w2[i]];
+      uint16_t pw = a;
+      for (int r = 0; r < d; r++) pw = F.sq(pw);
+      out.Lpow[i] = S.lead_term ? pw : 0;
+    }
+  });
+  if (bad) return -1;
+  for (int i = 0; i < n; i++) out.invL[out.L[i]] = (uint16_t)i;
   out.s.assign(sk + 40 + S.irr_bytes + S.cond_bytes, sk + 40 + S.irr_bytes + S.cond_bytes + S.e_bytes);
 
   // front-end matrix: row j*m+b, column i = bit b of w2_i * L_i^j, for every
@@ -269,26 +285,32 @@ int build_sk(int set, const uint8_t *sk, SkHost &out) {
   out.F.assign((size_t)out.frows_pad * out.ldf, 0u);
   out.ldh = round_up((t * m + 31) / 32, 32);
   out.HT.assign((size_t)n * out.ldh, 0u);
-  for (int i = 0; i < n; i++) {
-    uint16_t v = w2[i];
-    uint32_t *row = &out.HT[(size_t)i * out.ldh];
-    for (int j = 0; j < t; j++) {
-      for (int b = 0; b < m; b++)
-        if ((v >> b) & 1) row[(j * m + b) >> 5] |= 1u << ((j * m + b) & 31);
-      v = F.mul(v, out.L[i]);
+  // HT row i: the m-bit values w2_i L_i^j, j < t, packed m bits apart
+  parallel(n, [&](int lo, int hi) {
+    for (int i = lo; i < hi; i++) {
+      uint16_t v = w2[i];
+      uint32_t *row = &out.HT[(size_t)i * out.ldh];
+      for (int j = 0; j < t; j++) {
+        const int pos = j * m, w = pos >> 5, sh = pos & 31;
+        row[w] |= (uint32_t)v << sh;
+        if (sh + m > 32) row[w + 1] |= (uint32_t)v >> (32 - sh);
+        v = F.mul(v, out.L[i]);
+      }
     }
-  }
+  });
   const int ncols = std::min(n, 8 * S.synd_bytes);
-  for (int i = 0; i < ncols; i++) {
-    uint16_t v = w2[i];
-    const uint32_t bit = 1u << (i & 31);
-    const int word = i >> 5;
-    for (int j = 0; j < 2 * t; j++) {
-      for (int b = 0; b < m; b++)
-        if ((v >> b) & 1) out.F[(size_t)(j * m + b) * out.ldf + word] |= bit;
-      v = F.mul(v, out.L[i]);
-    }
-  }
+  parallel((ncols + 31) / 32, [&](int lo, int hi) {
+    for (int word = lo; word < hi; word++)
+      for (int i = 32 * word; i < std::min(ncols, 32 * word + 32); i++) {
+        uint16_t v = w2[i];
+        const uint32_t bit = 1u << (i & 31);
+        for (int j = 0; j < 2 * t; j++) {
+          for (int b = 0; b < m; b++)
+            if ((v >> b) & 1) out.F[(size_t)(j * m + b) * out.ldf + word] |= bit;
+          v = F.mul(v, out.L[i]);
+        }
+      }
+  });
   return 0;
 }
 
