@@ -61,6 +61,16 @@ int gmc_sk_load(gmc_key **out, int set, const unsigned char *sk);
 void gmc_key_free(gmc_key *key);
 int gmc_key_set(const gmc_key *key);
 
+/* Persistence of a resident key: gmc_key_export writes the key's device state
+ * (the tables gmc_pk_load / gmc_sk_load build on the host) as one
+ * self-checking byte string and returns its length (buf = NULL: only the
+ * length); gmc_key_import re-creates the handle on the current device with
+ * plain copies. The string carries the set id, key kind and dimensions and a
+ * SHAKE256 checksum; import rejects (GMC_EKEY) anything else. A secret-key
+ * string holds the secret key's material: store it as the secret key. */
+long long gmc_key_export(const gmc_key *key, unsigned char *buf, long long len);
+int gmc_key_import(gmc_key **out, const unsigned char *buf, long long len);
+
 /* ---- batched encapsulation --------------------------------------------
  * n requests against one public key. seeds: n x 32 bytes; request i draws its
  * randomness from the seed chain state_0 = seeds[i], each randombytes call of

@@ -74,6 +74,9 @@ def lib():
                 getattr(L, f"gmc_kem_{s}_{op}").argtypes = [c_u8p, c_u8p, c_u8p]
         L.gmc_keypair_seed.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p]
         L.gmc_keypair_batch.argtypes = [ctypes.c_int, c_u8p, c_u8p, c_u8p, ctypes.c_longlong]
+        L.gmc_key_export.argtypes = [ctypes.c_void_p, c_u8p, ctypes.c_longlong]
+        L.gmc_key_export.restype = ctypes.c_longlong
+        L.gmc_key_import.argtypes = [ctypes.POINTER(ctypes.c_void_p), c_u8p, ctypes.c_longlong]
         for s in VARIANTS:
             getattr(L, f"gmc_kem_{s}_keypair").argtypes = [c_u8p, c_u8p]
             getattr(L, f"gmc_kem_{s}_keypair").restype = None
@@ -159,6 +162,25 @@ class _Key:
     @property
     def handle(self):
         return self._h
+
+    def export(self):
+        """The key's device state as a self-checking byte string (gmc_key_export)."""
+        n = _check(int(lib().gmc_key_export(self._h, None, 0)), "gmc_key_export")
+        buf = np.zeros(n, np.uint8)
+        _check(int(lib().gmc_key_export(self._h, _ptr(buf), n)), "gmc_key_export")
+        return buf.tobytes()
+
+    @classmethod
+    def from_export(cls, blob):
+        """Re-creates a resident key from gmc_key_export's string, without the host-side table build."""
+        raw = _u8(blob)
+        h = ctypes.c_void_p()
+        _check(lib().gmc_key_import(ctypes.byref(h), _ptr(raw), raw.size), "gmc_key_import")
+        self = cls.__new__(cls)
+        self._h = h
+        self.set = int(lib().gmc_key_set(h))
+        self.sizes = set_sizes(self.set)
+        return self
 
     def close(self):
         if getattr(self, "_h", None):

@@ -1,0 +1,179 @@
+// Persistence of resident keys: gmc_key_export writes a loaded key's device
+// state (the tables gmc_pk_load / gmc_sk_load build on the host, once per key;
+// ~2.8 MB for an 8192128 secret key) into a self-checking byte string;
+// gmc_key_import re-creates the handle from it with plain copies after
+// verifying the checksum, without rebuilding the tables.
+//
+// Format (little-endian): header, then the sections in order
+//   public key: T (rows_pad x lda u32), TT ((k+1) x ldtt u32)
+//   secret key: F (frows_pad x ldf u32), support tables (3n + 2^m u16),
+//               s (n/8 bytes zero-padded to 16), HT (n x ldh u32)
+// The header's checksum is SHAKE256 of the whole string with the checksum
+// field zeroed; import rejects any string whose magic, version, set, sizes or
+// checksum do not match.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gmc.h"
+#include "engine_internal.h"
+#include "host_keys.h"
+
+namespace {
+using namespace gmc;
+
+constexpr char kMagic[8] = {'G', 'M', 'C', 'K', 'E', 'Y', '0', '1'};
+constexpr uint32_t kVersion = 1;
+
+struct KeyHeader {
+  char magic[8];
+  uint32_t version;
+  int32_t set, variant, kind;
+  int32_t lda, rows_pad, kw_pad, pad_bad, ldtt;  // public key
+  int32_t ldf, frows_pad, cw_pad, ldh;           // secret key
+  uint64_t section[4];                           // bytes of each section
+  uint8_t checksum[32];
+};
+static_assert(sizeof(KeyHeader) % 8 == 0, "header keeps the sections 8-byte aligned");
+
+int kf_fail(int code, const std::string &msg) {
+  set_last_error(msg.c_str());
+  return code;
+}
+
+size_t s_alloc_bytes(const gmc_setinfo &S) { return ((size_t)S.e_bytes + 15) / 16 * 16; }
+
+// section sizes implied by a header's dimensions
+bool section_sizes(const KeyHeader &h, uint64_t out[4]) {
+  const gmc_setinfo &S = set_info(h.set);
+  memset(out, 0, 4 * sizeof(uint64_t));
+  if (h.kind == 0) {
+    if (h.rows_pad < S.mt || h.lda < (S.k + 31) / 32 || h.ldtt < (S.mt + 31) / 32 || h.rows_pad > 1 << 16 ||
+        h.lda > 1 << 12 || h.ldtt > 1 << 12)
+      return false;
+    out[0] = (uint64_t)h.rows_pad * h.lda * 4;
+    out[1] = (uint64_t)(S.k + 1) * h.ldtt * 4;
+  } else {
+    if (h.frows_pad < 2 * S.t * S.m || h.ldf < (S.synd_bytes + 3) / 4 || h.ldh < (S.t * S.m + 31) / 32 ||
+        h.frows_pad > 1 << 16 || h.ldf > 1 << 12 || h.ldh > 1 << 12)
+      return false;
+    out[0] = (uint64_t)h.frows_pad * h.ldf * 4;
+    out[1] = (3ull * S.n + S.q) * 2;
+    out[2] = s_alloc_bytes(S);
+    out[3] = (uint64_t)S.n * h.ldh * 4;
+  }
+  return true;
+}
+
+void checksum(const uint8_t *buf, long long len, uint8_t out[32]) {
+  std::vector<uint8_t> copy(buf, buf + len);
+  memset(copy.data() + offsetof(KeyHeader, checksum), 0, 32);
+  host_shake256(out, 32, copy.data(), (size_t)len);
+}
+}  // namespace
+
+extern "C" long long gmc_key_export(const gmc_key *key, unsigned char *buf, long long len) {
+  if (!key) return kf_fail(GMC_EINVAL, "gmc_key_export: null key");
+  KeyHeader h{};
+  memcpy(h.magic, kMagic, 8);
+  h.version = kVersion;
+  h.set = key->set;
+  h.variant = key->variant;
+  h.kind = key->kind;
+  h.lda = key->lda; h.rows_pad = key->rows_pad; h.kw_pad = key->kw_pad; h.pad_bad = key->pad_bad; h.ldtt = key->ldtt;
+  h.ldf = key->ldf; h.frows_pad = key->frows_pad; h.cw_pad = key->cw_pad; h.ldh = key->dk.ldh;
+  if (!section_sizes(h, h.section)) return kf_fail(GMC_EKEY, "gmc_key_export: key dimensions out of range");
+  const long long total = (long long)sizeof(KeyHeader) + (long long)(h.section[0] + h.section[1] + h.section[2] + h.section[3]);
+  if (!buf) return total;
+  if (len < total) return kf_fail(GMC_EINVAL, "gmc_key_export: buffer too small");
+  const void *src[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (key->kind == 0) {
+    src[0] = key->T;
+    src[1] = key->TT;
+  } else {
+    src[0] = key->F;
+    src[1] = key->tabs;
+    src[2] = key->s;
+    src[3] = key->HT;
+  }
+  unsigned char *p = buf + sizeof(KeyHeader);
+  for (int i = 0; i < 4; i++) {
+    if (!h.section[i]) continue;
+    cudaError_t e = cudaMemcpy(p, src[i], h.section[i], cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return kf_fail(GMC_ECUDA, std::string("gmc_key_export: ") + cudaGetErrorString(e));
+    p += h.section[i];
+  }
+  memcpy(buf, &h, sizeof h);
+  uint8_t sum[32];
+  checksum(buf, total, sum);
+  memcpy(buf + offsetof(KeyHeader, checksum), sum, 32);
+  return total;
+}
+
+extern "C" int gmc_key_import(gmc_key **out, const unsigned char *buf, long long len) {
+  if (!out || !buf || len < (long long)sizeof(KeyHeader)) return kf_fail(GMC_EINVAL, "gmc_key_import: bad argument");
+  *out = nullptr;
+  KeyHeader h;
+  memcpy(&h, buf, sizeof h);
+  if (memcmp(h.magic, kMagic, 8) || h.version != kVersion) return kf_fail(GMC_EKEY, "gmc_key_import: not a key string");
+  if (h.set < 0 || h.set >= GMC_NSETS || h.variant < 0 || h.variant > 3 || (h.kind != 0 && h.kind != 1))
+    return kf_fail(GMC_EKEY, "gmc_key_import: bad set, variant or kind");
+  uint64_t sz[4];
+  if (!section_sizes(h, sz) || memcmp(sz, h.section, sizeof sz))
+    return kf_fail(GMC_EKEY, "gmc_key_import: section sizes do not match the key's dimensions");
+  const long long total = (long long)sizeof(KeyHeader) + (long long)(sz[0] + sz[1] + sz[2] + sz[3]);
+  if (len != total) return kf_fail(GMC_EKEY, "gmc_key_import: wrong length");
+  uint8_t sum[32];
+  checksum(buf, total, sum);
+  if (memcmp(sum, h.checksum, 32)) return kf_fail(GMC_EKEY, "gmc_key_import: checksum mismatch");
+  const gmc_setinfo &S = set_info(h.set);
+  gmc_key *k = new gmc_key();
+  k->a8_mu = new std::mutex();
+  k->set = h.set;
+  k->variant = h.variant;
+  k->pc = h.variant & 1;
+  k->kind = h.kind;
+  cudaGetDevice(&k->device);
+  void **dst[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (h.kind == 0) {
+    k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad; k->ldtt = h.ldtt;
+    dst[0] = (void **)&k->T;
+    dst[1] = (void **)&k->TT;
+  } else {
+    k->ldf = h.ldf; k->frows_pad = h.frows_pad; k->cw_pad = h.cw_pad;
+    dst[0] = (void **)&k->F;
+    dst[1] = (void **)&k->tabs;
+    dst[2] = (void **)&k->s;
+    dst[3] = (void **)&k->HT;
+  }
+  const unsigned char *p = buf + sizeof(KeyHeader);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+    if (!sz[i]) continue;
+    e = cudaMalloc(dst[i], sz[i]);
+    if (e == cudaSuccess) e = cudaMemcpy(*dst[i], p, sz[i], cudaMemcpyHostToDevice);
+    p += sz[i];
+  }
+  if (e != cudaSuccess) {
+    for (int i = 0; i < 4; i++)
+      if (dst[i] && *dst[i]) cudaFree(*dst[i]);
+    delete k->a8_mu;
+    delete k;
+    return kf_fail(GMC_ECUDA, std::string("gmc_key_import: ") + cudaGetErrorString(e));
+  }
+  if (h.kind == 1) {
+    const size_t n = S.n;
+    k->dk.L = k->tabs;
+    k->dk.LL = k->tabs + n;
+    k->dk.LW2 = k->tabs + 2 * n;
+    k->dk.invL = k->tabs + 3 * n;
+    k->dk.s = k->s;
+    k->dk.HT = k->HT;
+    k->dk.ldh = h.ldh;
+  }
+  *out = k;
+  return GMC_OK;
+}

@@ -124,3 +124,14 @@ def test_golden_fixtures_match_oracle(keys):
         for v in g[name]["flipped"] + ([g[name]["padding"]] if "padding" in g[name] else []):
             rc, k = O.dec(sid, bytes.fromhex(v["ct"]), sk)
             assert k.tobytes().hex() == v["k"] and rc == v["rc"]
+
+
+def test_key_import_rejects_foreign_strings():
+    """gmc_key_import checks magic, version, dimensions and checksum on the host, before any device work."""
+    import ctypes
+    import tensormceliece_gb300 as gmc
+    L = gmc.lib()
+    h = ctypes.c_void_p()
+    junk = np.frombuffer(b"not a key string" * 16, np.uint8).copy()
+    assert L.gmc_key_import(ctypes.byref(h), junk.ctypes.data_as(ctypes.c_void_p), junk.size) == -4  # GMC_EKEY
+    assert L.gmc_key_import(ctypes.byref(h), junk.ctypes.data_as(ctypes.c_void_p), 8) == -1  # too short
