@@ -792,8 +792,23 @@ __global__ void __launch_bounds__(kTailThreads) dec_tail_kernel(const uint32_t *
     for (int j = 0; j < 32; j++) diff |= (uint32_t)c[SB + j] ^ ((uint32_t)(cf[j >> 3] >> (8 * (j & 7))) & 0xFFu);
     ok = ok && diff == 0;
   }
-  // b || (e or s) || c; s is the key's n/8 bytes, stored zero-padded to whole words
-  const uint32_t *erow = ok ? E + opc * lde : reinterpret_cast<const uint32_t *>(key.s);
+  // b || (e or s) || c, s the key's n/8 bytes (stored zero-padded to whole words). The choice is a
+  // mask, not an address (mc:crypto_kem/348864/vec/kem_dec.c:51-55): the warp rewrites each of its
+  // 32 rows as (e & mask) | (s & ~mask), reading both e and s with the same coalesced loads whatever
+  // the outcome, and every lane hashes its own (blended) row.
+  {
+    const unsigned okmask = __ballot_sync(0xffffffffu, ok);
+    const long long g0 = opc - (threadIdx.x & 31);  // the warp's first row (clamped rows repeat N-1)
+    for (int r = 0; r < 32; r++) {
+      const long long row = g0 + r < N ? g0 + r : N - 1;
+      const uint32_t m = ((okmask >> r) & 1u) ? 0xFFFFFFFFu : 0u;
+      const uint32_t *sr = reinterpret_cast<const uint32_t *>(keys.k[seg_find(segs, row)].s);
+      uint32_t *er = const_cast<uint32_t *>(E) + row * lde;
+      for (int w = threadIdx.x & 31; w < p::ew; w += 32) er[w] = (er[w] & m) | (sr[w] & ~m);
+    }
+    __syncwarp();
+  }
+  const uint32_t *erow = E + opc * lde;
   // word loads when every ciphertext row is 4-byte aligned (the buffer and the row length), else bytes
   const bool c_words = (CB % 4 == 0) && ((reinterpret_cast<uintptr_t>(Cin) & 3) == 0);
   auto cword = [&](int w) -> uint32_t {
