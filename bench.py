@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-grouped", action="store_true", help="skip the mixed-key grouped-launch measurement")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--serve-seconds", type=float, default=3.0, help="seconds per serving load level (60 = the "
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="seconds per serving load level (60 = the "
                     "full serving configuration)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the N = 256..65536 throughput sweep")
     ap.add_argument("--no-engines", action="store_true", help="skip the syndrome-engine comparison")
