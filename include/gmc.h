@@ -112,7 +112,10 @@ int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsign
  * library's seed chain until an attempt gives an irreducible Goppa
  * polynomial, a repetition-free support and a systematic public key; the
  * attempts run on the GPU (seed expansion, minimal polynomial, support sort,
- * Gaussian elimination, Benes control bits). */
+ * Gaussian elimination, Benes control bits). Environment (optional):
+ * GMC_KG_CHUNK_KEYS caps the keys staged on the device per chunk (default:
+ * 2 GB of pk + sk), GMC_KG_AHEAD_LINKS the seed-chain links expanded ahead per
+ * key (default ln(nkeys)/0.34 + 8); GMC_KG_TRACE=1 prints one line per round. */
 int gmc_keypair_batch(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seeds, long long nkeys);
 
 /* ---- grouped launches over many keys and parameter sets -------------------

@@ -1037,6 +1037,8 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
   KG_CUDA(kg_attrs<SET>());
   cap = 4 * sms;
   kc = std::max<long long>(1, std::min<long long>(nkeys, kChunkBytes / (C::pk_bytes + C::sk_bytes)));
+  // GMC_KG_CHUNK_KEYS: keys per device-side staging chunk (lower than the default only)
+  if (const char *v = getenv("GMC_KG_CHUNK_KEYS")) kc = std::max(1ll, std::min(kc, atoll(v)));
   wcap = (int)std::min<long long>(kc, cap);
   for (KgRound &b : R) {
     KG_CUDA(dalloc(&b.status, (size_t)cap, s1));
@@ -1104,7 +1106,9 @@ int keypair_batch(uint8_t *pk, uint8_t *sk, const uint8_t *seeds, long long nkey
     // links ahead: a key needs more than L attempts with probability ~0.71^L
     // (29% of attempts succeed for every set), so ln(nk)/0.34 + 8 links cover
     // the whole chunk but in ~6% of calls
-    const int ahead = std::min(64, std::max(12, (int)std::ceil(std::log((double)nk) / 0.3425) + 8));
+    int ahead = std::min(64, std::max(12, (int)std::ceil(std::log((double)nk) / 0.3425) + 8));
+    // GMC_KG_AHEAD_LINKS: links expanded ahead (1..64); fewer make the extension blocks carry the chains
+    if (const char *v = getenv("GMC_KG_AHEAD_LINKS")) ahead = std::max(1, std::min(64, atoi(v)));
     KG_CUDA(add_block(nullptr, 0, ahead));
     KG_CUDA(cudaMemsetAsync(d_cbok, 0, (size_t)nk, s2));
     for (int round = 0; !pending.empty(); round++) {

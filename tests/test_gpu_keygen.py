@@ -85,6 +85,17 @@ def test_keygen_many_rounds(gmc):
     check(sid, seeds, pk, sk, oracle_keys(sid, seeds))
 
 
+def test_keygen_chunks_and_extension_blocks(gmc, monkeypatch):
+    """Staging chunks of 7 keys and 2 links expanded ahead: several chunks per call, and most chains carried
+    by extension blocks (an f set, so the window step runs in the same call)."""
+    monkeypatch.setenv("GMC_KG_CHUNK_KEYS", "7")
+    monkeypatch.setenv("GMC_KG_AHEAD_LINKS", "2")
+    for sid in (0, 10):
+        seeds = seeds_for(sid, 23, tag=b"kg-chunks")
+        pk, sk = gmc.keypair_batch(sid, seeds)
+        check(sid, seeds, pk, sk, oracle_keys(sid, seeds))
+
+
 def test_keygen_matches_single_calls(gmc):
     """The batched keys equal the engine's own single-key path (host keygen)."""
     sid = 1
