@@ -78,7 +78,6 @@ template <int SET> struct KG {
   static constexpr int rstride = dofs + 32;                       // per-attempt bytes: r (whole blocks), seed
   static constexpr int rw = (((n + 31) / 32) + 31) / 32 * 32;     // u32 words per full row
   static constexpr int rwl = (((mt + 31) / 32) + 31) / 32 * 32;   // u32 words per A_L row
-  static constexpr int npanel = (mt + 31) / 32;
   static constexpr int gstride = (t + 2) & ~1;                    // u16 per g (t+1 coefficients)
   static constexpr int cond_bytes = (q / 16) * (2 * m - 1);
   static constexpr int pk_row_bytes = (k + 7) / 8;
