@@ -16,7 +16,9 @@
 #include <string.h>
 #include <sys/random.h>
 
+#include <list>
 #include <map>
+#include <memory>
 #include <set>
 #include <mutex>
 #include <string>
@@ -773,27 +775,67 @@ static int draw_seed(uint8_t seed[32]) {
   return GMC_OK;
 }
 
+// Resident keys of the one-request entry points, most recently used first: a
+// caller of the libmceliece convention passes the key bytes with every
+// request, so loading them each time (host tables, device copies) would cost
+// milliseconds per call. An entry matches on set id, kind, device and the
+// whole key (byte comparison); entries are shared, so an eviction never frees
+// a handle that another thread is still using.
+struct CachedKey {
+  int id, kind, device;
+  std::vector<uint8_t> bytes;
+  std::shared_ptr<gmc_key> h;
+};
+static std::mutex g_kc_mu;
+static std::list<CachedKey> g_kc;
+constexpr size_t kKeyCacheEntries = 8;
+
+static int cached_key(int id, int kind, const unsigned char *bytes, std::shared_ptr<gmc_key> *out) {
+  if (!valid_id(id)) return fail(GMC_EINVAL, "bad set id");
+  const gmc_setinfo &S = set_info(base_of(id));
+  const size_t len = (size_t)(kind == 0 ? S.pk_bytes : S.sk_bytes);
+  int dev = 0;
+  GMC_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(g_kc_mu);
+    for (auto it = g_kc.begin(); it != g_kc.end(); ++it)
+      if (it->id == id && it->kind == kind && it->device == dev && !memcmp(it->bytes.data(), bytes, len)) {
+        g_kc.splice(g_kc.begin(), g_kc, it);
+        *out = g_kc.front().h;
+        return GMC_OK;
+      }
+  }
+  std::vector<uint8_t> copy(bytes, bytes + len);  // the caller's buffer may alias an output
+  gmc_key *h = nullptr;
+  const int r = kind == 0 ? gmc_pk_load(&h, id, copy.data()) : gmc_sk_load(&h, id, copy.data());
+  if (r != GMC_OK) return r;
+  std::shared_ptr<gmc_key> sp(h, gmc_key_free);
+  std::lock_guard<std::mutex> lk(g_kc_mu);
+  g_kc.push_front(CachedKey{id, kind, dev, std::move(copy), sp});
+  while (g_kc.size() > kKeyCacheEntries) g_kc.pop_back();
+  *out = sp;
+  return GMC_OK;
+}
+
 static int one_enc(int set, unsigned char *c, unsigned char *k, const unsigned char *pk) {
   uint8_t seed[32];
   int r = draw_seed(seed);
   if (r) return r;
-  gmc_key *h = nullptr;
-  if ((r = gmc_pk_load(&h, set, pk)) != GMC_OK) return r;
+  std::shared_ptr<gmc_key> h;
+  if ((r = cached_key(set, 0, pk, &h)) != GMC_OK) return r;
   int rc = 0;
-  r = gmc_enc_batch(h, c, k, seed, 1, &rc);
-  gmc_key_free(h);
+  r = gmc_enc_batch(h.get(), c, k, seed, 1, &rc);
   return r ? r : rc;
 }
 
 static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsigned char *sk) {
   std::vector<uint8_t> cc(c, c + ct_bytes_of(base_of(set), pc_of(set)));  // k may alias c or sk
-  gmc_key *h = nullptr;
-  int r = gmc_sk_load(&h, set, sk);
+  std::shared_ptr<gmc_key> h;
+  int r = cached_key(set, 1, sk, &h);
   if (r) return r;
   uint8_t kk[32];
   int rc = 0;
-  r = gmc_dec_batch(h, kk, cc.data(), 1, &rc);
-  gmc_key_free(h);
+  r = gmc_dec_batch(h.get(), kk, cc.data(), 1, &rc);
   if (r) return r;
   memcpy(k, kk, 32);
   return rc;
