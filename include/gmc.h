@@ -272,11 +272,18 @@ int gmc_get_gemm_engine(void);
  * batch of n requests (median of 5), keeps the fastest and, when cache_path is
  * given, writes the choices of all tuned sets to that JSON file;
  * gmc_autotune_load applies such a file (returns the number of sets loaded).
- * gmc_tune_get returns 1 when the set's configuration was tuned or loaded. */
+ * gmc_tune_get returns 1 when the set's configuration was tuned or loaded.
+ * The launch shape is tuned with them: the tcgen05 GEMM's pipeline depth
+ * (gemm_stages 2..4 A/X buffers per CTA, default 4) and the requests per block
+ * of the decoding kernels (bm_warps: Berlekamp-Massey warps of 32 requests,
+ * root_warps: root-finding warps of one request; 1..8, default 8);
+ * gmc_tune_set_launch / gmc_tune_get_launch set and read them by hand. */
 int gmc_autotune(int set, long long n, const char *cache_path);
 int gmc_autotune_load(const char *cache_path);
 int gmc_tune_set(int set, int enc_engine, int dec_engine, int sample_threads);
 int gmc_tune_get(int set, int *enc_engine, int *dec_engine, int *sample_threads);
+int gmc_tune_set_launch(int set, int gemm_stages, int bm_warps, int root_warps);
+int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warps);
 /* Reads and clears the tensor-core engine's error word on the current device:
  * 1 when a CTA gave up on a bounded wait (its outputs are then invalid). */
 int gmc_tc_status(void);

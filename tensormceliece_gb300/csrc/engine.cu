@@ -416,6 +416,7 @@ static cudaError_t gemm_keys(const gmc_key *const *keys, int nkeys, int engine, 
                              int **err) {
   *gk = GemmKeys{};
   *err = nullptr;
+  if (nkeys > 0) gk->tc_stages = tune_get(keys[0]->set).gemm_stages;
   for (int i = 0; i < nkeys; i++) {
     gk->A[i] = keys[i]->kind == 0 ? keys[i]->T : keys[i]->F;
     gk->TT[i] = keys[i]->TT;
@@ -510,10 +511,11 @@ static cudaError_t dec_front_decode_seg(const Segs &segs, const gmc_key *ref, co
                           st);
   if (e != cudaSuccess) return e;
   prof_mark("dec_front_gemm", st);
-  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st);
+  const SetTune tune = tune_get(SET);
+  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st, tune.bm_warps);
   if (e != cudaSuccess) return e;
   prof_mark("dec_bm", st);
-  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st);
+  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st, tune.root_warps);
   prof_mark("dec_fft_roots_reenc", st);
   return e;
 }

@@ -38,6 +38,9 @@ struct SetTune {
   int enc_engine = GEMM_SPARSE;  // engine of the encapsulation syndrome
   int dec_engine = GEMM_TC;   // GF(2) GEMM engine of the decapsulation front end
   int sample_threads = 128;   // sampler block size (32, 64 or 128)
+  int gemm_stages = 4;        // tcgen05 GEMM pipeline depth (2, 3 or 4 A/X buffers per CTA)
+  int bm_warps = 8;           // Berlekamp-Massey (bit-sliced form) warps per block: 32 requests each
+  int root_warps = 8;         // root-finding warps per block: one request each
   int tuned = 0;              // 1 when measured on this device
   double enc_ms = 0, dec_ms = 0;
   long long n = 0;

@@ -9,10 +9,10 @@ namespace gmc {
 constexpr int kSampleWarpsPerSM = 8;     // sampler: resident warps per SM (lanes fetch requests)
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
 constexpr int kTailThreads = 128;
-constexpr int kBMWarps = 8;     // Berlekamp-Massey kernel: warps per block (32 requests per warp)
+constexpr int kBMWarps = 8;     // Berlekamp-Massey kernel: default and largest warps per block (32 requests per warp)
 constexpr int kBMLatWarps = 24;  // Berlekamp-Massey latency form: warps per block (one request per warp)
 constexpr long long kBMBitslicedMinRows = 24576;  // smaller batches take the latency form
-constexpr int kRootWarps = 8;  // root-finding kernel: warps per block
+constexpr int kRootWarps = 8;  // root-finding kernel: default and largest warps per block
 
 // ---------------------------------------------------------------- segments
 // A launch covers up to kMaxSegs segments (one key each) laid out back to back
@@ -75,6 +75,7 @@ struct GemmKeys {
   const uint8_t *A8[kMaxSegs];
   const uint32_t *TT[kMaxSegs];
   int ldtt;
+  int tc_stages;  // tcgen05 engine pipeline depth (2, 3 or 4; 0 = default 4)
 };
 // Out rows follow X rows (padded row space). err: device word set to 1 when a
 // tensor-core CTA gave up on a bounded wait.
@@ -152,13 +153,15 @@ cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int 
 // Berlekamp-Massey: S2 (2t packed syndromes) -> Sig [N][2^fft_d] u16, the
 // error locator's coefficients by degree (the leading x^t term is implicit
 // when t = 2^fft_d).
+// warps: warps per block of the bit-sliced form (1..kBMWarps; 0 = kBMWarps).
 template <int SET>
 cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
-                          cudaStream_t st);
+                          cudaStream_t st, int warps = 0);
 // Root finding + weight + re-encryption check: Sig -> E (error vectors), ok.
+// warps: warps per block (1..kRootWarps; 0 = kRootWarps), one request per warp.
 template <int SET>
 cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
-                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st);
+                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps = 0);
 // With pc the decoded e must also give SHAKE256(2 || e, 32) = C1 (else implicit
 // rejection), and the session-key preimage covers C0 || C1.
 template <int SET>

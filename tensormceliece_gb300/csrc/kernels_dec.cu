@@ -122,7 +122,8 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
   uint32_t *BP = SP + LY::s_words;
   const long long N = seg_rows(segs);
   const long long ngroups = (N + 31) / 32;
-  for (long long g = (long long)blockIdx.x * kBMWarps + warp; g < ngroups; g += (long long)gridDim.x * kBMWarps) {
+  const int nwb = blockDim.x >> 5;  // warps per block (a launch parameter up to kBMWarps)
+  for (long long g = (long long)blockIdx.x * nwb + warp; g < ngroups; g += (long long)gridDim.x * nwb) {
     const long long op = g * 32 + lane;
     int seg;
     const bool live = op < N && seg_live(segs, op, &seg);
@@ -566,8 +567,9 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::v_off);
 
   const long long N = seg_rows(segs);
-  const long long nwarps = (long long)gridDim.x * kRootWarps;
-  for (long long op = (long long)blockIdx.x * kRootWarps + warp; op < N; op += nwarps) {
+  const int nwb = blockDim.x >> 5;  // warps per block (a launch parameter up to kRootWarps)
+  const long long nwarps = (long long)gridDim.x * nwb;
+  for (long long op = (long long)blockIdx.x * nwb + warp; op < N; op += nwarps) {
     int seg;
     if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
     const DecKeyDev &key = keys.k[seg];
@@ -860,9 +862,11 @@ static int persistent_blocks(K kernel, int threads, int smem, long long work_ite
 
 template <int SET>
 cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
-                          cudaStream_t st) {
+                          cudaStream_t st, int warps) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
+  if (warps < 0 || warps > kBMWarps) return cudaErrorInvalidValue;
+  if (warps == 0) warps = kBMWarps;
   if (N < kBMBitslicedMinRows) {  // small batch: warp per request (lower latency per request)
     const int smem_l = BMLatLayout<SET>::bytes(kBMLatWarps);
     cudaError_t err =
@@ -872,24 +876,28 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
     dec_bm_lat_kernel<SET><<<gl, kBMLatWarps * 32, smem_l, st>>>(S2, lds2, fd, segs, Sig);
     return cudaGetLastError();
   }
-  const int smem_bm = BMLayout<SET>::bytes(kBMWarps);
-  cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bm);
+  const int smem_bm = BMLayout<SET>::bytes(warps);
+  cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         BMLayout<SET>::bytes(kBMWarps));
   if (err != cudaSuccess) return err;
-  const int gb = persistent_blocks(dec_bm_kernel<SET>, kBMWarps * 32, smem_bm, (N + 31) / 32, kBMWarps);
-  dec_bm_kernel<SET><<<gb, kBMWarps * 32, smem_bm, st>>>(S2, lds2, fd, segs, Sig);
+  const int gb = persistent_blocks(dec_bm_kernel<SET>, warps * 32, smem_bm, (N + 31) / 32, warps);
+  dec_bm_kernel<SET><<<gb, warps * 32, smem_bm, st>>>(S2, lds2, fd, segs, Sig);
   return cudaGetLastError();
 }
 
 template <int SET>
 cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
-                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st) {
+                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
-  const int smem_rt = RootLayout<SET>::bytes(kRootWarps);
-  cudaError_t err = cudaFuncSetAttribute(dec_root_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_rt);
+  if (warps < 0 || warps > kRootWarps) return cudaErrorInvalidValue;
+  if (warps == 0) warps = kRootWarps;
+  const int smem_rt = RootLayout<SET>::bytes(warps);
+  cudaError_t err = cudaFuncSetAttribute(dec_root_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         RootLayout<SET>::bytes(kRootWarps));
   if (err != cudaSuccess) return err;
-  const int gr = persistent_blocks(dec_root_kernel<SET>, kRootWarps * 32, smem_rt, N, kRootWarps);
-  dec_root_kernel<SET><<<gr, kRootWarps * 32, smem_rt, st>>>(Sig, S2, lds2, keys, fd, segs, E, lde, ok);
+  const int gr = persistent_blocks(dec_root_kernel<SET>, warps * 32, smem_rt, N, warps);
+  dec_root_kernel<SET><<<gr, warps * 32, smem_rt, st>>>(Sig, S2, lds2, keys, fd, segs, E, lde, ok);
   return cudaGetLastError();
 }
 
@@ -909,9 +917,9 @@ cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uin
 #define GMC_INST_DEC(SET)                                                                                       \
   template cudaError_t launch_pack_ct<SET>(const uint8_t *, const Segs &, uint32_t *, int, bool, cudaStream_t);       \
   template cudaError_t launch_dec_bm<SET>(const uint32_t *, int, FieldDev, const Segs &, uint16_t *,             \
-                                         cudaStream_t);                                                          \
+                                         cudaStream_t, int);                                                     \
   template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, const DecKeys &, FieldDev,  \
-                                            const Segs &, uint32_t *, int, int *, cudaStream_t);                 \
+                                            const Segs &, uint32_t *, int, int *, cudaStream_t, int);            \
   template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, const DecKeys &, \
                                             uint8_t *, int *, const Segs &, bool, cudaStream_t);
 GMC_INST_DEC(0)

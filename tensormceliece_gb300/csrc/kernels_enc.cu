@@ -19,7 +19,11 @@ namespace gmc {
 // Work split: each lane owns one request and runs its Keccak chain; lanes
 // take requests from a launch-wide counter whenever their previous request
 // is done, so a request that needs many attempts does not hold the warp's
-// other lanes idle. After every attempt the warp checks, one lane's
+// other lanes idle. Small batches leave lanes idle instead (only the first
+// `lanes` of each warp take requests): more warps share the batch, so the
+// Keccak latency is hidden across warps and the warp-serial repeat check and
+// syndrome gather below run over fewer requests per warp. After every
+// attempt the warp checks, one lane's
 // candidates at a time, for repeats with a single n-bit bitmap per warp
 // (atomicOr returns the previous word); on success that bitmap is the error
 // vector e, written out by the whole warp (coalesced) together with e[mt:n]
@@ -40,7 +44,8 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
                                                                 uint32_t *__restrict__ E, int lde,
                                                                 uint32_t *__restrict__ Ens, int ldx,
                                                                 const GemmKeys keys, uint32_t *__restrict__ S,
-                                                                int lds, unsigned int *__restrict__ counter) {
+                                                                int lds, unsigned int *__restrict__ counter,
+                                                                int lanes) {
   using p = P<SET>;
   using LY = SampleLayout<SET>;
   constexpr int NCW = (p::t + 31) / 32;
@@ -51,7 +56,7 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
   for (int w = lane; w < LY::bm_words; w += 32) bm[w] = 0;
   __syncwarp();
   const long long N = seg_rows(segs);
-  bool has = false, exhausted = false;
+  bool has = false, exhausted = lane >= lanes;  // idle lanes never take a request
   long long op = 0;
   int myseg = 0;
   uint64_t st[4] = {0, 0, 0, 0};
@@ -342,11 +347,17 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
   const int warps = threads / 32;
   int per_sm_target = (kSampleWarpsPerSM + warps - 1) / warps;
   if (per_sm_target > per_sm) per_sm_target = per_sm;
-  const long long need = (N + threads - 1) / threads;
+  // active lanes per warp: the smallest power of two (<= 32) with which the
+  // resident warps hold the whole batch at once
+  const long long warp_slots = (long long)sms * per_sm_target * warps;
+  int lanes = 1;
+  while (lanes < 32 && (long long)lanes * warp_slots < N) lanes <<= 1;
+  const long long per_block = (long long)warps * lanes;
+  const long long need = (N + per_block - 1) / per_block;
   const long long resident = (long long)sms * per_sm_target;
   const long long blocks = need < resident ? need : resident;
   sample_kernel<SET, SPARSE><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx, keys, S, lds,
-                                                                      counter);
+                                                                      counter, lanes);
   return cudaGetLastError();
 }
 

@@ -144,7 +144,7 @@ constexpr int TC_THREADS = (TC_EXP_WARPS + 2 + 4) * 32;  // expanders, producer,
 constexpr int TC_EXP_THREADS = TC_EXP_WARPS * 32;
 constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
 constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
-constexpr int TC_SMEM = kTcStages * (TC_A_BYTES + TC_X_BYTES) + 512;
+constexpr int tc_smem(int stages) { return stages * (TC_A_BYTES + TC_X_BYTES) + 512; }
 constexpr uint32_t TC_TMEM_COLS = 2 * kTcN;  // two FP32 accumulators of 128 lanes x kTcN columns
 static_assert(kTcN % TC_EXP_THREADS == 0, "whole X rows per expander thread");
 
@@ -152,6 +152,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+template <int STAGES>
 __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys, const Segs segs, int kstages,
                                                               int mtiles, long long ntiles,
                                                               const uint32_t *__restrict__ X, int ldx,
@@ -159,21 +160,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
                                                               int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t tsm[];
   uint8_t *As = tsm;
-  uint8_t *Xs = tsm + kTcStages * TC_A_BYTES;
-  uint64_t *full_a = reinterpret_cast<uint64_t *>(Xs + kTcStages * TC_X_BYTES);
-  uint64_t *full_x = full_a + kTcStages;
-  uint64_t *empty = full_x + kTcStages;
-  uint64_t *acc_full = empty + kTcStages;  // [2]
+  uint8_t *Xs = tsm + STAGES * TC_A_BYTES;
+  uint64_t *full_a = reinterpret_cast<uint64_t *>(Xs + STAGES * TC_X_BYTES);
+  uint64_t *full_x = full_a + STAGES;
+  uint64_t *empty = full_x + STAGES;
+  uint64_t *acc_full = empty + STAGES;  // [2]
   uint64_t *acc_empty = acc_full + 2;      // [2]
   uint64_t *done = acc_empty + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-  int *last_copy = reinterpret_cast<int *>(tmem_slot + 2);  // [kTcStages]: last stage copied per buffer
+  int *last_copy = reinterpret_cast<int *>(tmem_slot + 2);  // [STAGES]: last stage copied per buffer
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long ntile_all = (long long)mtiles * ntiles;
   if (tid == 0) {
-    for (int i = 0; i < kTcStages; i++) {
+    for (int i = 0; i < STAGES; i++) {
       mbar_init(&full_a[i], 1);
       mbar_init(&full_x[i], TC_EXP_THREADS);
       mbar_init(&empty[i], 1);
@@ -209,8 +210,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
       for (int j = 0; j < RPT; j++)
         xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx);
       for (int s = 0; s < kstages; s++, g++) {
-        const int buf = (int)(g % kTcStages);
-        if (g >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(g / kTcStages - 1) & 1)) *abort_flag = 1;
+        const int buf = (int)(g % STAGES);
+        if (g >= STAGES && !mbar_wait(&empty[buf], (uint32_t)(g / STAGES - 1) & 1)) *abort_flag = 1;
         if (*abort_flag) break;
         uint4 xcur[RPT];
 #pragma unroll
@@ -252,8 +253,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
         const int seg = seg_find(segs, (tile / mtiles) * kTcN);  // a tile never straddles segments
         const uint8_t *Atile = keys.A8[seg] + (size_t)mtile * kstages * TC_A_BYTES;
         for (int s = 0; s < kstages; s++, g++) {
-          const int buf = (int)(g % kTcStages);
-          if (g >= kTcStages && !mbar_wait(&empty[buf], (uint32_t)(g / kTcStages - 1) & 1)) *abort_flag = 1;
+          const int buf = (int)(g % STAGES);
+          if (g >= STAGES && !mbar_wait(&empty[buf], (uint32_t)(g / STAGES - 1) & 1)) *abort_flag = 1;
           if (*abort_flag) break;
           mbar_expect_tx(&full_a[buf], TC_A_BYTES);
           bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &full_a[buf]);
@@ -273,8 +274,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
         tc_fence_after();
         const uint32_t dacc = tmem + (uint32_t)(ab * kTcN);
         for (int s = 0; s < kstages; s++, g++) {
-          const int buf = (int)(g % kTcStages);
-          const uint32_t par = (uint32_t)(g / kTcStages) & 1;
+          const int buf = (int)(g % STAGES);
+          const uint32_t par = (uint32_t)(g / STAGES) & 1;
           if (!mbar_wait(&full_a[buf], par) || !mbar_wait(&full_x[buf], par)) *abort_flag = 1;
           if (*abort_flag) break;
           tc_fence_after();
@@ -329,8 +330,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   // drain: the MMAs (done barrier) and any A copy still landing
   bool ok = mbar_wait(done, 0);
   if (warp == TC_EXP_WARPS && lane == 0) {
-    for (int b = 0; b < kTcStages; b++)
-      if (last_copy[b] >= 0 && !mbar_wait(&full_a[b], (uint32_t)(last_copy[b] / kTcStages) & 1)) ok = false;
+    for (int b = 0; b < STAGES; b++)
+      if (last_copy[b] >= 0 && !mbar_wait(&full_a[b], (uint32_t)(last_copy[b] / STAGES) & 1)) ok = false;
   }
   const int good = __syncthreads_and(ok && !*abort_flag);
   if (!good && tid == 0) atomicExch(err, 1);
@@ -378,7 +379,11 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
   if (!err || rows_pad % kTcM || kw_pad % (kTcKB / 32) || rows % kTcN || ldx < kw_pad) return cudaErrorInvalidValue;
   for (int i = 0; i < segs.nseg; i++)
     if (!keys.A8[i]) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(gf2_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+  // pipeline depth: the set's tuned stage count (2, 3 or 4 buffers of A and X per CTA)
+  const int stages = keys.tc_stages == 2 || keys.tc_stages == 3 ? keys.tc_stages : kTcStages;
+  auto kern = stages == 2 ? gf2_gemm_tc<2> : stages == 3 ? gf2_gemm_tc<3> : gf2_gemm_tc<kTcStages>;
+  const int smem = tc_smem(stages);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -386,8 +391,8 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
   const int mtiles = rows_pad / kTcM;
   const long long ntiles = rows / kTcN, tiles = ntiles * mtiles;
   const int grid = (int)(tiles < sms ? tiles : sms);  // persistent: one CTA per SM (smem and TMEM bound)
-  gf2_gemm_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(keys, segs, kw_pad / (kTcKB / 32), mtiles, ntiles, X, ldx, Out, ldo,
-                                                 out_words, err);
+  kern<<<grid, TC_THREADS, smem, st>>>(keys, segs, kw_pad / (kTcKB / 32), mtiles, ntiles, X, ldx, Out, ldo,
+                                       out_words, err);
   return cudaGetLastError();
 }
 

@@ -169,8 +169,10 @@ cudaError_t run(const DeviceSetup &su, const gmc_key *sk, uint8_t *k, const uint
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(GEMM_POPC, gk, segs, sk->ldf, sk->frows_pad, X, D::ldx, sk->cw_pad, S2, D::lds2,
                             P<SET>::s2w, nullptr, st);
-  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, D::lds2, su.fd[SET], segs, Sig, st);
-  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, D::lds2, dk, su.fd[SET], segs, E, D::lde, ok, st);
+  const SetTune tune = tune_get(SET);
+  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, D::lds2, su.fd[SET], segs, Sig, st, tune.bm_warps);
+  if (e == cudaSuccess)
+    e = launch_dec_root<SET>(Sig, S2, D::lds2, dk, su.fd[SET], segs, E, D::lde, ok, st, tune.root_warps);
   if (e == cudaSuccess) e = launch_dec_tail<SET>(E, D::lde, ok, c, dk, k, rc, segs, sk->pc != 0, st);
   return e;
 }

@@ -168,6 +168,7 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
     gk.A8[i] = pp.keys[i]->a8;
     gk.TT[i] = pp.keys[i]->TT;
     gk.ldtt = pp.keys[i]->ldtt;
+    gk.tc_stages = tune.gemm_stages;
     if (engine == GEMM_TC && !gk.A8[i]) return cudaErrorInvalidValue;  // registered keys carry their images
   }
   const gmc_setinfo &S = set_info(SET);
@@ -214,8 +215,8 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->ldf, ref->frows_pad, X, cw, ref->cw_pad, S2, s2, p::s2w,
                             tc_err_word_ptr(), pst);
-  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst);
-  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst);
+  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst, tune.bm_warps);
+  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst, tune.root_warps);
   if (e == cudaSuccess)
     e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, false, pst);
   return e;

@@ -3,11 +3,19 @@
 // the fastest, and persists the choices in a JSON cache that later processes
 // load with gmc_autotune_load.
 //
-// Candidates: the engine of the encapsulation syndrome (sparse column gather
-// in the sampler, or the tcgen05 GEMM) crossed with the sampler's block size
-// (32, 64, 128), and the GEMM engine of the decapsulation front end (CUDA-core
-// popcount or tcgen05). Timing: CUDA events
-// around whole batched calls (median of 5 after 2 warm-ups).
+// Candidates, tuned greedily in this order: the engine of the encapsulation
+// syndrome (sparse column gather in the sampler, or the tcgen05 GEMM) crossed
+// with the sampler's block size (32, 64, 128); the GEMM engine of the
+// decapsulation front end (CUDA-core popcount or tcgen05); the tcgen05 GEMM's
+// pipeline depth (2, 3 or 4 A/X stages per CTA, when either op uses that
+// engine); and the requests per block of the two decoding kernels
+// (Berlekamp-Massey: 2, 4 or 8 warps of 32 requests, timed only when the batch
+// takes its bit-sliced form; root finding: 2, 4 or 8 warps of one request).
+// The GEMM tile is fixed at 128 x 256 (one tcgen05 M=128 instruction shape
+// and a TMEM accumulator pair) and K is never split: every CTA owns whole
+// output tiles, so there is no split-K reduction to tune. A later candidate
+// replaces the current choice only when it is more than 1% faster. Timing:
+// CUDA events around whole batched calls (median of 5 after 2 warm-ups).
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
@@ -100,12 +108,13 @@ std::string object_of(const std::string &text, const std::string &name) {
 }
 
 std::string set_entry(int set, const SetTune &t) {
-  char buf[320];
+  char buf[400];
   snprintf(buf, sizeof buf,
-           "    \"%s\": {\"enc_engine\": \"%s\", \"dec_engine\": \"%s\", \"sample_threads\": %d, \"n\": %lld, "
-           "\"enc_ms\": %.4f, \"dec_ms\": %.4f}",
-           set_info(set).name, engine_name(t.enc_engine), engine_name(t.dec_engine), t.sample_threads, t.n, t.enc_ms,
-           t.dec_ms);
+           "    \"%s\": {\"enc_engine\": \"%s\", \"dec_engine\": \"%s\", \"sample_threads\": %d, "
+           "\"gemm_stages\": %d, \"bm_warps\": %d, \"root_warps\": %d, \"n\": %lld, \"enc_ms\": %.4f, "
+           "\"dec_ms\": %.4f}",
+           set_info(set).name, engine_name(t.enc_engine), engine_name(t.dec_engine), t.sample_threads, t.gemm_stages,
+           t.bm_warps, t.root_warps, t.n, t.enc_ms, t.dec_ms);
   return buf;
 }
 
@@ -150,6 +159,27 @@ extern "C" int gmc_tune_set(int set, int enc_engine, int dec_engine, int sample_
   t.sample_threads = sample_threads;
   tune_put(set, t);
   return GMC_OK;
+}
+
+extern "C" int gmc_tune_set_launch(int set, int gemm_stages, int bm_warps, int root_warps) {
+  if (set < 0 || set >= GMC_NSETS || gemm_stages < 2 || gemm_stages > kTcStages || bm_warps < 1 ||
+      bm_warps > kBMWarps || root_warps < 1 || root_warps > kRootWarps)
+    return tune_error(GMC_EINVAL, "gmc_tune_set_launch: bad argument");
+  SetTune t = tune_get(set);
+  t.gemm_stages = gemm_stages;
+  t.bm_warps = bm_warps;
+  t.root_warps = root_warps;
+  tune_put(set, t);
+  return GMC_OK;
+}
+
+extern "C" int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warps) {
+  if (set < 0 || set >= GMC_NSETS) return tune_error(GMC_EINVAL, "gmc_tune_get_launch: bad set");
+  SetTune t = tune_get(set);
+  if (gemm_stages) *gemm_stages = t.gemm_stages;
+  if (bm_warps) *bm_warps = t.bm_warps;
+  if (root_warps) *root_warps = t.root_warps;
+  return t.tuned;
 }
 
 extern "C" int gmc_tune_get(int set, int *enc_engine, int *dec_engine, int *sample_threads) {
@@ -220,6 +250,54 @@ extern "C" int gmc_autotune(int set, long long n, const char *cache_path) {
         best.dec_engine = engines[ei];
       }
     }
+    auto time_dec = [&](const SetTune &t) {
+      tune_put(set, t);
+      return time_median([&] { return gmc_dec_batch_dev(K, key2, ct, n, nullptr, st); }, st, a, b, &rc);
+    };
+    // pipeline depth of the tcgen05 GEMM (both ops share it)
+    if (best.enc_engine == GEMM_TC || best.dec_engine == GEMM_TC) {
+      const int stage_cand[3] = {4, 3, 2};
+      float best_sum = 1e30f;
+      for (int si = 0; si < 3; si++) {
+        SetTune t = best;
+        t.gemm_stages = stage_cand[si];
+        tune_put(set, t);
+        const float me =
+            best.enc_engine == GEMM_TC
+                ? time_median([&] { return gmc_enc_batch_dev(P, ct, key, seeds, n, nullptr, st); }, st, a, b, &rc)
+                : best_enc;
+        const float md = best.dec_engine == GEMM_TC ? time_dec(t) : best_dec;
+        if (si == 0 || me + md < 0.99f * best_sum) {
+          best_sum = me + md;
+          best.gemm_stages = stage_cand[si];
+          best_enc = me;
+          best_dec = md;
+        }
+      }
+      tune_put(set, best);
+      rc |= gmc_enc_batch_dev(P, ct, key, seeds, n, nullptr, st);  // the ciphertexts the dec timings read
+    }
+    // requests per block of the decoding kernels
+    const int warp_cand[3] = {8, 4, 2};
+    if (n >= kBMBitslicedMinRows)
+      for (int wi = 1; wi < 3; wi++) {
+        SetTune t = best;
+        t.bm_warps = warp_cand[wi];
+        const float ms = time_dec(t);
+        if (ms < 0.99f * best_dec) {
+          best_dec = ms;
+          best.bm_warps = warp_cand[wi];
+        }
+      }
+    for (int wi = 1; wi < 3; wi++) {
+      SetTune t = best;
+      t.root_warps = warp_cand[wi];
+      const float ms = time_dec(t);
+      if (ms < 0.99f * best_dec) {
+        best_dec = ms;
+        best.root_warps = warp_cand[wi];
+      }
+    }
     best.tuned = 1;
     best.enc_ms = best_enc;
     best.dec_ms = best_dec;
@@ -258,6 +336,11 @@ extern "C" int gmc_autotune_load(const char *cache_path) {
     if (t.dec_engine == GEMM_SPARSE) t.dec_engine = GEMM_TC;  // no sparse form for the front end
     const int th = atoi(field(o, "sample_threads").c_str());
     t.sample_threads = (th == 32 || th == 64 || th == 128) ? th : 128;
+    const int gs = atoi(field(o, "gemm_stages").c_str());
+    t.gemm_stages = (gs >= 2 && gs <= kTcStages) ? gs : kTcStages;
+    const int bw = atoi(field(o, "bm_warps").c_str()), rw = atoi(field(o, "root_warps").c_str());
+    t.bm_warps = (bw >= 1 && bw <= kBMWarps) ? bw : kBMWarps;
+    t.root_warps = (rw >= 1 && rw <= kRootWarps) ? rw : kRootWarps;
     t.n = atoll(field(o, "n").c_str());
     t.enc_ms = atof(field(o, "enc_ms").c_str());
     t.dec_ms = atof(field(o, "dec_ms").c_str());
