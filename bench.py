@@ -420,14 +420,32 @@ def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops):
     return out
 
 
-def keccak_rates(z, n, kernels):
+# 32-bit instruction count of one Keccak-f[1600] permutation on 32-bit halves, fully fused (a lower bound):
+# per round theta 20 lop3 (5-way column XORs) + 10 shf (rot 1) + 50 lop3 (A ^ C[x-1] ^ rot C[x+1]),
+# rho 48 shf (24 rotations, none by 0 or 32), chi 50 lop3 (b ^ (~c & d)), iota 2 lop3.
+KECCAK_LOP3_PER_PERM = 24 * (20 + 50 + 50 + 2)
+KECCAK_SHF_PER_PERM = 24 * (10 + 48)
+
+
+def keccak_rates(z, n, kernels, gmc=None):
     """Keccak-f[1600] permutations per second of the two session-key hash kernels (each request hashes the
-    1 + n/8 + ct-byte preimage: ceil((len + 1) / 136) permutations)."""
+    1 + n/8 + ct-byte preimage: ceil((len + 1) / 136) permutations), beside the integer-op ceiling: the
+    permutation's op count over the GPU's measured lop3 and funnel-shift rates."""
     perms = (1 + z["n"] // 8 + z["ct_bytes"] + 1 + 135) // 136
     out = {"perms_per_hash": perms}
+    ceiling = None
+    if gmc is not None:
+        pk = gmc.int32_peak()
+        ceiling = 1.0 / (KECCAK_LOP3_PER_PERM / pk["lop3_per_s"] + KECCAK_SHF_PER_PERM / pk["shf_per_s"])
+        out["int32_peak"] = {"lop3_per_s": pk["lop3_per_s"], "shf_per_s": pk["shf_per_s"],
+                             "ops_per_perm": {"lop3": KECCAK_LOP3_PER_PERM, "shf": KECCAK_SHF_PER_PERM},
+                             "ceiling_perms_per_s": ceiling}
     for kname in ("enc_finalize_hash", "dec_tail_hash"):
         if kname in kernels:
-            out[kname] = {"perms_per_s": n * perms / (kernels[kname]["ms"] / 1e3)}
+            r = n * perms / (kernels[kname]["ms"] / 1e3)
+            out[kname] = {"perms_per_s": r}
+            if ceiling:
+                out[kname]["frac_of_ceiling"] = r / ceiling
     return out
 
 
@@ -651,7 +669,7 @@ def main():
         "wall_s_timed_loop": wall,
     }
 
-    line["keccak"] = keccak_rates(z, N, kernels)
+    line["keccak"] = keccak_rates(z, N, kernels, gmc)
     if rank == 0 and not args.no_sweep:
         line["n_sweep"] = {"set": args.set, "flip": args.flip,
                            "ops_s": n_sweep(gmc, torch, dev, args.set, [256, 1024, 4096, 16384, 65536], 5, args.flip)}

@@ -287,6 +287,10 @@ int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warp
 /* Reads and clears the tensor-core engine's error word on the current device:
  * 1 when a CTA gave up on a bounded wait (its outputs are then invalid). */
 int gmc_tc_status(void);
+/* Measured integer-pipe rates of this GPU (lane-ops per second): 3-input
+ * logic ops (lop3) and 32-bit funnel shifts, the instruction kinds of a
+ * Keccak-f[1600] permutation on 32-bit halves. For the Keccak ceiling. */
+int gmc_int32_peak(double *lop3_per_s, double *shf_per_s);
 
 /* Stage outputs of a decapsulation batch (device pointers): the 2t packed
  * syndromes (s_words per request), the error vectors (e_words per request)

@@ -90,6 +90,7 @@ def lib():
         L.gmc_tune_set.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.gmc_tune_get.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                    ctypes.POINTER(ctypes.c_int)]
+        L.gmc_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.gmc_tune_set_launch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.gmc_tune_get_launch.argtypes = L.gmc_tune_get.argtypes
         vp = ctypes.c_void_p
@@ -423,6 +424,13 @@ def tune_set(set_name, enc_engine, dec_engine, sample_threads, gemm_stages=None,
         cur = tune_get(sid)
         _check(lib().gmc_tune_set_launch(sid, int(gemm_stages or cur["gemm_stages"]), int(bm_warps or cur["bm_warps"]),
                                          int(root_warps or cur["root_warps"])), "gmc_tune_set_launch")
+
+
+def int32_peak():
+    """Measured integer-pipe rates of the current GPU: {"lop3_per_s", "shf_per_s"} (lane-ops per second)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(lib().gmc_int32_peak(ctypes.byref(a), ctypes.byref(b)), "gmc_int32_peak")
+    return {"lop3_per_s": a.value, "shf_per_s": b.value}
 
 
 def set_gemm_engine(engine):

@@ -4,6 +4,8 @@
 // Reference behaviour: gen_e / syndrome / operation_enc of libmceliece
 // (mceliece-gpu-params/ref/348864.cuh:3434-3565, 8192128.cuh:5967-6006;
 // mc:crypto_kem/348864/vec/encrypt.c:41-132, kem_enc.c:18).
+#include <stdlib.h>
+
 #include "kernels.h"
 #include "device_common.cuh"
 
@@ -232,6 +234,254 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
   }
 }
 
+// ---------------------------------------------------------------- pipelined sampling (small batches)
+// The seed chain's next state is the first 32 bytes of an attempt's first
+// Keccak-f block, so only that block is on the chain's critical path; the
+// attempt's further squeeze blocks (P - 1 of them: P = 2 for 348864 and
+// 8192128, 3 for 460896, 4 for 6688128 and 6960119) are not. A request is
+// held by a group of G >= P lanes: at every step lane 0 of the group starts
+// the next attempt (absorb 64 || state, permute) while lane r < P permutes the
+// state lane r - 1 handed it a step earlier (block r of an older attempt); all
+// lanes permute in lockstep, so a step costs one permutation and an attempt
+// completes every step once the pipeline is full. Each block's 17 output
+// words go to the attempt's slot of a per-group ring in shared memory; when
+// block P - 1 lands, the warp checks the attempt (candidate filter, first t
+// kept, repeats) exactly as the lane-per-request form does, and a success
+// drops the group's younger attempts. Used when the batch is small enough that
+// every request gets its own group at once; larger batches are
+// throughput-bound and take the lane-per-request form (no speculative blocks).
+template <int SET>
+struct PipeLayout {
+  using p = P<SET>;
+  static constexpr int perms = (p::cand_bytes + 135) / 136;  // Keccak-f blocks per attempt
+  static constexpr int G = perms <= 2 ? 2 : 4;                // lanes per group
+  static constexpr int NG = 32 / G;                          // groups per warp at most
+  static constexpr int raw_words = (p::cand_bytes + 7) / 8;  // u64 words of one attempt's draw
+  static constexpr int bm_words = (p::ew + 1) & ~1;
+  static constexpr int cand_off = bm_words * 4;
+  static constexpr int ring_off = cand_off + (p::t * 2 + 7) / 8 * 8;
+  static constexpr int warp_bytes = ring_off + NG * perms * raw_words * 8;
+  static_assert(perms <= G && raw_words <= 17 * perms, "pipeline geometry");
+};
+
+template <int SET, bool SPARSE>
+__global__ void __launch_bounds__(kSampleThreadsMax)
+    sample_pipe_kernel(const uint8_t *__restrict__ seeds, const Segs segs, uint32_t *__restrict__ E, int lde,
+                       uint32_t *__restrict__ Ens, int ldx, const GemmKeys keys, uint32_t *__restrict__ S, int lds,
+                       unsigned int *__restrict__ counter, int groups) {
+  using p = P<SET>;
+  using LY = PipeLayout<SET>;
+  constexpr int PP = LY::perms, G = LY::G, RW = LY::raw_words, NCW = (p::t + 31) / 32;
+  constexpr int ncand = p::cand_bytes / 2;
+  constexpr uint32_t mask = p::q - 1;
+  constexpr int sh = p::mt % 32, w0 = p::mt / 32;
+  extern __shared__ __align__(16) uint32_t sm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint8_t *wb = reinterpret_cast<uint8_t *>(sm) + (size_t)warp * LY::warp_bytes;
+  uint32_t *bm = reinterpret_cast<uint32_t *>(wb);
+  uint16_t *cand = reinterpret_cast<uint16_t *>(wb + LY::cand_off);
+  uint64_t *ring = reinterpret_cast<uint64_t *>(wb + LY::ring_off);
+  for (int w = lane; w < LY::bm_words; w += 32) bm[w] = 0;
+  __syncwarp();
+  const int g = lane / G, r = lane % G;
+  const bool chain = r == 0 && g < groups;  // the lane that owns the group's request and seed chain
+  const long long N = seg_rows(segs);
+  bool has = false, exhausted = !chain;
+  long long op = 0;
+  int myseg = 0, attempt = 0;
+  uint64_t st[4] = {0, 0, 0, 0};
+  uint64_t s[25];
+#pragma unroll
+  for (int i = 0; i < 25; i++) s[i] = 0;
+  bool valid = false;  // this lane holds block r of attempt att of the group's request
+  int att = 0;
+#pragma unroll 1
+  while (true) {
+    // chain lanes without a request take the next ones (segment gaps are skipped)
+    const uint32_t need = __ballot_sync(0xffffffffu, !has && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned int base = 0;
+      if (lane == leader) base = atomicAdd(counter, (unsigned int)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if ((need >> lane) & 1) {
+        const long long idx = (long long)base + __popc(need & ((1u << lane) - 1));
+        if (idx >= N) {
+          exhausted = true;
+        } else {
+          op = idx;
+          has = seg_live(segs, idx, &myseg);
+          attempt = 0;
+          if (has) {
+            const uint8_t *sd = seeds + 32 * idx;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+              uint64_t v = 0;
+#pragma unroll
+              for (int b = 0; b < 8; b++) v |= (uint64_t)sd[8 * i + b] << (8 * b);
+              st[i] = v;
+            }
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, has || valid)) {
+      if (__all_sync(0xffffffffu, exhausted)) break;
+      continue;
+    }
+    // lane 0 of a group starts its request's next attempt: SHAKE256 absorb of {64} || state
+    if (r == 0) {
+      valid = has;
+      att = attempt;
+      if (has) {
+#pragma unroll
+        for (int i = 0; i < 25; i++) s[i] = 0;
+        s[0] = 64ull | (st[0] << 8);
+        s[1] = (st[0] >> 56) | (st[1] << 8);
+        s[2] = (st[1] >> 56) | (st[2] << 8);
+        s[3] = (st[2] >> 56) | (st[3] << 8);
+        s[4] = (st[3] >> 56) | (0x1Full << 8);
+        s[16] = 0x8000000000000000ull;
+      }
+    }
+    keccak_f1600(s);
+    if (valid) {
+      uint64_t *dst = ring + (size_t)(g * PP + att % PP) * RW;
+#pragma unroll
+      for (int i = 0; i < 17; i++) {
+        const int w = 17 * r + i;
+        if (w < RW) dst[w] = s[i];
+      }
+      if (r == 0) {
+        st[0] = s[0];
+        st[1] = s[1];
+        st[2] = s[2];
+        st[3] = s[3];
+        attempt++;
+      }
+    }
+    __syncwarp();
+    // attempts whose last block landed: filter, first t kept, repeats; one group at a time
+    uint32_t pend = __ballot_sync(0xffffffffu, valid && r == PP - 1);
+    uint32_t succ = 0;  // bit per group
+#pragma unroll 1
+    while (pend) {
+      const int L = __ffs(pend) - 1;
+      pend &= pend - 1;
+      const int gg = L / G, owner = gg * G;
+      const int a = __shfl_sync(0xffffffffu, att, L);
+      const uint16_t *raw = reinterpret_cast<const uint16_t *>(ring + (size_t)(gg * PP + a % PP) * RW);
+      int total = 0;
+#pragma unroll
+      for (int base = 0; base < ncand; base += 32) {
+        const int i = base + lane;
+        uint32_t v = 0;
+        bool keep = false;
+        if (i < ncand) {
+          v = raw[i] & mask;
+          keep = p::full || v < (uint32_t)p::n;
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+        const int idx = total + __popc(bal & ((1u << lane) - 1));
+        if (keep && idx < p::t) cand[idx] = (uint16_t)v;
+        total += __popc(bal);
+      }
+      __syncwarp();
+      if (total < p::t) continue;  // too few candidates below n: the attempt fails (warp-uniform)
+      uint32_t vv[NCW];
+      bool dup = false;
+#pragma unroll
+      for (int i = 0; i < NCW; i++) {
+        const int c = lane + 32 * i;
+        vv[i] = 0xFFFFFFFFu;
+        if (c < p::t) {
+          const uint32_t v = cand[c];
+          vv[i] = v;
+          const uint32_t bit = 1u << (v & 31);
+          dup |= (atomicOr(&bm[v >> 5], bit) & bit) != 0;
+        }
+      }
+      const bool anydup = __any_sync(0xffffffffu, dup);
+      if (!anydup) {
+        succ |= 1u << gg;
+        const long long opr = __shfl_sync(0xffffffffu, op, owner);
+        uint32_t *erow = E + opr * lde;
+        for (int w = lane; w < p::ew; w += 32) erow[w] = bm[w];
+        if (SPARSE) {
+          // S = T e[mt:n], lane-parallel over the t positions (as in sample_kernel)
+          const uint32_t *TT = keys.TT[__shfl_sync(0xffffffffu, myseg, owner)];
+          constexpr int MW4 = (p::mw + 3) / 4;
+          uint4 acc[MW4];
+#pragma unroll
+          for (int w = 0; w < MW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
+#pragma unroll
+          for (int i = 0; i < NCW; i++) {
+            const int c = lane + 32 * i;
+            const int pos = c < p::t ? cand[c] : 0;
+            const uint4 *col =
+                reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * keys.ldtt);
+#pragma unroll
+            for (int w = 0; w < MW4; w++) {
+              const uint4 v = col[w];
+              acc[w].x ^= v.x;
+              acc[w].y ^= v.y;
+              acc[w].z ^= v.z;
+              acc[w].w ^= v.w;
+            }
+          }
+          uint32_t my0 = 0, my1 = 0;
+#pragma unroll
+          for (int w = 0; w < MW4; w++) {
+            const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
+#pragma unroll
+            for (int e2 = 0; e2 < 4; e2++) {
+              const int word = 4 * w + e2;
+              if (word < p::mw) {
+                const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
+                if (word < 32) my0 = (lane == word) ? v : my0;
+                else my1 = (lane == word - 32) ? v : my1;
+              }
+            }
+          }
+          uint32_t *srow = S + opr * lds;
+          if (lane < p::mw) srow[lane] = my0;
+          if (p::mw > 32 && lane + 32 < p::mw) srow[lane + 32] = my1;
+        } else {
+          uint32_t *xrow = Ens + opr * ldx;
+          for (int w = lane; w < p::kw; w += 32) {
+            const uint32_t lo = bm[w0 + w];
+            const uint32_t hi = (w0 + w + 1 < p::ew) ? bm[w0 + w + 1] : 0u;
+            xrow[w] = sh ? ((lo >> sh) | (hi << (32 - sh))) : lo;
+          }
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NCW; i++)
+        if (vv[i] != 0xFFFFFFFFu) bm[vv[i] >> 5] = 0;
+      __syncwarp();
+    }
+    // a success ends the request: its younger attempts in flight are dropped
+    if ((succ >> g) & 1) {
+      valid = false;
+      if (r == 0) has = false;
+    }
+    // hand each block state one lane along the group (lane r permutes block r next step)
+#pragma unroll
+    for (int i = 0; i < 25; i++) {
+      const uint32_t lo = __shfl_up_sync(0xffffffffu, (uint32_t)s[i], 1, G);
+      const uint32_t hi = __shfl_up_sync(0xffffffffu, (uint32_t)(s[i] >> 32), 1, G);
+      s[i] = ((uint64_t)hi << 32) | lo;
+    }
+    const bool vin = __shfl_up_sync(0xffffffffu, valid ? 1 : 0, 1, G) != 0;
+    const int ain = __shfl_up_sync(0xffffffffu, att, 1, G);
+    if (r > 0) {
+      valid = vin && r < PP;
+      att = ain;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- finalize
 // c = e[0:mt] xor (T e[mt:n]); K = SHAKE256(1 || e || c). When the public
 // key's padding bits are set (6960119 only), c and K are zeroed
@@ -327,6 +577,16 @@ cudaError_t launch_transpose_pk(const uint32_t *T, int lda, int mt, int k, uint3
 }
 
 // ---------------------------------------------------------------- launchers
+// GMC_SAMPLE_PIPELINE=0 in the environment keeps every batch on the
+// lane-per-request sampler (read once per process).
+static bool sample_pipeline_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("GMC_SAMPLE_PIPELINE");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
 template <int SET, bool SPARSE>
 static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens,
                                      int ldx, const GemmKeys &keys, uint32_t *S, int lds, int threads,
@@ -346,6 +606,30 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
   // requests, so the last slow chains hold few warps (kSampleWarpsPerSM)
   const int warps = threads / 32;
   int per_sm_target = (kSampleWarpsPerSM + warps - 1) / warps;
+  // pipelined form when the resident warps can give every request its own lane group
+  if (sample_pipeline_enabled()) {
+    using PL = PipeLayout<SET>;
+    const int psmem = warps * PL::warp_bytes;
+    err = cudaFuncSetAttribute(sample_pipe_kernel<SET, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (kSampleThreadsMax / 32) * PL::warp_bytes);
+    if (err != cudaSuccess) return err;
+    int pper = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pper, sample_pipe_kernel<SET, SPARSE>, threads, psmem);
+    if (pper < 1) pper = 1;
+    const int ptarget = per_sm_target < pper ? per_sm_target : pper;
+    const long long pslots = (long long)sms * ptarget * warps;
+    if (N <= PL::NG * pslots) {
+      int groups = 1;
+      while (groups < PL::NG && (long long)groups * pslots < N) groups <<= 1;
+      const long long per_block = (long long)warps * groups;
+      const long long need = (N + per_block - 1) / per_block;
+      const long long resident = (long long)sms * ptarget;
+      const long long blocks = need < resident ? need : resident;
+      sample_pipe_kernel<SET, SPARSE><<<(unsigned)blocks, threads, psmem, st>>>(seeds, segs, E, lde, Ens, ldx, keys,
+                                                                                S, lds, counter, groups);
+      return cudaGetLastError();
+    }
+  }
   if (per_sm_target > per_sm) per_sm_target = per_sm;
   // active lanes per warp: the smallest power of two (<= 32) with which the
   // resident warps hold the whole batch at once

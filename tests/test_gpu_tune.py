@@ -87,3 +87,11 @@ def test_launch_shapes(gmc, keys, sid):
     finally:
         gmc.tune_set(sid, prev["enc_engine"], prev["dec_engine"], prev["sample_threads"],
                      gemm_stages=prev["gemm_stages"], bm_warps=prev["bm_warps"], root_warps=prev["root_warps"])
+
+
+def test_int32_peak(gmc):
+    """The integer-pipe microbenchmark behind the Keccak ceiling gives rates
+    between 1 and 1000 T lane-ops/s for both instruction kinds."""
+    pk = gmc.int32_peak()
+    for k in ("lop3_per_s", "shf_per_s"):
+        assert 1e12 < pk[k] < 1e15, pk
