@@ -82,7 +82,9 @@ int gmc_key_import(gmc_key **out, const unsigned char *buf, long long len);
  * -1 only for a 6960119 key with nonzero padding bits, as the library).
  * _dev: all pointers are device pointers, work is queued on `stream`
  * (a cudaStream_t, 0 = default stream) and the call returns without waiting.
- * Without _dev: host pointers; the call copies in, runs and copies out. */
+ * Without _dev: host pointers; the call copies in, runs and copies out.
+ * GMC_SAMPLE_PIPELINE=0 in the environment (read once) selects the
+ * lane-per-request sampler instead of the pipelined one (same outputs). */
 int gmc_enc_batch_dev(const gmc_key *pk, unsigned char *c, unsigned char *k, const unsigned char *seeds,
                       long long n, int *rc, void *stream);
 int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char *k, const unsigned char *seeds,

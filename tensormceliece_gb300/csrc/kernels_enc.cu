@@ -18,6 +18,8 @@ namespace gmc {
 // bits; for n < 2^m the first t values below n are kept, else all t. A
 // repeated position rejects the attempt (only the set of positions matters,
 // as in the library's sort-and-compare).
+// Two forms: sample_pipe_kernel (below, the default) and this lane-per-request
+// sample_kernel (GMC_SAMPLE_PIPELINE=0), which share the check and gather steps.
 // Work split: each lane owns one request and runs its Keccak chain; lanes
 // take requests from a launch-wide counter whenever their previous request
 // is done, so a request that needs many attempts does not hold the warp's
@@ -234,7 +236,7 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
   }
 }
 
-// ---------------------------------------------------------------- pipelined sampling (small batches)
+// ---------------------------------------------------------------- pipelined sampling
 // The seed chain's next state is the first 32 bytes of an attempt's first
 // Keccak-f block, so only that block is on the chain's critical path; the
 // attempt's further squeeze blocks (P - 1 of them: P = 2 for 348864 and
@@ -247,9 +249,12 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
 // words go to the attempt's slot of a per-group ring in shared memory; when
 // block P - 1 lands, the warp checks the attempt (candidate filter, first t
 // kept, repeats) exactly as the lane-per-request form does, and a success
-// drops the group's younger attempts. Used when the batch is small enough that
-// every request gets its own group at once; larger batches are
-// throughput-bound and take the lane-per-request form (no speculative blocks).
+// drops the group's younger attempts. Groups take further requests from the
+// launch-wide counter like the lanes of sample_kernel. Per request this costs
+// P - 1 speculative first blocks and P - 1 steps of pipeline fill, but the
+// chain's critical path is one permutation per attempt instead of P, which
+// matters most for the slowest chains of a batch (about 24 attempts for the
+// slowest of 65536 requests).
 template <int SET>
 struct PipeLayout {
   using p = P<SET>;
@@ -577,9 +582,9 @@ cudaError_t launch_transpose_pk(const uint32_t *T, int lda, int mt, int k, uint3
 }
 
 // ---------------------------------------------------------------- launchers
-// GMC_SAMPLE_PIPELINE=0 in the environment keeps every batch on the
-// lane-per-request sampler (read once per process).
-static bool sample_pipeline_enabled() {
+// GMC_SAMPLE_PIPELINE=0 in the environment (read once per process) puts
+// every batch on the lane-per-request sampler instead of the pipelined one.
+static bool sample_pipelined() {
   static const bool on = [] {
     const char *v = getenv("GMC_SAMPLE_PIPELINE");
     return !(v && v[0] == '0');
@@ -606,8 +611,12 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
   // requests, so the last slow chains hold few warps (kSampleWarpsPerSM)
   const int warps = threads / 32;
   int per_sm_target = (kSampleWarpsPerSM + warps - 1) / warps;
-  // pipelined form when the resident warps can give every request its own lane group
-  if (sample_pipeline_enabled()) {
+  // pipelined form (every set and batch size measured faster than the
+  // lane-per-request form: 348864 / 460896 / 6688128 / 6960119 / 8192128 at
+  // 65536 requests 0.31 / 0.63 / 0.89 / 0.77 / 0.57 ms against 0.37 / 0.80 /
+  // 1.00 / 0.82 / 0.70 ms, and up to 2.3x at 16384); groups take further
+  // requests when the batch outnumbers them
+  if (sample_pipelined()) {
     using PL = PipeLayout<SET>;
     const int psmem = warps * PL::warp_bytes;
     err = cudaFuncSetAttribute(sample_pipe_kernel<SET, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -618,17 +627,17 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
     if (pper < 1) pper = 1;
     const int ptarget = per_sm_target < pper ? per_sm_target : pper;
     const long long pslots = (long long)sms * ptarget * warps;
-    if (N <= PL::NG * pslots) {
-      int groups = 1;
-      while (groups < PL::NG && (long long)groups * pslots < N) groups <<= 1;
-      const long long per_block = (long long)warps * groups;
-      const long long need = (N + per_block - 1) / per_block;
-      const long long resident = (long long)sms * ptarget;
-      const long long blocks = need < resident ? need : resident;
-      sample_pipe_kernel<SET, SPARSE><<<(unsigned)blocks, threads, psmem, st>>>(seeds, segs, E, lde, Ens, ldx, keys,
-                                                                                S, lds, counter, groups);
-      return cudaGetLastError();
-    }
+    // active groups per warp: the smallest power of two with which the
+    // resident warps hold the whole batch at once, at most 32 / G
+    int groups = 1;
+    while (groups < PL::NG && (long long)groups * pslots < N) groups <<= 1;
+    const long long per_block = (long long)warps * groups;
+    const long long need = (N + per_block - 1) / per_block;
+    const long long resident = (long long)sms * ptarget;
+    const long long blocks = need < resident ? need : resident;
+    sample_pipe_kernel<SET, SPARSE><<<(unsigned)blocks, threads, psmem, st>>>(seeds, segs, E, lde, Ens, ldx, keys, S,
+                                                                              lds, counter, groups);
+    return cudaGetLastError();
   }
   if (per_sm_target > per_sm) per_sm_target = per_sm;
   // active lanes per warp: the smallest power of two (<= 32) with which the
