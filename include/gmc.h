@@ -278,14 +278,16 @@ int gmc_get_gemm_engine(void);
  * The launch shape is tuned with them: the tcgen05 GEMM's pipeline depth
  * (gemm_stages 2..4 A/X buffers per CTA, default 4) and the requests per block
  * of the decoding kernels (bm_warps: Berlekamp-Massey warps of 32 requests,
- * root_warps: root-finding warps of one request; 1..8, default 8);
- * gmc_tune_set_launch / gmc_tune_get_launch set and read them by hand. */
+ * root_warps: root-finding warps of one request; 1..8, default 8) and the
+ * pipelined sampler's resident warps per SM (sample_sm_warps, 0 = as many as
+ * fit, the default); gmc_tune_set_launch / gmc_tune_get_launch set and read
+ * them by hand. */
 int gmc_autotune(int set, long long n, const char *cache_path);
 int gmc_autotune_load(const char *cache_path);
 int gmc_tune_set(int set, int enc_engine, int dec_engine, int sample_threads);
 int gmc_tune_get(int set, int *enc_engine, int *dec_engine, int *sample_threads);
-int gmc_tune_set_launch(int set, int gemm_stages, int bm_warps, int root_warps);
-int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warps);
+int gmc_tune_set_launch(int set, int gemm_stages, int bm_warps, int root_warps, int sample_sm_warps);
+int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warps, int *sample_sm_warps);
 /* Reads and clears the tensor-core engine's error word on the current device:
  * 1 when a CTA gave up on a bounded wait (its outputs are then invalid). */
 int gmc_tc_status(void);

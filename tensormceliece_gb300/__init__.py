@@ -91,8 +91,8 @@ def lib():
         L.gmc_tune_get.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                    ctypes.POINTER(ctypes.c_int)]
         L.gmc_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
-        L.gmc_tune_set_launch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
-        L.gmc_tune_get_launch.argtypes = L.gmc_tune_get.argtypes
+        L.gmc_tune_set_launch.argtypes = [ctypes.c_int] * 5
+        L.gmc_tune_get_launch.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4
         vp = ctypes.c_void_p
         L.gmc_server_create.argtypes = [ctypes.POINTER(vp), ctypes.c_longlong, ctypes.c_int, ctypes.c_double]
         L.gmc_server_add_key.argtypes = [vp, vp]
@@ -408,22 +408,27 @@ def tune_get(set_name):
     a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     tuned = _check(lib().gmc_tune_get(sid, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "gmc_tune_get")
     names = {GEMM_POPC: "popc", GEMM_B1MMA: "b1mma", GEMM_TC: "tc", GEMM_SPARSE: "sparse"}
-    g, w1, w2 = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    _check(lib().gmc_tune_get_launch(sid, ctypes.byref(g), ctypes.byref(w1), ctypes.byref(w2)), "gmc_tune_get_launch")
+    g, w1, w2, w3 = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(lib().gmc_tune_get_launch(sid, ctypes.byref(g), ctypes.byref(w1), ctypes.byref(w2), ctypes.byref(w3)),
+           "gmc_tune_get_launch")
     return {"enc_engine": names[a.value], "dec_engine": names[b.value], "sample_threads": c.value,
-            "gemm_stages": g.value, "bm_warps": w1.value, "root_warps": w2.value, "tuned": bool(tuned)}
+            "sample_sm_warps": w3.value, "gemm_stages": g.value, "bm_warps": w1.value, "root_warps": w2.value,
+            "tuned": bool(tuned)}
 
 
-def tune_set(set_name, enc_engine, dec_engine, sample_threads, gemm_stages=None, bm_warps=None, root_warps=None):
+def tune_set(set_name, enc_engine, dec_engine, sample_threads, gemm_stages=None, bm_warps=None, root_warps=None,
+             sample_sm_warps=None):
     """Sets a parameter set's launch configuration; the launch-shape arguments
     left as None keep their current values."""
     sid = set_name if isinstance(set_name, int) else set_id(set_name)
     ids = {"popc": GEMM_POPC, "b1mma": GEMM_B1MMA, "tc": GEMM_TC, "sparse": GEMM_SPARSE}
     _check(lib().gmc_tune_set(sid, ids[enc_engine], ids[dec_engine], int(sample_threads)), "gmc_tune_set")
-    if gemm_stages is not None or bm_warps is not None or root_warps is not None:
+    shape = (gemm_stages, bm_warps, root_warps, sample_sm_warps)
+    if any(v is not None for v in shape):
         cur = tune_get(sid)
-        _check(lib().gmc_tune_set_launch(sid, int(gemm_stages or cur["gemm_stages"]), int(bm_warps or cur["bm_warps"]),
-                                         int(root_warps or cur["root_warps"])), "gmc_tune_set_launch")
+        vals = [cur[k] if v is None else v
+                for k, v in zip(("gemm_stages", "bm_warps", "root_warps", "sample_sm_warps"), shape)]
+        _check(lib().gmc_tune_set_launch(sid, *[int(v) for v in vals]), "gmc_tune_set_launch")
 
 
 def int32_peak():

@@ -107,10 +107,11 @@ cudaError_t launch_transpose_pk(const uint32_t *T, int lda, int mt, int k, uint3
 // counter: 4 bytes of device scratch (zeroed here, on st) that nothing else
 // touches until the sampler ends; the pipelines lend the first word of the
 // buffer the sampler does not write (S in dense mode, Ens in sparse mode).
+// sm_warps: resident warps per SM of the pipelined sampler (0 = as many as fit).
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
-                          cudaStream_t st);
+                          cudaStream_t st, int sm_warps = 0);
 // C rows: synd_bytes, or synd_bytes + 32 with plaintext confirmation (pc):
 // C0 || SHAKE256(2 || e, 32), K = SHAKE256(1 || e || C0 || C1).
 template <int SET>

@@ -243,7 +243,8 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
 // 8192128, 3 for 460896, 4 for 6688128 and 6960119) are not. A request is
 // held by a group of G >= P lanes: at every step lane 0 of the group starts
 // the next attempt (absorb 64 || state, permute) while lane r < P permutes the
-// state lane r - 1 handed it a step earlier (block r of an older attempt); all
+// state lane r - 1 left in shared memory a step earlier (block r of an older
+// attempt; the state is not held in registers through the check below); all
 // lanes permute in lockstep, so a step costs one permutation and an attempt
 // completes every step once the pipeline is full. Each block's 17 output
 // words go to the attempt's slot of a per-group ring in shared memory; when
@@ -263,9 +264,11 @@ struct PipeLayout {
   static constexpr int NG = 32 / G;                          // groups per warp at most
   static constexpr int raw_words = (p::cand_bytes + 7) / 8;  // u64 words of one attempt's draw
   static constexpr int bm_words = (p::ew + 1) & ~1;
+  static constexpr int group_words = perms * raw_words + 1;  // odd u64 stride: groups on distinct banks
   static constexpr int cand_off = bm_words * 4;
-  static constexpr int ring_off = cand_off + (p::t * 2 + 7) / 8 * 8;
-  static constexpr int warp_bytes = ring_off + NG * perms * raw_words * 8;
+  static constexpr int state_off = cand_off + (p::t * 2 + 7) / 8 * 8;  // [25][32] u64 block states
+  static constexpr int ring_off = state_off + 25 * 32 * 8;
+  static constexpr int warp_bytes = ring_off + NG * group_words * 8;
   static_assert(perms <= G && raw_words <= 17 * perms, "pipeline geometry");
 };
 
@@ -285,6 +288,7 @@ __global__ void __launch_bounds__(kSampleThreadsMax)
   uint8_t *wb = reinterpret_cast<uint8_t *>(sm) + (size_t)warp * LY::warp_bytes;
   uint32_t *bm = reinterpret_cast<uint32_t *>(wb);
   uint16_t *cand = reinterpret_cast<uint16_t *>(wb + LY::cand_off);
+  uint64_t *sts = reinterpret_cast<uint64_t *>(wb + LY::state_off);
   uint64_t *ring = reinterpret_cast<uint64_t *>(wb + LY::ring_off);
   for (int w = lane; w < LY::bm_words; w += 32) bm[w] = 0;
   __syncwarp();
@@ -295,9 +299,6 @@ __global__ void __launch_bounds__(kSampleThreadsMax)
   long long op = 0;
   int myseg = 0, attempt = 0;
   uint64_t st[4] = {0, 0, 0, 0};
-  uint64_t s[25];
-#pragma unroll
-  for (int i = 0; i < 25; i++) s[i] = 0;
   bool valid = false;  // this lane holds block r of attempt att of the group's request
   int att = 0;
 #pragma unroll 1
@@ -334,24 +335,33 @@ __global__ void __launch_bounds__(kSampleThreadsMax)
       if (__all_sync(0xffffffffu, exhausted)) break;
       continue;
     }
-    // lane 0 of a group starts its request's next attempt: SHAKE256 absorb of {64} || state
+    // lane 0 of a group starts its request's next attempt (SHAKE256 absorb of
+    // {64} || state); lane r > 0 continues the block state lane r - 1 left in
+    // shared memory a step earlier
     if (r == 0) {
       valid = has;
       att = attempt;
-      if (has) {
-#pragma unroll
-        for (int i = 0; i < 25; i++) s[i] = 0;
-        s[0] = 64ull | (st[0] << 8);
-        s[1] = (st[0] >> 56) | (st[1] << 8);
-        s[2] = (st[1] >> 56) | (st[2] << 8);
-        s[3] = (st[2] >> 56) | (st[3] << 8);
-        s[4] = (st[3] >> 56) | (0x1Full << 8);
-        s[16] = 0x8000000000000000ull;
-      }
     }
+    uint64_t s[25];
+    if (r == 0) {
+#pragma unroll
+      for (int i = 0; i < 25; i++) s[i] = 0;
+      s[0] = 64ull | (st[0] << 8);
+      s[1] = (st[0] >> 56) | (st[1] << 8);
+      s[2] = (st[1] >> 56) | (st[2] << 8);
+      s[3] = (st[2] >> 56) | (st[3] << 8);
+      s[4] = (st[3] >> 56) | (0x1Full << 8);
+      s[16] = 0x8000000000000000ull;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 25; i++) s[i] = sts[i * 32 + lane - 1];
+    }
+    __syncwarp();  // every predecessor state read before this step's states overwrite them
     keccak_f1600(s);
+#pragma unroll
+    for (int i = 0; i < 25; i++) sts[i * 32 + lane] = s[i];
     if (valid) {
-      uint64_t *dst = ring + (size_t)(g * PP + att % PP) * RW;
+      uint64_t *dst = ring + (size_t)g * LY::group_words + (size_t)(att % PP) * RW;
 #pragma unroll
       for (int i = 0; i < 17; i++) {
         const int w = 17 * r + i;
@@ -375,7 +385,7 @@ __global__ void __launch_bounds__(kSampleThreadsMax)
       pend &= pend - 1;
       const int gg = L / G, owner = gg * G;
       const int a = __shfl_sync(0xffffffffu, att, L);
-      const uint16_t *raw = reinterpret_cast<const uint16_t *>(ring + (size_t)(gg * PP + a % PP) * RW);
+      const uint16_t *raw = reinterpret_cast<const uint16_t *>(ring + (size_t)gg * LY::group_words + (size_t)(a % PP) * RW);
       int total = 0;
 #pragma unroll
       for (int base = 0; base < ncand; base += 32) {
@@ -471,13 +481,7 @@ __global__ void __launch_bounds__(kSampleThreadsMax)
       valid = false;
       if (r == 0) has = false;
     }
-    // hand each block state one lane along the group (lane r permutes block r next step)
-#pragma unroll
-    for (int i = 0; i < 25; i++) {
-      const uint32_t lo = __shfl_up_sync(0xffffffffu, (uint32_t)s[i], 1, G);
-      const uint32_t hi = __shfl_up_sync(0xffffffffu, (uint32_t)(s[i] >> 32), 1, G);
-      s[i] = ((uint64_t)hi << 32) | lo;
-    }
+    // block r of an attempt moves one lane along the group (its state is in shared memory)
     const bool vin = __shfl_up_sync(0xffffffffu, valid ? 1 : 0, 1, G) != 0;
     const int ain = __shfl_up_sync(0xffffffffu, att, 1, G);
     if (r > 0) {
@@ -595,7 +599,7 @@ static bool sample_pipelined() {
 template <int SET, bool SPARSE>
 static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens,
                                      int ldx, const GemmKeys &keys, uint32_t *S, int lds, int threads,
-                                     unsigned int *counter, cudaStream_t st) {
+                                     unsigned int *counter, cudaStream_t st, int sample_sm_warps) {
   const long long N = seg_rows(segs);
   const int smem = (threads / 32) * SampleLayout<SET>::warp_bytes;
   cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -625,7 +629,10 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
     int pper = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pper, sample_pipe_kernel<SET, SPARSE>, threads, psmem);
     if (pper < 1) pper = 1;
-    const int ptarget = per_sm_target < pper ? per_sm_target : pper;
+    // the pipelined form fills the SMs (no tail cap: each warp's tail is one chain's)
+    const int ptarget = sample_sm_warps > 0 && (sample_sm_warps + warps - 1) / warps < pper
+                            ? (sample_sm_warps + warps - 1) / warps
+                            : pper;
     const long long pslots = (long long)sms * ptarget * warps;
     // active groups per warp: the smallest power of two with which the
     // resident warps hold the whole batch at once, at most 32 / G
@@ -657,17 +664,19 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
-                          cudaStream_t st) {
+                          cudaStream_t st, int sm_warps) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
-  if ((threads != 32 && threads != 64 && threads != 128) || !counter) return cudaErrorInvalidValue;
+  if ((threads != 32 && threads != 64 && threads != 128) || !counter || sm_warps < 0) return cudaErrorInvalidValue;
   if (sparse) {
     if (!S || lds < P<SET>::mw || sparse->ldtt < 64) return cudaErrorInvalidValue;
     for (int i = 0; i < segs.nseg; i++)
       if (!sparse->TT[i]) return cudaErrorInvalidValue;
-    return launch_sample_mode<SET, true>(seeds, segs, E, lde, Ens, ldx, *sparse, S, lds, threads, counter, st);
+    return launch_sample_mode<SET, true>(seeds, segs, E, lde, Ens, ldx, *sparse, S, lds, threads, counter, st,
+                                         sm_warps);
   }
-  return launch_sample_mode<SET, false>(seeds, segs, E, lde, Ens, ldx, GemmKeys{}, S, lds, threads, counter, st);
+  return launch_sample_mode<SET, false>(seeds, segs, E, lde, Ens, ldx, GemmKeys{}, S, lds, threads, counter, st,
+                                        sm_warps);
 }
 
 template <int SET>
@@ -685,7 +694,8 @@ cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int l
 
 #define GMC_INST_ENC(SET)                                                                                        \
   template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int,       \
-                                          const GemmKeys *, uint32_t *, int, int, unsigned int *, cudaStream_t); \
+                                          const GemmKeys *, uint32_t *, int, int, unsigned int *, cudaStream_t,  \
+                                          int);                                                                  \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
                                             const Segs &, uint32_t, bool, cudaStream_t);
 GMC_INST_ENC(0)

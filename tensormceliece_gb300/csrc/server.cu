@@ -184,10 +184,10 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
     cudaError_t e;
     if (engine == GEMM_SPARSE) {
       e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, &gk, Sy, mw, tune.sample_threads,
-                             reinterpret_cast<unsigned int *>(Ens), pst);
+                             reinterpret_cast<unsigned int *>(Ens), pst, tune.sample_sm_warps);
     } else {
       e = launch_sample<SET>(in, pp.segs, E, ew, Ens, kw, nullptr, Sy, mw, tune.sample_threads,
-                             reinterpret_cast<unsigned int *>(Sy), pst);
+                             reinterpret_cast<unsigned int *>(Sy), pst, tune.sample_sm_warps);
       if (e == cudaSuccess)
         e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->lda, ref->rows_pad, Ens, kw, ref->kw_pad, Sy, mw, p::mw,
                                 tc_err_word_ptr(), pst);

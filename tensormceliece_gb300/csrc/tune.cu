@@ -5,7 +5,8 @@
 //
 // Candidates, tuned greedily in this order: the engine of the encapsulation
 // syndrome (sparse column gather in the sampler, or the tcgen05 GEMM) crossed
-// with the sampler's block size (32, 64, 128); the GEMM engine of the
+// with the sampler's block size (32, 64, 128); the pipelined sampler's resident
+// warps per SM (as many as fit, 16 or 8); the GEMM engine of the
 // decapsulation front end (CUDA-core popcount or tcgen05); the tcgen05 GEMM's
 // pipeline depth (2, 3 or 4 A/X stages per CTA, when either op uses that
 // engine); and the requests per block of the two decoding kernels
@@ -111,10 +112,10 @@ std::string set_entry(int set, const SetTune &t) {
   char buf[400];
   snprintf(buf, sizeof buf,
            "    \"%s\": {\"enc_engine\": \"%s\", \"dec_engine\": \"%s\", \"sample_threads\": %d, "
-           "\"gemm_stages\": %d, \"bm_warps\": %d, \"root_warps\": %d, \"n\": %lld, \"enc_ms\": %.4f, "
-           "\"dec_ms\": %.4f}",
-           set_info(set).name, engine_name(t.enc_engine), engine_name(t.dec_engine), t.sample_threads, t.gemm_stages,
-           t.bm_warps, t.root_warps, t.n, t.enc_ms, t.dec_ms);
+           "\"sample_sm_warps\": %d, \"gemm_stages\": %d, \"bm_warps\": %d, \"root_warps\": %d, \"n\": %lld, "
+           "\"enc_ms\": %.4f, \"dec_ms\": %.4f}",
+           set_info(set).name, engine_name(t.enc_engine), engine_name(t.dec_engine), t.sample_threads,
+           t.sample_sm_warps, t.gemm_stages, t.bm_warps, t.root_warps, t.n, t.enc_ms, t.dec_ms);
   return buf;
 }
 
@@ -161,24 +162,27 @@ extern "C" int gmc_tune_set(int set, int enc_engine, int dec_engine, int sample_
   return GMC_OK;
 }
 
-extern "C" int gmc_tune_set_launch(int set, int gemm_stages, int bm_warps, int root_warps) {
+extern "C" int gmc_tune_set_launch(int set, int gemm_stages, int bm_warps, int root_warps, int sample_sm_warps) {
   if (set < 0 || set >= GMC_NSETS || gemm_stages < 2 || gemm_stages > kTcStages || bm_warps < 1 ||
-      bm_warps > kBMWarps || root_warps < 1 || root_warps > kRootWarps)
+      bm_warps > kBMWarps || root_warps < 1 || root_warps > kRootWarps || sample_sm_warps < 0 ||
+      sample_sm_warps > 64)
     return tune_error(GMC_EINVAL, "gmc_tune_set_launch: bad argument");
   SetTune t = tune_get(set);
   t.gemm_stages = gemm_stages;
   t.bm_warps = bm_warps;
   t.root_warps = root_warps;
+  t.sample_sm_warps = sample_sm_warps;
   tune_put(set, t);
   return GMC_OK;
 }
 
-extern "C" int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warps) {
+extern "C" int gmc_tune_get_launch(int set, int *gemm_stages, int *bm_warps, int *root_warps, int *sample_sm_warps) {
   if (set < 0 || set >= GMC_NSETS) return tune_error(GMC_EINVAL, "gmc_tune_get_launch: bad set");
   SetTune t = tune_get(set);
   if (gemm_stages) *gemm_stages = t.gemm_stages;
   if (bm_warps) *bm_warps = t.bm_warps;
   if (root_warps) *root_warps = t.root_warps;
+  if (sample_sm_warps) *sample_sm_warps = t.sample_sm_warps;
   return t.tuned;
 }
 
@@ -238,6 +242,19 @@ extern "C" int gmc_autotune(int set, long long n, const char *cache_path) {
           best.sample_threads = threads[ti];
         }
       }
+    // resident warps per SM of the pipelined sampler (0: as many as fit)
+    const int smw[3] = {0, 16, 8};
+    for (int wi = 1; wi < 3; wi++) {
+      SetTune t = best;
+      t.sample_sm_warps = smw[wi];
+      tune_put(set, t);
+      const float ms =
+          time_median([&] { return gmc_enc_batch_dev(P, ct, key, seeds, n, nullptr, st); }, st, a, b, &rc);
+      if (ms < 0.99f * best_enc) {
+        best_enc = ms;
+        best.sample_sm_warps = smw[wi];
+      }
+    }
     tune_put(set, best);
     rc |= gmc_enc_batch_dev(P, ct, key, seeds, n, nullptr, st);  // valid ciphertexts for the dec timing
     for (int ei = 0; ei < 2; ei++) {
@@ -341,6 +358,8 @@ extern "C" int gmc_autotune_load(const char *cache_path) {
     const int bw = atoi(field(o, "bm_warps").c_str()), rw = atoi(field(o, "root_warps").c_str());
     t.bm_warps = (bw >= 1 && bw <= kBMWarps) ? bw : kBMWarps;
     t.root_warps = (rw >= 1 && rw <= kRootWarps) ? rw : kRootWarps;
+    const int sw = atoi(field(o, "sample_sm_warps").c_str());
+    t.sample_sm_warps = (sw >= 0 && sw <= 64) ? sw : 0;
     t.n = atoll(field(o, "n").c_str());
     t.enc_ms = atof(field(o, "enc_ms").c_str());
     t.dec_ms = atof(field(o, "dec_ms").c_str());

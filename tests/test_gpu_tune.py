@@ -29,10 +29,12 @@ def test_autotune_cache_roundtrip(gmc, keys, tmp_path):
     entry = data["sets"]["348864"]
     assert entry["enc_engine"] == cfg["enc_engine"]
     assert entry["gemm_stages"] in (2, 3, 4) and entry["root_warps"] in (2, 4, 8) and entry["bm_warps"] == 8
-    gmc.tune_set(0, "popc", "popc", 32, gemm_stages=2, bm_warps=1, root_warps=1)
+    assert entry["sample_sm_warps"] in (0, 8, 16)
+    gmc.tune_set(0, "popc", "popc", 32, gemm_stages=2, bm_warps=1, root_warps=1, sample_sm_warps=4)
     assert gmc.autotune_load(path) == 1
     got = gmc.tune_get(0)
-    for f in ("enc_engine", "dec_engine", "sample_threads", "gemm_stages", "bm_warps", "root_warps"):
+    for f in ("enc_engine", "dec_engine", "sample_threads", "gemm_stages", "bm_warps", "root_warps",
+              "sample_sm_warps"):
         assert got[f] == cfg[f], f
     pk, sk = keys(0)
     seeds = request_seeds(0, 200, b"tune")
@@ -68,7 +70,8 @@ def test_launch_shapes(gmc, keys, sid):
     n = 24576 + 77
     seeds = request_seeds(sid, n, b"shapes")
     try:
-        gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=4, bm_warps=8, root_warps=8)
+        gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=4, bm_warps=8, root_warps=8,
+                     sample_sm_warps=0)
         P, S = gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)
         c, k, rc = P.enc_batch(seeds)
         oc, ok_, _ = O.enc_batch(sid, pk, seeds[:64], threads=8)
@@ -77,8 +80,9 @@ def test_launch_shapes(gmc, keys, sid):
         bad[::5, 3] ^= 0x21
         kd, rcd = S.dec_batch(bad)
         assert (kd[1::5] == k[1::5]).all()
-        for stages, bw, rw in ((2, 4, 2), (3, 2, 4), (4, 1, 1)):
-            gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=stages, bm_warps=bw, root_warps=rw)
+        for stages, bw, rw, sw in ((2, 4, 2, 8), (3, 2, 4, 16), (4, 1, 1, 4)):
+            gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=stages, bm_warps=bw, root_warps=rw,
+                         sample_sm_warps=sw)
             c2, k2, rc2 = P.enc_batch(seeds)
             assert (c2 == c).all() and (k2 == k).all() and (rc2 == rc).all(), (stages, bw, rw)
             kd2, rcd2 = S.dec_batch(bad)
@@ -86,7 +90,8 @@ def test_launch_shapes(gmc, keys, sid):
         assert gmc.lib().gmc_tc_status() == 0
     finally:
         gmc.tune_set(sid, prev["enc_engine"], prev["dec_engine"], prev["sample_threads"],
-                     gemm_stages=prev["gemm_stages"], bm_warps=prev["bm_warps"], root_warps=prev["root_warps"])
+                     gemm_stages=prev["gemm_stages"], bm_warps=prev["bm_warps"], root_warps=prev["root_warps"],
+                     sample_sm_warps=prev["sample_sm_warps"])
 
 
 def test_int32_peak(gmc):
