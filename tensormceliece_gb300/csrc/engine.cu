@@ -438,16 +438,12 @@ static cudaError_t enc_sample_gemm_seg(const Segs &segs, const gmc_key *ref, con
   using p = P<SET>;
   prof_mark(nullptr, st);
   const SetTune tune = tune_get(SET);
-  if (engine == GEMM_SPARSE) {  // the sampler writes S itself; Ens lends its first word as the work counter
-    cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, &gk, S, d.lds, tune.sample_threads,
-                                       reinterpret_cast<unsigned int *>(Ens), st, tune.sample_sm_warps);
-    prof_mark("enc_sample_syndrome", st);
-    return e;
-  }
+  if (engine == GEMM_SPARSE)  // the sampler writes S itself; Ens lends its first word as the work counter
+    return launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, &gk, S, d.lds, tune.sample_threads,
+                              reinterpret_cast<unsigned int *>(Ens), st, tune.sample_sm_warps, prof_mark);
   cudaError_t e = launch_sample<SET>(seeds, segs, E, d.lde, Ens, d.ldx, nullptr, S, d.lds, tune.sample_threads,
-                                     reinterpret_cast<unsigned int *>(S), st, tune.sample_sm_warps);
+                                     reinterpret_cast<unsigned int *>(S), st, tune.sample_sm_warps, prof_mark);
   if (e != cudaSuccess) return e;
-  prof_mark("enc_sample", st);
   e = launch_gf2_gemm_seg(engine, gk, segs, ref->lda, ref->rows_pad, Ens, d.ldx, ref->kw_pad, S, d.lds, p::mw, err,
                           st);
   prof_mark("enc_syndrome_gemm", st);

@@ -108,10 +108,11 @@ cudaError_t launch_transpose_pk(const uint32_t *T, int lda, int mt, int k, uint3
 // touches until the sampler ends; the pipelines lend the first word of the
 // buffer the sampler does not write (S in dense mode, Ens in sparse mode).
 // sm_warps: resident warps per SM of the pipelined sampler (0 = as many as fit).
+// mark (optional): called after each kernel with its stage name (profiling).
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
-                          cudaStream_t st, int sm_warps = 0);
+                          cudaStream_t st, int sm_warps = 0, void (*mark)(const char *, cudaStream_t) = nullptr);
 // C rows: synd_bytes, or synd_bytes + 32 with plaintext confirmation (pc):
 // C0 || SHAKE256(2 || e, 32), K = SHAKE256(1 || e || C0 || C1).
 template <int SET>

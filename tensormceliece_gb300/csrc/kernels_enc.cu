@@ -33,6 +33,50 @@ namespace gmc {
 // vector e, written out by the whole warp (coalesced) together with e[mt:n]
 // shifted to bit 0 (the syndrome GEMM operand). Only the touched bitmap
 // words are cleared.
+// S row = T e[mt:n]: XOR of the columns of TT (row j = column j of T, row k
+// zero) at the request's t positions; positions < mt read the zero row.
+// Lane l takes positions l, l + 32, ... (16-byte loads, all in flight at
+// once), then one XOR reduction across the warp per syndrome word.
+template <int SET, typename PosFn>
+__device__ __forceinline__ void sparse_syndrome_row(PosFn pos_of, const uint32_t *__restrict__ TT, int ldtt,
+                                                    uint32_t *__restrict__ srow, int lane) {
+  using p = P<SET>;
+  constexpr int NCW = (p::t + 31) / 32, MW4 = (p::mw + 3) / 4;
+  uint4 acc[MW4];
+#pragma unroll
+  for (int w = 0; w < MW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
+#pragma unroll
+  for (int i = 0; i < NCW; i++) {
+    const int c = lane + 32 * i;
+    const int pos = c < p::t ? pos_of(c) : 0;
+    const uint4 *col = reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * ldtt);
+#pragma unroll
+    for (int w = 0; w < MW4; w++) {
+      const uint4 v = col[w];
+      acc[w].x ^= v.x;
+      acc[w].y ^= v.y;
+      acc[w].z ^= v.z;
+      acc[w].w ^= v.w;
+    }
+  }
+  uint32_t my0 = 0, my1 = 0;
+#pragma unroll
+  for (int w = 0; w < MW4; w++) {
+    const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
+#pragma unroll
+    for (int e2 = 0; e2 < 4; e2++) {
+      const int word = 4 * w + e2;
+      if (word < p::mw) {
+        const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
+        if (word < 32) my0 = (lane == word) ? v : my0;
+        else my1 = (lane == word - 32) ? v : my1;
+      }
+    }
+  }
+  if (lane < p::mw) srow[lane] = my0;
+  if (p::mw > 32 && lane + 32 < p::mw) srow[lane + 32] = my1;
+}
+
 template <int SET>
 struct SampleLayout {
   using p = P<SET>;
@@ -167,47 +211,8 @@ __global__ void __launch_bounds__(kSampleThreadsMax) sample_kernel(const uint8_t
         uint32_t *erow = E + opr * lde;
         for (int w = lane; w < p::ew; w += 32) erow[w] = bm[w];
         if (SPARSE) {
-          // S = T e[mt:n]: XOR of the columns at this request's positions >= mt.
-          // Lane l XORs the columns of positions l, l+32, ... (16-byte loads,
-          // all in flight at once; positions < mt read the zero column k),
-          // then one XOR reduction per syndrome word.
-          const uint32_t *TT = keys.TT[__shfl_sync(0xffffffffu, myseg, r)];
-          constexpr int MW4 = (p::mw + 3) / 4;
-          uint4 acc[MW4];
-#pragma unroll
-          for (int w = 0; w < MW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
-#pragma unroll
-          for (int i = 0; i < NCW; i++) {
-            const int c = lane + 32 * i;
-            const int pos = c < p::t ? cand[cand_slot(c, r)] : 0;
-            const uint4 *col =
-                reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * keys.ldtt);
-#pragma unroll
-            for (int w = 0; w < MW4; w++) {
-              const uint4 v = col[w];
-              acc[w].x ^= v.x;
-              acc[w].y ^= v.y;
-              acc[w].z ^= v.z;
-              acc[w].w ^= v.w;
-            }
-          }
-          uint32_t my0 = 0, my1 = 0;
-#pragma unroll
-          for (int w = 0; w < MW4; w++) {
-            const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
-#pragma unroll
-            for (int e2 = 0; e2 < 4; e2++) {
-              const int word = 4 * w + e2;
-              if (word < p::mw) {
-                const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
-                if (word < 32) my0 = (lane == word) ? v : my0;
-                else my1 = (lane == word - 32) ? v : my1;
-              }
-            }
-          }
-          uint32_t *srow = S + opr * lds;
-          if (lane < p::mw) srow[lane] = my0;
-          if (p::mw > 32 && lane + 32 < p::mw) srow[lane + 32] = my1;
+          sparse_syndrome_row<SET>([&](int c) { return (int)cand[cand_slot(c, r)]; },
+                                   keys.TT[__shfl_sync(0xffffffffu, myseg, r)], keys.ldtt, S + opr * lds, lane);
         } else {
           uint32_t *xrow = Ens + opr * ldx;
           for (int w = lane; w < p::kw; w += 32) {
@@ -423,44 +428,8 @@ __global__ void __launch_bounds__(kSampleThreadsMax)
         uint32_t *erow = E + opr * lde;
         for (int w = lane; w < p::ew; w += 32) erow[w] = bm[w];
         if (SPARSE) {
-          // S = T e[mt:n], lane-parallel over the t positions (as in sample_kernel)
-          const uint32_t *TT = keys.TT[__shfl_sync(0xffffffffu, myseg, owner)];
-          constexpr int MW4 = (p::mw + 3) / 4;
-          uint4 acc[MW4];
-#pragma unroll
-          for (int w = 0; w < MW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
-#pragma unroll
-          for (int i = 0; i < NCW; i++) {
-            const int c = lane + 32 * i;
-            const int pos = c < p::t ? cand[c] : 0;
-            const uint4 *col =
-                reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * keys.ldtt);
-#pragma unroll
-            for (int w = 0; w < MW4; w++) {
-              const uint4 v = col[w];
-              acc[w].x ^= v.x;
-              acc[w].y ^= v.y;
-              acc[w].z ^= v.z;
-              acc[w].w ^= v.w;
-            }
-          }
-          uint32_t my0 = 0, my1 = 0;
-#pragma unroll
-          for (int w = 0; w < MW4; w++) {
-            const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
-#pragma unroll
-            for (int e2 = 0; e2 < 4; e2++) {
-              const int word = 4 * w + e2;
-              if (word < p::mw) {
-                const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
-                if (word < 32) my0 = (lane == word) ? v : my0;
-                else my1 = (lane == word - 32) ? v : my1;
-              }
-            }
-          }
-          uint32_t *srow = S + opr * lds;
-          if (lane < p::mw) srow[lane] = my0;
-          if (p::mw > 32 && lane + 32 < p::mw) srow[lane + 32] = my1;
+          sparse_syndrome_row<SET>([&](int c) { return (int)cand[c]; },
+                                   keys.TT[__shfl_sync(0xffffffffu, myseg, owner)], keys.ldtt, S + opr * lds, lane);
         } else {
           uint32_t *xrow = Ens + opr * ldx;
           for (int w = lane; w < p::kw; w += 32) {
@@ -595,11 +564,11 @@ static bool sample_pipelined() {
   }();
   return on;
 }
-
 template <int SET, bool SPARSE>
 static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens,
                                      int ldx, const GemmKeys &keys, uint32_t *S, int lds, int threads,
-                                     unsigned int *counter, cudaStream_t st, int sample_sm_warps) {
+                                     unsigned int *counter, cudaStream_t st, int sample_sm_warps,
+                                     void (*mark)(const char *, cudaStream_t)) {
   const long long N = seg_rows(segs);
   const int smem = (threads / 32) * SampleLayout<SET>::warp_bytes;
   cudaError_t err = cudaFuncSetAttribute(sample_kernel<SET, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -622,12 +591,13 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
   // requests when the batch outnumbers them
   if (sample_pipelined()) {
     using PL = PipeLayout<SET>;
+    auto kern = sample_pipe_kernel<SET, SPARSE>;
     const int psmem = warps * PL::warp_bytes;
-    err = cudaFuncSetAttribute(sample_pipe_kernel<SET, SPARSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (kSampleThreadsMax / 32) * PL::warp_bytes);
     if (err != cudaSuccess) return err;
     int pper = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pper, sample_pipe_kernel<SET, SPARSE>, threads, psmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pper, kern, threads, psmem);
     if (pper < 1) pper = 1;
     // the pipelined form fills the SMs (no tail cap: each warp's tail is one chain's)
     const int ptarget = sample_sm_warps > 0 && (sample_sm_warps + warps - 1) / warps < pper
@@ -642,9 +612,10 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
     const long long need = (N + per_block - 1) / per_block;
     const long long resident = (long long)sms * ptarget;
     const long long blocks = need < resident ? need : resident;
-    sample_pipe_kernel<SET, SPARSE><<<(unsigned)blocks, threads, psmem, st>>>(seeds, segs, E, lde, Ens, ldx, keys, S,
-                                                                              lds, counter, groups);
-    return cudaGetLastError();
+    kern<<<(unsigned)blocks, threads, psmem, st>>>(seeds, segs, E, lde, Ens, ldx, keys, S, lds, counter, groups);
+    err = cudaGetLastError();
+    if (mark) mark(SPARSE ? "enc_sample_syndrome" : "enc_sample", st);
+    return err;
   }
   if (per_sm_target > per_sm) per_sm_target = per_sm;
   // active lanes per warp: the smallest power of two (<= 32) with which the
@@ -658,13 +629,15 @@ static cudaError_t launch_sample_mode(const uint8_t *seeds, const Segs &segs, ui
   const long long blocks = need < resident ? need : resident;
   sample_kernel<SET, SPARSE><<<(unsigned)blocks, threads, smem, st>>>(seeds, segs, E, lde, Ens, ldx, keys, S, lds,
                                                                       counter, lanes);
-  return cudaGetLastError();
+  err = cudaGetLastError();
+  if (mark) mark(SPARSE ? "enc_sample_syndrome" : "enc_sample", st);
+  return err;
 }
 
 template <int SET>
 cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, int lde, uint32_t *Ens, int ldx,
                           const GemmKeys *sparse, uint32_t *S, int lds, int threads, unsigned int *counter,
-                          cudaStream_t st, int sm_warps) {
+                          cudaStream_t st, int sm_warps, void (*mark)(const char *, cudaStream_t)) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   if ((threads != 32 && threads != 64 && threads != 128) || !counter || sm_warps < 0) return cudaErrorInvalidValue;
@@ -673,10 +646,10 @@ cudaError_t launch_sample(const uint8_t *seeds, const Segs &segs, uint32_t *E, i
     for (int i = 0; i < segs.nseg; i++)
       if (!sparse->TT[i]) return cudaErrorInvalidValue;
     return launch_sample_mode<SET, true>(seeds, segs, E, lde, Ens, ldx, *sparse, S, lds, threads, counter, st,
-                                         sm_warps);
+                                         sm_warps, mark);
   }
   return launch_sample_mode<SET, false>(seeds, segs, E, lde, Ens, ldx, GemmKeys{}, S, lds, threads, counter, st,
-                                        sm_warps);
+                                        sm_warps, mark);
 }
 
 template <int SET>
@@ -695,7 +668,7 @@ cudaError_t launch_finalize(const uint32_t *E, int lde, const uint32_t *S, int l
 #define GMC_INST_ENC(SET)                                                                                        \
   template cudaError_t launch_sample<SET>(const uint8_t *, const Segs &, uint32_t *, int, uint32_t *, int,       \
                                           const GemmKeys *, uint32_t *, int, int, unsigned int *, cudaStream_t,  \
-                                          int);                                                                  \
+                                          int, void (*)(const char *, cudaStream_t));                            \
   template cudaError_t launch_finalize<SET>(const uint32_t *, int, const uint32_t *, int, uint8_t *, uint8_t *, \
                                             const Segs &, uint32_t, bool, cudaStream_t);
 GMC_INST_ENC(0)
