@@ -501,6 +501,9 @@ def serving(gmc, torch, seconds):
         srv.add_key(P)
         srv.add_key(S)
     peak = srv.loadgen(pairs, rate=2e8, seconds=max(1.0, seconds / 2), seed=1)  # overload: saturated throughput
+    # untimed warm-up at the lowest level: the first small batches of a process paid one-time costs (a stall of
+    # tens of ms in the first level of some runs, never in later ones)
+    srv.loadgen(pairs, rate=0.1 * peak["ops_s"], seconds=1.0, seed=7)
     levels = {}
     for frac in (0.1, 0.5, 0.9):
         r = srv.loadgen(pairs, rate=frac * peak["ops_s"], seconds=seconds, seed=int(frac * 100))

@@ -12,9 +12,9 @@
 // copy -> per (parameter set, enc/dec) the segment-aware kernels over all its
 // keys, each pipeline on its own stream (forked from and joined back to the
 // slot's stream, so they overlap) -> one device-to-host copy -> a host
-// callback that scatters results,
-// marks the requests done and records their latency (arrival to completion)
-// in a log-bucket histogram (p50 / p99). Several slots keep several batches in
+// callback that hands the slot to the completion thread, which scatters the
+// results (on persistent host workers), marks the requests done and records
+// their latency (arrival to completion) in a log-bucket histogram (p50 / p99). Several slots keep several batches in
 // flight, so their work overlaps on the device.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -26,6 +26,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <functional>
 #include <mutex>
 #include <random>
 #include <set>
@@ -97,27 +98,78 @@ struct Slot {
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
-// Runs fn(begin, end) over [0, n) in up to kHostThreads pieces (the calling
-// thread takes the first): the per-request gather and scatter of a batch of
-// tens of thousands of requests touch every request's own host buffers.
+// Persistent host workers for the per-request gather and scatter of a batch
+// (threads are started once, not per batch: thread creation on every batch
+// showed up as latency jitter under load). Jobs from the dispatcher and from
+// the completion thread may run at the same time; each waits only for its own
+// pieces.
 constexpr int kHostThreads = 8;
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool *pool = new HostPool();  // never destroyed: workers idle in wait at exit
+    return *pool;
+  }
+  // runs `tasks` on the workers and `own` on the calling thread; returns when all are done
+  template <typename Own>
+  void run(std::vector<std::function<void()>> &tasks, Own own) {
+    int left = (int)tasks.size();  // under dmu: a worker's last touch of this frame is under the lock
+    std::mutex dmu;
+    std::condition_variable dcv;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      for (auto &t : tasks)
+        q_.push_back([&, fn = &t] {
+          (*fn)();
+          std::lock_guard<std::mutex> g(dmu);
+          if (--left == 0) dcv.notify_all();
+        });
+    }
+    cv_.notify_all();
+    own();
+    std::unique_lock<std::mutex> g(dmu);
+    dcv.wait(g, [&] { return left == 0; });
+  }
+
+ private:
+  HostPool() {
+    for (int i = 0; i < 2 * (kHostThreads - 1); i++) std::thread([this] { work(); }).detach();
+  }
+  void work() {
+    while (true) {
+      std::function<void()> fn;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return !q_.empty(); });
+        fn = std::move(q_.front());
+        q_.pop_front();
+      }
+      fn();
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::function<void()>> q_;
+};
+
+// Runs fn(begin, end) over [0, n) in up to kHostThreads pieces (the calling
+// thread takes the first, the pool the others).
 template <typename F>
 void parallel_for(size_t n, F fn) {
-  const size_t per = 4096;  // below this a piece is not worth a thread
+  const size_t per = 4096;  // below this a piece is not worth a hand-off
   const int parts = (int)std::min<size_t>(kHostThreads, (n + per - 1) / per);
   if (parts <= 1) {
     fn((size_t)0, n);
     return;
   }
-  std::vector<std::thread> th;
-  th.reserve(parts - 1);
   const size_t chunk = (n + parts - 1) / parts;
+  std::vector<std::function<void()>> tasks;
+  tasks.reserve(parts - 1);
   for (int i = 1; i < parts; i++) {
     const size_t b = (size_t)i * chunk, e = std::min(n, b + chunk);
-    th.emplace_back([=] { fn(b, e); });
+    tasks.emplace_back([=, &fn] { fn(b, e); });
   }
-  fn((size_t)0, std::min(n, chunk));
-  for (auto &t : th) t.join();
+  HostPool::get().run(tasks, [&] { fn((size_t)0, std::min(n, chunk)); });
 }
 
 // device bytes of one pipeline's work buffers for `rows` padded rows
@@ -143,6 +195,12 @@ struct gmc_server {
   std::deque<Req> queue;
   std::thread dispatcher;
   bool stop = false;
+  // finished batches, handed from the CUDA host callback to the completion thread
+  std::mutex done_mu;
+  std::condition_variable done_cv;
+  std::deque<Slot *> done_q;
+  bool done_stop = false;
+  std::thread completer;
   // statistics (under mu)
   std::vector<long long> hist = std::vector<long long>(kBuckets, 0);
   long long completed = 0, batches = 0, batched_requests = 0, errors = 0;
@@ -222,18 +280,30 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   return e;
 }
 
+// CUDA host callback at the end of a batch's stream work: only hands the slot
+// to the completion thread (host functions run on the driver's callback
+// thread, which the other slots' completions share).
 void CUDART_CB on_batch_done(void *arg) {
   Slot *sl = (Slot *)arg;
   gmc_server *srv = sl->srv;
-  const double t = now_s();
-  // scatter results and bucket latencies (outside the lock), in parallel pieces
+  {
+    std::lock_guard<std::mutex> lk(srv->done_mu);
+    srv->done_q.push_back(sl);
+  }
+  srv->done_cv.notify_one();
+}
+
+// Scatters a finished batch's results, marks its requests done, records their
+// latency (arrival to the results being in the caller's buffers) and frees
+// the slot.
+void complete_batch(Slot *sl) {
+  gmc_server *srv = sl->srv;
+  // scatter results, then bucket latencies (outside the lock), in parallel pieces
   const int parts = kHostThreads;
   std::vector<std::vector<long long>> local(parts, std::vector<long long>(kBuckets, 0));
   std::atomic<int> next_part{0};
   parallel_for(sl->pieces.size(), [&](size_t b, size_t e) {
     std::vector<long long> &h = local[next_part.fetch_add(1) % parts];
-    double last_t = -1.0;
-    int last_b = 0;
     for (size_t i = b; i < e; i++) {
       Piece &pc = sl->pieces[i];
       memcpy(pc.r.k, sl->h_out + pc.out_k, 32);
@@ -243,6 +313,12 @@ void CUDART_CB on_batch_done(void *arg) {
       } else if (pc.r.rc) {
         memcpy(pc.r.rc, sl->h_out + pc.out_rc, 4);
       }
+    }
+    const double t = now_s();  // this piece's results are in place
+    double last_t = -1.0;
+    int last_b = 0;
+    for (size_t i = b; i < e; i++) {
+      Piece &pc = sl->pieces[i];
       if (pc.r.t_arrive != last_t) {  // requests of a batch often share their bucket
         last_t = pc.r.t_arrive;
         last_b = bucket_of((t - last_t) * 1e3);
@@ -251,6 +327,7 @@ void CUDART_CB on_batch_done(void *arg) {
       if (pc.r.done) pc.r.done->store(1, std::memory_order_release);
     }
   });
+  const double t = now_s();
   std::lock_guard<std::mutex> lk(srv->mu);
   for (auto &h : local)
     for (int b = 0; b < kBuckets; b++) srv->hist[b] += h[b];
@@ -258,6 +335,20 @@ void CUDART_CB on_batch_done(void *arg) {
   srv->t_last = t;
   sl->busy = false;
   srv->cv.notify_all();
+}
+
+void completer_main(gmc_server *srv) {
+  while (true) {
+    Slot *sl = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(srv->done_mu);
+      srv->done_cv.wait(lk, [&] { return !srv->done_q.empty() || srv->done_stop; });
+      if (srv->done_q.empty()) break;  // stopping, nothing left
+      sl = srv->done_q.front();
+      srv->done_q.pop_front();
+    }
+    complete_batch(sl);
+  }
 }
 
 // device bytes of one pipeline (inputs, outputs, work) for `rows` padded rows
@@ -497,16 +588,26 @@ void server_release(gmc_server *s) {
     s->cv.notify_all();
     s->dispatcher.join();
   }
+  // every batch's device work and host callback ends before the completion
+  // thread is stopped (it finishes what the callbacks handed it) and before
+  // the slots' buffers go
   for (auto &sl : s->slots) {
-    if (sl.st) {
-      cudaStreamSynchronize(sl.st);
-      cudaStreamDestroy(sl.st);
+    for (int i = 0; i < kPipes; i++)
+      if (sl.pst[i]) cudaStreamSynchronize(sl.pst[i]);
+    if (sl.st) cudaStreamSynchronize(sl.st);
+  }
+  if (s->completer.joinable()) {
+    {
+      std::lock_guard<std::mutex> lk(s->done_mu);
+      s->done_stop = true;
     }
+    s->done_cv.notify_all();
+    s->completer.join();
+  }
+  for (auto &sl : s->slots) {
+    if (sl.st) cudaStreamDestroy(sl.st);
     for (int i = 0; i < kPipes; i++) {
-      if (sl.pst[i]) {
-        cudaStreamSynchronize(sl.pst[i]);
-        cudaStreamDestroy(sl.pst[i]);
-      }
+      if (sl.pst[i]) cudaStreamDestroy(sl.pst[i]);
       if (sl.join[i]) cudaEventDestroy(sl.join[i]);
     }
     if (sl.fork) cudaEventDestroy(sl.fork);
@@ -562,6 +663,7 @@ extern "C" int gmc_server_create(gmc_server **out, long long max_batch, int slot
     server_release(s);
     return srv_fail(GMC_ENOMEM, "gmc_server_create: slot allocation failed");
   }
+  s->completer = std::thread(completer_main, s);
   s->dispatcher = std::thread(dispatcher_main, s);
   *out = s;
   return GMC_OK;
