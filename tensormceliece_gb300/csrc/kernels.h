@@ -8,7 +8,10 @@ namespace gmc {
 
 constexpr int kSampleWarpsPerSM = 8;     // sampler: resident warps per SM (lanes fetch requests)
 constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parameter (32, 64 or 128)
-constexpr int kTailThreads = 128;
+// hash kernels (thread per request, one wave): 64-thread blocks spread a
+// 65536-request launch as 6-7 blocks per SM (128-thread blocks: 3-4, so a
+// third of the SMs carried a block more than the rest)
+constexpr int kTailThreads = 64;
 constexpr int kBMWarps = 8;     // Berlekamp-Massey kernel: default and largest warps per block (32 requests per warp)
 constexpr int kBMLatWarps = 24;  // Berlekamp-Massey latency form: warps per block (one request per warp)
 constexpr long long kBMBitslicedMinRows = 24576;  // smaller batches take the latency form

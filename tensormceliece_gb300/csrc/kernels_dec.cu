@@ -122,8 +122,12 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
   uint32_t *BP = SP + LY::s_words;
   const long long N = seg_rows(segs);
   const long long ngroups = (N + 31) / 32;
+  // each block (one per SM) takes an equal contiguous share of the groups and
+  // its warps stride over it: with a grid-wide stride, 2048 groups over 152 x 8
+  // warps left 48 SMs with half the work of the others
   const int nwb = blockDim.x >> 5;  // warps per block (a launch parameter up to kBMWarps)
-  for (long long g = (long long)blockIdx.x * nwb + warp; g < ngroups; g += (long long)gridDim.x * nwb) {
+  const long long g_lo = ngroups * blockIdx.x / gridDim.x, g_hi = ngroups * (blockIdx.x + 1) / gridDim.x;
+  for (long long g = g_lo + warp; g < g_hi; g += nwb) {
     const long long op = g * 32 + lane;
     int seg;
     const bool live = op < N && seg_live(segs, op, &seg);
