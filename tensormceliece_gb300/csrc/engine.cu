@@ -380,6 +380,27 @@ static void keep_pool_warm() {
   done.insert(dev);
 }
 
+// Stream of the host-pointer batch calls: one per calling thread and device,
+// created on first use (stream creation and destruction on every call cost
+// tens of microseconds per call).
+static cudaStream_t host_call_stream() {
+  struct Holder {
+    std::map<int, cudaStream_t> by_dev;
+    ~Holder() {
+      for (auto &kv : by_dev) cudaStreamDestroy(kv.second);
+    }
+  };
+  thread_local Holder h;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  auto it = h.by_dev.find(dev);
+  if (it != h.by_dev.end()) return it->second;
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  h.by_dev[dev] = st;
+  return st;
+}
+
 // Stream-ordered scratch: allocated from the device's default memory pool on
 // the caller's stream and released on it after the last kernel.
 struct Scratch {
@@ -617,8 +638,8 @@ extern "C" int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char 
   if (!n) return GMC_OK;
   const size_t cb = (size_t)ct_bytes_of(pk);
   keep_pool_warm();
-  cudaStream_t st;
-  GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaStream_t st = host_call_stream();
+  if (!st) return fail(GMC_ECUDA, "gmc_enc_batch: stream");
   uint8_t *d_seeds = nullptr, *d_c = nullptr, *d_k = nullptr;
   int *d_rc = nullptr;
   cudaError_t e = cudaMallocAsync(&d_seeds, (size_t)n * 32, st);
@@ -638,7 +659,6 @@ extern "C" int gmc_enc_batch(const gmc_key *pk, unsigned char *c, unsigned char 
   cudaFreeAsync(d_seeds, st); cudaFreeAsync(d_c, st); cudaFreeAsync(d_k, st);
   if (d_rc) cudaFreeAsync(d_rc, st);
   cudaError_t e2 = cudaStreamSynchronize(st);
-  cudaStreamDestroy(st);
   if (res != GMC_OK) return res;
   if (e != cudaSuccess) return cuda_fail(e, "gmc_enc_batch");
   if (e2 != cudaSuccess) return cuda_fail(e2, "gmc_enc_batch: sync");
@@ -652,8 +672,8 @@ extern "C" int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned
   if (!n) return GMC_OK;
   const size_t cb = (size_t)ct_bytes_of(sk);
   keep_pool_warm();
-  cudaStream_t st;
-  GMC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaStream_t st = host_call_stream();
+  if (!st) return fail(GMC_ECUDA, "gmc_dec_batch: stream");
   uint8_t *d_c = nullptr, *d_k = nullptr;
   int *d_rc = nullptr;
   cudaError_t e = cudaMallocAsync(&d_c, (size_t)n * cb, st);
@@ -671,7 +691,6 @@ extern "C" int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned
   cudaFreeAsync(d_c, st); cudaFreeAsync(d_k, st);
   if (d_rc) cudaFreeAsync(d_rc, st);
   cudaError_t e2 = cudaStreamSynchronize(st);
-  cudaStreamDestroy(st);
   if (res != GMC_OK) return res;
   if (e != cudaSuccess) return cuda_fail(e, "gmc_dec_batch");
   if (e2 != cudaSuccess) return cuda_fail(e2, "gmc_dec_batch: sync");

@@ -780,70 +780,87 @@ extern "C" int gmc_server_loadgen(gmc_server *s, const gmc_key *const *pks, cons
   std::vector<uint8_t> sink_ct(ring * 208), sink_k(ring * 32);
   std::vector<int> sink_rc(ring);
   gmc_server_reset_stats(s);
-  // splitmix64 draws: the generator must outpace the server it loads
-  uint64_t sm = seed ^ 0x9E3779B97F4A7C15ull;
-  auto next64 = [&]() {
-    uint64_t z = (sm += 0x9E3779B97F4A7C15ull);
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-  };
-  auto unit = [&]() { return (double)(next64() >> 11) * (1.0 / 9007199254740992.0); };  // [0, 1)
-  const double t0 = now_s();
-  double t_next = t0;
-  size_t idx = 0;
-  long long submitted = 0;
-  std::vector<Req> due;
+  // Arrivals come from kGenThreads generator threads, each a Poisson process at
+  // rate / kGenThreads (their superposition is Poisson at `rate`): one thread's
+  // per-request work (draws, logarithm, queue push) capped the offered rate
+  // near the server's peak, and a request's latency counts from its scheduled
+  // arrival, so a lagging generator showed up as queueing delay.
+  constexpr int kGenThreads = 4;
+  const size_t per_ring = ring / kGenThreads;
   const size_t queue_cap = (size_t)4 * (size_t)s->max_batch * s->slots.size();  // bounds host memory under overload
-  while (true) {
-    const double t = now_s();
-    if (t - t0 > seconds) break;
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      if (s->queue.size() > queue_cap) {
-        t_next = std::max(t_next, t);  // arrivals while the queue is over its cap are not offered
-      }
-    }
-    due.clear();
-    while (t_next <= t && due.size() < (1u << 20)) {
-      const uint64_t x = next64();
-      const int pair = (int)(((x & 0xFFFFFFFFull) * (uint64_t)npairs) >> 32);
-      const bool enc = (double)(x >> 40) * (1.0 / 16777216.0) < enc_fraction;
-      const size_t slot = idx++ % ring;
-      const int pi = (int)((x >> 32) & 0xFF) % pool_n;
-      Req r{};
-      r.key = enc ? pks[pair] : sks[pair];
-      r.in = enc ? seeds.data() + (size_t)pi * 32 : cts[pair].data() + (size_t)pi * set_info(sks[pair]->set).synd_bytes;
-      r.ct = sink_ct.data() + slot * 208;
-      r.k = sink_k.data() + slot * 32;
-      r.rc = &sink_rc[slot];
-      r.t_arrive = t_next;
-      r.done = nullptr;
-      due.push_back(r);
-      t_next += -log1p(-unit()) / rate;  // exponential inter-arrival gap
-    }
-    if (!due.empty()) {
+  const double t0 = now_s();
+  std::atomic<long long> submitted{0};
+  auto generate = [&](int gi) {
+    // splitmix64 draws
+    uint64_t sm = (seed + 0x632BE59BD9B4E019ull * (uint64_t)(gi + 1)) ^ 0x9E3779B97F4A7C15ull;
+    auto next64 = [&]() {
+      uint64_t z = (sm += 0x9E3779B97F4A7C15ull);
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      return z ^ (z >> 31);
+    };
+    auto unit = [&]() { return (double)(next64() >> 11) * (1.0 / 9007199254740992.0); };  // [0, 1)
+    const double grate = rate / kGenThreads;
+    double t_next = t0 - log1p(-unit()) / grate;
+    size_t idx = 0;
+    long long mine = 0;
+    std::vector<Req> due;
+    while (true) {
+      const double t = now_s();
+      if (t - t0 > seconds) break;
       {
         std::lock_guard<std::mutex> lk(s->mu);
-        if (!s->t_first) s->t_first = t0;
-        for (auto &r : due) s->queue.push_back(r);
+        if (s->queue.size() > queue_cap) {
+          t_next = std::max(t_next, t);  // arrivals while the queue is over its cap are not offered
+        }
       }
-      s->cv.notify_all();
-      submitted += (long long)due.size();
-    } else {
-      std::this_thread::yield();
+      due.clear();
+      while (t_next <= t && due.size() < (1u << 18)) {
+        const uint64_t x = next64();
+        const int pair = (int)(((x & 0xFFFFFFFFull) * (uint64_t)npairs) >> 32);
+        const bool enc = (double)(x >> 40) * (1.0 / 16777216.0) < enc_fraction;
+        const size_t slot = gi * per_ring + idx++ % per_ring;
+        const int pi = (int)((x >> 32) & 0xFF) % pool_n;
+        Req r{};
+        r.key = enc ? pks[pair] : sks[pair];
+        r.in = enc ? seeds.data() + (size_t)pi * 32
+                   : cts[pair].data() + (size_t)pi * set_info(sks[pair]->set).synd_bytes;
+        r.ct = sink_ct.data() + slot * 208;
+        r.k = sink_k.data() + slot * 32;
+        r.rc = &sink_rc[slot];
+        r.t_arrive = t_next;
+        r.done = nullptr;
+        due.push_back(r);
+        t_next += -log1p(-unit()) / grate;  // exponential inter-arrival gap
+      }
+      if (!due.empty()) {
+        {
+          std::lock_guard<std::mutex> lk(s->mu);
+          if (!s->t_first) s->t_first = t0;
+          s->queue.insert(s->queue.end(), due.begin(), due.end());
+        }
+        s->cv.notify_all();
+        mine += (long long)due.size();
+      } else {
+        std::this_thread::yield();
+      }
     }
-  }
+    submitted += mine;
+  };
+  std::vector<std::thread> gens;
+  for (int gi = 1; gi < kGenThreads; gi++) gens.emplace_back(generate, gi);
+  generate(0);
+  for (auto &g : gens) g.join();
   int r = gmc_server_drain(s, 60.0);
   double st[8];
   gmc_server_stats(s, st);
-  out[0] = (double)submitted;
+  out[0] = (double)submitted.load();
   out[1] = st[0];                       // completed
   out[2] = st[0] / (now_s() - t0);      // achieved ops/s over the run (incl. drain)
   out[3] = st[3];                       // p50 ms
   out[4] = st[4];                       // p99 ms
   out[5] = st[2];                       // mean batch size
   out[6] = st[1];                       // batches
-  out[7] = (double)submitted / seconds; // offered rate
+  out[7] = (double)submitted.load() / seconds; // offered rate
   return r;
 }
