@@ -482,24 +482,42 @@ bool form_batch(gmc_server *srv, Slot &sl) {
     sl.pieces.clear();
     return false;
   }
-  // gather inputs into pinned staging, mirroring the device input layout
-  for (auto &pp : sl.pipes) {
-    const gmc_setinfo &S = set_info(pp.set);
-    const size_t inb = pp.kind == 0 ? 32 : S.synd_bytes;
+  // gather inputs into pinned staging, mirroring the device input layout: one
+  // parallel pass over the batch's (pipeline, key) segments laid end to end
+  // (a pass per segment left the many small segments of a mixed batch on the
+  // dispatcher thread alone)
+  struct SegRef {
+    Pipe *pp;
+    int sg;
+    size_t first;  // index of the segment's first member in the flat order
+  };
+  std::vector<SegRef> segs;
+  size_t total = 0;
+  for (auto &pp : sl.pipes)
     for (size_t sg = 0; sg < pp.keys.size(); sg++) {
-      const std::vector<int> &mem = pp.members[sg];
-      parallel_for(mem.size(), [&](size_t b, size_t e) {
-        for (size_t j = b; j < e; j++) {
-          Piece &pc = sl.pieces[mem[j]];
-          const long long row = pp.segs.row0[sg] + (long long)j;
-          memcpy(sl.h_in + pp.in_off + row * inb, pc.r.in, inb);
-          pc.out_k = pp.k_off - sl.in_used + row * 32;
-          pc.out_ct = pp.ct_off - sl.in_used + row * S.synd_bytes;
-          pc.out_rc = pp.rc_off - sl.in_used + row * 4;
-        }
-      });
+      segs.push_back({&pp, (int)sg, total});
+      total += pp.members[sg].size();
     }
-  }
+  parallel_for(total, [&](size_t b, size_t e) {
+    // the segment holding flat index b, then walk forward
+    size_t si = (size_t)(std::upper_bound(segs.begin(), segs.end(), b,
+                                          [](size_t x, const SegRef &r) { return x < r.first; }) -
+                         segs.begin()) - 1;
+    for (size_t f = b; f < e; f++) {
+      while (si + 1 < segs.size() && segs[si + 1].first <= f) si++;
+      const SegRef &sr = segs[si];
+      const Pipe &pp = *sr.pp;
+      const gmc_setinfo &S = set_info(pp.set);
+      const size_t inb = pp.kind == 0 ? 32 : S.synd_bytes;
+      const size_t j = f - sr.first;
+      Piece &pc = sl.pieces[pp.members[sr.sg][j]];
+      const long long row = pp.segs.row0[sr.sg] + (long long)j;
+      memcpy(sl.h_in + pp.in_off + row * inb, pc.r.in, inb);
+      pc.out_k = pp.k_off - sl.in_used + row * 32;
+      pc.out_ct = pp.ct_off - sl.in_used + row * S.synd_bytes;
+      pc.out_rc = pp.rc_off - sl.in_used + row * 4;
+    }
+  });
   return true;
 }
 
