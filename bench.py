@@ -194,6 +194,16 @@ def cpu_baseline(sid, pk, sk, cts_host, seeds_host, c_gpu, k_gpu, kdec_gpu, thre
     }, {"checked_enc": m, "checked_dec": md, "mismatches": mism}
 
 
+def metric_name(set_name):
+    """The metric string both arms print (the reference arm measures the same workload on the host cores)."""
+    return f"mceliece{set_name} KEM enc+dec ops/s (batched, bit-exact)"
+
+
+def workload(set_name, n, flip):
+    return (f"mceliece{set_name} full KEM: {n} batched encapsulations + {n} batched decapsulations "
+            f"({int(flip * 100)}% with one flipped bit) per step, one resident key pair")
+
+
 def run_reference(args, rank):
     """CPU implementation of the path (oracle port) on all host threads."""
     if rank != 0:
@@ -225,12 +235,12 @@ def run_reference(args, rank):
     dt = (time.perf_counter() - t0) / args.steps
     value = 2 * sample / dt
     line = {
-        "impl": "reference", "metric": f"mceliece{args.set} KEM enc+dec ops/s", "value": value,
+        "impl": "reference", "metric": metric_name(args.set), "value": value,
         "unit": "KEM ops/s (enc+dec, 50/50)", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded keys, seeds and flips)",
-        "config": {"workload": f"mceliece{args.set} full KEM, {sample} enc + {sample} dec per step "
-                               f"({int(args.flip * 100)}% flipped)", "n": sample, "threads": threads},
+        "config": {"workload": workload(args.set, args.n, args.flip), "set": args.set, "n_per_gpu": args.n,
+                   "sample_per_step": sample, "threads": threads},
         "cpu_baseline": {"value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "cores": threads, "kind": "port",
                          "sample": f"{sample} enc + {sample} dec per step"},
         "e2e": {"value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "h2d_bytes_per_step": 0,
@@ -654,14 +664,12 @@ def main():
     }
 
     line = {
-        "metric": f"mceliece{args.set} KEM enc+dec ops/s (batched, bit-exact)",
+        "metric": metric_name(args.set),
         "value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8",
         "data": "synthetic: seeded key pair, random 32-byte request seeds, 10% bit-flipped ciphertexts",
-        "config": {"workload": f"mceliece{args.set} full KEM: {N} batched encapsulations + {N} batched "
-                               f"decapsulations ({int(args.flip * 100)}% with one flipped bit) per step, "
-                               f"one resident key pair", "set": args.set, "n_per_gpu": N,
+        "config": {"workload": workload(args.set, N, args.flip), "set": args.set, "n_per_gpu": N,
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MiB write) between timed steps",
                    "gemm_engine": args.engine,
                    "tuning": {k: gmc.tune_get(k) for k in gmc.SETS} if not tuning else tuning},
