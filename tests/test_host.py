@@ -135,3 +135,32 @@ def test_key_import_rejects_foreign_strings():
     junk = np.frombuffer(b"not a key string" * 16, np.uint8).copy()
     assert L.gmc_key_import(ctypes.byref(h), junk.ctypes.data_as(ctypes.c_void_p), junk.size) == -4  # GMC_EKEY
     assert L.gmc_key_import(ctypes.byref(h), junk.ctypes.data_as(ctypes.c_void_p), 8) == -1  # too short
+
+
+def test_tune_cache_load_on_host(tmp_path):
+    """gmc_autotune_load applies a JSON cache on the host (no device work):
+    known fields are taken, out-of-range launch shapes fall back to their
+    defaults, and sets absent from the file keep their configuration."""
+    import tensormceliece_gb300 as gmc
+    before = {s: gmc.tune_get(s) for s in ("460896", "6688128")}
+    cache = {"gpu": "any", "sets": {
+        "348864": {"enc_engine": "tc", "dec_engine": "popc", "sample_threads": 64, "sample_sm_warps": 8,
+                   "gemm_stages": 3, "bm_warps": 4, "root_warps": 2, "n": 4096, "enc_ms": 0.1, "dec_ms": 0.2},
+        "8192128": {"enc_engine": "sparse", "dec_engine": "sparse", "sample_threads": 100, "sample_sm_warps": 99,
+                    "gemm_stages": 7, "bm_warps": 0, "root_warps": 12, "n": 1, "enc_ms": 1, "dec_ms": 1}}}
+    path = tmp_path / "tune.json"
+    path.write_text(json.dumps(cache, indent=2))
+    try:
+        assert gmc.autotune_load(str(path)) == 2
+        a = gmc.tune_get("348864")
+        assert a["tuned"] and (a["enc_engine"], a["dec_engine"], a["sample_threads"]) == ("tc", "popc", 64)
+        assert (a["sample_sm_warps"], a["gemm_stages"], a["bm_warps"], a["root_warps"]) == (8, 3, 4, 2)
+        b = gmc.tune_get("8192128")
+        # no sparse front end for decapsulation; invalid shapes take the defaults
+        assert b["dec_engine"] == "tc" and b["sample_threads"] == 128
+        assert (b["sample_sm_warps"], b["gemm_stages"], b["bm_warps"], b["root_warps"]) == (0, 4, 8, 8)
+        for s, t in before.items():
+            assert gmc.tune_get(s) == t
+    finally:
+        for s in ("348864", "8192128"):
+            gmc.tune_set(s, "sparse", "tc", 128, gemm_stages=4, bm_warps=8, root_warps=8, sample_sm_warps=0)
