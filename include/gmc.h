@@ -39,9 +39,7 @@ typedef struct gmc_key gmc_key;
  *   v = 2  "f": semi-systematic key generation (different keys, the same
  *          encapsulation and decapsulation as the set);
  *   v = 3  "pcf": both.
- * Every entry point taking a set id or a key accepts all of them, except the
- * serving loop (gmc_server_*), which serves keys without plaintext
- * confirmation. */
+ * Every entry point taking a set id or a key accepts all of them. */
 #define GMC_NVARIANTS 20
 int gmc_set_count(void);
 const char *gmc_set_name(int set);
@@ -154,7 +152,8 @@ void gmc_plan_free(gmc_plan *plan);
  * them; their device state is completed at registration.
  * gmc_server_submit queues one request with host buffers (in: 32-byte seed for
  * a public key, ciphertext for a secret key; ct out for a public key; k out;
- * optional rc) and returns at once; *done (optional) becomes 1 when the
+ * optional rc; ciphertexts of pc keys are 32 bytes longer) and returns at
+ * once; *done (optional) becomes 1 when the
  * outputs are written (-1 on failure). A dispatcher thread forms each batch
  * from everything queued when a slot frees up, so requests that arrive while
  * others run join the next batch. Results equal the one-request calls.

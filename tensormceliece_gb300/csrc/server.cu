@@ -9,8 +9,8 @@
 // admitted only up to what its slot's arena holds (the arenas are carved from
 // the free device memory measured at start-up: admission by free HBM).
 // A batch runs as: gather inputs into pinned staging -> one host-to-device
-// copy -> per (parameter set, enc/dec) the segment-aware kernels over all its
-// keys, each pipeline on its own stream (forked from and joined back to the
+// copy -> per (parameter set, enc/dec, plaintext confirmation or not) the
+// segment-aware kernels over all its keys, each pipeline on its own stream (forked from and joined back to the
 // slot's stream, so they overlap) -> one device-to-host copy -> a host
 // callback that hands the slot to the completion thread, which scatters the
 // results (on persistent host workers), marks the requests done and records
@@ -71,14 +71,14 @@ struct Piece {  // one request inside a batch
 };
 
 struct Pipe {
-  int set, kind;
+  int set, kind, pc;  // pc: plaintext-confirmation keys (ciphertext C0 || C1)
   std::vector<const gmc_key *> keys;
   std::vector<std::vector<int>> members;  // piece indices per key
   Segs segs;
   size_t in_off, k_off, ct_off, rc_off, work_off;
 };
 
-constexpr int kPipes = 2 * GMC_NSETS;  // at most one pipeline per (set, op) in a batch
+constexpr int kPipes = 4 * GMC_NSETS;  // at most one pipeline per (set, op, pc) in a batch
 
 struct Slot {
   cudaStream_t st = nullptr;
@@ -97,6 +97,9 @@ struct Slot {
 };
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// ciphertext bytes of a set's keys: C0, plus the 32-byte C1 with plaintext confirmation
+size_t ct_len(int set, int pc) { return (size_t)set_info(set).synd_bytes + (pc ? 32 : 0); }
 
 // Persistent host workers for the per-request gather and scatter of a batch
 // (threads are started once, not per batch: thread creation on every batch
@@ -251,7 +254,7 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
                                 tc_err_word_ptr(), pst);
     }
     if (e == cudaSuccess)
-      e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, false, pst);
+      e = launch_finalize<SET>(E, ew, Sy, mw, sl.dev + pp.ct_off, kout, pp.segs, bad, pp.pc != 0, pst);
     return e;
   }
   const int cw = ref->cw_pad, s2 = round_up((2 * S.t * S.m + 31) / 32, 4);
@@ -269,14 +272,14 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   if (field_tables(SET, &fd) != GMC_OK) return cudaErrorUnknown;
   DecKeys dk{};
   for (size_t i = 0; i < pp.keys.size(); i++) dk.k[i] = pp.keys[i]->dk;
-  cudaError_t e = launch_pack_ct<SET>(in, pp.segs, X, cw, false, pst);
+  cudaError_t e = launch_pack_ct<SET>(in, pp.segs, X, cw, pp.pc != 0, pst);
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->ldf, ref->frows_pad, X, cw, ref->cw_pad, S2, s2, p::s2w,
                             tc_err_word_ptr(), pst);
   if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst, tune.bm_warps);
   if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst, tune.root_warps);
   if (e == cudaSuccess)
-    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, false, pst);
+    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, pp.pc != 0, pst);
   return e;
 }
 
@@ -308,7 +311,7 @@ void complete_batch(Slot *sl) {
       Piece &pc = sl->pieces[i];
       memcpy(pc.r.k, sl->h_out + pc.out_k, 32);
       if (pc.r.key->kind == 0) {
-        memcpy(pc.r.ct, sl->h_out + pc.out_ct, set_info(pc.r.key->set).synd_bytes);
+        memcpy(pc.r.ct, sl->h_out + pc.out_ct, ct_len(pc.r.key->set, pc.r.key->pc));
         if (pc.r.rc) *pc.r.rc = pc.r.key->pad_bad ? -1 : 0;
       } else if (pc.r.rc) {
         memcpy(pc.r.rc, sl->h_out + pc.out_rc, 4);
@@ -352,26 +355,25 @@ void completer_main(gmc_server *srv) {
 }
 
 // device bytes of one pipeline (inputs, outputs, work) for `rows` padded rows
-size_t pipe_bytes(int set, int kind, long long rows) {
+size_t pipe_bytes(int set, int kind, int pc, long long rows) {
   if (rows <= 0) return 0;
-  const gmc_setinfo &S = set_info(set);
-  const size_t inb = kind == 0 ? 32 : S.synd_bytes;
-  return align256(rows * inb) + align256(rows * 32) + align256(rows * S.synd_bytes) + align256(rows * 4) +
+  const size_t inb = kind == 0 ? 32 : ct_len(set, pc);
+  return align256(rows * inb) + align256(rows * 32) + align256(rows * ct_len(set, pc)) + align256(rows * 4) +
          work_bytes(set, kind, rows);
 }
 
 // staging bytes of one pipeline (padded rows, same layout as on the device)
-size_t in_bytes(int set, int kind, long long rows) {
+size_t in_bytes(int set, int kind, int pc, long long rows) {
   if (rows <= 0) return 0;
-  return align256(rows * (kind == 0 ? 32 : set_info(set).synd_bytes));
+  return align256(rows * (kind == 0 ? 32 : ct_len(set, pc)));
 }
-size_t out_bytes(int set, int kind, long long rows) {
+size_t out_bytes(int set, int kind, int pc, long long rows) {
   if (rows <= 0) return 0;
-  return align256(rows * 32) + (kind == 0 ? align256(rows * set_info(set).synd_bytes) : align256(rows * 4));
+  return align256(rows * 32) + (kind == 0 ? align256(rows * ct_len(set, pc)) : align256(rows * 4));
 }
 
-// the largest padding a batch can carry: 5 sets x {enc, dec} pipelines of kMaxSegs keys
-constexpr long long kPadRows = 10LL * kMaxSegs * kGemmOpPad;
+// the largest padding a batch can carry: kPipes pipelines of kMaxSegs keys
+constexpr long long kPadRows = (long long)kPipes * kMaxSegs * kGemmOpPad;
 
 // Lays out the next batch in a free slot from sl.incoming (moved out of the
 // queue by the dispatcher). Requests are taken in order while they fit the
@@ -391,13 +393,13 @@ bool form_batch(gmc_server *srv, Slot &sl) {
     int last = -1;
     long long rows = 0;
   };
-  Acc by[GMC_NSETS][2];
+  Acc by[GMC_NSETS][2][2];  // [set][op][pc]
   size_t in_b = 0, out_b = 0, dev_need = 0;
   size_t taken = 0;
   for (; taken < sl.incoming.size(); taken++) {
     const Req &r = sl.incoming[taken];
-    const int kind = r.key->kind, set = r.key->set;
-    Acc &acc = by[set][kind];
+    const int kind = r.key->kind, set = r.key->set, pc = r.key->pc ? 1 : 0;
+    Acc &acc = by[set][kind][pc];
     int ki = acc.last;
     if (ki < 0 || acc.keys[ki].key != r.key) {
       ki = -1;
@@ -411,9 +413,9 @@ bool form_batch(gmc_server *srv, Slot &sl) {
     if (cnt % kGemmOpPad == 0) {  // a new padded block of rows (or a new key): re-check the admission
       if (ki < 0 && acc.keys.size() >= (size_t)kMaxSegs) break;  // one pipeline per (set, op)
       const long long rows_new = acc.rows + kGemmOpPad;
-      const size_t dev_new = dev_need - pipe_bytes(set, kind, acc.rows) + pipe_bytes(set, kind, rows_new);
-      const size_t in_new = in_b - in_bytes(set, kind, acc.rows) + in_bytes(set, kind, rows_new);
-      const size_t out_new = out_b - out_bytes(set, kind, acc.rows) + out_bytes(set, kind, rows_new);
+      const size_t dev_new = dev_need - pipe_bytes(set, kind, pc, acc.rows) + pipe_bytes(set, kind, pc, rows_new);
+      const size_t in_new = in_b - in_bytes(set, kind, pc, acc.rows) + in_bytes(set, kind, pc, rows_new);
+      const size_t out_new = out_b - out_bytes(set, kind, pc, acc.rows) + out_bytes(set, kind, pc, rows_new);
       if (in_new > sl.h_in_bytes || out_new > sl.h_out_bytes || dev_new > sl.dev_bytes) break;
       acc.rows = rows_new;
       dev_need = dev_new;
@@ -437,36 +439,36 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   // device layout: [inputs of all pipes][outputs of all pipes][work of each pipe]
   size_t off = 0;
   for (int set = 0; set < GMC_NSETS; set++)
-    for (int kind = 0; kind < 2; kind++) {
-      Acc &acc = by[set][kind];
-      if (acc.keys.empty()) continue;
-      Pipe pp{};
-      pp.set = set;
-      pp.kind = kind;
-      pp.segs = Segs{};
-      long long row = 0;
-      for (auto &kk : acc.keys) {
+    for (int kind = 0; kind < 2; kind++)
+      for (int pc = 0; pc < 2; pc++) {
+        Acc &acc = by[set][kind][pc];
+        if (acc.keys.empty()) continue;
+        Pipe pp{};
+        pp.set = set;
+        pp.kind = kind;
+        pp.pc = pc;
+        pp.segs = Segs{};
+        long long row = 0;
+        for (auto &kk : acc.keys) {
+          pp.segs.row0[pp.keys.size()] = row;
+          pp.segs.nreq[pp.keys.size()] = (long long)kk.members.size();
+          row += (long long)((kk.members.size() + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad;
+          pp.keys.push_back(kk.key);
+          pp.members.push_back(std::move(kk.members));
+        }
+        pp.segs.nseg = (int)pp.keys.size();
         pp.segs.row0[pp.keys.size()] = row;
-        pp.segs.nreq[pp.keys.size()] = (long long)kk.members.size();
-        row += (long long)((kk.members.size() + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad;
-        pp.keys.push_back(kk.key);
-        pp.members.push_back(std::move(kk.members));
+        pp.in_off = off;
+        off += align256(row * (pp.kind == 0 ? 32 : ct_len(pp.set, pp.pc)));
+        sl.pipes.push_back(std::move(pp));
       }
-      pp.segs.nseg = (int)pp.keys.size();
-      pp.segs.row0[pp.keys.size()] = row;
-      const gmc_setinfo &S = set_info(pp.set);
-      pp.in_off = off;
-      off += align256(row * (pp.kind == 0 ? 32 : S.synd_bytes));
-      sl.pipes.push_back(std::move(pp));
-    }
   sl.in_used = off;
   for (auto &pp : sl.pipes) {
-    const gmc_setinfo &S = set_info(pp.set);
     const long long row = seg_rows(pp.segs);
     pp.k_off = off;
     off += align256(row * 32);
     pp.ct_off = off;
-    if (pp.kind == 0) off += align256(row * S.synd_bytes);
+    if (pp.kind == 0) off += align256(row * ct_len(pp.set, pp.pc));
     pp.rc_off = off;
     if (pp.kind == 1) off += align256(row * 4);
   }
@@ -507,14 +509,14 @@ bool form_batch(gmc_server *srv, Slot &sl) {
       while (si + 1 < segs.size() && segs[si + 1].first <= f) si++;
       const SegRef &sr = segs[si];
       const Pipe &pp = *sr.pp;
-      const gmc_setinfo &S = set_info(pp.set);
-      const size_t inb = pp.kind == 0 ? 32 : S.synd_bytes;
+      const size_t ctb = ct_len(pp.set, pp.pc);
+      const size_t inb = pp.kind == 0 ? 32 : ctb;
       const size_t j = f - sr.first;
       Piece &pc = sl.pieces[pp.members[sr.sg][j]];
       const long long row = pp.segs.row0[sr.sg] + (long long)j;
       memcpy(sl.h_in + pp.in_off + row * inb, pc.r.in, inb);
       pc.out_k = pp.k_off - sl.in_used + row * 32;
-      pc.out_ct = pp.ct_off - sl.in_used + row * S.synd_bytes;
+      pc.out_ct = pp.ct_off - sl.in_used + row * ctb;
       pc.out_rc = pp.rc_off - sl.in_used + row * 4;
     }
   });
@@ -665,8 +667,8 @@ extern "C" int gmc_server_create(gmc_server **out, long long max_batch, int slot
   for (auto &sl : s->slots) {
     sl.srv = s;
     sl.dev_bytes = arena;
-    sl.h_in_bytes = (size_t)(max_batch + kPadRows) * 208 + 10 * 256;
-    sl.h_out_bytes = (size_t)(max_batch + kPadRows) * (208 + 32 + 4) + 30 * 256;
+    sl.h_in_bytes = (size_t)(max_batch + kPadRows) * 240 + kPipes * 256;
+    sl.h_out_bytes = (size_t)(max_batch + kPadRows) * (240 + 32 + 4) + 3 * kPipes * 256;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
     for (int i = 0; i < kPipes && e == cudaSuccess; i++) {
       e = cudaStreamCreateWithFlags(&sl.pst[i], cudaStreamNonBlocking);
@@ -689,9 +691,6 @@ extern "C" int gmc_server_create(gmc_server **out, long long max_batch, int slot
 
 extern "C" int gmc_server_add_key(gmc_server *s, const gmc_key *key) {
   if (!s || !key) return srv_fail(GMC_EINVAL, "gmc_server_add_key: bad argument");
-  // the serving loop lays out rows of the five sets' ciphertexts; plaintext-confirmation keys take the
-  // per-key batch calls or grouped plans
-  if (key->pc) return srv_fail(GMC_EINVAL, "gmc_server_add_key: plaintext-confirmation (pc) keys are not served");
   // resident state needed by every engine choice is built now, outside the request path
   int r = key_prepare_resident(key);
   if (r) return r;
@@ -787,15 +786,15 @@ extern "C" int gmc_server_loadgen(gmc_server *s, const gmc_key *const *pks, cons
   std::mt19937_64 rng(seed);
   for (auto &b : seeds) b = (uint8_t)rng();
   for (int i = 0; i < npairs; i++) {
-    const gmc_setinfo &S = set_info(pks[i]->set);
-    cts[i].resize((size_t)pool_n * S.synd_bytes);
+    cts[i].resize((size_t)pool_n * ct_len(pks[i]->set, pks[i]->pc));
     std::vector<uint8_t> kk((size_t)pool_n * 32);
     int r = gmc_enc_batch(pks[i], cts[i].data(), kk.data(), seeds.data(), pool_n, nullptr);
     if (r) return r;
   }
   // output sinks (results are overwritten; correctness is checked by the tests on small runs)
   const size_t ring = 1 << 16;
-  std::vector<uint8_t> sink_ct(ring * 208), sink_k(ring * 32);
+  constexpr size_t kSinkCt = 256;  // the longest ciphertext (8192128 with plaintext confirmation: 240 bytes)
+  std::vector<uint8_t> sink_ct(ring * kSinkCt), sink_k(ring * 32);
   std::vector<int> sink_rc(ring);
   gmc_server_reset_stats(s);
   // Arrivals come from kGenThreads generator threads, each a Poisson process at
@@ -842,8 +841,8 @@ extern "C" int gmc_server_loadgen(gmc_server *s, const gmc_key *const *pks, cons
         Req r{};
         r.key = enc ? pks[pair] : sks[pair];
         r.in = enc ? seeds.data() + (size_t)pi * 32
-                   : cts[pair].data() + (size_t)pi * set_info(sks[pair]->set).synd_bytes;
-        r.ct = sink_ct.data() + slot * 208;
+                   : cts[pair].data() + (size_t)pi * ct_len(sks[pair]->set, sks[pair]->pc);
+        r.ct = sink_ct.data() + slot * kSinkCt;
         r.k = sink_k.data() + slot * 32;
         r.rc = &sink_rc[slot];
         r.t_arrive = t_next;

@@ -162,9 +162,31 @@ def test_semi_systematic_keys_enc_dec_parity(gmc, sid):
     assert (rcd == orcd).all() and (kd == okd).all()
 
 
-def test_pc_keys_are_not_served(gmc, keys):
-    pk, _ = keys(0)
-    srv = gmc.Server(max_batch=1024, slots=1, mem_fraction=0.05)
-    with pytest.raises(gmc.GmcError):
-        srv.add_key(gmc.PublicKey(5, pk))
+def test_pc_keys_in_the_serving_loop(gmc, keys):
+    """pc keys are served next to plain keys of the same set (separate
+    pipelines): results equal the batch calls, ciphertexts 32 bytes longer."""
+    import ctypes
+    pk, sk = keys(0)
+    P, S, Pp, Sp = gmc.PublicKey(0, pk), gmc.SecretKey(0, sk), gmc.PublicKey(5, pk), gmc.SecretKey(5, sk)
+    srv = gmc.Server(max_batch=1024, slots=2, mem_fraction=0.05)
+    for key in (P, S, Pp, Sp):
+        srv.add_key(key)
+    seeds = request_seeds(0, 40, b"pcsrv")
+    ref_c, ref_k, _ = Pp.enc_batch(seeds)
+    plain_c, plain_k, _ = P.enc_batch(seeds)
+    z = gmc.set_sizes(5)
+    c_out = np.zeros((40, z["ct_bytes"]), np.uint8)
+    k_out = np.zeros((40, 32), np.uint8)
+    c2_out = np.zeros((40, gmc.set_sizes(0)["ct_bytes"]), np.uint8)
+    k2_out = np.zeros((40, 32), np.uint8)
+    kd_out = np.zeros((40, 32), np.uint8)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for i in range(40):
+        srv.submit(Pp, p(seeds[i]), p(c_out[i]), p(k_out[i]))
+        srv.submit(P, p(seeds[i]), p(c2_out[i]), p(k2_out[i]))
+        srv.submit(Sp, p(ref_c[i]), None, p(kd_out[i]))
+    srv.drain(60)
+    assert srv.stats()["errors"] == 0
+    assert (c_out == ref_c).all() and (k_out == ref_k).all() and (kd_out == ref_k).all()
+    assert (c2_out == plain_c).all() and (k2_out == plain_k).all()
     srv.close()

@@ -1,5 +1,6 @@
 """Serving loop (gmc_server_*): requests submitted from several host threads,
-in random order, over all five parameter sets, enc and dec mixed; each result
+in random order, over all five parameter sets and two plaintext-confirmation
+(pc) forms, enc and dec mixed; each result
 must be the one the request gets alone (one-request batch), bit for bit; the
 dispatcher must have formed multi-request batches; the open-loop Poisson load
 generator completes every request it submits."""
@@ -30,6 +31,10 @@ def pairs(gmc):
     for sid in range(5):
         pk, sk = gmc.keypair(sid, key_seed(sid))
         out.append((sid, pk, sk, gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)))
+    # plaintext-confirmation forms of two sets (same key bytes, 32-byte-longer ciphertexts)
+    for sid in (0, 4):
+        _, pk, sk, _, _ = out[sid]
+        out.append((sid + 5, pk, sk, gmc.PublicKey(sid + 5, pk), gmc.SecretKey(sid + 5, sk)))
     return out
 
 
@@ -42,8 +47,8 @@ def test_results_in_the_mix_equal_results_alone(gmc, pairs):
     reqs = []
     for sid, pk, sk, P, S in pairs:
         z = gmc.set_sizes(sid)
-        seeds = request_seeds(sid, 150, b"srv")
-        cts, _, _ = P.enc_batch(request_seeds(sid, 150, b"srvd"))
+        seeds = request_seeds(sid % 5, 150, b"srv" + bytes([sid]))
+        cts, _, _ = P.enc_batch(request_seeds(sid % 5, 150, b"srvd" + bytes([sid])))
         flip = rng.choice(150, 15, replace=False)
         for i in flip:
             b = int(rng.integers(0, z["mt"]))
