@@ -780,6 +780,10 @@ extern "C" int gmc_server_loadgen(gmc_server *s, const gmc_key *const *pks, cons
                                   double *out /* [8] */) {
   if (!s || !pks || !sks || npairs <= 0 || rate <= 0 || seconds <= 0 || !out)
     return srv_fail(GMC_EINVAL, "gmc_server_loadgen: bad argument");
+  for (int i = 0; i < npairs; i++)  // each pair's ciphertext pool is sized by its public key
+    if (!pks[i] || !sks[i] || pks[i]->kind != 0 || sks[i]->kind != 1 || pks[i]->set != sks[i]->set ||
+        pks[i]->pc != sks[i]->pc)
+      return srv_fail(GMC_EINVAL, "gmc_server_loadgen: pair i must be a public and a secret key of one set and form");
   constexpr int pool_n = 256;
   std::vector<std::vector<uint8_t>> cts(npairs);
   std::vector<uint8_t> seeds((size_t)pool_n * 32);
