@@ -161,37 +161,75 @@ def algorithmic_bytes(kernel, z, n):
     return per * n + fixed.get(kernel, 0)
 
 
-def cpu_baseline(sid, pk, sk, cts_host, seeds_host, c_gpu, k_gpu, kdec_gpu, threads):
-    """Oracle port timed on the host cores on a bounded sample; also checks GPU outputs on a sample."""
+def host_cpu():
+    """Model name of the host CPU (lscpu), for the baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_impl():
+    """The CPU implementation of the path: libmceliece-20250507 itself (its portable `vec` code, built by
+    oracle/build_ref.py from the reference's tarball; the implementation libmceliece runs on arm64) when its
+    sources are here, else the oracle port. Returns (module, kind, description)."""
+    from oracle import pyref
+    note = None
+    if pyref.available():
+        try:
+            pyref.lib()
+            return pyref, "reference", pyref.implementation()
+        except Exception as e:  # a failed build is reported, and the port stands in
+            note = f"libmceliece build failed: {str(e).splitlines()[0][:120]}"
     from oracle import pyoracle as O
     O.lib()
-    # calibrate, then size each leg to a few seconds
+    return O, "port", "oracle/mceliece_oracle.c (plain C restatement of libmceliece-20250507)" + (
+        f"; {note}" if note else "; libmceliece sources absent")
+
+
+def cpu_baseline(sid, pk, sk, cts_host, seeds_host, c_gpu, k_gpu, kdec_gpu, threads):
+    """The CPU implementation timed on the host cores, and every GPU output of the e2e batch checked against it.
+    With libmceliece itself the whole batch (N encapsulations + N decapsulations) is both the timed sample and
+    the parity check; with the slower oracle port a bounded sample of a few seconds is timed and checked."""
+    M, kind, impl = cpu_impl()
+    n = len(seeds_host)
+    if kind == "port":
+        t0 = time.perf_counter()
+        M.dec_batch(sid, sk, cts_host[:threads], threads=threads)
+        t_dec1 = (time.perf_counter() - t0) / threads
+        n_dec = int(min(n, max(threads, 6.0 / max(t_dec1, 1e-9))))
+        t0 = time.perf_counter()
+        M.enc_batch(sid, pk, seeds_host[:threads], threads=threads)
+        t_enc1 = (time.perf_counter() - t0) / threads
+        n_enc = int(min(n, max(threads, 3.0 / max(t_enc1, 1e-9))))
+    else:
+        n_enc = n_dec = n
     t0 = time.perf_counter()
-    O.dec_batch(sid, sk, cts_host[:threads], threads=threads)
-    t_dec1 = (time.perf_counter() - t0) / threads
-    n_dec = int(min(len(cts_host), max(threads, 6.0 / max(t_dec1, 1e-9))))
-    t0 = time.perf_counter()
-    O.enc_batch(sid, pk, seeds_host[:threads], threads=threads)
-    t_enc1 = (time.perf_counter() - t0) / threads
-    n_enc = int(min(len(seeds_host), max(threads, 3.0 / max(t_enc1, 1e-9))))
-    t0 = time.perf_counter()
-    oc, ok_, _ = O.enc_batch(sid, pk, seeds_host[:n_enc], threads=threads)
+    oc, ok_, _ = M.enc_batch(sid, pk, seeds_host[:n_enc], threads=threads)
     t_enc = time.perf_counter() - t0
     t0 = time.perf_counter()
-    okd, _ = O.dec_batch(sid, sk, cts_host[:n_dec], threads=threads)
+    okd, _ = M.dec_batch(sid, sk, cts_host[:n_dec], threads=threads)
     t_dec = time.perf_counter() - t0
     enc_rate, dec_rate = n_enc / t_enc, n_dec / t_dec
-    value = 2.0 / (1.0 / enc_rate + 1.0 / dec_rate)
-    m = min(n_enc, len(c_gpu))
-    md = min(n_dec, len(kdec_gpu))
-    mism = int((oc[:m] != c_gpu[:m]).any(1).sum() + (ok_[:m] != k_gpu[:m]).any(1).sum() +
-               (okd[:md] != kdec_gpu[:md]).any(1).sum())
+    value = (n_enc + n_dec) / (n_enc / enc_rate + n_dec / dec_rate)
+    bad_c = int((oc != c_gpu[:n_enc]).any(1).sum())
+    bad_k = int((ok_ != k_gpu[:n_enc]).any(1).sum())
+    bad_kd = int((okd != kdec_gpu[:n_dec]).any(1).sum())
+    what = "the whole e2e batch" if (n_enc, n_dec) == (n, n) else "a bounded sample of the same workload"
     return {
-        "value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "cores": threads, "kind": "port",
-        "sample": f"{n_enc} encapsulations + {n_dec} decapsulations (10% bit-flipped) of the same workload, "
-                  f"{threads} threads; enc {enc_rate:.0f}/s, dec {dec_rate:.0f}/s",
+        "value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "cores": threads, "kind": kind,
+        "implementation": impl, "host_cpu": host_cpu(),
+        "sample": f"{what}: {n_enc} encapsulations + {n_dec} decapsulations (10% bit-flipped), {threads} threads; "
+                  f"enc {enc_rate:.0f}/s, dec {dec_rate:.0f}/s",
         "enc_ops_s": enc_rate, "dec_ops_s": dec_rate,
-    }, {"checked_enc": m, "checked_dec": md, "mismatches": mism}
+    }, {"checked_against": kind, "checked_enc": n_enc, "checked_dec": n_dec, "of": n,
+        "mismatched_ct": bad_c, "mismatched_enc_key": bad_k, "mismatched_dec_key": bad_kd,
+        "mismatches": bad_c + bad_k + bad_kd}
 
 
 def metric_name(set_name):
@@ -205,27 +243,29 @@ def workload(set_name, n, flip):
 
 
 def run_reference(args, rank):
-    """CPU implementation of the path (oracle port) on all host threads."""
+    """The reference's CPU implementation of the path on all host threads: libmceliece-20250507 itself (its
+    portable `vec` code, built from the reference's bundled sources; the oracle port stands in only when those are
+    absent). Each step is a bounded sample of the workload: 512 encapsulations and 512 decapsulations (10% with
+    one flipped bit) per host thread, the same key pair, seeds and flips as the GPU arm's kind of input."""
     if rank != 0:
         return
-    import tensormceliece_gb300 as gmc
-    from oracle import pyoracle as O
-    sid = gmc.set_id(args.set)
-    z = O.sizes(sid)
+    M, kind, impl = cpu_impl()
+    sid = M.sid(args.set)
+    z = M.sizes(sid)
     threads = os.cpu_count() or 1
-    pk, sk = O.keypair(sid, b"\x01" * 32)
+    pk, sk = M.keypair(sid, bytes([0x5A]) * 32)
     rng = np.random.default_rng(7)
-    sample = max(threads, 16 * threads)
+    sample = min(args.n, (512 if kind == "reference" else 16) * threads)
     seeds = rng.integers(0, 256, (sample, 32), dtype=np.uint8)
-    cts, _, _ = O.enc_batch(sid, pk, seeds, threads=threads)
+    cts, _, _ = M.enc_batch(sid, pk, rng.integers(0, 256, (sample, 32), dtype=np.uint8), threads=threads)
     flip = rng.choice(sample, int(args.flip * sample), replace=False)
     for i in flip:
         b = int(rng.integers(0, z["mt"]))
         cts[i, b // 8] ^= np.uint8(1 << (b % 8))
 
     def step():
-        O.enc_batch(sid, pk, seeds, threads=threads)
-        O.dec_batch(sid, sk, cts, threads=threads)
+        M.enc_batch(sid, pk, seeds, threads=threads)
+        M.dec_batch(sid, sk, cts, threads=threads)
 
     for _ in range(args.warmup):
         step()
@@ -239,10 +279,10 @@ def run_reference(args, rank):
         "unit": "KEM ops/s (enc+dec, 50/50)", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded keys, seeds and flips)",
-        "config": {"workload": workload(args.set, args.n, args.flip), "set": args.set, "n_per_gpu": args.n,
-                   "sample_per_step": sample, "threads": threads},
-        "cpu_baseline": {"value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "cores": threads, "kind": "port",
-                         "sample": f"{sample} enc + {sample} dec per step"},
+        "config": {"workload": workload(args.set, args.n, args.flip), "set": args.set, "n_per_gpu": args.n},
+        "cpu_baseline": {"value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "cores": threads, "kind": kind,
+                         "implementation": impl, "host_cpu": host_cpu(),
+                         "sample": f"{sample} enc + {sample} dec (10% bit-flipped) per step, {threads} threads"},
         "e2e": {"value": value, "unit": "KEM ops/s (enc+dec, 50/50)", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -461,14 +501,13 @@ def keccak_rates(z, n, kernels, gmc=None):
 
 def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True, sets=None, calls=2, warmup=True):
     """Batched key generation (gmc_keypair_batch, host buffers in and out) per parameter set: keys/s
-    over nkeys seeds, beside the oracle's keypair on the host threads (a bounded sample whose
-    keys are also compared byte for byte with the GPU's)."""
+    over nkeys seeds, beside the CPU implementation's keypair (libmceliece itself, else the oracle port) on the
+    host threads: a bounded sample whose keys are also compared byte for byte with the GPU's."""
     import hashlib
     out = {"nkeys": nkeys, "sets": {}}
     if with_cpu:
         from concurrent.futures import ThreadPoolExecutor
-        from oracle import pyoracle as O
-        O.lib()
+        O, kind, impl = cpu_impl()
     for name in (sets or gmc.SETS):
         sid = gmc.set_id(name)
         seeds = np.frombuffer(b"".join(hashlib.sha256(b"bench-kg" + bytes([sid]) + i.to_bytes(4, "little")).digest()
@@ -490,7 +529,8 @@ def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True, sets=None, calls
             t_cpu = time.perf_counter() - t0
             bad = sum(int(not (np.array_equal(pk[i], np.asarray(ref[i][0])) and
                                np.array_equal(sk[i], np.asarray(ref[i][1])))) for i in range(ns))
-            e["cpu_baseline"] = {"value": ns / t_cpu, "unit": "keys/s", "cores": cpu_threads, "kind": "port",
+            e["cpu_baseline"] = {"value": ns / t_cpu, "unit": "keys/s", "cores": cpu_threads, "kind": kind,
+                                 "implementation": impl,
                                  "sample": f"{ns} keypairs of the same seeds, {cpu_threads} threads"}
             e["checked_keys"] = ns
             e["mismatches"] = bad
