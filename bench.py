@@ -13,13 +13,16 @@ already in HBM, L2 flushed (256 MiB write) between timed steps.
 e2e: the same step through the host-pointer C ABI calls (gmc_enc_batch /
 gmc_dec_batch) from pinned host buffers, host<->device copies included.
 roofline: the dominant kernel of the step, from the engine's own per-kernel
-event timing (gmc_prof_*).
-cpu_baseline: the CPU oracle port (oracle/), threaded over the host cores, on
-a bounded sample of the same workload; it also spot-checks GPU outputs.
+event timing (gmc_prof_*). The decoding kernels are bounded by the integer ALU
+pipe: their algorithmic 32-bit lane operations (alu_lane_ops) over the launch
+time, against the measured LOP3 rate of the GPU; the HBM figure rides along.
+cpu_baseline: the reference's own CPU implementation (libmceliece-20250507,
+portable vec code, built by oracle/build_ref.py; the oracle port only where
+its sources are absent), threaded over the host cores, timed on the whole e2e
+batch, every output of which is also checked against it (parity_check).
 
---impl reference: times the CPU implementation of the path (the oracle port;
-the reference's own libmceliece cannot be built on the GPU host) with all host
-threads, rank 0 only.
+--impl reference: times that CPU implementation with all host threads on a
+bounded sample of the workload, rank 0 only.
 """
 import argparse
 import json
@@ -159,6 +162,35 @@ def algorithmic_bytes(kernel, z, n):
     fixed = {"enc_syndrome_gemm": z["mt"] * kw, "enc_sample_syndrome": z["k"] * mw,
              "dec_front_gemm": 2 * z["t"] * z["m"] * ((ct + 3) // 4 * 4)}
     return per * n + fixed.get(kernel, 0)
+
+
+def gf_mul_lane_ops(m):
+    """32-bit lane operations of one bit-sliced GF(2^m) product (32 products at once): m^2 fused AND-XOR steps
+    (one LOP3 each) and the reduction by the field polynomial, 4 (m = 13: x^13 + x^4 + x^3 + x + 1) or 2
+    (m = 12: x^12 + x^3 + 1) XORs per high plane."""
+    return m * m + (4 if m == 13 else 2) * (m - 1)
+
+
+def alu_lane_ops(kernel, z):
+    """Algorithmic 32-bit lane operations per request of the bit-sliced decoding kernels (None for the others).
+
+    dec_bm: Berlekamp-Massey over 2t iterations; iteration n needs the discrepancy over coefficients
+    i <= min(L, t) and the update C_i += f B_i over i <= min(max(L, n+1-L), t), one GF(2^m) product each, with
+    the length profile L = ceil(n/2) of a full-rank syndrome sequence; 32 requests per lane operation.
+    dec_fft_roots_reenc: the additive FFT's bottom-up pass, d = log2(2^d >= t) levels of 2^(m-1) butterflies,
+    each one product and two m-plane additions, 32 chunks per lane operation (the top-down pass, the root
+    extraction and the syndrome check are not counted)."""
+    m, t = z["m"], z["t"]
+    if kernel == "dec_bm":
+        prods = 0
+        for n in range(2 * t):
+            L = min((n + 1) // 2, t)
+            prods += min(L, t) + 1 + min(max(L, n + 1 - L), t) + 1
+        return prods * gf_mul_lane_ops(m) / 32.0
+    if kernel == "dec_fft_roots_reenc":
+        d = max(1, (t - 1).bit_length())
+        return d * 2 ** (m - 1) * (gf_mul_lane_ops(m) + 2 * m) / 32.0
+    return None
 
 
 def host_cpu():
@@ -477,15 +509,14 @@ KECCAK_LOP3_PER_PERM = 24 * (20 + 50 + 50 + 2)
 KECCAK_SHF_PER_PERM = 24 * (10 + 48)
 
 
-def keccak_rates(z, n, kernels, gmc=None):
+def keccak_rates(z, n, kernels, pk=None):
     """Keccak-f[1600] permutations per second of the two session-key hash kernels (each request hashes the
     1 + n/8 + ct-byte preimage: ceil((len + 1) / 136) permutations), beside the integer-op ceiling: the
     permutation's op count over the GPU's measured lop3 and funnel-shift rates."""
     perms = (1 + z["n"] // 8 + z["ct_bytes"] + 1 + 135) // 136
     out = {"perms_per_hash": perms}
     ceiling = None
-    if gmc is not None:
-        pk = gmc.int32_peak()
+    if pk is not None:
         ceiling = 1.0 / (KECCAK_LOP3_PER_PERM / pk["lop3_per_s"] + KECCAK_SHF_PER_PERM / pk["shf_per_s"])
         out["int32_peak"] = {"lop3_per_s": pk["lop3_per_s"], "shf_per_s": pk["shf_per_s"],
                              "ops_per_perm": {"lop3": KECCAK_LOP3_PER_PERM, "shf": KECCAK_SHF_PER_PERM},
@@ -686,22 +717,36 @@ def main():
     launches_per_step = sum(v["launches"] for v in kernels.values())
     tot = sum(v["ms"] for v in kernels.values()) or 1.0
     hbm_peak, tc_peak, peak_kind = measured_peaks()
+    ipk = gmc.int32_peak()  # measured LOP3 / funnel-shift lane-op rates of this GPU
     for name, v in kernels.items():
         v["share"] = v["ms"] / tot
         v["gbs"] = algorithmic_bytes(name, z, N) / (v["ms"] / 1e3) / 1e9
+        ops = alu_lane_ops(name, z)
+        if ops is not None:
+            v["alu_lane_ops_per_request"] = ops
+            v["alu_frac"] = ops * N / (v["ms"] / 1e3) / ipk["lop3_per_s"]
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     dom_bytes = algorithmic_bytes(dom, z, N)
-    achieved = dom_bytes / (kernels[dom]["ms"] / 1e3) / 1e9
+    achieved_gbs = dom_bytes / (kernels[dom]["ms"] / 1e3) / 1e9
     traffic = ncu_traffic(args.set, N).get(dom)
-    roofline = {
-        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-        "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_kind,
-        "algorithmic_bytes_per_launch": dom_bytes,
-        "traffic_source": (f"profiles/dram_traffic_kem{args.set}_n{N}.txt (one ncu capture)" if traffic else None),
-        "note": "the decapsulation kernels (bit-sliced Berlekamp-Massey, bit-sliced additive FFT) are bounded by "
-                "the integer ALU pipe (79% / 70% of its peak in profiles/kernels_kem8192128_n65536.md), not by "
-                "HBM: their HBM bytes per request are ~1-2 KB",
-    }
+    hbm = {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+           "algorithmic_bytes_per_launch": dom_bytes, "peak_source": peak_kind}
+    dom_ops = alu_lane_ops(dom, z)
+    if dom_ops is not None:
+        # the decoding kernels are bounded by the integer ALU pipe: algorithmic lane operations of one launch
+        # over its duration, against the measured LOP3 rate of this GPU
+        achieved = dom_ops * N / (kernels[dom]["ms"] / 1e3)
+        roofline = {
+            "bound": "int-alu", "kernel": dom, "achieved": achieved / 1e12, "peak": ipk["lop3_per_s"] / 1e12,
+            "unit": "T lane-ops/s", "frac": achieved / ipk["lop3_per_s"], "traffic": traffic,
+            "algorithmic_lane_ops_per_launch": dom_ops * N, "algorithmic_lane_ops_per_request": dom_ops,
+            "peak_source": "measured on this GPU (gmc_int32_peak: dependent-free LOP3 stream)",
+            "traffic_source": ("one ncu capture of the same command (dram__bytes_read.sum + "
+                               "dram__bytes_write.sum)" if traffic else None),
+            "hbm": hbm,
+        }
+    else:
+        roofline = dict(hbm, bound="hbm", kernel=dom, traffic=traffic)
 
     line = {
         "metric": metric_name(args.set),
@@ -720,7 +765,7 @@ def main():
         "wall_s_timed_loop": wall,
     }
 
-    line["keccak"] = keccak_rates(z, N, kernels, gmc)
+    line["keccak"] = keccak_rates(z, N, kernels, ipk)
     if rank == 0 and not args.no_sweep:
         line["n_sweep"] = {"set": args.set, "flip": args.flip,
                            "ops_s": n_sweep(gmc, torch, dev, args.set, [256, 1024, 4096, 16384, 65536], 5, args.flip)}

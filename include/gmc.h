@@ -100,8 +100,8 @@ int gmc_dec_batch(const gmc_key *sk, unsigned char *k, const unsigned char *c, l
 /* ---- key generation -----------------------------------------------------
  * Keys in libmceliece's format (mc:crypto_kem/348864/vec/kem_keypair.c:20):
  * the keypair whose single 32-byte randombytes draw returns seed32.
- * pk/sk buffers of the set's public/secret-key size. Runs on the host (key
- * generation is outside the batched enc/dec path). */
+ * pk/sk buffers of the set's public/secret-key size. Runs on the GPU: the
+ * batched key generation below with one key. */
 int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32);
 
 /* Batched key generation on the device: nkeys keypairs, key i from the
@@ -247,7 +247,7 @@ void gmc_kem_8192128pcf_keypair(unsigned char *pk, unsigned char *sk);
 int gmc_kem_8192128pcf_enc(unsigned char *c, unsigned char *k, const unsigned char *pk);
 int gmc_kem_8192128pcf_dec(unsigned char *k, const unsigned char *c, const unsigned char *sk);
 
-/* randombytes source of the one-request enc entry points
+/* randombytes source of the one-request keypair and enc entry points
  * (librandombytes' randombytes(), rb:include/randombytes.h:10). NULL restores
  * the OS generator. */
 typedef void (*gmc_randombytes_fn)(void *ctx, unsigned char *out, long long len);
@@ -322,7 +322,8 @@ int gmc_gf2_gemm_dev(int engine, const unsigned int *A, int lda, int rows_pad, c
  * front-end product runs on the CUDA-core engine. At most
  * GMC_NOALLOC_MAX_REQUESTS ciphertexts per call (larger n: GMC_EINVAL).
  * The first call on a device does a one-time set-up (symbol lookup and a
- * synchronous table copy): make it before any stream capture. Calls share the
+ * synchronous table copy): make it before any stream capture. The key must
+ * have been loaded on the current device (GMC_EKEY otherwise). Calls share the
  * array: calls that overlap on the GPU race, so order them on one stream. */
 #define GMC_NOALLOC_MAX_REQUESTS 4096
 int gmc_dec_batch_noalloc(const gmc_key *sk, unsigned char *k, const unsigned char *c, long long n, int *rc,

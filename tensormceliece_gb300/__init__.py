@@ -451,7 +451,7 @@ _rng_keepalive = None
 
 
 def set_randombytes(fn):
-    """fn(n) -> bytes of length n, or None for the OS generator (one-request enc only)."""
+    """fn(n) -> bytes of length n, or None for the OS generator (the one-request enc and keypair calls)."""
     global _rng_keepalive
     if fn is None:
         lib().gmc_set_randombytes(None, None)

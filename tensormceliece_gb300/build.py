@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgmc.so")
 
-SOURCES = ["engine.cu", "kernels_enc.cu", "kernels_gemm.cu", "kernels_gemm_tc.cu", "kernels_dec.cu", "host_keys.cpp", "host_keygen.cpp", "noalloc.cu", "tune.cu", "server.cu", "keygen.cu", "keyfile.cu", "peaks.cu"]
+SOURCES = ["engine.cu", "kernels_enc.cu", "kernels_gemm.cu", "kernels_gemm_tc.cu", "kernels_dec.cu", "host_keys.cpp", "noalloc.cu", "tune.cu", "server.cu", "keygen.cu", "keyfile.cu", "peaks.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

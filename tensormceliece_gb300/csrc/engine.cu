@@ -859,12 +859,12 @@ static int one_dec(int set, unsigned char *k, const unsigned char *c, const unsi
   return rc;
 }
 
+// One key pair: the GPU key generation with a batch of one (there is no host
+// key generation; a plaintext-confirmation variant has the keys of its
+// parameter set, an f variant the semi-systematic form).
 extern "C" int gmc_keypair_seed(int set, unsigned char *pk, unsigned char *sk, const unsigned char *seed32) {
   if (!valid_id(set) || !pk || !sk || !seed32) return fail(GMC_EINVAL, "gmc_keypair_seed: bad argument");
-  // a plaintext-confirmation variant has the keys of its parameter set; f variants the semi-systematic form
-  if (host_keypair(base_of(set), pk, sk, seed32, semi_of(set)))
-    return fail(GMC_EKEY, "gmc_keypair_seed: key generation failed");
-  return GMC_OK;
+  return gmc_keypair_batch(set, pk, sk, seed32, 1);
 }
 
 static int one_keypair(int set, unsigned char *pk, unsigned char *sk) {

@@ -69,10 +69,7 @@ struct SkHost {
 };
 int build_sk(int set, const uint8_t *sk, SkHost &out);
 
-// Key generation in libmceliece's format (host); delta32 is the single
-// 32-byte randombytes draw of the library's keypair; semi: the "f" variants'
-// semi-systematic form (mc:crypto_kem/<set>f/vec/pk_gen.c).
-int host_keypair(int set, uint8_t *pk, uint8_t *sk, const uint8_t delta32[32], bool semi = false);
+// SHAKE256 on the host (the checksum of exported key strings, keyfile.cu)
 void host_shake256(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen);
 
 inline int round_up(int x, int m) { return (x + m - 1) / m * m; }

@@ -15,12 +15,95 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
 #include "../../include/gmc.h"
 #include "engine_internal.h"
 #include "host_keys.h"
+
+namespace gmc {
+// SHAKE256 on the host, for the key string's checksum (FIPS 202: Keccak-f[1600],
+// rate 136 bytes, domain byte 0x1F)
+namespace {
+struct Keccak {
+  uint64_t rc[24];
+  int rho[25];
+  Keccak() {
+    unsigned r = 1;
+    for (int ir = 0; ir < 24; ir++) {
+      uint64_t c = 0;
+      for (int j = 0; j < 7; j++) {
+        if (r & 1) c |= 1ull << ((1 << j) - 1);
+        r = ((r << 1) ^ ((r & 0x80) ? 0x71 : 0)) & 0xFF;
+      }
+      rc[ir] = c;
+    }
+    int x = 1, y = 0;
+    rho[0] = 0;
+    for (int t = 0; t < 24; t++) {
+      rho[x + 5 * y] = ((t + 1) * (t + 2) / 2) % 64;
+      int nx = y, ny = (2 * x + 3 * y) % 5;
+      x = nx;
+      y = ny;
+    }
+  }
+  static uint64_t rot(uint64_t v, int n) { return n ? (v << n) | (v >> (64 - n)) : v; }
+  void f(uint64_t *s) const {
+    uint64_t C[5], D[5], B[25];
+    for (int round = 0; round < 24; round++) {
+      for (int x = 0; x < 5; x++) C[x] = s[x] ^ s[x + 5] ^ s[x + 10] ^ s[x + 15] ^ s[x + 20];
+      for (int x = 0; x < 5; x++) D[x] = C[(x + 4) % 5] ^ rot(C[(x + 1) % 5], 1);
+      for (int x = 0; x < 5; x++)
+        for (int y = 0; y < 5; y++) B[y + 5 * ((2 * x + 3 * y) % 5)] = rot(s[x + 5 * y] ^ D[x], rho[x + 5 * y]);
+      for (int y = 0; y < 5; y++)
+        for (int x = 0; x < 5; x++)
+          s[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
+      s[0] ^= rc[round];
+    }
+  }
+};
+const Keccak &keccak() {
+  static Keccak k;
+  return k;
+}
+}  // namespace
+
+void host_shake256(uint8_t *out, size_t outlen, const uint8_t *in, size_t inlen) {
+  const Keccak &K = keccak();
+  uint64_t s[25] = {0};
+  uint8_t blk[136];
+  while (inlen >= 136) {
+    for (int i = 0; i < 17; i++) {
+      uint64_t w = 0;
+      for (int b = 0; b < 8; b++) w |= (uint64_t)in[8 * i + b] << (8 * b);
+      s[i] ^= w;
+    }
+    K.f(s);
+    in += 136;
+    inlen -= 136;
+  }
+  memset(blk, 0, sizeof blk);
+  memcpy(blk, in, inlen);
+  blk[inlen] ^= 0x1F;
+  blk[135] ^= 0x80;
+  for (int i = 0; i < 17; i++) {
+    uint64_t w = 0;
+    for (int b = 0; b < 8; b++) w |= (uint64_t)blk[8 * i + b] << (8 * b);
+    s[i] ^= w;
+  }
+  for (;;) {
+    K.f(s);
+    size_t take = std::min<size_t>(outlen, 136);
+    for (size_t j = 0; j < take; j++) out[j] = (uint8_t)(s[j / 8] >> (8 * (j % 8)));
+    out += take;
+    outlen -= take;
+    if (!outlen) break;
+  }
+}
+
+}  // namespace gmc
 
 namespace {
 using namespace gmc;
@@ -46,19 +129,26 @@ int kf_fail(int code, const std::string &msg) {
 
 size_t s_alloc_bytes(const gmc_setinfo &S) { return ((size_t)S.e_bytes + 15) / 16 * 16; }
 
-// section sizes implied by a header's dimensions
+// Section sizes implied by a header's dimensions. The dimensions must be
+// exactly the ones gmc_pk_load / gmc_sk_load give a key of this set (the
+// kernels assume that layout: a smaller padded width would make the GEMM skip
+// words of the key or ciphertext and return wrong session keys with rc = 0),
+// and the public key's padding flag must be 0 or 1.
 bool section_sizes(const KeyHeader &h, uint64_t out[4]) {
   const gmc_setinfo &S = set_info(h.set);
   memset(out, 0, 4 * sizeof(uint64_t));
   if (h.kind == 0) {
-    if (h.rows_pad < S.mt || h.lda < (S.k + 31) / 32 || h.ldtt < (S.mt + 31) / 32 || h.rows_pad > 1 << 16 ||
-        h.lda > 1 << 12 || h.ldtt > 1 << 12)
+    const int kw_pad = round_up((S.k + 31) / 32, kGemmKTile);
+    const int ldtt = round_up((S.mt + 31) / 32, 32) < 64 ? 64 : round_up((S.mt + 31) / 32, 32);
+    if (h.kw_pad != kw_pad || h.lda != kw_pad || h.rows_pad != round_up(S.mt, kGemmRowTile) || h.ldtt != ldtt ||
+        (h.pad_bad != 0 && h.pad_bad != 1))
       return false;
     out[0] = (uint64_t)h.rows_pad * h.lda * 4;
     out[1] = (uint64_t)(S.k + 1) * h.ldtt * 4;
   } else {
-    if (h.frows_pad < 2 * S.t * S.m || h.ldf < (S.synd_bytes + 3) / 4 || h.ldh < (S.t * S.m + 31) / 32 ||
-        h.frows_pad > 1 << 16 || h.ldf > 1 << 12 || h.ldh > 1 << 12)
+    const int cw_pad = round_up((S.synd_bytes + 3) / 4, kGemmKTile);
+    if (h.cw_pad != cw_pad || h.ldf != cw_pad || h.frows_pad != round_up(2 * S.t * S.m, kGemmRowTile) ||
+        h.ldh != round_up((S.t * S.m + 31) / 32, 32))
       return false;
     out[0] = (uint64_t)h.frows_pad * h.ldf * 4;
     out[1] = (3ull * S.n + S.q) * 2;

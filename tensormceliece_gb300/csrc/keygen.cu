@@ -719,8 +719,8 @@ __global__ void __launch_bounds__(ElimCfg<TB>::nt, ElimCfg<TB>::minb) kg_elim_ke
 }
 
 // ---------------------------------------------------------------- control bits
-// CTA per winner. The library's recursion (controlbits.c:29-150, restated in
-// host_keygen.cpp) processes a permutation of 2^w entries and recurses into
+// CTA per winner. The library's recursion (controlbits.c:29-150) processes a
+// permutation of 2^w entries and recurses into
 // two halves with doubled bit stride; here every depth d runs all 2^d
 // sub-permutations at once, each a segment of 2^(w-d) entries. Segment s at
 // depth d writes layer d and layer 2w-2-d at bits offset_s + 2^d j,

@@ -15,7 +15,8 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // device addresses of the two arrays with cudaGetSymbolAddress and copies the
 // field tables into the second one (cudaMemcpy, synchronous). Make that first
-// call before any stream capture. Later calls do no set-up.
+// call before any stream capture. Later calls do no set-up. The key must have
+// been loaded on the current device (the call refuses it otherwise).
 //
 // All calls share the arrays and the arrays keep the last call's contents.
 // Every intermediate is written in full before it is read, so nothing has to
@@ -26,8 +27,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
-#include <set>
 #include <string>
 #include <vector>
 
@@ -87,8 +88,14 @@ struct DeviceSetup {
   FieldDev fd[GMC_NSETS];
 };
 
+// One set-up record per device ordinal, in a fixed array so that a record's
+// address never changes: a call keeps using its record after the mutex is
+// released while another thread sets up a different device. A record is
+// written once, under the mutex, before its ready flag is published.
+constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
-std::vector<std::pair<int, DeviceSetup>> g_setups;  // per device (set-up done)
+DeviceSetup g_setups[kMaxDevices];
+std::atomic<bool> g_ready[kMaxDevices];
 
 int set_error(int code, const char *msg) {
   gmc::set_last_error(msg);
@@ -96,16 +103,19 @@ int set_error(int code, const char *msg) {
 }
 
 // once per device: symbol addresses, field tables copied into the static array
-int device_setup(const DeviceSetup **out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: no device");
+int device_setup(int dev, const DeviceSetup **out) {
+  if (dev < 0 || dev >= kMaxDevices)
+    return set_error(GMC_EINVAL, "gmc_dec_batch_noalloc: device ordinal too large");
+  if (g_ready[dev].load(std::memory_order_acquire)) {
+    *out = &g_setups[dev];
+    return GMC_OK;
+  }
   std::lock_guard<std::mutex> lk(g_setup_mu);
-  for (auto &e : g_setups)
-    if (e.first == dev) {
-      *out = &e.second;
-      return GMC_OK;
-    }
-  DeviceSetup su;
+  if (g_ready[dev].load(std::memory_order_acquire)) {
+    *out = &g_setups[dev];
+    return GMC_OK;
+  }
+  DeviceSetup &su = g_setups[dev];
   if (cudaGetSymbolAddress((void **)&su.scratch, g_noalloc_scratch) != cudaSuccess ||
       cudaGetSymbolAddress((void **)&su.fields, g_noalloc_fields) != cudaSuccess)
     return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: cudaGetSymbolAddress failed");
@@ -141,8 +151,8 @@ int device_setup(const DeviceSetup **out) {
     su.fd[set].frob_hi_bs = reinterpret_cast<const uint32_t *>(base + o_fhbs);
     su.fd[set].zech = base + o_zech;
   }
-  g_setups.push_back({dev, su});
-  *out = &g_setups.back().second;
+  g_ready[dev].store(true, std::memory_order_release);
+  *out = &su;
   return GMC_OK;
 }
 
@@ -186,8 +196,13 @@ extern "C" int gmc_dec_batch_noalloc(const gmc_key *sk, unsigned char *k, const 
   if (n > kMaxRequests)
     return set_error(GMC_EINVAL, "gmc_dec_batch_noalloc: more than GMC_NOALLOC_MAX_REQUESTS requests; split the "
                                  "batch or use gmc_dec_batch_dev");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return set_error(GMC_ECUDA, "gmc_dec_batch_noalloc: no device");
+  if (sk->device != dev)
+    return set_error(GMC_EKEY, "gmc_dec_batch_noalloc: the key was loaded on another device; make that device "
+                               "current");
   const DeviceSetup *su = nullptr;
-  int r = device_setup(&su);
+  int r = device_setup(dev, &su);
   if (r) return r;
   if (!n) return GMC_OK;
   cudaStream_t st = (cudaStream_t)stream;

@@ -47,3 +47,30 @@ def test_import_rejects_altered_strings(gmc, keys):
             gmc.SecretKey.from_export(bytes(b))
     with pytest.raises(gmc.GmcError):
         gmc.SecretKey.from_export(bytes(blob[:-8]))
+
+
+def _reseal(blob):
+    """Recomputes the string's checksum (SHAKE256 over the string with the checksum field zeroed), as a crafted
+    string would carry it: the checksum guards against corruption, not against a chosen header."""
+    import hashlib
+    b = bytearray(blob)
+    b[96:128] = bytes(32)
+    b[96:128] = hashlib.shake_256(bytes(b)).digest(32)
+    return bytes(b)
+
+
+def test_import_rejects_layouts_the_kernels_do_not_use(gmc, keys):
+    """Header fields at their offsets: kw_pad 32, pad_bad 36 (public); cw_pad 52 (secret); checksum 96..128."""
+    import struct
+    pk, sk = keys(4)
+    sblob = gmc.SecretKey(4, sk).export()
+    pblob = gmc.PublicKey(4, pk).export()
+    gmc.SecretKey.from_export(_reseal(sblob))  # resealing an unchanged string keeps it valid
+    gmc.PublicKey.from_export(_reseal(pblob))
+    for blob, off, value in ((sblob, 52, struct.unpack_from("<i", sblob, 52)[0] - 8),
+                             (pblob, 32, struct.unpack_from("<i", pblob, 32)[0] - 8),
+                             (pblob, 36, 2)):
+        b = bytearray(blob)
+        struct.pack_into("<i", b, off, value)
+        with pytest.raises(gmc.GmcError):
+            (gmc.SecretKey if blob is sblob else gmc.PublicKey).from_export(_reseal(b))

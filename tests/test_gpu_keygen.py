@@ -96,14 +96,26 @@ def test_keygen_chunks_and_extension_blocks(gmc, monkeypatch):
         check(sid, seeds, pk, sk, oracle_keys(sid, seeds))
 
 
-def test_keygen_matches_single_calls(gmc):
-    """The batched keys equal the engine's own single-key path (host keygen)."""
-    sid = 1
+@pytest.mark.parametrize("sid", [1, 6, 11, 16], ids=["460896", "460896pc", "460896f", "460896pcf"])
+def test_single_key_entry_points(gmc, sid):
+    """gmc_keypair_seed and libmceliece's calling convention gmc_kem_<set>_keypair (randomness from the
+    randombytes source, overridden here) run the GPU key generation with one key: the oracle's keys for plain,
+    pc, f and pcf ids (pc keys are the plain set's, pcf keys the f set's), equal to the batched keys."""
     seeds = seeds_for(sid, 2, tag=b"kg-single")
     pk, sk = gmc.keypair_batch(sid, seeds)
+    ref = oracle_keys(sid, seeds)
+    check(sid, seeds, pk, sk, ref)
     for i in range(2):
         hpk, hsk = gmc.keypair(sid, bytes(seeds[i]))
         assert np.array_equal(pk[i], hpk) and np.array_equal(sk[i], hsk)
+    draws = []
+    gmc.set_randombytes(lambda n: (draws.append(n), bytes(seeds[1]))[1])
+    try:
+        kpk, ksk = gmc.keypair(sid)  # gmc_kem_<set>_keypair: one 32-byte draw
+    finally:
+        gmc.set_randombytes(None)
+    assert draws == [32]
+    assert np.array_equal(kpk, pk[1]) and np.array_equal(ksk, sk[1])
 
 
 def test_keygen_keys_serve(gmc):
