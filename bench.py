@@ -387,6 +387,7 @@ def grouped_mix(gmc, torch, dev, total, steps, warmup):
     same = all(torch.equal(a, b) for a, b in zip(k_plain, k_group))
     info = plan.info()
     plan.close()
+    live = int(sum(counts))
     return {
         "workload": f"{len(MIX_SETS)} keys over the five sets (2x348864, 2x460896, 6688128, 6960119, 2x8192128), "
                     f"Zipf(1.2) request counts summing to {total}, 50/50 enc/dec",
@@ -394,6 +395,8 @@ def grouped_mix(gmc, torch, dev, total, steps, warmup):
         "plain_ms": ms_plain, "plain_ops_s": total / (ms_plain / 1e3),
         "grouped_ms": ms_group, "grouped_ops_s": total / (ms_group / 1e3),
         "speedup": ms_plain / ms_group, "pipelines": info["pipelines"], "outputs_identical": same,
+        "padded_rows": info["padded_rows"], "live_rows": live,
+        "padding_share": (info["padded_rows"] - live) / max(1, info["padded_rows"]),
     }
 
 
@@ -444,12 +447,13 @@ def n_sweep(gmc, torch, dev, set_name, ns, steps, flip=0.10):
     return out
 
 
-def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops):
+def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops, fp8_mac_peak):
     """The encapsulation syndrome c[0:mt] = e[0:mt] ^ T e[mt:n] of n requests with each engine, from the
     engine's per-kernel events: the GF(2) GEMM (mt x k bits times k x n) for the CUDA-core, legacy b1 mma and
     tcgen05 engines, and for the sparse engine the sampler time it adds over the sampler alone.
-    Work = mt*k bit-MACs per request; the tensor-core figures also as a fraction of the measured dense bf16
-    peak (the tcgen05 FP8 kind used here has twice the nominal rate of bf16)."""
+    Work = mt*k bit-MACs per request; the tcgen05 figure as a fraction of the measured rate of its own MMA
+    instruction (gmc_tc_f8_peak: FP8 E4M3, M = 128, N = 256, K = 32, operands resident in shared memory), and
+    for context of the measured dense bf16 cuBLAS peak."""
     import ctypes
     stream = torch.cuda.current_stream(dev)
     st = stream.cuda_stream
@@ -486,15 +490,16 @@ def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops):
         times[name] = ks
     gmc.set_gemm_engine(prev)
     sample_only = times["tc"].get("enc_sample", 0.0)
-    out = {"set": set_name, "n": n, "bit_macs": macs, "engines": {}}
+    out = {"set": set_name, "n": n, "bit_macs": macs, "engines": {},
+           "fp8_mma_peak_tflops": 2.0 * fp8_mac_peak / 1e12}
     for name in ("popc", "b1mma", "tc"):
         ms = times[name]["enc_syndrome_gemm"]
         e = {"ms": ms, "bit_macs_per_s": macs / (ms / 1e3)}
         if name == "tc":
             tf = 2.0 * macs / (ms / 1e3) / 1e12
             e["fp8_equivalent_tflops"] = tf
+            e["frac_of_measured_fp8_mma_peak"] = macs / (ms / 1e3) / fp8_mac_peak
             e["frac_of_measured_bf16_peak"] = tf / tc_peak_tflops
-            e["frac_of_fp8_nominal_2x_bf16"] = tf / (2 * tc_peak_tflops)
         out["engines"][name] = e
     sp = times["sparse"]["enc_sample_syndrome"]
     out["engines"]["sparse"] = {"ms_sampler_with_syndrome": sp, "ms_added_over_sampler": sp - sample_only,
@@ -570,8 +575,9 @@ def keygen_rates(gmc, torch, nkeys, cpu_threads, with_cpu=True, sets=None, calls
 
 
 def serving(gmc, torch, seconds):
-    """16 device-resident key pairs over the five sets, 50/50 enc/dec, Poisson arrivals at 10/50/90% of the
-    measured peak; p50/p99 latency (arrival to completion) against sequential one-request calls."""
+    """16 device-resident key pairs over the five sets, 50/50 enc/dec, Poisson arrivals at 10, 25, 50, 75, 90 and
+    100% of the measured peak; p50/p99/p99.9/max latency (arrival to completion) against sequential one-request
+    calls."""
     pairs = []
     for i in range(16):
         sid = i % 5
@@ -586,10 +592,10 @@ def serving(gmc, torch, seconds):
     # tens of ms in the first level of some runs, never in later ones)
     srv.loadgen(pairs, rate=0.1 * peak["ops_s"], seconds=1.0, seed=7)
     levels = {}
-    for frac in (0.1, 0.5, 0.9):
+    for frac in (0.1, 0.25, 0.5, 0.75, 0.9, 1.0):
         r = srv.loadgen(pairs, rate=frac * peak["ops_s"], seconds=seconds, seed=int(frac * 100))
-        levels[f"{int(frac * 100)}%"] = {k: r[k] for k in ("offered_rate", "ops_s", "p50_ms", "p99_ms", "mean_batch",
-                                                             "completed", "submitted")}
+        levels[f"{int(frac * 100)}%"] = {k: r[k] for k in ("offered_rate", "ops_s", "p50_ms", "p99_ms", "p999_ms",
+                                                             "max_ms", "mean_batch", "completed", "submitted")}
     srv.close()
     # sequential one-request calls (libmceliece calling convention, resident keys, host buffers)
     lat = []
@@ -773,8 +779,17 @@ def main():
         line["config1"] = {"set": "348864", "n": 256, "flip": args.flip,
                            "ops_s": n_sweep(gmc, torch, dev, "348864", [256], 20, args.flip)["256"]}
     if rank == 0 and not args.no_engines:
-        line["syndrome_engines"] = [syndrome_engines(gmc, torch, dev, L, s_, 65536, 5, tc_peak)
+        fp8_peak = gmc.tc_f8_peak()
+        line["syndrome_engines"] = [syndrome_engines(gmc, torch, dev, L, s_, 65536, 5, tc_peak, fp8_peak)
                                     for s_ in dict.fromkeys(("348864", args.set))]
+        # the decapsulation front end on the tcgen05 engine (the step's GEMM) against the same measured peak
+        fe = kernels.get("dec_front_gemm")
+        if fe:
+            fmacs = 2 * z["t"] * z["m"] * z["mt"] * N
+            line["front_end_gemm_tensor"] = {
+                "bit_macs": fmacs, "ms": fe["ms"], "tflops_fp8_equivalent": 2.0 * fmacs / (fe["ms"] / 1e3) / 1e12,
+                "fp8_mma_peak_tflops": 2.0 * fp8_peak / 1e12, "frac_of_measured_fp8_mma_peak":
+                    fmacs / (fe["ms"] / 1e3) / fp8_peak}
     if rank == 0 and not args.no_grouped:
         line["grouped"] = grouped_mix(gmc, torch, dev, N, max(5, args.steps // 2), args.warmup)
     if rank == 0 and not args.no_serving:

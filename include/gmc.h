@@ -163,7 +163,9 @@ void gmc_plan_free(gmc_plan *plan);
  * requests/s for `seconds` over npairs (public, secret) key pairs, a fraction
  * enc_fraction of them encapsulations, and writes out[8]: submitted,
  * completed, achieved ops/s, p50 ms, p99 ms, mean batch, batches, offered
- * rate. */
+ * rate. gmc_server_latency_ms gives any quantile q (0 < q <= 1; 1 = the
+ * slowest request) of the latencies recorded since the last reset (the
+ * histogram's buckets are 2% wide). */
 typedef struct gmc_server gmc_server;
 int gmc_server_create(gmc_server **server, long long max_batch, int slots, double mem_fraction);
 int gmc_server_add_key(gmc_server *server, const gmc_key *key);
@@ -172,6 +174,7 @@ int gmc_server_submit(gmc_server *server, const gmc_key *key, const unsigned cha
 int gmc_server_drain(gmc_server *server, double timeout_s);
 int gmc_server_stats(gmc_server *server, double *out);
 int gmc_server_reset_stats(gmc_server *server);
+int gmc_server_latency_ms(gmc_server *server, double q, double *ms);
 int gmc_server_loadgen(gmc_server *server, const gmc_key *const *pks, const gmc_key *const *sks, int npairs,
                        double rate, double seconds, double enc_fraction, unsigned long long seed, double *out);
 void gmc_server_destroy(gmc_server *server);
@@ -294,6 +297,12 @@ int gmc_tc_status(void);
  * logic ops (lop3) and 32-bit funnel shifts, the instruction kinds of a
  * Keccak-f[1600] permutation on 32-bit halves. For the Keccak ceiling. */
 int gmc_int32_peak(double *lop3_per_s, double *shf_per_s);
+/* Measured rate of the GF(2) GEMM engine's tensor-core instruction
+ * (tcgen05.mma .kind::f8f6f4, E4M3, M = 128, N = 256, K = 32, FP32
+ * accumulator in tensor memory) with its operands resident in shared memory:
+ * multiply-accumulates per second on the current device (the denominator of
+ * the engine's tensor-pipe fraction). */
+int gmc_tc_f8_peak(double *mac_per_s);
 
 /* Stage outputs of a decapsulation batch (device pointers): the 2t packed
  * syndromes (s_words per request), the error vectors (e_words per request)

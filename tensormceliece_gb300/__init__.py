@@ -91,6 +91,8 @@ def lib():
         L.gmc_tune_get.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                    ctypes.POINTER(ctypes.c_int)]
         L.gmc_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.gmc_tc_f8_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        L.gmc_server_latency_ms.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
         L.gmc_tune_set_launch.argtypes = [ctypes.c_int] * 5
         L.gmc_tune_get_launch.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4
         vp = ctypes.c_void_p
@@ -324,7 +326,16 @@ class Server:
         out = (ctypes.c_double * 8)()
         _check(lib().gmc_server_loadgen(self._h, pk, sk, len(pairs), float(rate), float(seconds),
                                         float(enc_fraction), int(seed), out), "gmc_server_loadgen")
-        return dict(zip(self.LOADGEN, list(out)))
+        res = dict(zip(self.LOADGEN, list(out)))
+        res["p999_ms"] = self.latency_ms(0.999)
+        res["max_ms"] = self.latency_ms(1.0)
+        return res
+
+    def latency_ms(self, q):
+        """q-quantile (0 < q <= 1) of the request latencies recorded since the last reset, in ms."""
+        ms = ctypes.c_double()
+        _check(lib().gmc_server_latency_ms(self._h, ctypes.c_double(q), ctypes.byref(ms)), "gmc_server_latency_ms")
+        return ms.value
 
     def close(self):
         if getattr(self, "_h", None):
@@ -436,6 +447,13 @@ def int32_peak():
     a, b = ctypes.c_double(), ctypes.c_double()
     _check(lib().gmc_int32_peak(ctypes.byref(a), ctypes.byref(b)), "gmc_int32_peak")
     return {"lop3_per_s": a.value, "shf_per_s": b.value}
+
+
+def tc_f8_peak():
+    """Measured multiply-accumulates per second of the tcgen05 FP8 MMA the GF(2) GEMM engine issues."""
+    a = ctypes.c_double()
+    _check(lib().gmc_tc_f8_peak(ctypes.byref(a)), "gmc_tc_f8_peak")
+    return a.value
 
 
 def set_gemm_engine(engine):

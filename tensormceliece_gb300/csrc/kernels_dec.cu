@@ -74,7 +74,8 @@ struct BMLayout {
   static constexpr int Q = p::q, T = p::t, M = p::m;
   static constexpr int NS = (T + 1 + 31) / 32;
   static constexpr int exp_off = 0, log_off = 2 * Q;           // u16 tables
-  static constexpr int shared_u32 = (3 * Q) / 2;
+  static constexpr int zero_off = (3 * Q) / 2, zero_len = 16;   // u32: M zero planes (s_j, j < 0)
+  static constexpr int shared_u32 = zero_off + zero_len;
   static constexpr int s_words = 2 * T * M;                    // syndrome planes [j][b]
   static constexpr int b_words = (32 * NS + 1) * M;            // B planes [i][b]
   static constexpr int warp_u32 = s_words + b_words;
@@ -116,7 +117,9 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
   uint16_t *glog = reinterpret_cast<uint16_t *>(bsm) + LY::log_off;
   for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
   for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
+  for (int i = threadIdx.x; i < LY::zero_len; i += blockDim.x) bsm[LY::zero_off + i] = 0u;
   __syncthreads();
+  const uint32_t *ZP = bsm + LY::zero_off;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t *SP = bsm + LY::shared_u32 + warp * LY::warp_u32;
   uint32_t *BP = SP + LY::s_words;
@@ -174,12 +177,11 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
 #pragma unroll
         for (int k = 0; k < NS; k++) {
           if (32 * k <= bd) {
-            const int j = n - lane - 32 * k;  // s_j, j < 0 reads as zero
-            const uint32_t jm = j >= 0 ? 0xFFFFFFFFu : 0u;
-            const uint32_t *sp = SP + (j >= 0 ? j : 0) * M;
+            const int j = n - lane - 32 * k;  // s_j, j < 0 reads the zero planes
+            const uint32_t *sp = j >= 0 ? SP + j * M : ZP;
 #pragma unroll
             for (int b2 = 0; b2 < M; b2++) {
-              const uint32_t sv = sp[b2] & jm;
+              const uint32_t sv = sp[b2];
 #pragma unroll
               for (int b1 = 0; b1 < M; b1++) acc[b1 + b2] ^= C[k][b1] & sv;
             }
@@ -469,13 +471,16 @@ struct RootLayout {
   static constexpr int frlo_off = twist_off + twist_len, frlo_len = SIG;
   static constexpr int shared_u16 = (frlo_off + frlo_len + 1) & ~1;
   // u32 region: bit-sliced alpha, bit-sliced frob_hi
-  static constexpr int abs_off = shared_u16 / 2, abs_len = (SIG - 1) * NH * M;
+  // bit-sliced butterfly constants, one row of NH * M planes per (level, block): rows padded to an odd
+  // stride so that 32 lanes reading 32 different rows hit 32 different banks
+  static constexpr int abs_row = NH * M, abs_stride = abs_row | 1;
+  static constexpr int abs_off = shared_u16 / 2, abs_len = (SIG - 1) * abs_stride;
   static constexpr int fhbs_off = abs_off + abs_len, fhbs_len = NH * M;
   static constexpr int shared_u32 = fhbs_off + fhbs_len;
   static constexpr int ewp = (p::ew + 1) & ~1;
-  // per warp (u32): e words | roots [t] (pos << 16 | element) | count | V[SIG] u16
-  static constexpr int roots_off = ewp, cnt_off = roots_off + p::t, v_off = cnt_off + 2;
-  static constexpr int warp_u32 = v_off + SIG / 2;
+  // per warp (u32): e words | roots [t] (pos << 16 | element) | count
+  static constexpr int roots_off = ewp, cnt_off = roots_off + p::t;
+  static constexpr int warp_u32 = cnt_off + 2;
   static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
 };
 
@@ -533,6 +538,47 @@ __device__ __forceinline__ void bs_mul(uint32_t (&r)[M], const uint32_t *__restr
   }
 }
 
+// One radix-conversion step of the top-down pass on the coefficient slots
+// x = lane + 32 j held in registers: with tau = 2^pb (a bit of x), pass 1
+// adds slot x + tau into every slot x whose bits (pb+1, pb) are (1, 0), then
+// pass 2 adds slot x + tau into every slot whose bits are (0, 1) (whose
+// partner is a pass-1 target). Bits 0..4 of x are lane bits, bits 5.. the
+// register index: a pair inside a lane is an XOR, a pair across lanes one
+// shuffle per register.
+template <int VPL>
+__device__ __forceinline__ void radix_step(uint32_t (&v)[VPL], int pb, int lane) {
+  if (pb >= 5) {  // bits 6, 5 = register bits 1, 0 (VPL == 4)
+    if constexpr (VPL == 4) {
+      v[2] ^= v[3];
+      v[1] ^= v[2];
+    }
+  } else if (pb == 4) {  // bit 5 = register bit 0, bit 4 = lane bit 4
+    const bool hi = (lane & 16) != 0;
+#pragma unroll
+    for (int j = 1; j < VPL; j += 2) {  // (1, 0) <- (1, 1): register bit 0 set, partner lane ^ 16
+      const uint32_t got = __shfl_xor_sync(0xffffffffu, v[j], 16);
+      if (!hi) v[j] ^= got;
+    }
+#pragma unroll
+    for (int j = 0; j < VPL; j += 2) {  // (0, 1) <- (1, 0): register j + 1 of lane ^ 16
+      const uint32_t got = __shfl_xor_sync(0xffffffffu, v[j + 1], 16);
+      if (hi) v[j] ^= got;
+    }
+  } else {  // both lane bits
+    const int b = (lane >> pb) & 3;
+#pragma unroll
+    for (int j = 0; j < VPL; j++) {
+      const uint32_t got = __shfl_xor_sync(0xffffffffu, v[j], 1 << pb);
+      if (b == 2) v[j] ^= got;
+    }
+#pragma unroll
+    for (int j = 0; j < VPL; j++) {
+      const uint32_t got = __shfl_xor_sync(0xffffffffu, v[j], 3 << pb);
+      if (b == 1) v[j] ^= got;
+    }
+  }
+}
+
 template <int SET>
 __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint16_t *__restrict__ Sig,
                                                                    const uint32_t *__restrict__ S2, int lds2,
@@ -559,7 +605,8 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
   for (int i = threadIdx.x; i < (2 << D); i += blockDim.x) tlog[i] = fd.fft_twist_log[i];
   for (int i = threadIdx.x; i < SIG; i += blockDim.x) frlo[i] = fd.frob_lo[i];
-  for (int i = threadIdx.x; i < LY::abs_len; i += blockDim.x) abs_[i] = fd.fft_alpha_bs[i];
+  for (int i = threadIdx.x; i < (SIG - 1) * LY::abs_row; i += blockDim.x)
+    abs_[(i / LY::abs_row) * LY::abs_stride + i % LY::abs_row] = fd.fft_alpha_bs[i];
   for (int i = threadIdx.x; i < LY::fhbs_len; i += blockDim.x) fhbs[i] = fd.frob_hi_bs[i];
   __syncthreads();
 
@@ -568,7 +615,6 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   uint32_t *esm = wbase;
   uint32_t *roots = wbase + LY::roots_off;
   uint32_t *cnt = wbase + LY::cnt_off;
-  uint16_t *V = reinterpret_cast<uint16_t *>(wbase + LY::v_off);
 
   const long long N = seg_rows(segs);
   const int nwb = blockDim.x >> 5;  // warps per block (a launch parameter up to kRootWarps)
@@ -578,44 +624,38 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
     const DecKeyDev &key = keys.k[seg];
     const uint16_t *sig = Sig + op * SIG;
-    const bool long_lfsr = (sig[0] >> 15) != 0;  // BM ended with L > t
-    for (int x = lane; x < SIG; x += 32) V[x] = sig[x] & 0x7FFFu;
     for (int w = lane; w < NW; w += 32) esm[w] = 0;
     if (lane == 0) *cnt = 0;
-    __syncwarp();
-    // top-down: twist by the level's first basis element, then radix-convert
-    // g(x) = g0(x^2+x) + x g1(x^2+x); children interleave (even/odd) in place
+    // top-down, in registers: lane holds the coefficient slots x = lane + 32 j
+    // (j < VPL): twist by the level's first basis element, then radix-convert
+    // g(x) = g0(x^2+x) + x g1(x^2+x) on the 2^l interleaved sub-polynomials
+    uint32_t vv[VPL];
+#pragma unroll
+    for (int j = 0; j < VPL; j++) vv[j] = sig[lane + 32 * j];
+    const bool long_lfsr = (__shfl_sync(0xffffffffu, vv[0], 0) >> 15) != 0;  // BM ended with L > t
+    vv[0] &= 0x7FFFu;
 #pragma unroll 1
     for (int l = 0; l < D; l++) {
-      const int sz = 1 << (D - l);
       if (l) {
         const uint16_t *tw = tlog + ((2 << D) - (2 << (D - l)));
-        for (int x = lane; x < SIG; x += 32) V[x] = gf_mul_log<M>(gexp, glog[V[x]], tw[x >> l]);
-        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < VPL; j++) vv[j] = gf_mul_log<M>(gexp, glog[vv[j]], tw[(lane + 32 * j) >> l]);
       }
 #pragma unroll 1
-      for (int s = sz; s >= 4; s >>= 1) {
-        const int tau = s >> 2;
-        for (int it = lane; it < SIG / 4; it += 32) {
-          const int path = it & ((1 << l) - 1), rest = it >> l;
-          const int u = rest & (tau - 1), bl = rest / tau;
-          const int i2 = bl * s + 2 * tau + u;
-          V[path + (i2 << l)] ^= V[path + ((i2 + tau) << l)];
-        }
-        __syncwarp();
-        for (int it = lane; it < SIG / 4; it += 32) {
-          const int path = it & ((1 << l) - 1), rest = it >> l;
-          const int u = rest & (tau - 1), bl = rest / tau;
-          const int i1 = bl * s + tau + u;
-          V[path + (i1 << l)] ^= V[path + ((i1 + tau) << l)];
-        }
-        __syncwarp();
-      }
+      for (int pb = D - 2; pb >= l; pb--) radix_step<VPL>(vv, pb, lane);
     }
+    __syncwarp();  // esm and cnt cleared before the root stores below
+    // leaves in the bottom-up pass's slot order (chunk_slot at level D - 1)
     uint32_t leaf[VPL];
+    if constexpr (VPL == 4) {  // slot = lane | j1 << 5 | j0 << 6
+      leaf[0] = vv[0];
+      leaf[1] = vv[2];
+      leaf[2] = vv[1];
+      leaf[3] = vv[3];
+    } else {  // slot = lane | j << 5
 #pragma unroll
-    for (int j = 0; j < VPL; j++) leaf[j] = V[chunk_slot<D>(D - 1, lane, j)];
-    __syncwarp();
+      for (int j = 0; j < VPL; j++) leaf[j] = vv[j];
+    }
 
     int weight = 0;
 #pragma unroll 1
@@ -634,7 +674,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
 #pragma unroll
           for (int j = 0; j < 2; j++) {
             const int xh = chunk_slot<D>(l, lane, j) >> (l + 1);
-            const uint32_t *ap = abs_ + (((SIG - (SIG >> l)) + xh) * NH + h) * M;
+            const uint32_t *ap = abs_ + ((SIG - (SIG >> l)) + xh) * LY::abs_stride + h * M;
             uint32_t pr[M];
             bs_mul<M>(pr, ap, v[j + 2]);
 #pragma unroll
@@ -663,7 +703,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
 #pragma unroll
         for (int j = 0; j < VPL; j += 2) {
           const int xh = chunk_slot<D>(l, lane, j) >> (l + 1);
-          const uint32_t *ap = abs_ + (((SIG - (SIG >> l)) + xh) * NH + h) * M;
+          const uint32_t *ap = abs_ + ((SIG - (SIG >> l)) + xh) * LY::abs_stride + h * M;
           uint32_t pr[M];
           bs_mul<M>(pr, ap, v[j + 1]);
 #pragma unroll

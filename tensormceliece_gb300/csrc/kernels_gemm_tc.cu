@@ -1,10 +1,11 @@
 // Tensor-core engines for the batched GF(2) products Out[op] = A * X[op].
 //
 // GEMM_TC: 5th-generation tensor cores (tcgen05). 0/1 operands carried as FP8
-// e4m3 (0x00 / 0x38 = 1.0) through tcgen05.mma .kind::f8f6f4 with FP32
-// accumulators in tensor memory. Sums of products are integer counts <= K
-// (at most 6656 here), exact in FP32, so parity = (int)acc & 1. (.kind::i8 is
-// not available on sm_103a.)
+// e4m3 (key bits 0x00 / 0x38 = 1.0, request bits 0x00 / 0x01 = 2^-9) through
+// tcgen05.mma .kind::f8f6f4 with FP32 accumulators in tensor memory. Sums of
+// products are integer counts <= K (at most 6656 here) times 2^-9, exact in
+// FP32, so parity = (int)(acc * 2^9) & 1. (.kind::i8 is not available on
+// sm_103a.)
 //   A (key matrix, fixed per key) is pre-expanded once into FP8 tiles laid
 //   out exactly as the shared-memory image of one pipeline stage, so a stage
 //   is one cp.async.bulk (TMA engine) completing on an mbarrier.
@@ -127,10 +128,16 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
       : "r"(taddr))
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// 4 bits -> 4 FP8 bytes (bit i -> byte i = 0x38 or 0)
+// 4 bits -> 4 FP8 bytes (bit i -> byte i = 0x38 = 1.0 or 0): the key matrix
 __device__ __forceinline__ uint32_t expand4(uint32_t v) {
   return ((v * 0x00204081u) & 0x01010101u) * 0x38u;
 }
+// 4 bits -> 4 FP8 bytes (bit i -> byte i = 0x01 or 0): the request bits, as
+// the E4M3 subnormal 2^-9, one multiply fewer per nibble than 1.0. Products
+// with the key's 1.0 are 2^-9, a K-sum is count * 2^-9 with count <= K
+// (exact in FP32), and the epilogue scales it back by 2^9 before the parity.
+__device__ __forceinline__ uint32_t expand4_x(uint32_t v) { return (v * 0x00204081u) & 0x01010101u; }
+constexpr float kTcXScale = 512.0f;
 
 // ---------------------------------------------------------------- tcgen05 engine
 // Persistent: one CTA per SM walks the (m-tile, n-tile) list. The stage ring
@@ -234,10 +241,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
           for (int kc = 0; kc < 8; kc++) {
             const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
             uint4 v;
-            v.x = expand4(bits & 0xFu);
-            v.y = expand4((bits >> 4) & 0xFu);
-            v.z = expand4((bits >> 8) & 0xFu);
-            v.w = expand4((bits >> 12) & 0xFu);
+            v.x = expand4_x(bits & 0xFu);
+            v.y = expand4_x((bits >> 4) & 0xFu);
+            v.z = expand4_x((bits >> 8) & 0xFu);
+            v.w = expand4_x((bits >> 12) & 0xFu);
             *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
           }
         }
@@ -314,7 +321,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
         uint32_t mine = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) {
-          const uint32_t par = (uint32_t)__float2int_rz(__uint_as_float(r[j])) & 1u;
+          const uint32_t par = (uint32_t)__float2int_rz(__uint_as_float(r[j]) * kTcXScale) & 1u;
           const uint32_t word = __ballot_sync(0xffffffffu, par);
           if (lane == j) mine = word;
         }
@@ -394,6 +401,83 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
   kern<<<grid, TC_THREADS, smem, st>>>(keys, segs, kw_pad / (kTcKB / 32), mtiles, ntiles, X, ldx, Out, ldo,
                                        out_words, err);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- tcgen05 FP8 peak
+// The MMA rate of this GPU for the engine's instruction: tcgen05.mma
+// .kind::f8f6f4, E4M3 operands, M = 128, N = 256, K = 32, FP32 accumulator in
+// tensor memory, operands resident in shared memory (no copies, no
+// expansion). One CTA per SM; lane 0 of warp 1 issues `iters` MMAs into one
+// accumulator, cycling over the 4 K-slices of a 128-bit stage, then one
+// commit; every thread waits (bounded) for it. The denominator of the GEMM's
+// tensor-pipe fraction.
+constexpr int TCP_THREADS = 128;
+
+__global__ void __launch_bounds__(TCP_THREADS, 1) tc_f8_peak_kernel(int iters, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t psm[];
+  uint8_t *As = psm;
+  uint8_t *Xs = psm + TC_A_BYTES;
+  uint64_t *done = reinterpret_cast<uint64_t *>(Xs + TC_X_BYTES);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int i = tid; i < (TC_A_BYTES + TC_X_BYTES) / 16; i += TCP_THREADS)
+    reinterpret_cast<uint4 *>(psm)[i] = make_uint4(0x38383838u, 0, 0x38383838u, 0);
+  if (tid == 0) {
+    mbar_init(done, 1);
+    fence_mbar_init();
+  }
+  fence_proxy_async();  // operand writes visible to the tensor core
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, kTcN);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = idesc_f8f6f4_e4m3(kTcM, kTcN);
+    const uint32_t a0 = smem_u32(As), x0 = smem_u32(Xs);
+#pragma unroll 1
+    for (int i = 0; i < iters; i++) {
+      const int kk = i & (kTcKB / 32 - 1);
+      mma_f8(tmem, smem_desc(a0 + kk * 256, 128, 1024), smem_desc(x0 + kk * 256, 128, 1024), idesc, i ? 1u : 0u);
+    }
+    mma_commit(done);
+  }
+  const bool ok = mbar_wait(done, 0);
+  if (!__syncthreads_and(ok) && tid == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTcN);
+}
+
+cudaError_t time_tc_f8_peak(double *mac_per_s, int *err_dev, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int smem = TC_A_BYTES + TC_X_BYTES + 64;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(tc_f8_peak_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int iters = 1 << 16;  // ~4.7 ms per launch at the nominal dense rate
+  float best = 0;
+  for (int rep = 0; rep < 5 && e == cudaSuccess; rep++) {
+    cudaEventRecord(e0, st);
+    tc_f8_peak_kernel<<<sms, TCP_THREADS, smem, st>>>(iters, err_dev);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (rep >= 1 && (best == 0 || t < best)) best = t;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return e;
+  *mac_per_s = (double)sms * iters * kTcM * kTcN * 32.0 / (best * 1e-3);
+  return cudaSuccess;
 }
 
 // ---------------------------------------------------------------- legacy b1 MMA engine

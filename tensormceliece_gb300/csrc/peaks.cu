@@ -17,6 +17,7 @@
 
 #include "../../include/gmc.h"
 #include "engine_internal.h"
+#include "kernels.h"
 
 using namespace gmc;
 
@@ -75,6 +76,35 @@ cudaError_t time_kernel(int blocks, int iters, uint32_t *out, cudaStream_t st, d
 }
 
 }  // namespace
+
+// Tensor-pipe peak for the GF(2) GEMM engine: the measured rate of its own
+// tcgen05.mma (kind::f8f6f4, E4M3, M = 128, N = 256, K = 32) with the operands
+// resident in shared memory, in multiply-accumulates per second.
+extern "C" int gmc_tc_f8_peak(double *mac_per_s) {
+  if (!mac_per_s) {
+    set_last_error("gmc_tc_f8_peak: null output");
+    return GMC_EINVAL;
+  }
+  int *err = nullptr;
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaMalloc(&err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = time_tc_f8_peak(mac_per_s, err, st);
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (st) cudaStreamDestroy(st);
+  if (err) cudaFree(err);
+  if (e != cudaSuccess) {
+    set_last_error((std::string("gmc_tc_f8_peak: ") + cudaGetErrorString(e)).c_str());
+    return GMC_ECUDA;
+  }
+  if (h) {
+    set_last_error("gmc_tc_f8_peak: a bounded wait expired");
+    return GMC_ECUDA;
+  }
+  return GMC_OK;
+}
 
 extern "C" int gmc_int32_peak(double *lop3_per_s, double *shf_per_s) {
   if (!lop3_per_s || !shf_per_s) {

@@ -751,6 +751,26 @@ extern "C" int gmc_server_stats(gmc_server *s, double *out /* [8] */) {
   return GMC_OK;
 }
 
+extern "C" int gmc_server_latency_ms(gmc_server *s, double q, double *ms) {
+  if (!s || !ms || !(q > 0.0 && q <= 1.0)) return srv_fail(GMC_EINVAL, "gmc_server_latency_ms: bad argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  long long tot = 0;
+  for (long long c : s->hist) tot += c;
+  *ms = 0.0;
+  if (!tot) return GMC_OK;
+  const long long target = (long long)ceil(q * (double)tot);
+  long long acc = 0;
+  for (int b = 0; b < kBuckets; b++) {
+    acc += s->hist[b];
+    if (acc >= target) {
+      *ms = bucket_ms(b);
+      return GMC_OK;
+    }
+  }
+  *ms = bucket_ms(kBuckets - 1);
+  return GMC_OK;
+}
+
 extern "C" int gmc_server_reset_stats(gmc_server *s) {
   if (!s) return srv_fail(GMC_EINVAL, "gmc_server_reset_stats: bad argument");
   std::lock_guard<std::mutex> lk(s->mu);
