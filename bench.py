@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-sweep", action="store_true", help="skip the N = 256..65536 throughput sweep")
     ap.add_argument("--no-engines", action="store_true", help="skip the syndrome-engine comparison")
     ap.add_argument("--no-keygen", action="store_true", help="skip the batched key-generation measurement")
+    ap.add_argument("--no-ct", action="store_true", help="skip the constant-time decapsulation measurement")
     ap.add_argument("--keygen-keys", type=int, default=608, help="keys per batched key-generation call")
     ap.add_argument("--keygen-only", action="store_true",
                     help="measure only batched key generation (--keygen-sets, default all five) and print its JSON")
@@ -319,6 +320,64 @@ def run_reference(args, rank):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def constant_time_cost(gmc, torch, dev, L, set_name, n, steps, flip=0.10):
+    """Decapsulation of n ciphertexts (10% one-bit-flipped) with the table forms and with the constant-time
+    kernels (gmc_set_dec_constant_time): device ms per batch (CUDA events, L2 flushed), the per-kernel split of
+    both, and whether every session key and return code agrees."""
+    import ctypes
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+    sid = gmc.set_id(set_name)
+    z = gmc.set_sizes(sid)
+    pk, sk = gmc.keypair(sid, bytes([0x6B]) * 32)
+    P, S = gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(71)
+    seeds = torch.randint(0, 256, (n, 32), dtype=torch.uint8, device=dev, generator=gen)
+    cts = torch.empty((n, z["ct_bytes"]), dtype=torch.uint8, device=dev)
+    k = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+    P.enc_batch_dev(cts.data_ptr(), k.data_ptr(), seeds.data_ptr(), n, 0, st)
+    rng = np.random.default_rng(17)
+    nflip = int(flip * n)
+    idx = torch.from_numpy(rng.choice(n, nflip, replace=False)).to(dev)
+    bits = torch.from_numpy(rng.integers(0, z["mt"], nflip)).to(dev)
+    cts[idx, bits // 8] ^= (1 << (bits % 8)).to(torch.uint8)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device=dev)
+    out = {"set": set_name, "n": n}
+    keys_rc = {}
+    for name, on in (("table", False), ("constant_time", True)):
+        gmc.set_dec_constant_time(on)
+        kd = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+        rc = torch.empty(n, dtype=torch.int32, device=dev)
+        for _ in range(3):
+            S.dec_batch_dev(kd.data_ptr(), cts.data_ptr(), n, rc.data_ptr(), st)
+        torch.cuda.synchronize()
+        L.gmc_prof_enable(1)
+        ms = []
+        for i in range(steps):
+            flush.fill_(i)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            S.dec_batch_dev(kd.data_ptr(), cts.data_ptr(), n, rc.data_ptr(), st)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        buf = ctypes.create_string_buffer(4096)
+        L.gmc_prof_report(buf, 4096)
+        L.gmc_prof_enable(0)
+        ks = {}
+        for ln in buf.value.decode().strip().splitlines():
+            nm, cnt, t = ln.split()
+            ks[nm] = float(t) / steps
+        out[name] = {"ms_per_batch": sum(ms) / len(ms), "dec_ops_s": n / (sum(ms) / len(ms) / 1e3), "kernels_ms": ks}
+        keys_rc[name] = (kd.clone(), rc.clone())
+    gmc.set_dec_constant_time(False)
+    out["outputs_identical"] = bool(torch.equal(keys_rc["table"][0], keys_rc["constant_time"][0]) and
+                                    torch.equal(keys_rc["table"][1], keys_rc["constant_time"][1]))
+    out["slowdown"] = out["constant_time"]["ms_per_batch"] / out["table"]["ms_per_batch"]
+    return out
 
 
 MIX_SETS = [0, 0, 1, 1, 2, 3, 4, 4]  # 2x348864, 2x460896, 6688128, 6960119, 2x8192128
@@ -790,6 +849,8 @@ def main():
                 "bit_macs": fmacs, "ms": fe["ms"], "tflops_fp8_equivalent": 2.0 * fmacs / (fe["ms"] / 1e3) / 1e12,
                 "fp8_mma_peak_tflops": 2.0 * fp8_peak / 1e12, "frac_of_measured_fp8_mma_peak":
                     fmacs / (fe["ms"] / 1e3) / fp8_peak}
+    if rank == 0 and not args.no_ct:
+        line["constant_time"] = constant_time_cost(gmc, torch, dev, L, args.set, N, 5, args.flip)
     if rank == 0 and not args.no_grouped:
         line["grouped"] = grouped_mix(gmc, torch, dev, N, max(5, args.steps // 2), args.warmup)
     if rank == 0 and not args.no_serving:

@@ -269,6 +269,18 @@ void gmc_set_randombytes(gmc_randombytes_fn fn, void *ctx);
 int gmc_set_gemm_engine(int engine);
 int gmc_get_gemm_engine(void);
 
+/* Constant-time decapsulation (no counterpart in the reference, whose device
+ * code disclaims side channels; libmceliece's own CPU code is constant-time).
+ * on = 1: Berlekamp-Massey runs inversion-free with no tables and slot
+ * counts fixed by the iteration alone (the same locators, normalized by one
+ * bit-sliced inversion), and the root finder's top-down pass multiplies by
+ * table-free columns of its public constants; 0 restores the table forms.
+ * Session keys are identical either way. Process-wide, read at each batch
+ * launch; GMC_DEC_CT=1 in the environment sets it at load. The
+ * no-allocation entry point keeps the table forms. */
+int gmc_set_dec_constant_time(int on);
+int gmc_get_dec_constant_time(void);
+
 /* ---- autotuner --------------------------------------------------------------
  * Per parameter set: the engine of the encapsulation syndrome (sparse or a
  * GEMM engine) and the GEMM engine of the decapsulation front end, and the

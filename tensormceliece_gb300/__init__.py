@@ -449,6 +449,15 @@ def int32_peak():
     return {"lop3_per_s": a.value, "shf_per_s": b.value}
 
 
+def set_dec_constant_time(on):
+    """Constant-time decapsulation kernels (True) or the table forms (False); identical session keys."""
+    _check(lib().gmc_set_dec_constant_time(1 if on else 0), "gmc_set_dec_constant_time")
+
+
+def get_dec_constant_time():
+    return bool(lib().gmc_get_dec_constant_time())
+
+
 def tc_f8_peak():
     """Measured multiply-accumulates per second of the tcgen05 FP8 MMA the GF(2) GEMM engine issues."""
     a = ctypes.c_double()

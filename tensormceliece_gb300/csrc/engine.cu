@@ -13,9 +13,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 #include <sys/random.h>
 
+#include <atomic>
 #include <list>
 #include <map>
 #include <memory>
@@ -56,6 +58,12 @@ void gmc::set_last_error(const char *msg) { g_last_error = msg; }
 // global GEMM-engine override (gmc_set_gemm_engine).
 static SetTune g_tune[GMC_NSETS];
 static int g_engine_override = -1;
+// constant-time decapsulation kernels (gmc_set_dec_constant_time; GMC_DEC_CT=1)
+static std::atomic<int> g_dec_ct{[] {
+  const char *v = getenv("GMC_DEC_CT");
+  return (v && v[0] == '1') ? 1 : 0;
+}()};
+bool gmc::dec_constant_time() { return g_dec_ct.load(std::memory_order_relaxed) != 0; }
 static std::mutex g_tune_mu;
 // op 0: encapsulation syndrome, 1: decapsulation front end (no sparse form:
 // c is dense), where a GEMM_SPARSE override leaves the per-set engine.
@@ -160,7 +168,8 @@ static int get_field(int set, FieldDev *out) {
     return at;
   };
   const size_t o_exp = put(F.exp), o_log = put(F.log), o_twist = put(ft.twist_log), o_frlo = put(ft.frob_lo),
-               o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs), o_zech = put(ft.zech);
+               o_abs = put(ft.alpha_bs), o_fhbs = put(ft.frob_hi_bs), o_zech = put(ft.zech),
+               o_tcols = put(ft.twist_cols);
   FieldEntry e;
   GMC_CUDA(cudaMalloc(&e.buf, all.size() * 2));
   GMC_CUDA(cudaMemcpy(e.buf, all.data(), all.size() * 2, cudaMemcpyHostToDevice));
@@ -171,6 +180,7 @@ static int get_field(int set, FieldDev *out) {
   e.fd.fft_alpha_bs = reinterpret_cast<const uint32_t *>(e.buf + o_abs);
   e.fd.frob_hi_bs = reinterpret_cast<const uint32_t *>(e.buf + o_fhbs);
   e.fd.zech = e.buf + o_zech;
+  e.fd.fft_twist_cols = e.buf + o_tcols;
   g_fields[key] = e;
   *out = e.fd;
   return GMC_OK;
@@ -360,6 +370,13 @@ extern "C" int gmc_set_gemm_engine(int engine) {
 }
 extern "C" int gmc_get_gemm_engine(void) { return g_engine_override; }
 
+extern "C" int gmc_set_dec_constant_time(int on) {
+  if (on != 0 && on != 1) return fail(GMC_EINVAL, "gmc_set_dec_constant_time: 0 or 1");
+  g_dec_ct.store(on, std::memory_order_relaxed);
+  return GMC_OK;
+}
+extern "C" int gmc_get_dec_constant_time(void) { return g_dec_ct.load(std::memory_order_relaxed); }
+
 // ---------------------------------------------------------------- workspace
 // The default memory pool of the current device keeps freed blocks for reuse
 // (release threshold raised once per device, for this process): without it
@@ -530,10 +547,11 @@ static cudaError_t dec_front_decode_seg(const Segs &segs, const gmc_key *ref, co
   if (e != cudaSuccess) return e;
   prof_mark("dec_front_gemm", st);
   const SetTune tune = tune_get(SET);
-  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st, tune.bm_warps);
+  const bool ct = dec_constant_time();
+  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st, tune.bm_warps, ct);
   if (e != cudaSuccess) return e;
   prof_mark("dec_bm", st);
-  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st, tune.root_warps);
+  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st, tune.root_warps, ct);
   prof_mark("dec_fft_roots_reenc", st);
   return e;
 }

@@ -32,6 +32,8 @@ struct gmc_key {
 namespace gmc {
 // sets the calling thread's message returned by gmc_last_error()
 void set_last_error(const char *msg);
+// the constant-time decapsulation switch (gmc_set_dec_constant_time)
+bool dec_constant_time();
 
 // per-parameter-set launch configuration chosen by the autotuner
 struct SetTune {

@@ -148,6 +148,10 @@ FftTables build_fft_tables(int m, int d) {
     for (int i = 1; i < dim; i++) nb[i - 1] = (uint16_t)(F.sq(delta[i]) ^ delta[i]);
     beta = nb;
   }
+  t.twist_cols.assign((size_t)(2 << d) * m, 0);
+  for (int e = 0; e < (2 << d); e++)
+    if (t.twist_log[e] < F.zero_log())
+      for (int i = 0; i < m; i++) t.twist_cols[(size_t)e * m + i] = F.mul(F.exp[t.twist_log[e]], (uint16_t)(1u << i));
   auto frob = [&](uint16_t a) {
     for (int r = 0; r < d; r++) a = F.sq(a);
     return a;

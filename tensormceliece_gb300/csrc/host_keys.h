@@ -28,6 +28,7 @@ const HostField &host_field(int m);
 // element's powers (twist) and of the butterfly constants alpha_{l,c'}.
 struct FftTables {
   std::vector<uint16_t> twist_log;  // levels concatenated, 2^(d-l) each (2^(d+1) total)
+  std::vector<uint16_t> twist_cols; // [2^(d+1)][m]: c x^i for the constant c of each twist_log entry
   std::vector<uint16_t> alpha_log;  // levels concatenated, 2^(m-l-1) each (padded to 2^m)
   std::vector<uint16_t> frob_lo;    // x^(2^d), x < 2^d
   std::vector<uint16_t> frob_hi;    // (c 2^d)^(2^d), c < 2^(m-d)

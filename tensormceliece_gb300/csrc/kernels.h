@@ -146,6 +146,9 @@ struct FieldDev {
   const uint32_t *fft_alpha_bs;   // [(2^d - 2^(d-l) + xh) * H + h][m]: alpha_{l, (c << (d-1-l)) + xh}
   const uint32_t *frob_hi_bs;     // [h][m]: (c 2^d)^(2^d)
   const uint16_t *zech;           // [q]: log(1 + g^k), zech[0] = 3q (zero)
+  // [2^(d+1)][m]: for the twist constant c of each fft_twist_log entry, c x^i (i < m), so a product
+  // with c needs no table indexed by the other factor (constant-time form); null where not built
+  const uint16_t *fft_twist_cols = nullptr;
 };
 
 // Per-key decapsulation tables of the segments of a launch.
@@ -162,14 +165,18 @@ cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int 
 // error locator's coefficients by degree (the leading x^t term is implicit
 // when t = 2^fft_d).
 // warps: warps per block of the bit-sliced form (1..kBMWarps; 0 = kBMWarps).
+// ct: the constant-time form (inversion-free, no tables, slot bounds from the
+// iteration alone; the same locators).
 template <int SET>
 cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
-                          cudaStream_t st, int warps = 0);
+                          cudaStream_t st, int warps = 0, bool ct = false);
 // Root finding + weight + re-encryption check: Sig -> E (error vectors), ok.
 // warps: warps per block (1..kRootWarps; 0 = kRootWarps), one request per warp.
+// ct: the twist multiplies by table-free columns (needs fd.fft_twist_cols).
 template <int SET>
 cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
-                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps = 0);
+                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps = 0,
+                            bool ct = false);
 // With pc the decoded e must also give SHAKE256(2 || e, 32) = C1 (else implicit
 // rejection), and the session-key preimage covers C0 || C1.
 template <int SET>

@@ -289,6 +289,269 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
   }
 }
 
+// ---------------------------------------------------------------- BM, constant-time form
+// Bit-sliced products with both operands in registers (the multiplier a is
+// warp-uniform in the callers below): Horner over the planes of a, as bs_mul.
+template <int M>
+__device__ __forceinline__ void bs_mul_reg(uint32_t (&r)[M], const uint32_t (&a)[M], const uint32_t (&b)[M]) {
+#pragma unroll
+  for (int i = 0; i < M; i++) r[i] = b[i] & a[M - 1];
+#pragma unroll
+  for (int j = M - 2; j >= 0; j--) {
+    const uint32_t top = r[M - 1];
+#pragma unroll
+    for (int i = M - 1; i > 0; i--) r[i] = r[i - 1];
+    r[0] = top;
+    if (M == 13) {
+      r[1] ^= top;
+      r[3] ^= top;
+      r[4] ^= top;
+    } else {
+      r[3] ^= top;
+    }
+#pragma unroll
+    for (int i = 0; i < M; i++) r[i] ^= b[i] & a[j];
+  }
+}
+
+// r = a^2: the planes spread to the even positions, then the reduction
+template <int M>
+__device__ __forceinline__ void bs_sqr(uint32_t (&r)[M], const uint32_t (&a)[M]) {
+  uint32_t acc[2 * M - 1];
+#pragma unroll
+  for (int k = 0; k < 2 * M - 1; k++) acc[k] = (k & 1) ? 0u : a[k >> 1];
+  bs_reduce<M>(r, acc);
+}
+
+template <int M>
+__device__ __forceinline__ void bs_sqr_n(uint32_t (&r)[M], const uint32_t (&a)[M], int n) {
+#pragma unroll
+  for (int i = 0; i < M; i++) r[i] = a[i];
+#pragma unroll 1
+  for (int k = 0; k < n; k++) {
+    uint32_t t[M];
+    bs_sqr<M>(t, r);
+#pragma unroll
+    for (int i = 0; i < M; i++) r[i] = t[i];
+  }
+}
+
+// r = a^(2^M - 2) = a^-1 (0 for a = 0), by the chain of a^(2^k - 1):
+// M = 13: k = 1, 2, 3, 6, 12, then one squaring; M = 12: k = 1, 2, 3, 5, 6, 11.
+template <int M>
+__device__ __forceinline__ void bs_inv(uint32_t (&r)[M], const uint32_t (&a)[M]) {
+  uint32_t t[M], a2[M], a3[M];
+  bs_sqr<M>(t, a);
+  bs_mul_reg<M>(a2, t, a);  // a^(2^2 - 1)
+  bs_sqr<M>(t, a2);
+  bs_mul_reg<M>(a3, t, a);  // a^(2^3 - 1)
+  if (M == 13) {
+    uint32_t a6[M], a12[M];
+    bs_sqr_n<M>(t, a3, 3);
+    bs_mul_reg<M>(a6, t, a3);  // a^(2^6 - 1)
+    bs_sqr_n<M>(t, a6, 6);
+    bs_mul_reg<M>(a12, t, a6);  // a^(2^12 - 1)
+    bs_sqr<M>(r, a12);
+  } else {
+    uint32_t a5[M], a6[M], a11[M];
+    bs_sqr_n<M>(t, a3, 2);
+    bs_mul_reg<M>(a5, t, a2);  // a^(2^5 - 1)
+    bs_sqr_n<M>(t, a3, 3);
+    bs_mul_reg<M>(a6, t, a3);  // a^(2^6 - 1)
+    bs_sqr_n<M>(t, a6, 5);
+    bs_mul_reg<M>(a11, t, a5);  // a^(2^11 - 1)
+    bs_sqr<M>(r, a11);
+  }
+}
+
+// The bit-sliced layout of dec_bm_kernel with nothing that depends on the
+// syndromes in an address, a branch or a trip count:
+//  - inversion-free update, no division d / b and no log tables: with b the
+//    discrepancy of the last length change, C <- b C + d B (B carrying its x
+//    shift as in dec_bm_kernel). By induction C = lambda C_lib for a nonzero
+//    scalar lambda per request (a product of b's), with the same length L and
+//    the same update decisions as the library's rule (d != 0 exactly when the
+//    library's d is), also under the truncation to t + 1 coefficients;
+//  - slot bounds from n alone: deg C <= L <= n and deg B <= n + 1;
+//  - at the end every coefficient is multiplied by lambda^-1 (C_0 = lambda;
+//    one bit-sliced inversion per group), which gives the library's locator
+//    (C_0 = 1) exactly.
+// The update decisions stay per-request masks (ballots), L is selected, never
+// branched on.
+template <int SET>
+struct BMCtLayout {
+  using LY = BMLayout<SET>;
+  static constexpr int zero_len = LY::zero_len;  // u32: zero planes first, then the warps' areas
+  static constexpr int warp_u32 = LY::warp_u32;
+  static constexpr int bytes(int warps) { return zero_len * 4 + warps * warp_u32 * 4; }
+};
+
+template <int SET>
+__global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_ct_kernel(const uint32_t *__restrict__ S2, int lds2,
+                                                                     const Segs segs, uint16_t *__restrict__ Sig) {
+  using p = P<SET>;
+  using LY = BMLayout<SET>;
+  constexpr int M = p::m, T = p::t, D = p::fft_d;
+  constexpr int NS = LY::NS;
+  constexpr int SIG = 1 << D;
+  static_assert(M == 12 || M == 13, "field polynomial");
+  extern __shared__ __align__(16) uint32_t csm[];
+  for (int i = threadIdx.x; i < LY::zero_len; i += blockDim.x) csm[i] = 0u;
+  __syncthreads();
+  const uint32_t *ZP = csm;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *SP = csm + LY::zero_len + warp * LY::warp_u32;
+  uint32_t *BP = SP + LY::s_words;
+  const long long N = seg_rows(segs);
+  const long long ngroups = (N + 31) / 32;
+  const int nwb = blockDim.x >> 5;
+  const long long g_lo = ngroups * blockIdx.x / gridDim.x, g_hi = ngroups * (blockIdx.x + 1) / gridDim.x;
+  for (long long g = g_lo + warp; g < g_hi; g += nwb) {
+    const long long op = g * 32 + lane;
+    int seg;
+    const bool live = op < N && seg_live(segs, op, &seg);
+    const uint32_t *srow = S2 + op * lds2;
+#pragma unroll 1
+    for (int j = 0; j < 2 * T; j++) {
+      uint32_t v = 0;
+      if (live) {
+        const int bb = j * M, w = bb >> 5, sh = bb & 31;
+        v = srow[w] >> sh;
+        if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
+      }
+      uint32_t mine = 0;
+#pragma unroll
+      for (int b = 0; b < M; b++) {
+        const uint32_t pl = __ballot_sync(0xffffffffu, (v >> b) & 1u);
+        mine = (lane == b) ? pl : mine;
+      }
+      if (lane < M) SP[j * M + lane] = mine;
+    }
+    uint32_t C[NS][M];
+#pragma unroll
+    for (int k = 0; k < NS; k++)
+#pragma unroll
+      for (int b = 0; b < M; b++) C[k][b] = (k == 0 && lane == 0 && b == 0) ? 0xFFFFFFFFu : 0u;
+    for (int w = lane; w < LY::b_words; w += 32) BP[w] = (w == M) ? 0xFFFFFFFFu : 0u;
+    uint32_t bq[M];  // b of every request (warp-uniform planes); b = 1
+#pragma unroll
+    for (int b = 0; b < M; b++) bq[b] = b == 0 ? 0xFFFFFFFFu : 0u;
+    __syncwarp();
+    int L = 0;  // this lane's request
+#pragma unroll 1
+    for (int n = 0; n < 2 * T; n++) {
+      const int bd = n < T ? n : T;          // deg C <= L <= n
+      const int bu = n + 1 < T ? n + 1 : T;  // deg B <= n + 1
+      uint32_t d[M];
+      {
+        uint32_t acc[2 * M - 1];
+#pragma unroll
+        for (int k = 0; k < 2 * M - 1; k++) acc[k] = 0;
+#pragma unroll
+        for (int k = 0; k < NS; k++) {
+          if (32 * k <= bd) {
+            const int j = n - lane - 32 * k;  // s_j, j < 0 reads the zero planes
+            const uint32_t *sp = j >= 0 ? SP + j * M : ZP;
+#pragma unroll
+            for (int b2 = 0; b2 < M; b2++) {
+              const uint32_t sv = sp[b2];
+#pragma unroll
+              for (int b1 = 0; b1 < M; b1++) acc[b1 + b2] ^= C[k][b1] & sv;
+            }
+          }
+        }
+        bs_reduce<M>(d, acc);
+#pragma unroll
+        for (int b = 0; b < M; b++) d[b] = __reduce_xor_sync(0xffffffffu, d[b]);
+      }
+      uint32_t nz = 0;
+#pragma unroll
+      for (int b = 0; b < M; b++) nz |= d[b];
+      const uint32_t U = nz & __ballot_sync(0xffffffffu, 2 * L <= n);
+      L = ((U >> lane) & 1u) ? n + 1 - L : L;
+      // C_i <- b C_i + d B_i; B_{i+1} <- (U ? C_i(old) : B_i); slots in
+      // descending order (slot k's write of B_{32(k+1)} follows slot k+1's read)
+#pragma unroll
+      for (int k = NS - 1; k >= 0; k--) {
+        if (32 * k <= bu) {
+          const int i = lane + 32 * k;
+          const uint32_t *bp = BP + i * M;
+          uint32_t bi[M];
+#pragma unroll
+          for (int b = 0; b < M; b++) bi[b] = bp[b];
+          __syncwarp();
+          const bool in = (k < NS - 1) || (i <= T);
+          uint32_t r[M];
+#pragma unroll
+          for (int b = 0; b < M; b++) r[b] = (C[k][b] & bq[M - 1]) ^ (bi[b] & d[M - 1]);
+#pragma unroll
+          for (int jj = M - 2; jj >= 0; jj--) {
+            const uint32_t top = r[M - 1];
+#pragma unroll
+            for (int b = M - 1; b > 0; b--) r[b] = r[b - 1];
+            r[0] = top;
+            if (M == 13) {
+              r[1] ^= top;
+              r[3] ^= top;
+              r[4] ^= top;
+            } else {
+              r[3] ^= top;
+            }
+#pragma unroll
+            for (int b = 0; b < M; b++) r[b] ^= (C[k][b] & bq[jj]) ^ (bi[b] & d[jj]);
+          }
+          uint32_t *bn = BP + (i + 1) * M;
+#pragma unroll
+          for (int b = 0; b < M; b++) {
+            const uint32_t cold = C[k][b];
+            if (in) C[k][b] = r[b];
+            if (i + 1 <= T) bn[b] = (U & cold) | (~U & bi[b]);
+          }
+          __syncwarp();
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < M; b++) bq[b] = (U & d[b]) | (~U & bq[b]);
+      if (lane < M) BP[lane] = 0;
+      __syncwarp();
+    }
+    // C <- C / C_0 (C_0 = lambda != 0)
+    {
+      uint32_t c0[M], inv[M];
+#pragma unroll
+      for (int b = 0; b < M; b++) c0[b] = __shfl_sync(0xffffffffu, C[0][b], 0);
+      bs_inv<M>(inv, c0);
+#pragma unroll
+      for (int k = 0; k < NS; k++) {
+        uint32_t r[M];
+        bs_mul_reg<M>(r, inv, C[k]);
+#pragma unroll
+        for (int b = 0; b < M; b++) C[k][b] = r[b];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NS; k++)
+#pragma unroll
+      for (int b = 0; b < M; b++) SP[(lane + 32 * k) * M + b] = C[k][b];
+    __syncwarp();
+    if (live) {
+      uint16_t *sig = Sig + op * SIG;
+#pragma unroll 1
+      for (int deg = 0; deg < SIG; deg++) {
+        const int i = T - deg;
+        uint32_t v = 0;
+        if (i >= 0) {
+#pragma unroll
+          for (int b = 0; b < M; b++) v |= ((SP[i * M + b] >> lane) & 1u) << b;
+        }
+        v |= (deg == 0 && L > T) ? 0x8000u : 0u;
+        sig[deg] = (uint16_t)v;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------- BM, latency form
 // Used for small batches (fewer requests than the bit-sliced form needs to
 // fill the GPU): per-request latency is one warp walking 2t iterations of
@@ -461,13 +724,15 @@ __global__ void __launch_bounds__(kBMLatWarps * 32, 2) dec_bm_lat_kernel(const u
 // Frobenius tables, since (hi + lo)^(2^d) = hi^(2^d) + lo^(2^d)) is mapped to
 // its code position through the key's inverse support table; only roots touch
 // that table.
-template <int SET>
+template <int SET, bool CT>
 struct RootLayout {
   using p = P<SET>;
   static constexpr int Q = p::q, D = p::fft_d, SIG = 1 << D, NC = Q >> D, NH = NC / 32, M = p::m;
-  static constexpr int exp_off = 0, exp_len = 2 * Q;
-  static constexpr int log_off = exp_off + exp_len, log_len = Q;
-  static constexpr int twist_off = log_off + log_len, twist_len = 2 << D;
+  // u16 region: the table form's log/antilog tables and twist logs, or (constant-time form) the
+  // multiplication columns c x^i of every twist constant c; then the Frobenius table
+  static constexpr int exp_off = 0, exp_len = CT ? 0 : 2 * Q;
+  static constexpr int log_off = exp_off + exp_len, log_len = CT ? 0 : Q;
+  static constexpr int twist_off = log_off + log_len, twist_len = CT ? (2 << D) * M : 2 << D;
   static constexpr int frlo_off = twist_off + twist_len, frlo_len = SIG;
   static constexpr int shared_u16 = (frlo_off + frlo_len + 1) & ~1;
   // u32 region: bit-sliced alpha, bit-sliced frob_hi
@@ -579,14 +844,26 @@ __device__ __forceinline__ void radix_step(uint32_t (&v)[VPL], int pb, int lane)
   }
 }
 
-template <int SET>
+// v * c for a public constant c given by its columns c x^i (i < M): no
+// address or branch depends on v
+template <int M>
+__device__ __forceinline__ uint32_t gf_mul_cols(uint32_t v, const uint16_t *cols) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int i = 0; i < M; i++) r ^= (uint32_t)cols[i] & (0u - ((v >> i) & 1u));
+  return r;
+}
+
+// CT: the constant-time form (the twist multiplies by table-free columns; the
+// tables indexed by coefficient values are not loaded)
+template <int SET, bool CT>
 __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint16_t *__restrict__ Sig,
                                                                    const uint32_t *__restrict__ S2, int lds2,
                                                                    const DecKeys keys, FieldDev fd, const Segs segs,
                                                                    uint32_t *__restrict__ E, int lde,
                                                                    int *__restrict__ okout) {
   using p = P<SET>;
-  using LY = RootLayout<SET>;
+  using LY = RootLayout<SET, CT>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d, SIG = LY::SIG, NH = LY::NH;
   constexpr int NW = (p::n + 31) / 32;
   constexpr int VPL = SIG / 32;  // chunk slots per lane
@@ -601,9 +878,13 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   uint16_t *frlo = sh16 + LY::frlo_off;
   uint32_t *abs_ = rsm + LY::abs_off;
   uint32_t *fhbs = rsm + LY::fhbs_off;
-  for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
-  for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
-  for (int i = threadIdx.x; i < (2 << D); i += blockDim.x) tlog[i] = fd.fft_twist_log[i];
+  if constexpr (CT) {
+    for (int i = threadIdx.x; i < LY::twist_len; i += blockDim.x) tlog[i] = fd.fft_twist_cols[i];
+  } else {
+    for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
+    for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
+    for (int i = threadIdx.x; i < (2 << D); i += blockDim.x) tlog[i] = fd.fft_twist_log[i];
+  }
   for (int i = threadIdx.x; i < SIG; i += blockDim.x) frlo[i] = fd.frob_lo[i];
   for (int i = threadIdx.x; i < (SIG - 1) * LY::abs_row; i += blockDim.x)
     abs_[(i / LY::abs_row) * LY::abs_stride + i % LY::abs_row] = fd.fft_alpha_bs[i];
@@ -637,9 +918,14 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
 #pragma unroll 1
     for (int l = 0; l < D; l++) {
       if (l) {
-        const uint16_t *tw = tlog + ((2 << D) - (2 << (D - l)));
+        const int tw0 = (2 << D) - (2 << (D - l));
+        if constexpr (CT) {
 #pragma unroll
-        for (int j = 0; j < VPL; j++) vv[j] = gf_mul_log<M>(gexp, glog[vv[j]], tw[(lane + 32 * j) >> l]);
+          for (int j = 0; j < VPL; j++) vv[j] = gf_mul_cols<M>(vv[j], tlog + (tw0 + ((lane + 32 * j) >> l)) * M);
+        } else {
+#pragma unroll
+          for (int j = 0; j < VPL; j++) vv[j] = gf_mul_log<M>(gexp, glog[vv[j]], tlog[tw0 + ((lane + 32 * j) >> l)]);
+        }
       }
 #pragma unroll 1
       for (int pb = D - 2; pb >= l; pb--) radix_step<VPL>(vv, pb, lane);
@@ -906,11 +1192,20 @@ static int persistent_blocks(K kernel, int threads, int smem, long long work_ite
 
 template <int SET>
 cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
-                          cudaStream_t st, int warps) {
+                          cudaStream_t st, int warps, bool ct) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   if (warps < 0 || warps > kBMWarps) return cudaErrorInvalidValue;
   if (warps == 0) warps = kBMWarps;
+  if (ct) {  // constant-time form, every batch size
+    const int smem_ct = BMCtLayout<SET>::bytes(warps);
+    cudaError_t err = cudaFuncSetAttribute(dec_bm_ct_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           BMCtLayout<SET>::bytes(kBMWarps));
+    if (err != cudaSuccess) return err;
+    const int gb = persistent_blocks(dec_bm_ct_kernel<SET>, warps * 32, smem_ct, (N + 31) / 32, warps);
+    dec_bm_ct_kernel<SET><<<gb, warps * 32, smem_ct, st>>>(S2, lds2, segs, Sig);
+    return cudaGetLastError();
+  }
   if (N < kBMBitslicedMinRows) {  // small batch: warp per request (lower latency per request)
     const int smem_l = BMLatLayout<SET>::bytes(kBMLatWarps);
     cudaError_t err =
@@ -929,20 +1224,32 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
   return cudaGetLastError();
 }
 
+template <int SET, bool CT>
+static cudaError_t launch_dec_root_form(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys,
+                                        FieldDev fd, const Segs &segs, uint32_t *E, int lde, int *ok,
+                                        cudaStream_t st, int warps) {
+  const long long N = seg_rows(segs);
+  const int smem_rt = RootLayout<SET, CT>::bytes(warps);
+  cudaError_t err = cudaFuncSetAttribute(dec_root_kernel<SET, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         RootLayout<SET, CT>::bytes(kRootWarps));
+  if (err != cudaSuccess) return err;
+  const int gr = persistent_blocks(dec_root_kernel<SET, CT>, warps * 32, smem_rt, N, warps);
+  dec_root_kernel<SET, CT><<<gr, warps * 32, smem_rt, st>>>(Sig, S2, lds2, keys, fd, segs, E, lde, ok);
+  return cudaGetLastError();
+}
+
 template <int SET>
 cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
-                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps) {
+                            const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps, bool ct) {
   const long long N = seg_rows(segs);
   if (N <= 0) return cudaSuccess;
   if (warps < 0 || warps > kRootWarps) return cudaErrorInvalidValue;
   if (warps == 0) warps = kRootWarps;
-  const int smem_rt = RootLayout<SET>::bytes(warps);
-  cudaError_t err = cudaFuncSetAttribute(dec_root_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         RootLayout<SET>::bytes(kRootWarps));
-  if (err != cudaSuccess) return err;
-  const int gr = persistent_blocks(dec_root_kernel<SET>, warps * 32, smem_rt, N, warps);
-  dec_root_kernel<SET><<<gr, warps * 32, smem_rt, st>>>(Sig, S2, lds2, keys, fd, segs, E, lde, ok);
-  return cudaGetLastError();
+  if (ct) {
+    if (!fd.fft_twist_cols) return cudaErrorInvalidValue;
+    return launch_dec_root_form<SET, true>(Sig, S2, lds2, keys, fd, segs, E, lde, ok, st, warps);
+  }
+  return launch_dec_root_form<SET, false>(Sig, S2, lds2, keys, fd, segs, E, lde, ok, st, warps);
 }
 
 template <int SET>
@@ -961,9 +1268,9 @@ cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uin
 #define GMC_INST_DEC(SET)                                                                                       \
   template cudaError_t launch_pack_ct<SET>(const uint8_t *, const Segs &, uint32_t *, int, bool, cudaStream_t);       \
   template cudaError_t launch_dec_bm<SET>(const uint32_t *, int, FieldDev, const Segs &, uint16_t *,             \
-                                         cudaStream_t, int);                                                     \
+                                         cudaStream_t, int, bool);                                               \
   template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, const DecKeys &, FieldDev,  \
-                                            const Segs &, uint32_t *, int, int *, cudaStream_t, int);            \
+                                            const Segs &, uint32_t *, int, int *, cudaStream_t, int, bool);      \
   template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, const DecKeys &, \
                                             uint8_t *, int *, const Segs &, bool, cudaStream_t);
 GMC_INST_DEC(0)

@@ -276,8 +276,9 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->ldf, ref->frows_pad, X, cw, ref->cw_pad, S2, s2, p::s2w,
                             tc_err_word_ptr(), pst);
-  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst, tune.bm_warps);
-  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst, tune.root_warps);
+  const bool ct = dec_constant_time();
+  if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst, tune.bm_warps, ct);
+  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst, tune.root_warps, ct);
   if (e == cudaSuccess)
     e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, pp.pc != 0, pst);
   return e;

@@ -1,0 +1,104 @@
+"""Constant-time decapsulation (gmc_set_dec_constant_time): the inversion-free, table-free Berlekamp-Massey with
+slot counts fixed by the iteration, and the root finder's table-free twist. Session keys and return codes must be
+the oracle's and the table forms' on valid, one-bit-flipped and random ciphertexts, for every set, a pc variant,
+batches on either side of the table form's bit-sliced threshold, and the per-request error vectors and decode
+flags must be the oracle's decrypt stages."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from tests.conftest import SETS, request_seeds
+from tests.test_gpu_kem import flipped_and_random
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+THREADS = os.cpu_count() or 8
+
+
+@pytest.fixture(scope="module")
+def gmc():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import tensormceliece_gb300 as g
+    g.lib()
+    yield g
+    g.set_dec_constant_time(False)
+
+
+def dec_both(gmc, sid, sk, cts):
+    key = gmc.SecretKey(sid, sk)
+    gmc.set_dec_constant_time(True)
+    try:
+        k_ct, rc_ct = key.dec_batch(cts)
+    finally:
+        gmc.set_dec_constant_time(False)
+    k_tab, rc_tab = key.dec_batch(cts)
+    return k_ct, rc_ct, k_tab, rc_tab
+
+
+@pytest.mark.parametrize("sid", [0, 1, 2, 3, 4, 9], ids=list(SETS) + ["8192128pc"])
+def test_ct_decapsulation_matches_oracle(gmc, keys, sid):
+    pk, sk = keys(sid % 5)
+    oc, _, _ = O.enc_batch(sid, pk, request_seeds(sid % 5, 300, b"ct"), threads=THREADS)
+    cts, _ = flipped_and_random(sid, oc, frac=0.2, nrand=16, seed=21)
+    k_ct, rc_ct, k_tab, rc_tab = dec_both(gmc, sid, sk, cts)
+    ok_, orc = O.dec_batch(sid, sk, cts, threads=THREADS)
+    assert (k_ct == ok_).all() and (rc_ct == orc).all(), "constant-time keys differ from the oracle"
+    assert (k_ct == k_tab).all() and (rc_ct == rc_tab).all()
+
+
+@pytest.mark.parametrize("sid", [0, 4], ids=["348864", "8192128"])
+def test_ct_large_batch_matches_table_form(gmc, keys, sid):
+    """32768 rows (the table form's bit-sliced Berlekamp-Massey) against the constant-time form, plus an oracle
+    sample of valid, flipped and random ciphertexts."""
+    pk, sk = keys(sid)
+    n = 32768
+    rng = np.random.default_rng(31 + sid)
+    c, _, _ = gmc.PublicKey(sid, pk).enc_batch(rng.integers(0, 256, (n, 32), dtype=np.uint8))
+    cts, flipped = flipped_and_random(sid, c, frac=0.1, nrand=64, seed=13)
+    k_ct, rc_ct, k_tab, rc_tab = dec_both(gmc, sid, sk, cts)
+    assert (k_ct == k_tab).all() and (rc_ct == rc_tab).all()
+    sample = np.concatenate([rng.choice(n, 16, replace=False), flipped[:16], np.arange(n, n + 16)])
+    ok_, orc = O.dec_batch(sid, sk, cts[sample], threads=THREADS)
+    assert (k_ct[sample] == ok_).all() and (rc_ct[sample] == orc).all()
+
+
+@pytest.mark.parametrize("sid", range(5), ids=SETS)
+def test_ct_error_vectors_match_oracle_stages(gmc, keys, sid):
+    pk, sk = keys(sid)
+    z = O.sizes(sid)
+    oc, _, _ = O.enc_batch(sid, pk, request_seeds(sid, 64, b"ct-stages"), threads=THREADS)
+    cts, _ = flipped_and_random(sid, oc, frac=0.25, nrand=4)
+    n = len(cts)
+    lde = (((z["n"] + 31) // 32) + 3) // 4 * 4
+    lds2 = (((2 * z["t"] * z["m"] + 31) // 32) + 3) // 4 * 4
+    dev = torch.device("cuda")
+    d_c = torch.from_numpy(cts).to(dev)
+    d_s = torch.zeros((n, lds2), dtype=torch.int32, device=dev)
+    d_e = torch.zeros((n, lde), dtype=torch.int32, device=dev)
+    d_ok = torch.zeros(n, dtype=torch.int32, device=dev)
+    key = gmc.SecretKey(sid, sk)
+    gmc.set_dec_constant_time(True)
+    try:
+        assert gmc.lib().gmc_dec_stages_dev(key.handle, d_c.data_ptr(), n, d_s.data_ptr(), lds2, d_e.data_ptr(),
+                                            lde, d_ok.data_ptr(), None) == 0
+        torch.cuda.synchronize()
+    finally:
+        gmc.set_dec_constant_time(False)
+    E = d_e.cpu().numpy().view(np.uint32)
+    OK = d_ok.cpu().numpy()
+    for i in range(n):
+        orc, _, _, e = O.decrypt_stages(sid, sk, cts[i])
+        assert OK[i] == (1 if orc == 0 else 0), f"request {i}: decode flag"
+        if orc == 0:
+            assert (E[i].view(np.uint8)[: z["n"] // 8] == e).all(), f"request {i}: error vector differs"
+
+
+def test_ct_switch(gmc):
+    assert gmc.get_dec_constant_time() is False
+    gmc.set_dec_constant_time(True)
+    assert gmc.get_dec_constant_time() is True
+    gmc.set_dec_constant_time(False)
+    assert gmc.lib().gmc_set_dec_constant_time(2) == -1
