@@ -331,8 +331,10 @@ extern "C" int gmc_sk_load(gmc_key **out, int id, const unsigned char *sk) {
   if (e == cudaSuccess) e = cudaMemcpy(k->s, h.s.data(), S.e_bytes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&k->HT, h.HT.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpy(k->HT, h.HT.data(), h.HT.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&k->cond, S.cond_bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(k->cond, sk + 40 + S.irr_bytes, S.cond_bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
-    cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s); cudaFree(k->HT);
+    cudaFree(k->F); cudaFree(k->tabs); cudaFree(k->s); cudaFree(k->HT); cudaFree(k->cond);
     delete k->a8_mu;
     delete k;
     return cuda_fail(e, "gmc_sk_load");
@@ -344,6 +346,7 @@ extern "C" int gmc_sk_load(gmc_key **out, int id, const unsigned char *sk) {
   k->dk.s = k->s;
   k->dk.HT = k->HT;
   k->dk.ldh = h.ldh;
+  k->dk.cond = k->cond;
   *out = k;
   return GMC_OK;
 }
@@ -358,6 +361,9 @@ extern "C" void gmc_key_free(gmc_key *key) {
   cudaFree(key->tabs);
   cudaFree(key->s);
   cudaFree(key->HT);
+  cudaFree(key->cond);
+  cudaFree(key->htt);
+  cudaFree(key->htt8);
   delete key;
 }
 
@@ -468,6 +474,57 @@ static cudaError_t gemm_keys(const gmc_key *const *keys, int nkeys, int engine, 
   return cudaSuccess;
 }
 
+int gmc::dec_e_words(int set, bool ct) {
+  const gmc_setinfo &S = set_info(set);
+  const int tab = round_up((S.n + 31) / 32, 4);
+  return ct ? std::max(S.q / 32, ct_htt_words(S.n)) : tab;
+}
+
+// the first-t syndrome matrix of a secret key (and its FP8 image for the tensor-core engine), built on first use
+static cudaError_t key_ct(const gmc_key *kc, int engine, cudaStream_t st) {
+  gmc_key *k = const_cast<gmc_key *>(kc);
+  std::lock_guard<std::mutex> lk(*k->a8_mu);
+  if (!k->cond) return cudaErrorInvalidValue;  // a key without control bits (see gmc_key_import)
+  const gmc_setinfo &S = set_info(k->set);
+  const int tm = S.t * S.m, rows_pad = round_up(tm, kGemmRowTile), kwn = ct_htt_words(S.n);
+  cudaError_t e = cudaSuccess;
+  if (!k->htt) {
+    uint32_t *p = nullptr;
+    e = cudaMalloc(&p, (size_t)rows_pad * kwn * 4);
+    if (e == cudaSuccess) e = launch_ct_htt(k->HT, k->dk.ldh, S.n, tm, p, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return e;
+    }
+    k->htt = p;
+  }
+  if (engine == GEMM_TC && !k->htt8) {
+    uint8_t *p = nullptr;
+    e = cudaMalloc(&p, tc_a8_bytes(rows_pad, kwn));
+    if (e == cudaSuccess) e = launch_expand_a(k->htt, kwn, rows_pad, kwn, p, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return e;
+    }
+    k->htt8 = p;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t gmc::ct_gemm_keys(const gmc_key *const *keys, int nkeys, int engine, cudaStream_t st, GemmKeys *gk) {
+  *gk = GemmKeys{};
+  if (nkeys > 0) gk->tc_stages = tune_get(keys[0]->set).gemm_stages;
+  for (int i = 0; i < nkeys; i++) {
+    cudaError_t e = key_ct(keys[i], engine, st);
+    if (e != cudaSuccess) return e;
+    gk->A[i] = keys[i]->htt;
+    gk->A8[i] = keys[i]->htt8;
+  }
+  return cudaSuccess;
+}
+
 // encapsulation kernels for the segments of one set: seeds / c / k rows in padded row space
 template <int SET>
 static cudaError_t enc_sample_gemm_seg(const Segs &segs, const gmc_key *ref, const GemmKeys &gk, int engine, int *err,
@@ -517,13 +574,15 @@ static cudaError_t enc_run(const gmc_key *pk, uint8_t *c, uint8_t *k, const uint
 struct DecDims {
   int ldx, lds2, lde;
   long long n_pad;
+  bool ct;  // constant-time kernels (the switch as read once for this batch)
 };
 static DecDims dec_dims(int set, int cw_pad, long long rows) {
   const gmc_setinfo &S = set_info(set);
   DecDims d;
+  d.ct = dec_constant_time();
   d.ldx = cw_pad;
   d.lds2 = round_up((2 * S.t * S.m + 31) / 32, 4);
-  d.lde = round_up((S.n + 31) / 32, 4);
+  d.lde = dec_e_words(set, d.ct);
   d.n_pad = (rows + kGemmOpPad - 1) / kGemmOpPad * kGemmOpPad;
   return d;
 }
@@ -534,7 +593,7 @@ template <int SET>
 static cudaError_t dec_front_decode_seg(const Segs &segs, const gmc_key *ref, const GemmKeys &gk, const DecKeys &dk,
                                         int engine, int *err, const uint8_t *c, uint32_t *X, uint32_t *S2,
                                         uint16_t *Sig, uint32_t *E, int *ok, const DecDims &d, cudaStream_t st,
-                                        bool pc = false) {
+                                        bool pc = false, const GemmKeys *ctk = nullptr) {
   using p = P<SET>;
   FieldDev fd;
   if (get_field(SET, &fd) != GMC_OK) return cudaErrorUnknown;
@@ -547,12 +606,17 @@ static cudaError_t dec_front_decode_seg(const Segs &segs, const gmc_key *ref, co
   if (e != cudaSuccess) return e;
   prof_mark("dec_front_gemm", st);
   const SetTune tune = tune_get(SET);
-  const bool ct = dec_constant_time();
-  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st, tune.bm_warps, ct);
+  e = launch_dec_bm<SET>(S2, d.lds2, fd, segs, Sig, st, tune.bm_warps, d.ct);
   if (e != cudaSuccess) return e;
   prof_mark("dec_bm", st);
-  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st, tune.root_warps, ct);
+  e = launch_dec_root<SET>(Sig, S2, d.lds2, dk, fd, segs, E, d.lde, ok, st, tune.root_warps, d.ct);
   prof_mark("dec_fft_roots_reenc", st);
+  if (e != cudaSuccess || !d.ct) return e;
+  // constant time: the Benes network to code positions, then the dense first-t syndrome check
+  // (the packed ciphertexts in X are no longer needed: X takes the check's syndromes)
+  if (!ctk) return cudaErrorInvalidValue;
+  e = launch_dec_ct_finish<SET>(dk, *ctk, engine, segs, E, d.lde, S2, d.lds2, X, d.ldx, ok, err, st);
+  prof_mark("dec_ct_positions_check", st);
   return e;
 }
 
@@ -566,8 +630,10 @@ static cudaError_t dec_front_decode(const gmc_key *sk, const uint8_t *c, long lo
   if (e != cudaSuccess) return e;
   DecKeys dk{};
   dk.k[0] = sk->dk;
+  GemmKeys ctk;
+  if (d.ct && (e = ct_gemm_keys(&sk, 1, engine, st, &ctk)) != cudaSuccess) return e;
   return dec_front_decode_seg<SET>(one_segment(n), sk, gk, dk, engine, err, c, X, S2, Sig, E, ok, d, st,
-                                   sk->pc != 0);
+                                   sk->pc != 0, d.ct ? &ctk : nullptr);
 }
 
 template <int SET>
@@ -980,6 +1046,7 @@ struct PlanPipe {
   int set = 0, kind = 0;  // kind 0 enc, 1 dec
   int pc = 0;             // plaintext-confirmation keys (ciphertexts C0 || C1)
   int engine = GEMM_TC;
+  bool const_time = false;  // constant-time decapsulation kernels (the switch at plan creation)
   std::vector<int> groups;
   Segs segs{};
   uint32_t pk_bad_mask = 0;
@@ -1036,10 +1103,15 @@ static cudaError_t plan_pipe_kernels(gmc_plan *p, PlanPipe &pp) {
       e = launch_finalize<SET>(pp.w0, d.lde, pp.w2, d.lds, pp.ct, pp.k, pp.segs, pp.pk_bad_mask, pp.pc != 0, pp.st);
   } else {
     DecDims d = dec_dims(SET, ref->cw_pad, rows);
+    d.ct = pp.const_time;  // the buffers were laid out for the form chosen at creation
+    d.lde = dec_e_words(SET, pp.const_time);
     DecKeys dk{};
     for (size_t i = 0; i < pp.groups.size(); i++) dk.k[i] = keys[i]->dk;
-    e = dec_front_decode_seg<SET>(pp.segs, ref, gk, dk, pp.engine, err, pp.in, pp.w0, pp.w1, pp.sig, pp.w2, pp.ok, d,
-                                  pp.st, pp.pc != 0);
+    GemmKeys ctk;
+    if (d.ct) e = ct_gemm_keys(keys, (int)pp.groups.size(), pp.engine, pp.st, &ctk);
+    if (e == cudaSuccess)
+      e = dec_front_decode_seg<SET>(pp.segs, ref, gk, dk, pp.engine, err, pp.in, pp.w0, pp.w1, pp.sig, pp.w2, pp.ok,
+                                    d, pp.st, pp.pc != 0, d.ct ? &ctk : nullptr);
     if (e == cudaSuccess)
       e = launch_dec_tail<SET>(pp.w2, d.lde, pp.ok, pp.in, dk, pp.k, pp.rc, pp.segs, pp.pc != 0, pp.st);
   }
@@ -1109,6 +1181,7 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w2, row * d.lds * 4);
     } else {
       DecDims d = dec_dims(pp.set, ref->cw_pad, row);
+      pp.const_time = d.ct;
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.rc, row * 4);
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w0, row * d.ldx * 4);
       if (e == cudaSuccess) e = plan_alloc(p, (void **)&pp.w1, row * d.lds2 * 4);
@@ -1127,6 +1200,12 @@ extern "C" int gmc_plan_create(gmc_plan **out, const gmc_group *groups, int ngro
         if ((e = key_a8(p->groups[gi].key, pp.st, &a8)) != cudaSuccess) break;
       }
     if (e == cudaSuccess && pp.engine == GEMM_TC && !tc_err_word()) e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess && pp.kind == 1 && pp.const_time) {  // the constant-time check's matrices, before capture
+      const gmc_key *ks[kMaxSegs];
+      for (size_t j = 0; j < pp.groups.size(); j++) ks[j] = p->groups[pp.groups[j]].key;
+      GemmKeys ctk;
+      e = ct_gemm_keys(ks, (int)pp.groups.size(), pp.engine, pp.st, &ctk);
+    }
   }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);

@@ -25,6 +25,11 @@ struct gmc_key {
   std::mutex *a8_mu = nullptr;
   uint8_t *s = nullptr;
   uint32_t *HT = nullptr;  // first t syndromes per code position (re-encryption check)
+  uint32_t *cond = nullptr;  // the sk's Benes control bits (constant-time decapsulation)
+  // constant-time decapsulation, built on first use: the first-t syndrome matrix (t m rows x n bits) and its
+  // FP8 stage image for the tensor-core engine (under a8_mu)
+  uint32_t *htt = nullptr;
+  uint8_t *htt8 = nullptr;
   gmc::DecKeyDev dk{};
 };
 
@@ -58,4 +63,9 @@ int field_tables(int set, FieldDev *out);
 // builds everything a key needs resident on the device for any engine choice
 // (FP8 image of its matrix, per-set tables), so later launches allocate nothing for it
 int key_prepare_resident(const gmc_key *key);
+// GEMM operands of the constant-time check (the keys' first-t syndrome matrices), built on first use
+cudaError_t ct_gemm_keys(const gmc_key *const *keys, int nkeys, int engine, cudaStream_t st, GemmKeys *gk);
+// decapsulation rows of the error-vector buffer: the table form needs ceil(n/32) words, the constant-time form
+// the field-order vector (q/32 words) and the check product's K (ct_htt_words(n))
+int dec_e_words(int set, bool ct);
 }  // namespace gmc

@@ -134,6 +134,7 @@ struct DecKeyDev {
   const uint8_t *s;      // implicit-rejection string [n/8]
   const uint32_t *HT;    // first t syndromes of each unit error [n][ldh] (m bits per syndrome)
   int ldh;
+  const uint32_t *cond;  // the sk's Benes control bits ((2m - 1) 2^(m-1) bits, as 32-bit words)
 };
 
 // Per-field / per-set device tables (shared by all keys of a set).
@@ -177,6 +178,18 @@ template <int SET>
 cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, const DecKeys &keys, FieldDev fd,
                             const Segs &segs, uint32_t *E, int lde, int *ok, cudaStream_t st, int warps = 0,
                             bool ct = false);
+// Constant-time decapsulation, after launch_dec_root(ct = true) left the field-order error vectors in E and the
+// BM-length flag in ok: the key's Benes network to code order (E in place, weight == t into ok), the dense product
+// of the first-t syndrome matrices (htt: per segment A / A8, rows t m padded to kGemmRowTile, ct_htt_words(n)
+// words) with E into S3, and ok &= (S3 == the first t m bits of S2). E rows: lde >= max(q/32, ct_htt_words(n)).
+// S3 rows: lds3 >= ceil(t m / 32) words (the packed-ciphertext buffer is large enough).
+constexpr int ct_htt_words(int n) { return ((n + 31) / 32 + kGemmKTile - 1) / kGemmKTile * kGemmKTile; }
+template <int SET>
+cudaError_t launch_dec_ct_finish(const DecKeys &keys, const GemmKeys &htt, int engine, const Segs &segs, uint32_t *E,
+                                 int lde, const uint32_t *S2, int lds2, uint32_t *S3, int lds3, int *ok, int *err,
+                                 cudaStream_t st);
+// HT (n rows of ldh words) -> HTT ((t m padded to kGemmRowTile) rows x ct_htt_words(n) words), once per key
+cudaError_t launch_ct_htt(const uint32_t *HT, int ldh, int n, int tm, uint32_t *HTT, cudaStream_t st);
 // With pc the decoded e must also give SHAKE256(2 || e, 32) = C1 (else implicit
 // rejection), and the session-key preimage covers C0 || C1.
 template <int SET>

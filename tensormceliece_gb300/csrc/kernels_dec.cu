@@ -844,6 +844,26 @@ __device__ __forceinline__ void radix_step(uint32_t (&v)[VPL], int pb, int lane)
   }
 }
 
+// the even bits of x, compacted into the low 16 bits
+__device__ __forceinline__ uint32_t comp_even16(uint32_t x) {
+  x &= 0x55555555u;
+  x = (x | (x >> 1)) & 0x33333333u;
+  x = (x | (x >> 2)) & 0x0F0F0F0Fu;
+  x = (x | (x >> 4)) & 0x00FF00FFu;
+  x = (x | (x >> 8)) & 0x0000FFFFu;
+  return x;
+}
+// exchanges the bits at p and p + d for every p in mask
+__device__ __forceinline__ uint32_t delta_swap(uint32_t x, int d, uint32_t mask) {
+  const uint32_t t = ((x >> d) ^ x) & mask;
+  return x ^ t ^ (t << d);
+}
+// bit i -> bit bitrev_5(i): index bits 0 <-> 4 and 1 <-> 3 exchanged
+__device__ __forceinline__ uint32_t rev5_bits(uint32_t x) {
+  x = delta_swap(x, 15, 0x0000AAAAu);
+  return delta_swap(x, 6, 0x00CC00CCu);
+}
+
 // v * c for a public constant c given by its columns c x^i (i < M): no
 // address or branch depends on v
 template <int M>
@@ -944,6 +964,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     }
 
     int weight = 0;
+    uint32_t zm0[VPL], zm1[VPL];  // constant-time form: the zero masks of both chunk halves
 #pragma unroll 1
     for (int h = 0; h < NH; h++) {
       uint32_t v[VPL][M];
@@ -1015,6 +1036,14 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
         }
         zero[j] = ~nz;
       }
+      if constexpr (CT) {
+#pragma unroll
+        for (int j = 0; j < VPL; j++) {
+          if (h == 0) zm0[j] = zero[j];
+          else zm1[j] = zero[j];
+        }
+        continue;
+      }
 #pragma unroll
       for (int j = 0; j < VPL; j++) {
         uint32_t z = zero[j];
@@ -1031,6 +1060,27 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
           }
         }
       }
+    }
+    if constexpr (CT) {
+      // the error vector in field-element order with bit-reversed index, the input order of the key's Benes
+      // network: word w holds y[32 w + i] = zero(alpha) for alpha = bitrev_m(32 w + i), i.e. the slot
+      // bitrev_d(w >> 1) of the chunks 2 bitrev_5(i) + (w & 1). Lane and register j hold that slot's zero
+      // masks over all 64 chunks: every other bit, compacted, with its 5-bit index reversed.
+      static_assert(NH == 2 && M - D == 6, "64 chunks of 2^d slots");
+      uint32_t *erow = E + op * lde;
+#pragma unroll
+      for (int j = 0; j < VPL; j++) {
+        const int sl = chunk_slot<D>(-1, lane, j);
+        const int wb = (int)(__brev((unsigned)sl) >> (32 - D)) << 1;
+#pragma unroll
+        for (int b0 = 0; b0 < 2; b0++) {
+          const uint32_t e32 = comp_even16(zm0[j] >> b0) | (comp_even16(zm1[j] >> b0) << 16);
+          erow[wb | b0] = rev5_bits(e32);
+        }
+      }
+      if (lane == 0) okout[op] = long_lfsr ? 0 : 1;  // weight and syndromes are checked after the Benes network
+      __syncwarp();
+      continue;
     }
     weight = __reduce_add_sync(0xffffffffu, weight);
     __syncwarp();
@@ -1252,6 +1302,165 @@ cudaError_t launch_dec_root(const uint16_t *Sig, const uint32_t *S2, int lds2, c
   return launch_dec_root_form<SET, false>(Sig, S2, lds2, keys, fd, segs, E, lde, ok, st, warps);
 }
 
+// ---------------------------------------------------------------- constant-time positions and check
+// The key's Benes network (its sk control bits, 2m - 1 layers of conditional
+// swaps with strides 2^0 .. 2^(m-1) .. 2^0) applied to the field-order error
+// vector y (y[v] = e at field element bitrev_m(v)) gives x[i] = y[pi(i)] with
+// L_i = bitrev_m(pi(i)), i.e. the error at code position i: the same network
+// and bit order that define the support (support_gen in the library). Warp per
+// request, the q-bit vector in registers (word w = lane + 32 r); every layer
+// touches every word with the control words as masks, so nothing depends on the
+// error's positions. Then: bits >= n cleared, weight == t folded into ok.
+// a layer whose pairs are registers r and r + DR of one lane (stride 2^s, s >= 10)
+template <int WPL, int DR>
+__device__ __forceinline__ void benes_reg_layer(uint32_t (&x)[WPL], const uint32_t *cw, int lane, int s) {
+#pragma unroll
+  for (int r = 0; r < WPL; r++) {
+    if ((r & DR) || r + DR >= WPL) continue;
+    const int wlo = lane + 32 * r;
+    const uint32_t c = __ldg(cw + (((wlo >> (s - 4)) << (s - 5)) | (wlo & (32 * DR - 1))));
+    const uint32_t t = (x[r] ^ x[r + DR]) & c;
+    x[r] ^= t;
+    x[r + DR] ^= t;
+  }
+}
+
+template <int SET>
+__global__ void __launch_bounds__(256) benes_ct_kernel(uint32_t *__restrict__ E, int lde, int *__restrict__ okio,
+                                                       const DecKeys keys, const Segs segs) {
+  using p = P<SET>;
+  constexpr int M = p::m, Q = p::q, T = p::t, N = p::n;
+  constexpr int WPL = Q / 32 / 32;  // words per lane
+  constexpr int LW = Q / 64;         // control words per layer
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long NR = seg_rows(segs);
+  for (long long op = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); op < NR; op += nwarps) {
+    int seg;
+    if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
+    const uint32_t *cond = keys.k[seg].cond;
+    uint32_t *row = E + op * lde;
+    uint32_t x[WPL];
+#pragma unroll
+    for (int r = 0; r < WPL; r++) x[r] = row[lane + 32 * r];
+#pragma unroll 1
+    for (int li = 0; li < 2 * M - 1; li++) {
+      const int s = li < M ? li : 2 * M - 2 - li;
+      const uint32_t *cw = cond + li * LW;
+      if (s < 5) {
+        const int d = 1 << s;
+#pragma unroll
+        for (int r = 0; r < WPL; r++) {
+          const int w = lane + 32 * r;
+          uint32_t c = (__ldg(cw + (w >> 1)) >> (16 * (w & 1))) & 0xFFFFu;
+          // deposit the 16 control bits at the pairs' lower positions (bit s of the position clear)
+#pragma unroll
+          for (int pb = 3; pb >= 0; pb--) {
+            if (pb >= s) {
+              const uint32_t mp = pb == 3 ? 0xFF00FF00u : pb == 2 ? 0xF0F0F0F0u : pb == 1 ? 0xCCCCCCCCu : 0xAAAAAAAAu;
+              c = (c & ~mp) | ((c & mp) << (1 << pb));
+            }
+          }
+          const uint32_t t = ((x[r] >> d) ^ x[r]) & c;
+          x[r] ^= t ^ (t << d);
+        }
+      } else if (s < 10) {  // partner word in lane ^ 2^(s-5)
+        const int dl = 1 << (s - 5);
+#pragma unroll
+        for (int r = 0; r < WPL; r++) {
+          const int wlo = (lane & ~dl) + 32 * r;
+          const uint32_t c = __ldg(cw + (((wlo >> (s - 4)) << (s - 5)) | (wlo & (dl - 1))));
+          const uint32_t xp = __shfl_xor_sync(0xffffffffu, x[r], dl);
+          x[r] ^= (x[r] ^ xp) & c;
+        }
+      } else if (s == 10) {  // partner word in register r ^ 2^(s-10)
+        benes_reg_layer<WPL, 1>(x, cw, lane, 10);
+      } else if (s == 11) {
+        benes_reg_layer<WPL, 2>(x, cw, lane, 11);
+      } else {
+        benes_reg_layer<WPL, 4>(x, cw, lane, 12);
+      }
+    }
+    int weight = 0;
+#pragma unroll
+    for (int r = 0; r < WPL; r++) {
+      const int w = lane + 32 * r;
+      const uint32_t keep = 32 * w + 32 <= N ? 0xFFFFFFFFu : 32 * w >= N ? 0u : (1u << (N % 32)) - 1u;
+      x[r] &= keep;
+      weight += __popc(x[r]);
+      if (w < lde) row[w] = x[r];
+    }
+    weight = __reduce_add_sync(0xffffffffu, weight);
+    if (lane == 0) okio[op] = okio[op] & (weight == T ? 1 : 0);
+  }
+}
+
+// ok &= (first t syndromes of the decoded error == the received ones): S3 from
+// the dense product with the key's first-t syndrome matrix, S2 the received 2t
+// syndromes (same packing, m bits each). Thread per request, every word.
+template <int SET>
+__global__ void ct_check_kernel(const uint32_t *__restrict__ S3, int lds3, const uint32_t *__restrict__ S2, int lds2,
+                                int *__restrict__ okio, const Segs segs) {
+  using p = P<SET>;
+  constexpr int TM = p::t * p::m, TW = (TM + 31) / 32;
+  const long long op = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int seg;
+  if (op >= seg_rows(segs) || !seg_live(segs, op, &seg)) return;
+  uint32_t mism = 0;
+#pragma unroll 4
+  for (int w = 0; w < TW; w++) {
+    const uint32_t msk = (w == TW - 1 && (TM % 32)) ? ((1u << (TM % 32)) - 1u) : 0xFFFFFFFFu;
+    mism |= (S3[op * lds3 + w] ^ S2[op * lds2 + w]) & msk;
+  }
+  okio[op] = okio[op] & (mism == 0 ? 1 : 0);
+}
+
+template <int SET>
+cudaError_t launch_dec_ct_finish(const DecKeys &keys, const GemmKeys &htt, int engine, const Segs &segs, uint32_t *E,
+                                 int lde, const uint32_t *S2, int lds2, uint32_t *S3, int lds3, int *ok, int *err,
+                                 cudaStream_t st) {
+  using p = P<SET>;
+  const long long N = seg_rows(segs);
+  if (N <= 0) return cudaSuccess;
+  if (lde < p::q / 32 || lde < ct_htt_words(p::n)) return cudaErrorInvalidValue;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (N + 7) / 8;
+  const int blocks = (int)(want < 8LL * sms ? want : 8LL * sms);
+  benes_ct_kernel<SET><<<blocks, 256, 0, st>>>(E, lde, ok, keys, segs);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = launch_gf2_gemm_seg(engine, htt, segs, ct_htt_words(p::n), (p::t * p::m + kGemmRowTile - 1) / kGemmRowTile *
+                          kGemmRowTile, E, lde, ct_htt_words(p::n), S3, lds3, (p::t * p::m + 31) / 32, err, st);
+  if (e != cudaSuccess) return e;
+  ct_check_kernel<SET><<<(unsigned)((N + 127) / 128), 128, 0, st>>>(S3, lds3, S2, lds2, ok, segs);
+  return cudaGetLastError();
+}
+
+// HTT[r][w] bit b = bit r of HT[32 w + b] (r < t m, 32 w + b < n): the first t syndromes of every code position
+// as a (t m) x n GF(2) matrix, rows_pad x kwn words
+__global__ void ct_htt_kernel(const uint32_t *__restrict__ HT, int ldh, int n, int tm, int rows_pad, int kwn,
+                              uint32_t *__restrict__ HTT) {
+  const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= (long long)rows_pad * kwn) return;
+  const int r = (int)(item / kwn), w = (int)(item % kwn);
+  uint32_t v = 0;
+  if (r < tm)
+    for (int b = 0; b < 32; b++) {
+      const int i = 32 * w + b;
+      if (i < n) v |= ((HT[(size_t)i * ldh + (r >> 5)] >> (r & 31)) & 1u) << b;
+    }
+  HTT[item] = v;
+}
+
+cudaError_t launch_ct_htt(const uint32_t *HT, int ldh, int n, int tm, uint32_t *HTT, cudaStream_t st) {
+  const int rows_pad = (tm + kGemmRowTile - 1) / kGemmRowTile * kGemmRowTile, kwn = ct_htt_words(n);
+  const long long total = (long long)rows_pad * kwn;
+  ct_htt_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(HT, ldh, n, tm, rows_pad, kwn, HTT);
+  return cudaGetLastError();
+}
+
 template <int SET>
 cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uint8_t *C, const DecKeys &keys,
                             uint8_t *K, int *rc, const Segs &segs, bool pc, cudaStream_t st) {
@@ -1272,7 +1481,10 @@ cudaError_t launch_dec_tail(const uint32_t *E, int lde, const int *ok, const uin
   template cudaError_t launch_dec_root<SET>(const uint16_t *, const uint32_t *, int, const DecKeys &, FieldDev,  \
                                             const Segs &, uint32_t *, int, int *, cudaStream_t, int, bool);      \
   template cudaError_t launch_dec_tail<SET>(const uint32_t *, int, const int *, const uint8_t *, const DecKeys &, \
-                                            uint8_t *, int *, const Segs &, bool, cudaStream_t);
+                                            uint8_t *, int *, const Segs &, bool, cudaStream_t);                 \
+  template cudaError_t launch_dec_ct_finish<SET>(const DecKeys &, const GemmKeys &, int, const Segs &, uint32_t *, \
+                                                 int, const uint32_t *, int, uint32_t *, int, int *, int *,      \
+                                                 cudaStream_t);
 GMC_INST_DEC(0)
 GMC_INST_DEC(1)
 GMC_INST_DEC(2)

@@ -7,7 +7,8 @@
 // Format (little-endian): header, then the sections in order
 //   public key: T (rows_pad x lda u32), TT ((k+1) x ldtt u32)
 //   secret key: F (frows_pad x ldf u32), support tables (3n + 2^m u16),
-//               s (n/8 bytes zero-padded to 16), HT (n x ldh u32)
+//               s (n/8 bytes zero-padded to 16), HT (n x ldh u32),
+//               the sk's Benes control bits (for constant-time decapsulation)
 // The header's checksum is SHAKE256 of the whole string with the checksum
 // field zeroed; import rejects any string whose magic, version, set, sizes or
 // checksum do not match.
@@ -109,7 +110,7 @@ namespace {
 using namespace gmc;
 
 constexpr char kMagic[8] = {'G', 'M', 'C', 'K', 'E', 'Y', '0', '1'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;  // 2: secret keys carry their Benes control bits
 
 struct KeyHeader {
   char magic[8];
@@ -117,7 +118,7 @@ struct KeyHeader {
   int32_t set, variant, kind;
   int32_t lda, rows_pad, kw_pad, pad_bad, ldtt;  // public key
   int32_t ldf, frows_pad, cw_pad, ldh;           // secret key
-  uint64_t section[4];                           // bytes of each section
+  uint64_t section[5];                           // bytes of each section
   uint8_t checksum[32];
 };
 static_assert(sizeof(KeyHeader) % 8 == 0, "header keeps the sections 8-byte aligned");
@@ -134,9 +135,9 @@ size_t s_alloc_bytes(const gmc_setinfo &S) { return ((size_t)S.e_bytes + 15) / 1
 // kernels assume that layout: a smaller padded width would make the GEMM skip
 // words of the key or ciphertext and return wrong session keys with rc = 0),
 // and the public key's padding flag must be 0 or 1.
-bool section_sizes(const KeyHeader &h, uint64_t out[4]) {
+bool section_sizes(const KeyHeader &h, uint64_t out[5]) {
   const gmc_setinfo &S = set_info(h.set);
-  memset(out, 0, 4 * sizeof(uint64_t));
+  memset(out, 0, 5 * sizeof(uint64_t));
   if (h.kind == 0) {
     const int kw_pad = round_up((S.k + 31) / 32, kGemmKTile);
     const int ldtt = round_up((S.mt + 31) / 32, 32) < 64 ? 64 : round_up((S.mt + 31) / 32, 32);
@@ -154,6 +155,7 @@ bool section_sizes(const KeyHeader &h, uint64_t out[4]) {
     out[1] = (3ull * S.n + S.q) * 2;
     out[2] = s_alloc_bytes(S);
     out[3] = (uint64_t)S.n * h.ldh * 4;
+    out[4] = (uint64_t)S.cond_bytes;
   }
   return true;
 }
@@ -176,10 +178,12 @@ extern "C" long long gmc_key_export(const gmc_key *key, unsigned char *buf, long
   h.lda = key->lda; h.rows_pad = key->rows_pad; h.kw_pad = key->kw_pad; h.pad_bad = key->pad_bad; h.ldtt = key->ldtt;
   h.ldf = key->ldf; h.frows_pad = key->frows_pad; h.cw_pad = key->cw_pad; h.ldh = key->dk.ldh;
   if (!section_sizes(h, h.section)) return kf_fail(GMC_EKEY, "gmc_key_export: key dimensions out of range");
-  const long long total = (long long)sizeof(KeyHeader) + (long long)(h.section[0] + h.section[1] + h.section[2] + h.section[3]);
+  const long long total = (long long)sizeof(KeyHeader) +
+                          (long long)(h.section[0] + h.section[1] + h.section[2] + h.section[3] + h.section[4]);
   if (!buf) return total;
   if (len < total) return kf_fail(GMC_EINVAL, "gmc_key_export: buffer too small");
-  const void *src[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (key->kind == 1 && !key->cond) return kf_fail(GMC_EKEY, "gmc_key_export: key without control bits");
+  const void *src[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   if (key->kind == 0) {
     src[0] = key->T;
     src[1] = key->TT;
@@ -188,9 +192,10 @@ extern "C" long long gmc_key_export(const gmc_key *key, unsigned char *buf, long
     src[1] = key->tabs;
     src[2] = key->s;
     src[3] = key->HT;
+    src[4] = key->cond;
   }
   unsigned char *p = buf + sizeof(KeyHeader);
-  for (int i = 0; i < 4; i++) {
+  for (int i = 0; i < 5; i++) {
     if (!h.section[i]) continue;
     cudaError_t e = cudaMemcpy(p, src[i], h.section[i], cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return kf_fail(GMC_ECUDA, std::string("gmc_key_export: ") + cudaGetErrorString(e));
@@ -211,10 +216,10 @@ extern "C" int gmc_key_import(gmc_key **out, const unsigned char *buf, long long
   if (memcmp(h.magic, kMagic, 8) || h.version != kVersion) return kf_fail(GMC_EKEY, "gmc_key_import: not a key string");
   if (h.set < 0 || h.set >= GMC_NSETS || h.variant < 0 || h.variant > 3 || (h.kind != 0 && h.kind != 1))
     return kf_fail(GMC_EKEY, "gmc_key_import: bad set, variant or kind");
-  uint64_t sz[4];
+  uint64_t sz[5];
   if (!section_sizes(h, sz) || memcmp(sz, h.section, sizeof sz))
     return kf_fail(GMC_EKEY, "gmc_key_import: section sizes do not match the key's dimensions");
-  const long long total = (long long)sizeof(KeyHeader) + (long long)(sz[0] + sz[1] + sz[2] + sz[3]);
+  const long long total = (long long)sizeof(KeyHeader) + (long long)(sz[0] + sz[1] + sz[2] + sz[3] + sz[4]);
   if (len != total) return kf_fail(GMC_EKEY, "gmc_key_import: wrong length");
   uint8_t sum[32];
   checksum(buf, total, sum);
@@ -227,7 +232,7 @@ extern "C" int gmc_key_import(gmc_key **out, const unsigned char *buf, long long
   k->pc = h.variant & 1;
   k->kind = h.kind;
   cudaGetDevice(&k->device);
-  void **dst[4] = {nullptr, nullptr, nullptr, nullptr};
+  void **dst[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   if (h.kind == 0) {
     k->lda = h.lda; k->rows_pad = h.rows_pad; k->kw_pad = h.kw_pad; k->pad_bad = h.pad_bad; k->ldtt = h.ldtt;
     dst[0] = (void **)&k->T;
@@ -238,17 +243,18 @@ extern "C" int gmc_key_import(gmc_key **out, const unsigned char *buf, long long
     dst[1] = (void **)&k->tabs;
     dst[2] = (void **)&k->s;
     dst[3] = (void **)&k->HT;
+    dst[4] = (void **)&k->cond;
   }
   const unsigned char *p = buf + sizeof(KeyHeader);
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+  for (int i = 0; i < 5 && e == cudaSuccess; i++) {
     if (!sz[i]) continue;
     e = cudaMalloc(dst[i], sz[i]);
     if (e == cudaSuccess) e = cudaMemcpy(*dst[i], p, sz[i], cudaMemcpyHostToDevice);
     p += sz[i];
   }
   if (e != cudaSuccess) {
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 5; i++)
       if (dst[i] && *dst[i]) cudaFree(*dst[i]);
     delete k->a8_mu;
     delete k;
@@ -263,6 +269,7 @@ extern "C" int gmc_key_import(gmc_key **out, const unsigned char *buf, long long
     k->dk.s = k->s;
     k->dk.HT = k->HT;
     k->dk.ldh = h.ldh;
+    k->dk.cond = k->cond;
   }
   *out = k;
   return GMC_OK;

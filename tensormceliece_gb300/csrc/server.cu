@@ -182,8 +182,10 @@ size_t work_bytes(int set, int kind, long long rows) {
                mw = (size_t)round_up((S.mt + 31) / 32, 4), cw = (size_t)round_up((S.synd_bytes + 3) / 4, kGemmKTile),
                s2 = (size_t)round_up((2 * S.t * S.m + 31) / 32, 4);
   if (kind == 0) return align256(rows * ew * 4) + align256(rows * kw * 4) + align256(rows * mw * 4);
+  // decapsulation rows are laid out for either form, so the constant-time switch can change between batches
+  const size_t ewd = (size_t)dec_e_words(set, true);
   return align256(rows * cw * 4) + align256(rows * s2 * 4) + align256(rows * (2u << S.fft_d)) +
-         align256(rows * ew * 4) + align256(rows * 4);
+         align256(rows * ewd * 4) + align256(rows * 4);
 }
 
 }  // namespace
@@ -258,6 +260,8 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
     return e;
   }
   const int cw = ref->cw_pad, s2 = round_up((2 * S.t * S.m + 31) / 32, 4);
+  const bool ct = dec_constant_time();
+  const int ewd = dec_e_words(SET, ct);
   uint8_t *q = work;
   uint32_t *X = (uint32_t *)q;
   q += align256(rows * cw * 4);
@@ -266,7 +270,7 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   uint16_t *Sig = (uint16_t *)q;
   q += align256(rows * (2u << S.fft_d));
   uint32_t *E = (uint32_t *)q;
-  q += align256(rows * ew * 4);
+  q += align256(rows * (size_t)dec_e_words(SET, true) * 4);
   int *ok = (int *)q;
   FieldDev fd;
   if (field_tables(SET, &fd) != GMC_OK) return cudaErrorUnknown;
@@ -276,11 +280,17 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
   if (e == cudaSuccess)
     e = launch_gf2_gemm_seg(engine, gk, pp.segs, ref->ldf, ref->frows_pad, X, cw, ref->cw_pad, S2, s2, p::s2w,
                             tc_err_word_ptr(), pst);
-  const bool ct = dec_constant_time();
   if (e == cudaSuccess) e = launch_dec_bm<SET>(S2, s2, fd, pp.segs, Sig, pst, tune.bm_warps, ct);
-  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ew, ok, pst, tune.root_warps, ct);
+  if (e == cudaSuccess) e = launch_dec_root<SET>(Sig, S2, s2, dk, fd, pp.segs, E, ewd, ok, pst, tune.root_warps, ct);
+  if (e == cudaSuccess && ct) {
+    // the keys' first-t syndrome matrices are built on a key's first constant-time batch
+    GemmKeys ctk;
+    e = ct_gemm_keys(pp.keys.data(), (int)pp.keys.size(), engine, pst, &ctk);
+    if (e == cudaSuccess)
+      e = launch_dec_ct_finish<SET>(dk, ctk, engine, pp.segs, E, ewd, S2, s2, X, cw, ok, tc_err_word_ptr(), pst);
+  }
   if (e == cudaSuccess)
-    e = launch_dec_tail<SET>(E, ew, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, pp.pc != 0, pst);
+    e = launch_dec_tail<SET>(E, ewd, ok, in, dk, kout, (int *)(sl.dev + pp.rc_off), pp.segs, pp.pc != 0, pst);
   return e;
 }
 

@@ -1,8 +1,10 @@
 """Constant-time decapsulation (gmc_set_dec_constant_time): the inversion-free, table-free Berlekamp-Massey with
-slot counts fixed by the iteration, and the root finder's table-free twist. Session keys and return codes must be
-the oracle's and the table forms' on valid, one-bit-flipped and random ciphertexts, for every set, a pc variant,
-batches on either side of the table form's bit-sliced threshold, and the per-request error vectors and decode
-flags must be the oracle's decrypt stages."""
+slot counts fixed by the iteration, the root finder's table-free twist, the error vector taken to code positions
+by the key's Benes network and checked by a dense product with the key's first-t syndrome matrix (no gather at an
+error position anywhere). Session keys and return codes must be the oracle's and the table forms' on valid,
+one-bit-flipped and random ciphertexts, for every set, a pc variant, batches on either side of the table form's
+bit-sliced threshold, an imported key and a grouped plan; the per-request error vectors and decode flags must be
+the oracle's decrypt stages."""
 import os
 
 import numpy as np
@@ -72,7 +74,7 @@ def test_ct_error_vectors_match_oracle_stages(gmc, keys, sid):
     oc, _, _ = O.enc_batch(sid, pk, request_seeds(sid, 64, b"ct-stages"), threads=THREADS)
     cts, _ = flipped_and_random(sid, oc, frac=0.25, nrand=4)
     n = len(cts)
-    lde = (((z["n"] + 31) // 32) + 3) // 4 * 4
+    lde = max((1 << z["m"]) // 32, ((z["n"] + 31) // 32 + 7) // 8 * 8)  # the constant-time row stride
     lds2 = (((2 * z["t"] * z["m"] + 31) // 32) + 3) // 4 * 4
     dev = torch.device("cuda")
     d_c = torch.from_numpy(cts).to(dev)
@@ -94,6 +96,43 @@ def test_ct_error_vectors_match_oracle_stages(gmc, keys, sid):
         assert OK[i] == (1 if orc == 0 else 0), f"request {i}: decode flag"
         if orc == 0:
             assert (E[i].view(np.uint8)[: z["n"] // 8] == e).all(), f"request {i}: error vector differs"
+
+
+def test_ct_imported_key_and_grouped_plan(gmc, keys):
+    """A secret key re-created from its exported string (which carries the Benes control bits), and a grouped plan
+    created under the switch, give the table forms' keys."""
+    dev = torch.device("cuda")
+    sids = [4, 3]
+    bufs, groups, refs = [], [], []
+    for sid in sids:
+        pk, sk = keys(sid)
+        oc, _, _ = O.enc_batch(sid, pk, request_seeds(sid, 200, b"ct-plan"), threads=THREADS)
+        cts, _ = flipped_and_random(sid, oc, frac=0.2, nrand=8, seed=5)
+        S = gmc.SecretKey(sid, sk)
+        k_tab, rc_tab = S.dec_batch(cts)
+        S2 = gmc.SecretKey.from_export(S.export())
+        gmc.set_dec_constant_time(True)
+        try:
+            k_imp, rc_imp = S2.dec_batch(cts)
+        finally:
+            gmc.set_dec_constant_time(False)
+        assert (k_imp == k_tab).all() and (rc_imp == rc_tab).all()
+        d_c = torch.from_numpy(cts).to(dev)
+        d_k = torch.zeros((len(cts), 32), dtype=torch.uint8, device=dev)
+        d_rc = torch.zeros(len(cts), dtype=torch.int32, device=dev)
+        bufs.append((S, d_c, d_k, d_rc))
+        groups.append((S, len(cts), d_c.data_ptr(), 0, d_k.data_ptr(), d_rc.data_ptr()))
+        refs.append((k_tab, rc_tab))
+    gmc.set_dec_constant_time(True)
+    try:
+        plan = gmc.Plan(groups)
+    finally:
+        gmc.set_dec_constant_time(False)
+    plan.launch(torch.cuda.current_stream().cuda_stream)  # the form is fixed when the plan is created
+    torch.cuda.synchronize()
+    plan.close()
+    for (S, d_c, d_k, d_rc), (k_tab, rc_tab) in zip(bufs, refs):
+        assert (d_k.cpu().numpy() == k_tab).all() and (d_rc.cpu().numpy() == rc_tab).all()
 
 
 def test_ct_switch(gmc):

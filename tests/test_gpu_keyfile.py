@@ -54,13 +54,13 @@ def _reseal(blob):
     string would carry it: the checksum guards against corruption, not against a chosen header."""
     import hashlib
     b = bytearray(blob)
-    b[96:128] = bytes(32)
-    b[96:128] = hashlib.shake_256(bytes(b)).digest(32)
+    b[104:136] = bytes(32)
+    b[104:136] = hashlib.shake_256(bytes(b)).digest(32)
     return bytes(b)
 
 
 def test_import_rejects_layouts_the_kernels_do_not_use(gmc, keys):
-    """Header fields at their offsets: kw_pad 32, pad_bad 36 (public); cw_pad 52 (secret); checksum 96..128."""
+    """Header fields at their offsets: kw_pad 32, pad_bad 36 (public); cw_pad 52 (secret); checksum 104..136."""
     import struct
     pk, sk = keys(4)
     sblob = gmc.SecretKey(4, sk).export()
