@@ -654,7 +654,8 @@ def serving(gmc, torch, seconds):
     for frac in (0.1, 0.25, 0.5, 0.75, 0.9, 1.0):
         r = srv.loadgen(pairs, rate=frac * peak["ops_s"], seconds=seconds, seed=int(frac * 100))
         levels[f"{int(frac * 100)}%"] = {k: r[k] for k in ("offered_rate", "ops_s", "p50_ms", "p99_ms", "p999_ms",
-                                                             "max_ms", "mean_batch", "completed", "submitted")}
+                                                             "max_ms", "mean_batch", "completed", "submitted",
+                                                             "worst_batch")}
     srv.close()
     # sequential one-request calls (libmceliece calling convention, resident keys, host buffers)
     lat = []

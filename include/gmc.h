@@ -165,7 +165,13 @@ void gmc_plan_free(gmc_plan *plan);
  * completed, achieved ops/s, p50 ms, p99 ms, mean batch, batches, offered
  * rate. gmc_server_latency_ms gives any quantile q (0 < q <= 1; 1 = the
  * slowest request) of the latencies recorded since the last reset (the
- * histogram's buckets are 2% wide). */
+ * histogram's buckets are 2% wide). gmc_server_worst_batch writes out[10] for
+ * the batch whose oldest request had the longest latency since the last
+ * reset: that latency, then its parts in ms (waiting in the queue for a free
+ * slot, moving the requests out of the queue, grouping them by key with the
+ * admission check, copying the inputs into pinned staging, issuing copies and
+ * kernels, device work with the copies and the completion callback, scattering
+ * the results), then the number of batches and of batches over 5 ms. */
 typedef struct gmc_server gmc_server;
 int gmc_server_create(gmc_server **server, long long max_batch, int slots, double mem_fraction);
 int gmc_server_add_key(gmc_server *server, const gmc_key *key);
@@ -175,6 +181,7 @@ int gmc_server_drain(gmc_server *server, double timeout_s);
 int gmc_server_stats(gmc_server *server, double *out);
 int gmc_server_reset_stats(gmc_server *server);
 int gmc_server_latency_ms(gmc_server *server, double q, double *ms);
+int gmc_server_worst_batch(gmc_server *server, double *out);
 int gmc_server_loadgen(gmc_server *server, const gmc_key *const *pks, const gmc_key *const *sks, int npairs,
                        double rate, double seconds, double enc_fraction, unsigned long long seed, double *out);
 void gmc_server_destroy(gmc_server *server);

@@ -93,6 +93,7 @@ def lib():
         L.gmc_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.gmc_tc_f8_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
         L.gmc_server_latency_ms.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+        L.gmc_server_worst_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gmc_tune_set_launch.argtypes = [ctypes.c_int] * 5
         L.gmc_tune_get_launch.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 4
         vp = ctypes.c_void_p
@@ -329,7 +330,17 @@ class Server:
         res = dict(zip(self.LOADGEN, list(out)))
         res["p999_ms"] = self.latency_ms(0.999)
         res["max_ms"] = self.latency_ms(1.0)
+        res["worst_batch"] = self.worst_batch()
         return res
+
+    WORST = ("latency_ms", "queue_wait_ms", "take_ms", "group_ms", "stage_copy_ms", "issue_ms", "device_ms",
+             "scatter_ms", "batches", "batches_over_5ms")
+
+    def worst_batch(self):
+        """The batch whose oldest request waited longest since the last reset, split by stage (ms)."""
+        out = (ctypes.c_double * 10)()
+        _check(lib().gmc_server_worst_batch(self._h, out), "gmc_server_worst_batch")
+        return dict(zip(self.WORST, list(out)))
 
     def latency_ms(self, q):
         """q-quantile (0 < q <= 1) of the request latencies recorded since the last reset, in ms."""

@@ -66,14 +66,14 @@ struct Req {
 };
 
 struct Piece {  // one request inside a batch
-  Req r;
+  const Req *r;                  // in the slot's incoming requests, which live as long as the batch
   size_t out_k, out_ct, out_rc;  // offsets in the slot's output staging
 };
 
 struct Pipe {
   int set, kind, pc;  // pc: plaintext-confirmation keys (ciphertext C0 || C1)
   std::vector<const gmc_key *> keys;
-  std::vector<std::vector<int>> members;  // piece indices per key
+  std::vector<const std::vector<int> *> members;  // piece indices per key (the slot's member lists)
   Segs segs;
   size_t in_off, k_off, ct_off, rc_off, work_off;
 };
@@ -90,10 +90,16 @@ struct Slot {
   size_t h_in_bytes = 0, h_out_bytes = 0;
   std::vector<Piece> pieces;
   std::vector<Pipe> pipes;
-  std::vector<Req> incoming;  // requests moved out of the queue for the next batch
+  std::deque<Req> incoming;  // the requests of the batch being formed or in flight (moved out of the queue)
+  // per-key member lists of a batch, kept from batch to batch so their storage is reused (a deque: the
+  // lists keep their addresses while more are added)
+  std::deque<std::vector<int>> member_pool;
   size_t in_used = 0, out_used = 0;
   bool busy = false;
   struct gmc_server *srv = nullptr;
+  // stage times of the batch in flight (seconds, now_s clock): the oldest request's arrival, requests taken
+  // from the queue, batch formed (inputs gathered), launches issued, device work and copies done (callback)
+  double t_oldest = 0, t_take = 0, t_taken = 0, t_bucketed = 0, t_formed = 0, t_issued = 0, t_done = 0;
 };
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
@@ -210,6 +216,9 @@ struct gmc_server {
   std::vector<long long> hist = std::vector<long long>(kBuckets, 0);
   long long completed = 0, batches = 0, batched_requests = 0, errors = 0;
   double t_first = 0, t_last = 0;
+  // the batch whose oldest request waited longest (arrival to results), by stage, and batches over 5 ms
+  double worst[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long slow_batches = 0;
   std::string last_error;
 };
 
@@ -300,6 +309,7 @@ cudaError_t run_pipe(Slot &sl, Pipe &pp, cudaStream_t pst) {
 void CUDART_CB on_batch_done(void *arg) {
   Slot *sl = (Slot *)arg;
   gmc_server *srv = sl->srv;
+  sl->t_done = now_s();
   {
     std::lock_guard<std::mutex> lk(srv->done_mu);
     srv->done_q.push_back(sl);
@@ -320,12 +330,13 @@ void complete_batch(Slot *sl) {
     std::vector<long long> &h = local[next_part.fetch_add(1) % parts];
     for (size_t i = b; i < e; i++) {
       Piece &pc = sl->pieces[i];
-      memcpy(pc.r.k, sl->h_out + pc.out_k, 32);
-      if (pc.r.key->kind == 0) {
-        memcpy(pc.r.ct, sl->h_out + pc.out_ct, ct_len(pc.r.key->set, pc.r.key->pc));
-        if (pc.r.rc) *pc.r.rc = pc.r.key->pad_bad ? -1 : 0;
-      } else if (pc.r.rc) {
-        memcpy(pc.r.rc, sl->h_out + pc.out_rc, 4);
+      const Req &r = *pc.r;
+      memcpy(r.k, sl->h_out + pc.out_k, 32);
+      if (r.key->kind == 0) {
+        memcpy(r.ct, sl->h_out + pc.out_ct, ct_len(r.key->set, r.key->pc));
+        if (r.rc) *r.rc = r.key->pad_bad ? -1 : 0;
+      } else if (r.rc) {
+        memcpy(r.rc, sl->h_out + pc.out_rc, 4);
       }
     }
     const double t = now_s();  // this piece's results are in place
@@ -333,12 +344,12 @@ void complete_batch(Slot *sl) {
     int last_b = 0;
     for (size_t i = b; i < e; i++) {
       Piece &pc = sl->pieces[i];
-      if (pc.r.t_arrive != last_t) {  // requests of a batch often share their bucket
-        last_t = pc.r.t_arrive;
+      if (pc.r->t_arrive != last_t) {  // requests of a batch often share their bucket
+        last_t = pc.r->t_arrive;
         last_b = bucket_of((t - last_t) * 1e3);
       }
       h[last_b]++;
-      if (pc.r.done) pc.r.done->store(1, std::memory_order_release);
+      if (pc.r->done) pc.r->done->store(1, std::memory_order_release);
     }
   });
   const double t = now_s();
@@ -347,6 +358,18 @@ void complete_batch(Slot *sl) {
     for (int b = 0; b < kBuckets; b++) srv->hist[b] += h[b];
   srv->completed += (long long)sl->pieces.size();
   srv->t_last = t;
+  const double lat = (t - sl->t_oldest) * 1e3;
+  if (lat > 5.0) srv->slow_batches++;
+  if (lat > srv->worst[0]) {
+    srv->worst[0] = lat;
+    srv->worst[1] = (sl->t_take - sl->t_oldest) * 1e3;      // waiting in the queue (no free slot yet)
+    srv->worst[2] = (sl->t_taken - sl->t_take) * 1e3;       // moving the requests out of the queue
+    srv->worst[3] = (sl->t_bucketed - sl->t_taken) * 1e3;   // grouping them by key, admission, layout
+    srv->worst[4] = (sl->t_formed - sl->t_bucketed) * 1e3;  // copying the inputs into pinned staging
+    srv->worst[5] = (sl->t_issued - sl->t_formed) * 1e3;    // issuing copies and kernels
+    srv->worst[6] = (sl->t_done - sl->t_issued) * 1e3;      // device work, copies and the callback
+    srv->worst[7] = (t - sl->t_done) * 1e3;                 // scattering the results
+  }
   sl->busy = false;
   srv->cv.notify_all();
 }
@@ -397,7 +420,14 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   sl.pipes.clear();
   struct KeyAcc {
     const gmc_key *key;
-    std::vector<int> members;
+    std::vector<int> *members;  // from the slot's pool
+  };
+  size_t pool_used = 0;
+  auto member_list = [&]() {
+    if (pool_used == sl.member_pool.size()) sl.member_pool.emplace_back();
+    std::vector<int> *v = &sl.member_pool[pool_used++];
+    v->clear();
+    return v;
   };
   struct Acc {
     std::vector<KeyAcc> keys;
@@ -407,8 +437,8 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   Acc by[GMC_NSETS][2][2];  // [set][op][pc]
   size_t in_b = 0, out_b = 0, dev_need = 0;
   size_t taken = 0;
-  for (; taken < sl.incoming.size(); taken++) {
-    const Req &r = sl.incoming[taken];
+  for (auto it = sl.incoming.cbegin(); it != sl.incoming.cend(); ++it, taken++) {
+    const Req &r = *it;
     const int kind = r.key->kind, set = r.key->set, pc = r.key->pc ? 1 : 0;
     Acc &acc = by[set][kind][pc];
     int ki = acc.last;
@@ -420,7 +450,7 @@ bool form_batch(gmc_server *srv, Slot &sl) {
           break;
         }
     }
-    const size_t cnt = ki < 0 ? 0 : acc.keys[ki].members.size();
+    const size_t cnt = ki < 0 ? 0 : acc.keys[ki].members->size();
     if (cnt % kGemmOpPad == 0) {  // a new padded block of rows (or a new key): re-check the admission
       if (ki < 0 && acc.keys.size() >= (size_t)kMaxSegs) break;  // one pipeline per (set, op)
       const long long rows_new = acc.rows + kGemmOpPad;
@@ -433,19 +463,21 @@ bool form_batch(gmc_server *srv, Slot &sl) {
       in_b = in_new;
       out_b = out_new;
       if (ki < 0) {
-        acc.keys.push_back({r.key, {}});
+        acc.keys.push_back({r.key, member_list()});
         ki = (int)acc.keys.size() - 1;
       }
     }
     acc.last = ki;
-    acc.keys[ki].members.push_back((int)sl.pieces.size());
-    sl.pieces.push_back({r, 0, 0, 0});
+    acc.keys[ki].members->push_back((int)sl.pieces.size());
+    sl.pieces.push_back({&r, 0, 0, 0});
   }
   if (taken < sl.incoming.size()) {  // what did not fit waits for the next batch, in order
-    std::lock_guard<std::mutex> lk(srv->mu);
-    for (size_t i = sl.incoming.size(); i-- > taken;) srv->queue.push_front(sl.incoming[i]);
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      for (size_t i = sl.incoming.size(); i-- > taken;) srv->queue.push_front(sl.incoming[i]);
+    }
+    sl.incoming.resize(taken);  // the pieces point at the requests kept (the front of the deque)
   }
-  sl.incoming.clear();
   if (sl.pieces.empty()) return false;
   // device layout: [inputs of all pipes][outputs of all pipes][work of each pipe]
   size_t off = 0;
@@ -462,10 +494,10 @@ bool form_batch(gmc_server *srv, Slot &sl) {
         long long row = 0;
         for (auto &kk : acc.keys) {
           pp.segs.row0[pp.keys.size()] = row;
-          pp.segs.nreq[pp.keys.size()] = (long long)kk.members.size();
-          row += (long long)((kk.members.size() + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad;
+          pp.segs.nreq[pp.keys.size()] = (long long)kk.members->size();
+          row += (long long)((kk.members->size() + kGemmOpPad - 1) / kGemmOpPad) * kGemmOpPad;
           pp.keys.push_back(kk.key);
-          pp.members.push_back(std::move(kk.members));
+          pp.members.push_back(kk.members);
         }
         pp.segs.nseg = (int)pp.keys.size();
         pp.segs.row0[pp.keys.size()] = row;
@@ -491,10 +523,11 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   if (sl.in_used > sl.h_in_bytes || sl.out_used > sl.h_out_bytes || off > sl.dev_bytes) {
     // cannot happen when the admission above holds; never write past the buffers
     std::lock_guard<std::mutex> lk(srv->mu);
-    for (size_t i = sl.pieces.size(); i-- > 0;) srv->queue.push_front(sl.pieces[i].r);
+    for (size_t i = sl.pieces.size(); i-- > 0;) srv->queue.push_front(*sl.pieces[i].r);
     sl.pieces.clear();
     return false;
   }
+  sl.t_bucketed = now_s();
   // gather inputs into pinned staging, mirroring the device input layout: one
   // parallel pass over the batch's (pipeline, key) segments laid end to end
   // (a pass per segment left the many small segments of a mixed batch on the
@@ -509,7 +542,7 @@ bool form_batch(gmc_server *srv, Slot &sl) {
   for (auto &pp : sl.pipes)
     for (size_t sg = 0; sg < pp.keys.size(); sg++) {
       segs.push_back({&pp, (int)sg, total});
-      total += pp.members[sg].size();
+      total += pp.members[sg]->size();
     }
   parallel_for(total, [&](size_t b, size_t e) {
     // the segment holding flat index b, then walk forward
@@ -523,9 +556,9 @@ bool form_batch(gmc_server *srv, Slot &sl) {
       const size_t ctb = ct_len(pp.set, pp.pc);
       const size_t inb = pp.kind == 0 ? 32 : ctb;
       const size_t j = f - sr.first;
-      Piece &pc = sl.pieces[pp.members[sr.sg][j]];
+      Piece &pc = sl.pieces[(*pp.members[sr.sg])[j]];
       const long long row = pp.segs.row0[sr.sg] + (long long)j;
-      memcpy(sl.h_in + pp.in_off + row * inb, pc.r.in, inb);
+      memcpy(sl.h_in + pp.in_off + row * inb, pc.r->in, inb);
       pc.out_k = pp.k_off - sl.in_used + row * 32;
       pc.out_ct = pp.ct_off - sl.in_used + row * ctb;
       pc.out_rc = pp.rc_off - sl.in_used + row * 4;
@@ -553,10 +586,19 @@ void dispatcher_main(gmc_server *srv) {
     Slot &sl = *free_slot;
     sl.busy = true;  // reserved while its batch is formed outside the lock
     const size_t take = std::min(srv->queue.size(), (size_t)srv->max_batch);
-    sl.incoming.assign(srv->queue.begin(), srv->queue.begin() + (long)take);
-    srv->queue.erase(srv->queue.begin(), srv->queue.begin() + (long)take);
+    sl.t_take = now_s();
+    sl.t_oldest = srv->queue.front().t_arrive;  // first in, first out: the batch's oldest request
+    sl.incoming.clear();  // the slot's previous batch is complete
+    if (take == srv->queue.size()) {
+      sl.incoming.swap(srv->queue);  // the whole queue: no copy under the lock
+    } else {
+      sl.incoming.assign(srv->queue.begin(), srv->queue.begin() + (long)take);
+      srv->queue.erase(srv->queue.begin(), srv->queue.begin() + (long)take);
+    }
+    sl.t_taken = now_s();
     lk.unlock();
     const bool formed = form_batch(srv, sl);
+    sl.t_formed = now_s();
     lk.lock();
     if (!formed) {  // the head request does not fit an empty slot: reject it
       sl.busy = false;
@@ -594,6 +636,7 @@ void dispatcher_main(gmc_server *srv) {
       step = "output copy";
       e = cudaMemcpyAsync(sl.h_out, sl.dev + sl.in_used, sl.out_used, cudaMemcpyDeviceToHost, sl.st);
     }
+    sl.t_issued = now_s();
     if (e == cudaSuccess) {
       step = "completion callback";
       e = cudaLaunchHostFunc(sl.st, on_batch_done, &sl);
@@ -603,7 +646,7 @@ void dispatcher_main(gmc_server *srv) {
       srv->errors += (long long)sl.pieces.size();
       srv->last_error = std::string(step) + ": " + cudaGetErrorString(e);
       for (auto &pc : sl.pieces)
-        if (pc.r.done) pc.r.done->store(-1);
+        if (pc.r->done) pc.r->done->store(-1);
       sl.busy = false;
     }
   }
@@ -782,11 +825,22 @@ extern "C" int gmc_server_latency_ms(gmc_server *s, double q, double *ms) {
   return GMC_OK;
 }
 
+extern "C" int gmc_server_worst_batch(gmc_server *s, double *out /* [10] */) {
+  if (!s || !out) return srv_fail(GMC_EINVAL, "gmc_server_worst_batch: bad argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (int i = 0; i < 8; i++) out[i] = s->worst[i];
+  out[8] = (double)s->batches;
+  out[9] = (double)s->slow_batches;
+  return GMC_OK;
+}
+
 extern "C" int gmc_server_reset_stats(gmc_server *s) {
   if (!s) return srv_fail(GMC_EINVAL, "gmc_server_reset_stats: bad argument");
   std::lock_guard<std::mutex> lk(s->mu);
   std::fill(s->hist.begin(), s->hist.end(), 0);
   s->completed = s->batches = s->batched_requests = s->errors = 0;
+  std::fill(s->worst, s->worst + 8, 0.0);
+  s->slow_batches = 0;
   s->t_first = s->t_last = 0;
   return GMC_OK;
 }
