@@ -506,7 +506,7 @@ def n_sweep(gmc, torch, dev, set_name, ns, steps, flip=0.10):
     return out
 
 
-def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops, fp8_mac_peak):
+def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops, fp8_mac_peak, b1_mac_peak=None):
     """The encapsulation syndrome c[0:mt] = e[0:mt] ^ T e[mt:n] of n requests with each engine, from the
     engine's per-kernel events: the GF(2) GEMM (mt x k bits times k x n) for the CUDA-core, legacy b1 mma and
     tcgen05 engines, and for the sparse engine the sampler time it adds over the sampler alone.
@@ -554,6 +554,9 @@ def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops, fp8
     for name in ("popc", "b1mma", "tc"):
         ms = times[name]["enc_syndrome_gemm"]
         e = {"ms": ms, "bit_macs_per_s": macs / (ms / 1e3)}
+        if name == "b1mma" and b1_mac_peak:
+            e["b1mma_peak_bit_macs_per_s"] = b1_mac_peak
+            e["frac_of_measured_b1mma_peak"] = macs / (ms / 1e3) / b1_mac_peak
         if name == "tc":
             tf = 2.0 * macs / (ms / 1e3) / 1e12
             e["fp8_equivalent_tflops"] = tf
@@ -840,7 +843,8 @@ def main():
                            "ops_s": n_sweep(gmc, torch, dev, "348864", [256], 20, args.flip)["256"]}
     if rank == 0 and not args.no_engines:
         fp8_peak = gmc.tc_f8_peak()
-        line["syndrome_engines"] = [syndrome_engines(gmc, torch, dev, L, s_, 65536, 5, tc_peak, fp8_peak)
+        b1_peak = gmc.b1mma_peak()
+        line["syndrome_engines"] = [syndrome_engines(gmc, torch, dev, L, s_, 65536, 5, tc_peak, fp8_peak, b1_peak)
                                     for s_ in dict.fromkeys(("348864", args.set))]
         # the decapsulation front end on the tcgen05 engine (the step's GEMM) against the same measured peak
         fe = kernels.get("dec_front_gemm")

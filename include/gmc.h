@@ -322,6 +322,10 @@ int gmc_int32_peak(double *lop3_per_s, double *shf_per_s);
  * multiply-accumulates per second on the current device (the denominator of
  * the engine's tensor-pipe fraction). */
 int gmc_tc_f8_peak(double *mac_per_s);
+/* Measured rate of the legacy 1-bit tensor instruction the GMC_GEMM_B1MMA
+ * engine issues (mma.sync m8n8k128 .b1 AND.POPC, register operands): bit
+ * multiply-accumulates per second on the current device. */
+int gmc_b1mma_peak(double *mac_per_s);
 
 /* Stage outputs of a decapsulation batch (device pointers): the 2t packed
  * syndromes (s_words per request), the error vectors (e_words per request)

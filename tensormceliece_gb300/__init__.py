@@ -92,6 +92,7 @@ def lib():
                                    ctypes.POINTER(ctypes.c_int)]
         L.gmc_int32_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         L.gmc_tc_f8_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        L.gmc_b1mma_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
         L.gmc_server_latency_ms.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
         L.gmc_server_worst_batch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.gmc_tune_set_launch.argtypes = [ctypes.c_int] * 5
@@ -467,6 +468,13 @@ def set_dec_constant_time(on):
 
 def get_dec_constant_time():
     return bool(lib().gmc_get_dec_constant_time())
+
+
+def b1mma_peak():
+    """Measured bit-MACs per second of mma.sync m8n8k128 .b1 AND.POPC with register operands."""
+    a = ctypes.c_double()
+    _check(lib().gmc_b1mma_peak(ctypes.byref(a)), "gmc_b1mma_peak")
+    return a.value
 
 
 def tc_f8_peak():

@@ -93,6 +93,8 @@ size_t tc_a8_bytes(int rows_pad, int kw_pad);
 // measured MMA rate of the engine's tcgen05 instruction (FP8 E4M3, M = 128, N = 256, K = 32), MACs per second;
 // err_dev: a device word set to 1 if a bounded wait expired
 cudaError_t time_tc_f8_peak(double *mac_per_s, int *err_dev, cudaStream_t st);
+// measured rate of the legacy mma.sync m8n8k128 .b1 AND.POPC (register operands), bit-MACs per second
+cudaError_t time_b1_peak(double *mac_per_s, int *out_dev, cudaStream_t st);
 cudaError_t launch_expand_a(const uint32_t *A, int lda, int rows_pad, int kw_pad, uint8_t *A8, cudaStream_t st);
 cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_pad, const uint32_t *X, int ldx,
                                int kw_pad, uint32_t *Out, int ldo, int out_words, int *err, cudaStream_t st);

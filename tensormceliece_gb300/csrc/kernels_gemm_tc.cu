@@ -531,6 +531,56 @@ __global__ void __launch_bounds__(128) gf2_gemm_b1(const GemmKeys keys, const Se
   if (op < live_end && wd < out_words) Out[op * ldo + wd] = words[warp][lane];
 }
 
+// The rate of the legacy 1-bit MMA on this GPU: every warp runs 8 independent
+// accumulator chains of mma.sync m8n8k128 .b1 AND.POPC on register operands
+// (no memory traffic), 8 blocks of 256 threads per SM. The denominator of the
+// b1 engine's fraction.
+constexpr int kB1Chains = 8;
+__global__ void __launch_bounds__(256) b1_peak_kernel(int iters, uint32_t salt, int *__restrict__ out) {
+  int acc[kB1Chains][2];
+#pragma unroll
+  for (int c = 0; c < kB1Chains; c++) acc[c][0] = acc[c][1] = 0;
+  const uint32_t a = (threadIdx.x * 2654435761u) ^ salt, b = (blockIdx.x * 40503u) ^ (salt >> 3);
+#pragma unroll 1
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int c = 0; c < kB1Chains; c++)
+      asm volatile("mma.sync.aligned.m8n8k128.row.col.s32.b1.b1.s32.and.popc {%0,%1}, {%2}, {%3}, {%0,%1};"
+                   : "+r"(acc[c][0]), "+r"(acc[c][1])
+                   : "r"(a ^ (uint32_t)c), "r"(b));
+  }
+  int x = 0;
+#pragma unroll
+  for (int c = 0; c < kB1Chains; c++) x ^= acc[c][0] ^ acc[c][1];
+  if (x == 0x7fffffff) out[0] = x;  // keeps the chains live; practically never stored
+}
+
+cudaError_t time_b1_peak(double *mac_per_s, int *out_dev, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int blocks = 8 * sms, iters = 2048;
+  float best = 0;
+  for (int rep = 0; rep < 5 && e == cudaSuccess; rep++) {
+    cudaEventRecord(e0, st);
+    b1_peak_kernel<<<blocks, 256, 0, st>>>(iters, 0x9e3779b9u + rep, out_dev);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (rep >= 1 && (best == 0 || t < best)) best = t;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return e;
+  *mac_per_s = (double)blocks * 8 /* warps */ * iters * kB1Chains * 8.0 * 8.0 * 128.0 / (best * 1e-3);
+  return cudaSuccess;
+}
+
 cudaError_t launch_gf2_gemm_b1(const GemmKeys &keys, const Segs &segs, int lda, int rows_pad, const uint32_t *X,
                                int ldx, int kw_pad, uint32_t *Out, int ldo, int out_words, cudaStream_t st) {
   const long long rows = seg_rows(segs);

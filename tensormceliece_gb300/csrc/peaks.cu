@@ -106,6 +106,27 @@ extern "C" int gmc_tc_f8_peak(double *mac_per_s) {
   return GMC_OK;
 }
 
+// The legacy 1-bit tensor path's rate: mma.sync m8n8k128 .b1 AND.POPC with
+// register operands, in bit multiply-accumulates per second.
+extern "C" int gmc_b1mma_peak(double *mac_per_s) {
+  if (!mac_per_s) {
+    set_last_error("gmc_b1mma_peak: null output");
+    return GMC_EINVAL;
+  }
+  int *out = nullptr;
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = time_b1_peak(mac_per_s, out, st);
+  if (st) cudaStreamDestroy(st);
+  if (out) cudaFree(out);
+  if (e != cudaSuccess) {
+    set_last_error((std::string("gmc_b1mma_peak: ") + cudaGetErrorString(e)).c_str());
+    return GMC_ECUDA;
+  }
+  return GMC_OK;
+}
+
 extern "C" int gmc_int32_peak(double *lop3_per_s, double *shf_per_s) {
   if (!lop3_per_s || !shf_per_s) {
     set_last_error("gmc_int32_peak: null output");

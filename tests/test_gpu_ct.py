@@ -141,3 +141,36 @@ def test_ct_switch(gmc):
     assert gmc.get_dec_constant_time() is True
     gmc.set_dec_constant_time(False)
     assert gmc.lib().gmc_set_dec_constant_time(2) == -1
+
+
+def test_ct_serving_loop(gmc, keys):
+    """Decapsulations served under the switch (several keys and sets in one batch, the keys' first-t syndrome
+    matrices built on their first constant-time batch) equal the table form's results."""
+    import ctypes
+    srv = gmc.Server(max_batch=4096, slots=2, mem_fraction=0.1)
+    items = []
+    for sid in (0, 3, 4, 9):
+        pk, sk = keys(sid % 5)
+        S = gmc.SecretKey(sid, sk)
+        srv.add_key(S)
+        oc, _, _ = O.enc_batch(sid, pk, request_seeds(sid % 5, 40, b"ct-srv"), threads=THREADS)
+        cts, _ = flipped_and_random(sid, oc, frac=0.2, nrand=4, seed=9)
+        k_tab, rc_tab = S.dec_batch(cts)
+        items += [(S, cts[i].copy(), k_tab[i], rc_tab[i]) for i in range(len(cts))]
+    n = len(items)
+    k_out = np.zeros((n, 32), np.uint8)
+    rc_out = np.full(n, 7, np.int32)
+    done = np.zeros(n, np.int32)
+    gmc.set_dec_constant_time(True)
+    try:
+        for j, (S, c, _, _) in enumerate(items):
+            srv.submit(S, c.ctypes.data_as(ctypes.c_void_p), None, ctypes.c_void_p(k_out.ctypes.data + 32 * j),
+                       ctypes.c_void_p(rc_out.ctypes.data + 4 * j), ctypes.c_void_p(done.ctypes.data + 4 * j))
+        srv.drain(120)
+    finally:
+        gmc.set_dec_constant_time(False)
+    st = srv.stats()
+    srv.close()
+    assert (done == 1).all(), st["last_error"]
+    for j, (_, _, k_tab, rc_tab) in enumerate(items):
+        assert (k_out[j] == k_tab).all() and rc_out[j] == rc_tab, j

@@ -103,5 +103,9 @@ def test_poisson_loadgen(gmc, pairs):
         plist.append((P, S))
     r = srv.loadgen(plist, rate=20000.0, seconds=1.0, seed=9)
     assert r["submitted"] > 10000 and r["completed"] == r["submitted"]
-    assert 0 < r["p50_ms"] <= r["p99_ms"]
+    assert 0 < r["p50_ms"] <= r["p99_ms"] <= r["p999_ms"] <= r["max_ms"]
+    w = r["worst_batch"]  # the slowest batch and its stages (all non-negative, summing to its latency)
+    parts = ("queue_wait_ms", "take_ms", "group_ms", "stage_copy_ms", "issue_ms", "device_ms", "scatter_ms")
+    assert w["batches"] > 0 and all(w[p_] >= 0 for p_ in parts)
+    assert abs(sum(w[p_] for p_ in parts) - w["latency_ms"]) < 0.05 * w["latency_ms"] + 0.01
     srv.close()
