@@ -299,7 +299,8 @@ int gmc_get_dec_constant_time(void);
  * The launch shape is tuned with them: the tcgen05 GEMM's pipeline depth
  * (gemm_stages 2..4 A/X buffers per CTA, default 4) and the requests per block
  * of the decoding kernels (bm_warps: Berlekamp-Massey warps of 32 requests,
- * root_warps: root-finding warps of one request; 1..8, default 8) and the
+ * 1..14, default 14, the constant-time form using at most 8; root_warps:
+ * root-finding warps of one request, 1..8, default 8) and the
  * pipelined sampler's resident warps per SM (sample_sm_warps, 0 = as many as
  * fit, the default); gmc_tune_set_launch / gmc_tune_get_launch set and read
  * them by hand. */

@@ -46,7 +46,7 @@ struct SetTune {
   int dec_engine = GEMM_TC;   // GF(2) GEMM engine of the decapsulation front end
   int sample_threads = 128;   // sampler block size (32, 64 or 128)
   int gemm_stages = 4;        // tcgen05 GEMM pipeline depth (2, 3 or 4 A/X buffers per CTA)
-  int bm_warps = 8;           // Berlekamp-Massey (bit-sliced form) warps per block: 32 requests each
+  int bm_warps = kBMWarps;    // Berlekamp-Massey (bit-sliced form) warps per block: 32 requests each
   int root_warps = 8;         // root-finding warps per block: one request each
   int sample_sm_warps = 0;    // pipelined sampler: resident warps per SM (0 = as many as fit)
   int tuned = 0;              // 1 when measured on this device

@@ -12,7 +12,8 @@ constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parame
 // 65536-request launch as 6-7 blocks per SM (128-thread blocks: 3-4, so a
 // third of the SMs carried a block more than the rest)
 constexpr int kTailThreads = 64;
-constexpr int kBMWarps = 8;     // Berlekamp-Massey kernel: default and largest warps per block (32 requests per warp)
+constexpr int kBMWarps = 14;    // Berlekamp-Massey kernel: default and largest warps per block (32 requests per warp)
+constexpr int kBMCtWarps = 8;   // its constant-time form: largest warps per block
 constexpr int kBMLatWarps = 24;  // Berlekamp-Massey latency form: warps per block (one request per warp)
 constexpr long long kBMBitslicedMinRows = 24576;  // smaller batches take the latency form
 constexpr int kRootWarps = 8;  // root-finding kernel: default and largest warps per block
@@ -167,7 +168,8 @@ cudaError_t launch_pack_ct(const uint8_t *C, const Segs &segs, uint32_t *X, int 
 // Berlekamp-Massey: S2 (2t packed syndromes) -> Sig [N][2^fft_d] u16, the
 // error locator's coefficients by degree (the leading x^t term is implicit
 // when t = 2^fft_d).
-// warps: warps per block of the bit-sliced form (1..kBMWarps; 0 = kBMWarps).
+// warps: warps per block of the bit-sliced form (1..kBMWarps; 0 = kBMWarps;
+// the constant-time form takes at most kBMCtWarps).
 // ct: the constant-time form (inversion-free, no tables, slot bounds from the
 // iteration alone; the same locators).
 template <int SET>

@@ -68,19 +68,29 @@ __global__ void pack_ct_kernel(const uint8_t *__restrict__ C, const Segs segs, u
 // deg B <= n+1-L, so the discrepancy needs i <= min(L, t) and the update
 // i <= min(max(L, n+1-L), t). Rows that are not live run with zero
 // syndromes (d = 0) and write nothing.
+// Shared memory per warp is what fourteen warps per SM can hold (one round
+// for 2048 groups on 152 SMs): iteration n reads s_{n-t} .. s_n only, so the
+// syndromes sit in a ring of t+1 entries, filled one syndrome per iteration
+// (its global load issued an iteration ahead); B keeps coefficients 0..t
+// (reads above t are zero); the exponent table keeps the q-1 entries the
+// division indexes. Lanes above deg C in an active discrepancy slot read
+// ring entries of other iterations: C_i = 0 there (coefficients above t are
+// never updated), so they add nothing.
 template <int SET>
 struct BMLayout {
   using p = P<SET>;
   static constexpr int Q = p::q, T = p::t, M = p::m;
   static constexpr int NS = (T + 1 + 31) / 32;
-  static constexpr int exp_off = 0, log_off = 2 * Q;           // u16 tables
-  static constexpr int zero_off = (3 * Q) / 2, zero_len = 16;   // u32: M zero planes (s_j, j < 0)
+  static constexpr int R = T + 1;                              // syndrome ring entries
+  static constexpr int exp_off = 0, log_off = Q;               // u16 tables (exp: indexes 0..q-2)
+  static constexpr int zero_off = Q, zero_len = 16;            // u32: M zero planes (s_j, j < 0)
   static constexpr int shared_u32 = zero_off + zero_len;
-  static constexpr int s_words = 2 * T * M;                    // syndrome planes [j][b]
-  static constexpr int b_words = (32 * NS + 1) * M;            // B planes [i][b]
+  static constexpr int s_words = R * M;                        // syndrome planes [j mod R][b]
+  static constexpr int b_words = (T + 1) * M;                  // B planes [i][b], i <= t
   static constexpr int warp_u32 = s_words + b_words;
   static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
-  static_assert(32 * NS * M <= s_words, "C planes are staged in the syndrome area");
+  static_assert(32 * NS * M <= warp_u32, "C planes are staged in the warp's area");
+  static_assert(2 * T <= 2 * R, "ring index j - R for j < 2t");
 };
 
 // acc (2M-1 planes, unreduced) -> r (M planes) mod the field polynomial
@@ -109,13 +119,13 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
   using p = P<SET>;
   using LY = BMLayout<SET>;
   constexpr int M = p::m, Q = p::q, T = p::t, D = p::fft_d;
-  constexpr int NS = LY::NS;
+  constexpr int NS = LY::NS, R = LY::R;
   constexpr int SIG = 1 << D;
   static_assert(M == 12 || M == 13, "field polynomial");
   extern __shared__ __align__(16) uint32_t bsm[];
   uint16_t *gexp = reinterpret_cast<uint16_t *>(bsm) + LY::exp_off;
   uint16_t *glog = reinterpret_cast<uint16_t *>(bsm) + LY::log_off;
-  for (int i = threadIdx.x; i < 2 * Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
+  for (int i = threadIdx.x; i < Q - 1; i += blockDim.x) gexp[i] = fd.gexp[i];
   for (int i = threadIdx.x; i < Q; i += blockDim.x) glog[i] = fd.glog[i];
   for (int i = threadIdx.x; i < LY::zero_len; i += blockDim.x) bsm[LY::zero_off + i] = 0u;
   __syncthreads();
@@ -134,24 +144,28 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
     const long long op = g * 32 + lane;
     int seg;
     const bool live = op < N && seg_live(segs, op, &seg);
-    // syndromes -> planes (lane b < M stores plane b of s_j)
     const uint32_t *srow = S2 + op * lds2;
-#pragma unroll 1
-    for (int j = 0; j < 2 * T; j++) {
+    // this lane's request's s_j (low M bits; 0 past the live rows)
+    auto synd = [&](int j) -> uint32_t {
       uint32_t v = 0;
       if (live) {
         const int bb = j * M, w = bb >> 5, sh = bb & 31;
         v = srow[w] >> sh;
         if (sh + M > 32) v |= srow[w + 1] << (32 - sh);
       }
+      return v;
+    };
+    // one syndrome of all 32 requests -> M planes in ring entry e (lane b < M stores plane b)
+    auto to_ring = [&](uint32_t v, int e) {
       uint32_t mine = 0;
 #pragma unroll
       for (int b = 0; b < M; b++) {
         const uint32_t pl = __ballot_sync(0xffffffffu, (v >> b) & 1u);
         mine = (lane == b) ? pl : mine;
       }
-      if (lane < M) SP[j * M + lane] = mine;
-    }
+      if (lane < M) SP[e * M + lane] = mine;
+    };
+    to_ring(synd(0), 0);
     // C = 1, B = x
     uint32_t C[NS][M];
 #pragma unroll
@@ -163,6 +177,7 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
     int L = 0, lb = 0;  // this lane's request: LFSR length, log b
 #pragma unroll 1
     for (int n = 0; n < 2 * T; n++) {
+      const uint32_t s_next = n + 1 < 2 * T ? synd(n + 1) : 0u;  // consumed at the end of the iteration
       const int Lc = L < T ? L : T;
       int Lu = (L > n + 1 - L) ? L : n + 1 - L;
       Lu = Lu < T ? Lu : T;
@@ -177,8 +192,8 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
 #pragma unroll
         for (int k = 0; k < NS; k++) {
           if (32 * k <= bd) {
-            const int j = n - lane - 32 * k;  // s_j, j < 0 reads the zero planes
-            const uint32_t *sp = j >= 0 ? SP + j * M : ZP;
+            const int j = n - lane - 32 * k;  // s_j (ring entry j mod R), j < 0 reads the zero planes
+            const uint32_t *sp = j >= 0 ? SP + (j >= R ? j - R : j) * M : ZP;
 #pragma unroll
             for (int b2 = 0; b2 < M; b2++) {
               const uint32_t sv = sp[b2];
@@ -222,9 +237,9 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
           const uint32_t *bp = BP + i * M;
           uint32_t bi[M];
 #pragma unroll
-          for (int b = 0; b < M; b++) bi[b] = bp[b];
+          for (int b = 0; b < M; b++) bi[b] = i <= T ? bp[b] : 0u;
           __syncwarp();  // every lane holds its B_i before B_{i+1} is replaced
-          const bool in = (k < NS - 1) || (i <= T);  // coefficients above t stay zero
+          const bool in = i <= T;  // coefficients above t stay zero
           uint32_t r[M];
           if (anyf) {
             // r = f * B_i, Horner over the planes of f
@@ -261,6 +276,8 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
         }
       }
       if (lane < M) BP[lane] = 0;  // B_0 of x * (...) is zero
+      // s_{n+1} replaces s_{n-t}, the oldest entry (read above, before the update's warp barriers)
+      if (n + 1 < 2 * T) to_ring(s_next, n + 1 >= R ? n + 1 - R : n + 1);
       __syncwarp();
     }
     // sigma(x) = sum_deg C[t-deg] x^deg -> FFT coefficient slots (deg < 2^d);
@@ -378,19 +395,28 @@ __device__ __forceinline__ void bs_inv(uint32_t (&r)[M], const uint32_t (&a)[M])
 //    (C_0 = 1) exactly.
 // The update decisions stay per-request masks (ballots), L is selected, never
 // branched on.
+// Shared memory: M zero planes, then per warp all 2t syndromes as planes and
+// B over the 32 NS + 1 coefficient positions the slot loops address (the
+// form needs about twice the registers of the table form, so it runs at
+// kBMCtWarps warps per SM, where this layout fits).
 template <int SET>
 struct BMCtLayout {
-  using LY = BMLayout<SET>;
-  static constexpr int zero_len = LY::zero_len;  // u32: zero planes first, then the warps' areas
-  static constexpr int warp_u32 = LY::warp_u32;
+  using p = P<SET>;
+  static constexpr int T = p::t, M = p::m;
+  static constexpr int NS = (T + 1 + 31) / 32;
+  static constexpr int zero_len = 16;                 // u32: zero planes first, then the warps' areas
+  static constexpr int s_words = 2 * T * M;           // syndrome planes [j][b]
+  static constexpr int b_words = (32 * NS + 1) * M;   // B planes [i][b]
+  static constexpr int warp_u32 = s_words + b_words;
   static constexpr int bytes(int warps) { return zero_len * 4 + warps * warp_u32 * 4; }
+  static_assert(32 * NS * M <= s_words, "C planes are staged in the syndrome area");
 };
 
 template <int SET>
-__global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_ct_kernel(const uint32_t *__restrict__ S2, int lds2,
-                                                                     const Segs segs, uint16_t *__restrict__ Sig) {
+__global__ void __launch_bounds__(kBMCtWarps * 32, 1) dec_bm_ct_kernel(const uint32_t *__restrict__ S2, int lds2,
+                                                                       const Segs segs, uint16_t *__restrict__ Sig) {
   using p = P<SET>;
-  using LY = BMLayout<SET>;
+  using LY = BMCtLayout<SET>;
   constexpr int M = p::m, T = p::t, D = p::fft_d;
   constexpr int NS = LY::NS;
   constexpr int SIG = 1 << D;
@@ -1240,6 +1266,18 @@ static int persistent_blocks(K kernel, int threads, int smem, long long work_ite
   return (int)(blocks < need ? blocks : need);
 }
 
+// Warps per block of the bit-sliced forms: at most `warps`, and no more than
+// the groups of 32 requests need to spread over every SM (1024 groups take 7
+// warps on 147 SMs, not 14 on 74).
+static int bm_block_warps(long long N, int warps) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms < 1) return warps;
+  const long long per_sm = ((N + 31) / 32 + sms - 1) / sms;
+  return per_sm < warps ? (int)(per_sm > 0 ? per_sm : 1) : warps;
+}
+
 template <int SET>
 cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs &segs, uint16_t *Sig,
                           cudaStream_t st, int warps, bool ct) {
@@ -1248,9 +1286,10 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
   if (warps < 0 || warps > kBMWarps) return cudaErrorInvalidValue;
   if (warps == 0) warps = kBMWarps;
   if (ct) {  // constant-time form, every batch size
+    warps = bm_block_warps(N, warps < kBMCtWarps ? warps : kBMCtWarps);
     const int smem_ct = BMCtLayout<SET>::bytes(warps);
     cudaError_t err = cudaFuncSetAttribute(dec_bm_ct_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           BMCtLayout<SET>::bytes(kBMWarps));
+                                           BMCtLayout<SET>::bytes(kBMCtWarps));
     if (err != cudaSuccess) return err;
     const int gb = persistent_blocks(dec_bm_ct_kernel<SET>, warps * 32, smem_ct, (N + 31) / 32, warps);
     dec_bm_ct_kernel<SET><<<gb, warps * 32, smem_ct, st>>>(S2, lds2, segs, Sig);
@@ -1265,6 +1304,7 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
     dec_bm_lat_kernel<SET><<<gl, kBMLatWarps * 32, smem_l, st>>>(S2, lds2, fd, segs, Sig);
     return cudaGetLastError();
   }
+  warps = bm_block_warps(N, warps);
   const int smem_bm = BMLayout<SET>::bytes(warps);
   cudaError_t err = cudaFuncSetAttribute(dec_bm_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          BMLayout<SET>::bytes(kBMWarps));

@@ -295,15 +295,16 @@ extern "C" int gmc_autotune(int set, long long n, const char *cache_path) {
       rc |= gmc_enc_batch_dev(P, ct, key, seeds, n, nullptr, st);  // the ciphertexts the dec timings read
     }
     // requests per block of the decoding kernels
-    const int warp_cand[3] = {8, 4, 2};
+    const int bm_cand[3] = {kBMWarps, 8, 4};
+    const int warp_cand[3] = {kRootWarps, 4, 2};
     if (n >= kBMBitslicedMinRows)
       for (int wi = 1; wi < 3; wi++) {
         SetTune t = best;
-        t.bm_warps = warp_cand[wi];
+        t.bm_warps = bm_cand[wi];
         const float ms = time_dec(t);
         if (ms < 0.99f * best_dec) {
           best_dec = ms;
-          best.bm_warps = warp_cand[wi];
+          best.bm_warps = bm_cand[wi];
         }
       }
     for (int wi = 1; wi < 3; wi++) {

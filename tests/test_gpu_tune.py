@@ -28,7 +28,7 @@ def test_autotune_cache_roundtrip(gmc, keys, tmp_path):
     data = json.load(open(path))
     entry = data["sets"]["348864"]
     assert entry["enc_engine"] == cfg["enc_engine"]
-    assert entry["gemm_stages"] in (2, 3, 4) and entry["root_warps"] in (2, 4, 8) and entry["bm_warps"] == 8
+    assert entry["gemm_stages"] in (2, 3, 4) and entry["root_warps"] in (2, 4, 8) and entry["bm_warps"] == 14
     assert entry["sample_sm_warps"] in (0, 8, 16)
     gmc.tune_set(0, "popc", "popc", 32, gemm_stages=2, bm_warps=1, root_warps=1, sample_sm_warps=4)
     assert gmc.autotune_load(path) == 1
@@ -70,7 +70,7 @@ def test_launch_shapes(gmc, keys, sid):
     n = 24576 + 77
     seeds = request_seeds(sid, n, b"shapes")
     try:
-        gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=4, bm_warps=8, root_warps=8,
+        gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=4, bm_warps=14, root_warps=8,
                      sample_sm_warps=0)
         P, S = gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)
         c, k, rc = P.enc_batch(seeds)
@@ -80,7 +80,7 @@ def test_launch_shapes(gmc, keys, sid):
         bad[::5, 3] ^= 0x21
         kd, rcd = S.dec_batch(bad)
         assert (kd[1::5] == k[1::5]).all()
-        for stages, bw, rw, sw in ((2, 4, 2, 8), (3, 2, 4, 16), (4, 1, 1, 4)):
+        for stages, bw, rw, sw in ((2, 8, 2, 8), (3, 5, 4, 16), (4, 1, 1, 4)):
             gmc.tune_set(sid, "tc", "tc", prev["sample_threads"], gemm_stages=stages, bm_warps=bw, root_warps=rw,
                          sample_sm_warps=sw)
             c2, k2, rc2 = P.enc_batch(seeds)

@@ -143,9 +143,9 @@ def test_tune_cache_load_on_host(tmp_path):
         b = gmc.tune_get("8192128")
         # no sparse front end for decapsulation; invalid shapes take the defaults
         assert b["dec_engine"] == "tc" and b["sample_threads"] == 128
-        assert (b["sample_sm_warps"], b["gemm_stages"], b["bm_warps"], b["root_warps"]) == (0, 4, 8, 8)
+        assert (b["sample_sm_warps"], b["gemm_stages"], b["bm_warps"], b["root_warps"]) == (0, 4, 14, 8)
         for s, t in before.items():
             assert gmc.tune_get(s) == t
     finally:
         for s in ("348864", "8192128"):
-            gmc.tune_set(s, "sparse", "tc", 128, gemm_stages=4, bm_warps=8, root_warps=8, sample_sm_warps=0)
+            gmc.tune_set(s, "sparse", "tc", 128, gemm_stages=4, bm_warps=14, root_warps=8, sample_sm_warps=0)
