@@ -769,9 +769,9 @@ struct RootLayout {
   static constexpr int fhbs_off = abs_off + abs_len, fhbs_len = NH * M;
   static constexpr int shared_u32 = fhbs_off + fhbs_len;
   static constexpr int ewp = (p::ew + 1) & ~1;
-  // per warp (u32): e words | roots [t] (pos << 16 | element) | count
-  static constexpr int roots_off = ewp, cnt_off = roots_off + p::t;
-  static constexpr int warp_u32 = cnt_off + 2;
+  // per warp (u32): e words | roots [t] (element, then pos << 16 | element)
+  static constexpr int roots_off = ewp;
+  static constexpr int warp_u32 = (roots_off + p::t + 1) & ~1;
   static constexpr int bytes(int warps) { return shared_u32 * 4 + warps * warp_u32 * 4; }
 };
 
@@ -914,7 +914,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   constexpr int NW = (p::n + 31) / 32;
   constexpr int VPL = SIG / 32;  // chunk slots per lane
   constexpr int LOGV = (VPL == 4) ? 2 : 1;
-  static_assert(VPL == (1 << LOGV) && (LY::NC % 32) == 0, "chunk geometry");
+  static_assert(VPL == (1 << LOGV) && NH == 2, "chunk geometry: 64 chunks, two halves of 32");
   static_assert(M == 12 || M == 13, "field polynomial");
   extern __shared__ __align__(16) uint32_t rsm[];
   uint16_t *sh16 = reinterpret_cast<uint16_t *>(rsm);
@@ -941,7 +941,6 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
   uint32_t *wbase = rsm + LY::shared_u32 + warp * LY::warp_u32;
   uint32_t *esm = wbase;
   uint32_t *roots = wbase + LY::roots_off;
-  uint32_t *cnt = wbase + LY::cnt_off;
 
   const long long N = seg_rows(segs);
   const int nwb = blockDim.x >> 5;  // warps per block (a launch parameter up to kRootWarps)
@@ -952,7 +951,6 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     const DecKeyDev &key = keys.k[seg];
     const uint16_t *sig = Sig + op * SIG;
     for (int w = lane; w < NW; w += 32) esm[w] = 0;
-    if (lane == 0) *cnt = 0;
     // top-down, in registers: lane holds the coefficient slots x = lane + 32 j
     // (j < VPL): twist by the level's first basis element, then radix-convert
     // g(x) = g0(x^2+x) + x g1(x^2+x) on the 2^l interleaved sub-polynomials
@@ -976,7 +974,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
 #pragma unroll 1
       for (int pb = D - 2; pb >= l; pb--) radix_step<VPL>(vv, pb, lane);
     }
-    __syncwarp();  // esm and cnt cleared before the root stores below
+    __syncwarp();  // esm cleared before the root stores below
     // leaves in the bottom-up pass's slot order (chunk_slot at level D - 1)
     uint32_t leaf[VPL];
     if constexpr (VPL == 4) {  // slot = lane | j1 << 5 | j0 << 6
@@ -989,8 +987,11 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
       for (int j = 0; j < VPL; j++) leaf[j] = vv[j];
     }
 
-    int weight = 0;
     uint32_t zm0[VPL], zm1[VPL];  // constant-time form: the zero masks of both chunk halves
+    // table form: the roots, listed per half as found. sigma is monic of
+    // degree t, so it has at most t zeros; each lane writes its own at an
+    // offset from a warp prefix sum of the counts (shared memory only)
+    int nfound = 0;
 #pragma unroll 1
     for (int h = 0; h < NH; h++) {
       uint32_t v[VPL][M];
@@ -1070,20 +1071,25 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
         }
         continue;
       }
+      int mine = 0;
+#pragma unroll
+      for (int j = 0; j < VPL; j++) mine += __popc(zero[j]);
+      int incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+      }
+      int off = nfound + incl - mine;
+      nfound += __shfl_sync(0xffffffffu, incl, 31);
 #pragma unroll
       for (int j = 0; j < VPL; j++) {
         uint32_t z = zero[j];
         while (z) {
           const int k = __ffs(z) - 1;
           z &= z - 1;
-          const int elt = ((32 * h + k) << D) | chunk_slot<D>(-1, lane, j);
-          const uint32_t pos = key.invL[elt];
-          if (pos < (uint32_t)p::n) {
-            weight++;
-            atomicOr(&esm[pos >> 5], 1u << (pos & 31));
-            const uint32_t slot = atomicAdd(cnt, 1u);
-            if (slot < (uint32_t)T) roots[slot] = (pos << 16) | (uint32_t)elt;
-          }
+          if (off < T) roots[off] = (uint32_t)(((32 * h + k) << D) | chunk_slot<D>(-1, lane, j));
+          off++;
         }
       }
     }
@@ -1092,7 +1098,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
       // network: word w holds y[32 w + i] = zero(alpha) for alpha = bitrev_m(32 w + i), i.e. the slot
       // bitrev_d(w >> 1) of the chunks 2 bitrev_5(i) + (w & 1). Lane and register j hold that slot's zero
       // masks over all 64 chunks: every other bit, compacted, with its 5-bit index reversed.
-      static_assert(NH == 2 && M - D == 6, "64 chunks of 2^d slots");
+      static_assert(M - D == 6, "64 chunks of 2^d slots");
       uint32_t *erow = E + op * lde;
 #pragma unroll
       for (int j = 0; j < VPL; j++) {
@@ -1108,6 +1114,29 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
       __syncwarp();
       continue;
     }
+    // code positions of the listed roots: independent loads, lane r taking
+    // entries r, r + 32, ...
+    constexpr int NSC = (T + 31) / 32;
+    const int nroots = nfound < T ? nfound : T;
+    __syncwarp();
+    int weight = 0;
+    {
+      uint32_t pos[NSC];
+#pragma unroll
+      for (int k = 0; k < NSC; k++) {
+        const int r = lane + 32 * k;
+        pos[k] = r < nroots ? key.invL[roots[r]] : 0xFFFFu;
+      }
+#pragma unroll
+      for (int k = 0; k < NSC; k++) {
+        const int r = lane + 32 * k;
+        if (r < nroots && pos[k] < (uint32_t)p::n) {
+          weight++;
+          atomicOr(&esm[pos[k] >> 5], 1u << (pos[k] & 31));
+          roots[r] |= pos[k] << 16;
+        }
+      }
+    }
     weight = __reduce_add_sync(0xffffffffu, weight);
     __syncwarp();
 
@@ -1122,41 +1151,39 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
     bool ok = (weight == T) && !long_lfsr;
     if (ok) {
       // first t syndromes of the found error: XOR of the key's columns at the
-      // t positions (lane l takes roots l, l+32, ...; 16-byte loads), then one
-      // XOR reduction per word, compared with the received words
-      constexpr int NSC = (T + 31) / 32;
+      // t positions (then every root is in the support and in the list). Each
+      // half-warp reads whole rows, lane c of a half the 16-byte chunk c, so a
+      // load instruction covers two rows contiguously; the halves are added by
+      // one shuffle and compared with the received words.
       constexpr int TW = (T * M + 31) / 32;
       constexpr int TW4 = (TW + 3) / 4;
-      uint4 acc[TW4];
-#pragma unroll
-      for (int w = 0; w < TW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
-#pragma unroll
-      for (int k = 0; k < NSC; k++) {
-        const int r = lane + 32 * k;
-        if (r < T) {
-          const uint4 *col = reinterpret_cast<const uint4 *>(key.HT + (size_t)(roots[r] >> 16) * key.ldh);
-#pragma unroll
-          for (int w = 0; w < TW4; w++) {
-            const uint4 v = col[w];
-            acc[w].x ^= v.x;
-            acc[w].y ^= v.y;
-            acc[w].z ^= v.z;
-            acc[w].w ^= v.w;
-          }
+      static_assert(TW4 <= 16, "a row of the first t syndromes fits half a warp of 16-byte chunks");
+      const int c = lane & 15;
+      uint4 acc = make_uint4(0, 0, 0, 0);
+      if (c < TW4) {
+#pragma unroll 8
+        for (int r = lane >> 4; r < T; r += 2) {
+          const uint4 v = reinterpret_cast<const uint4 *>(key.HT + (size_t)(roots[r] >> 16) * key.ldh)[c];
+          acc.x ^= v.x;
+          acc.y ^= v.y;
+          acc.z ^= v.z;
+          acc.w ^= v.w;
         }
       }
-      const uint32_t *srow = S2 + op * lds2;
+      acc.x ^= __shfl_xor_sync(0xffffffffu, acc.x, 16);
+      acc.y ^= __shfl_xor_sync(0xffffffffu, acc.y, 16);
+      acc.z ^= __shfl_xor_sync(0xffffffffu, acc.z, 16);
+      acc.w ^= __shfl_xor_sync(0xffffffffu, acc.w, 16);
       uint32_t mism = 0;
-#pragma unroll
-      for (int w = 0; w < TW4; w++) {
-        const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
+      if (lane < TW4) {
+        const uint32_t *srow = S2 + op * lds2;
+        const uint32_t q4[4] = {acc.x, acc.y, acc.z, acc.w};
 #pragma unroll
         for (int e2 = 0; e2 < 4; e2++) {
-          const int word = 4 * w + e2;
+          const int word = 4 * lane + e2;
           if (word < TW) {
-            const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
             const uint32_t msk = (word == TW - 1 && (T * M) % 32) ? ((1u << ((T * M) % 32)) - 1u) : 0xFFFFFFFFu;
-            if ((word & 31) == lane) mism |= (v ^ srow[word]) & msk;
+            mism |= (q4[e2] ^ srow[word]) & msk;
           }
         }
       }
