@@ -35,46 +35,39 @@ namespace gmc {
 // words are cleared.
 // S row = T e[mt:n]: XOR of the columns of TT (row j = column j of T, row k
 // zero) at the request's t positions; positions < mt read the zero row.
-// Lane l takes positions l, l + 32, ... (16-byte loads, all in flight at
-// once), then one XOR reduction across the warp per syndrome word.
+// Each half-warp reads whole rows, lane c of a half the 16-byte chunk c, so a
+// load instruction covers two rows contiguously (positions 2i and 2i + 1);
+// the halves are added by one shuffle and lane c stores words 4c .. 4c + 3.
 template <int SET, typename PosFn>
 __device__ __forceinline__ void sparse_syndrome_row(PosFn pos_of, const uint32_t *__restrict__ TT, int ldtt,
                                                     uint32_t *__restrict__ srow, int lane) {
   using p = P<SET>;
-  constexpr int NCW = (p::t + 31) / 32, MW4 = (p::mw + 3) / 4;
-  uint4 acc[MW4];
-#pragma unroll
-  for (int w = 0; w < MW4; w++) acc[w] = make_uint4(0, 0, 0, 0);
-#pragma unroll
-  for (int i = 0; i < NCW; i++) {
-    const int c = lane + 32 * i;
-    const int pos = c < p::t ? pos_of(c) : 0;
-    const uint4 *col = reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * ldtt);
-#pragma unroll
-    for (int w = 0; w < MW4; w++) {
-      const uint4 v = col[w];
-      acc[w].x ^= v.x;
-      acc[w].y ^= v.y;
-      acc[w].z ^= v.z;
-      acc[w].w ^= v.w;
+  constexpr int MW4 = (p::mw + 3) / 4;
+  static_assert(MW4 <= 16, "a syndrome row fits half a warp of 16-byte chunks");
+  const int c = lane & 15;
+  uint4 acc = make_uint4(0, 0, 0, 0);
+  if (c < MW4) {
+#pragma unroll 8
+    for (int i = lane >> 4; i < p::t; i += 2) {
+      const int pos = pos_of(i);
+      const uint4 v =
+          reinterpret_cast<const uint4 *>(TT + (size_t)(pos >= p::mt ? pos - p::mt : p::k) * ldtt)[c];
+      acc.x ^= v.x;
+      acc.y ^= v.y;
+      acc.z ^= v.z;
+      acc.w ^= v.w;
     }
   }
-  uint32_t my0 = 0, my1 = 0;
+  acc.x ^= __shfl_xor_sync(0xffffffffu, acc.x, 16);
+  acc.y ^= __shfl_xor_sync(0xffffffffu, acc.y, 16);
+  acc.z ^= __shfl_xor_sync(0xffffffffu, acc.z, 16);
+  acc.w ^= __shfl_xor_sync(0xffffffffu, acc.w, 16);
+  if (lane < MW4) {
+    const uint32_t q4[4] = {acc.x, acc.y, acc.z, acc.w};
 #pragma unroll
-  for (int w = 0; w < MW4; w++) {
-    const uint32_t q4[4] = {acc[w].x, acc[w].y, acc[w].z, acc[w].w};
-#pragma unroll
-    for (int e2 = 0; e2 < 4; e2++) {
-      const int word = 4 * w + e2;
-      if (word < p::mw) {
-        const uint32_t v = __reduce_xor_sync(0xffffffffu, q4[e2]);
-        if (word < 32) my0 = (lane == word) ? v : my0;
-        else my1 = (lane == word - 32) ? v : my1;
-      }
-    }
+    for (int e2 = 0; e2 < 4; e2++)
+      if (4 * lane + e2 < p::mw) srow[4 * lane + e2] = q4[e2];
   }
-  if (lane < p::mw) srow[lane] = my0;
-  if (p::mw > 32 && lane + 32 < p::mw) srow[lane + 32] = my1;
 }
 
 template <int SET>
