@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="seconds per serving load level (60 = the "
                     "full serving configuration)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the N = 256..65536 throughput sweep")
+    ap.add_argument("--no-per-set", action="store_true", help="skip the per-set enc/s and dec/s at N = 65536")
     ap.add_argument("--no-engines", action="store_true", help="skip the syndrome-engine comparison")
     ap.add_argument("--no-keygen", action="store_true", help="skip the batched key-generation measurement")
     ap.add_argument("--no-ct", action="store_true", help="skip the constant-time decapsulation measurement")
@@ -506,6 +507,56 @@ def n_sweep(gmc, torch, dev, set_name, ns, steps, flip=0.10):
     return out
 
 
+def per_set(gmc, torch, dev, n, steps, flip=0.10):
+    """Encapsulations/s and decapsulations/s of every parameter set at N requests, each operation timed on its own
+    (device-resident inputs, L2 flushed between launches, CUDA events), the form in which the reference's GPU harness
+    reports its engines (N / mean launch time)."""
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device=dev)
+    out = {}
+    for set_name in gmc.SETS:
+        sid = gmc.set_id(set_name)
+        z = gmc.set_sizes(sid)
+        pk, sk = gmc.keypair(sid, bytes([0x3C]) * 32)
+        P, S = gmc.PublicKey(sid, pk), gmc.SecretKey(sid, sk)
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(7)
+        seeds = torch.randint(0, 256, (n, 32), dtype=torch.uint8, device=dev, generator=gen)
+        c = torch.empty((n, z["ct_bytes"]), dtype=torch.uint8, device=dev)
+        k = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+        kd = torch.empty((n, 32), dtype=torch.uint8, device=dev)
+        P.enc_batch_dev(c.data_ptr(), k.data_ptr(), seeds.data_ptr(), n, 0, st)
+        cts = c.clone()
+        nflip = int(flip * n)
+        if nflip:
+            rng = np.random.default_rng(n)
+            idx = torch.from_numpy(rng.choice(n, nflip, replace=False)).to(dev)
+            bits = torch.from_numpy(rng.integers(0, z["mt"], nflip)).to(dev)
+            cts[idx, bits // 8] ^= (1 << (bits % 8)).to(torch.uint8)
+
+        def timed(fn):
+            for _ in range(3):
+                fn()
+            ms = []
+            for i in range(steps):
+                flush.fill_(i)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            return sum(ms) / len(ms)
+
+        enc_ms = timed(lambda: P.enc_batch_dev(c.data_ptr(), k.data_ptr(), seeds.data_ptr(), n, 0, st))
+        dec_ms = timed(lambda: S.dec_batch_dev(kd.data_ptr(), cts.data_ptr(), n, 0, st))
+        out[set_name] = {"enc_ops_s": n / (enc_ms / 1e3), "dec_ops_s": n / (dec_ms / 1e3), "enc_ms": enc_ms,
+                         "dec_ms": dec_ms}
+        del P, S, seeds, c, k, kd, cts
+    return out
+
+
 def syndrome_engines(gmc, torch, dev, L, set_name, n, steps, tc_peak_tflops, fp8_mac_peak, b1_mac_peak=None):
     """The encapsulation syndrome c[0:mt] = e[0:mt] ^ T e[mt:n] of n requests with each engine, from the
     engine's per-kernel events: the GF(2) GEMM (mt x k bits times k x n) for the CUDA-core, legacy b1 mma and
@@ -841,6 +892,9 @@ def main():
         # config 1: mceliece348864, one key, 256 encapsulations + 256 decapsulations per step
         line["config1"] = {"set": "348864", "n": 256, "flip": args.flip,
                            "ops_s": n_sweep(gmc, torch, dev, "348864", [256], 20, args.flip)["256"]}
+    if rank == 0 and not args.no_per_set:
+        # every parameter set at 65536 requests, enc and dec timed separately (the reference GPU harness's form)
+        line["per_set_n65536"] = per_set(gmc, torch, dev, 65536, 5, args.flip)
     if rank == 0 and not args.no_engines:
         fp8_peak = gmc.tc_f8_peak()
         b1_peak = gmc.b1mma_peak()
