@@ -272,10 +272,12 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
             if (in) C[k][b] = cold ^ r[b];
             if (i + 1 <= T) bq[b] = (U & cold) | (~U & bi[b]);
           }
-          __syncwarp();
+          // no barrier before the next (lower) slot: its reads, B_{32(k-1)} ..
+          // B_{32k-1}, miss this slot's writes, B_{32k+1} .. B_{32k+32}, and
+          // its writes follow its own barrier above, after this slot's reads
         }
       }
-      if (lane < M) BP[lane] = 0;  // B_0 of x * (...) is zero
+      if (lane < M) BP[lane] = 0;  // B_0 of x * (...) is zero (slot 0 read it before its barrier)
       // s_{n+1} replaces s_{n-t}, the oldest entry (read above, before the update's warp barriers)
       if (n + 1 < 2 * T) to_ring(s_next, n + 1 >= R ? n + 1 - R : n + 1);
       __syncwarp();
