@@ -4,8 +4,8 @@
 // e4m3 (key bits 0x00 / 0x38 = 1.0, request bits 0x00 / 0x01 = 2^-9) through
 // tcgen05.mma .kind::f8f6f4 with FP32 accumulators in tensor memory. Sums of
 // products are integer counts <= K (at most 6656 here) times 2^-9, exact in
-// FP32, so parity = (int)(acc * 2^9) & 1. (.kind::i8 is not available on
-// sm_103a.)
+// FP32, so parity = the last mantissa bit of acc * 2^9 + 2^23 (K < 2^23).
+// (.kind::i8 is not available on sm_103a.)
 //   A (key matrix, fixed per key) is pre-expanded once into FP8 tiles laid
 //   out exactly as the shared-memory image of one pipeline stage, so a stage
 //   is one cp.async.bulk (TMA engine) completing on an mbarrier.
@@ -321,7 +321,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
         uint32_t mine = 0;
 #pragma unroll
         for (int j = 0; j < 32; j++) {
-          const uint32_t par = (uint32_t)__float2int_rz(__uint_as_float(r[j]) * kTcXScale) & 1u;
+          // acc * 2^9 + 2^23 = count + 2^23 exactly (count <= 6656 < 2^23): the
+          // float's last mantissa bit is the count's parity, no conversion needed
+          const uint32_t par = __float_as_uint(__fmaf_rn(__uint_as_float(r[j]), kTcXScale, 8388608.0f)) & 1u;
           const uint32_t word = __ballot_sync(0xffffffffu, par);
           if (lane == j) mine = word;
         }
