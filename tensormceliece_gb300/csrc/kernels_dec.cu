@@ -1163,7 +1163,7 @@ __global__ void __launch_bounds__(kRootWarps * 32, 2) dec_root_kernel(const uint
       const int c = lane & 15;
       uint4 acc = make_uint4(0, 0, 0, 0);
       if (c < TW4) {
-#pragma unroll 8
+#pragma unroll 16
         for (int r = lane >> 4; r < T; r += 2) {
           const uint4 v = reinterpret_cast<const uint4 *>(key.HT + (size_t)(roots[r] >> 16) * key.ldh)[c];
           acc.x ^= v.x;
