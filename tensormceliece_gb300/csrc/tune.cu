@@ -10,8 +10,9 @@
 // decapsulation front end (CUDA-core popcount or tcgen05); the tcgen05 GEMM's
 // pipeline depth (2, 3 or 4 A/X stages per CTA, when either op uses that
 // engine); and the requests per block of the two decoding kernels
-// (Berlekamp-Massey: 2, 4 or 8 warps of 32 requests, timed only when the batch
-// takes its bit-sliced form; root finding: 2, 4 or 8 warps of one request).
+// (Berlekamp-Massey: at most 14, 8 or 4 warps of 32 requests per block, fewer
+// when the groups spread over every SM with fewer, timed only when the batch
+// takes its bit-sliced form; root finding: 8, 4 or 2 warps of one request).
 // The GEMM tile is fixed at 128 x 256 (one tcgen05 M=128 instruction shape
 // and a TMEM accumulator pair) and K is never split: every CTA owns whole
 // output tiles, so there is no split-K reduction to tune. A later candidate
