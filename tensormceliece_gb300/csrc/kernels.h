@@ -14,7 +14,7 @@ constexpr int kSampleThreadsMax = 128;  // sampler block size is a launch parame
 constexpr int kTailThreads = 64;
 constexpr int kBMWarps = 14;    // Berlekamp-Massey kernel: default and largest warps per block (32 requests per warp)
 constexpr int kBMCtWarps = 8;   // its constant-time form: largest warps per block
-constexpr int kBMLatWarps = 24;  // Berlekamp-Massey latency form: warps per block (one request per warp)
+constexpr int kBMLatWarps = 28;  // Berlekamp-Massey latency form: largest warps per block (one request per warp)
 constexpr long long kBMBitslicedMinRows = 24576;  // smaller batches take the latency form
 constexpr int kRootWarps = 8;  // root-finding kernel: default and largest warps per block
 

@@ -641,8 +641,9 @@ __global__ void __launch_bounds__(kBMLatWarps * 32, 2) dec_bm_lat_kernel(const u
   for (int i = lane; i < LY::bguard; i += 32) wsm[LY::b_off + i] = (uint16_t)ZL;
   __syncthreads();
   const long long N = seg_rows(segs);
-  const long long nwarps = (long long)gridDim.x * kBMLatWarps;
-  for (long long op = (long long)blockIdx.x * kBMLatWarps + warp; op < N; op += nwarps) {
+  const int nwb = blockDim.x >> 5;  // warps per block (a launch parameter up to kBMLatWarps)
+  const long long nwarps = (long long)gridDim.x * nwb;
+  for (long long op = (long long)blockIdx.x * nwb + warp; op < N; op += nwarps) {
     int seg;
     if (!seg_live(segs, op, &seg)) continue;  // warp-uniform
     const uint32_t *srow = S2 + op * lds2;
@@ -1325,12 +1326,20 @@ cudaError_t launch_dec_bm(const uint32_t *S2, int lds2, FieldDev fd, const Segs 
     return cudaGetLastError();
   }
   if (N < kBMBitslicedMinRows) {  // small batch: warp per request (lower latency per request)
-    const int smem_l = BMLatLayout<SET>::bytes(kBMLatWarps);
-    cudaError_t err =
-        cudaFuncSetAttribute(dec_bm_lat_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_l);
+    // warps per block: the requests in one round over two blocks per SM when
+    // they fit (8192 requests: 27 warps on 304 blocks, where fixed 24-warp
+    // blocks left 896 requests for a second round), else kBMLatWarps
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long per_block = sms > 0 ? (N + 2LL * sms - 1) / (2LL * sms) : kBMLatWarps;
+    const int lw = per_block < kBMLatWarps ? (per_block > 0 ? (int)per_block : 1) : kBMLatWarps;
+    const int smem_l = BMLatLayout<SET>::bytes(lw);
+    cudaError_t err = cudaFuncSetAttribute(dec_bm_lat_kernel<SET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           BMLatLayout<SET>::bytes(kBMLatWarps));
     if (err != cudaSuccess) return err;
-    const int gl = persistent_blocks(dec_bm_lat_kernel<SET>, kBMLatWarps * 32, smem_l, N, kBMLatWarps);
-    dec_bm_lat_kernel<SET><<<gl, kBMLatWarps * 32, smem_l, st>>>(S2, lds2, fd, segs, Sig);
+    const int gl = persistent_blocks(dec_bm_lat_kernel<SET>, lw * 32, smem_l, N, lw);
+    dec_bm_lat_kernel<SET><<<gl, lw * 32, smem_l, st>>>(S2, lds2, fd, segs, Sig);
     return cudaGetLastError();
   }
   warps = bm_block_warps(N, warps);
