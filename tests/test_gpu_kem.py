@@ -240,7 +240,8 @@ def test_full_size_every_request(gmc, keys, sid):
 def test_bm_forms_agree_on_corrupted_batches(gmc, keys, sid):
     """A batch large enough for the bit-sliced Berlekamp-Massey (>= 24576 rows) and the same ciphertexts in
     small batches (warp-per-request form) give identical keys and return codes, on valid, single-bit-flipped
-    and random ciphertexts; an oracle sample of each kind agrees."""
+    and random ciphertexts; an oracle sample of each kind agrees. The small batches take every block shape of
+    the warp-per-request launch: 1 warp per block, a few, one round of up to 28 warps, several rounds."""
     pk, sk = keys(sid)
     n = 32768
     rng = np.random.default_rng(7 + sid)
@@ -249,7 +250,9 @@ def test_bm_forms_agree_on_corrupted_batches(gmc, keys, sid):
     cts, flipped = flipped_and_random(sid, c, frac=0.1, nrand=256, seed=3)
     key = gmc.SecretKey(sid, sk)
     k_big, rc_big = key.dec_batch(cts)
-    parts = [key.dec_batch(cts[i:i + 4096]) for i in range(0, len(cts), 4096)]
+    cuts = np.cumsum([0, 1, 300, 4096, 9000])
+    bounds = list(zip(cuts, list(cuts[1:]) + [len(cts)]))
+    parts = [key.dec_batch(cts[a:b]) for a, b in bounds]
     k_small = np.concatenate([p[0] for p in parts])
     rc_small = np.concatenate([p[1] for p in parts])
     assert (k_big == k_small).all() and (rc_big == rc_small).all()
