@@ -140,20 +140,33 @@ __device__ __forceinline__ uint32_t expand4_x(uint32_t v) { return (v * 0x002040
 constexpr float kTcXScale = 512.0f;
 
 // ---------------------------------------------------------------- tcgen05 engine
-// Persistent: one CTA per SM walks the (m-tile, n-tile) list. The stage ring
-// runs on across tiles, and the FP32 accumulator is double-buffered in tensor
-// memory (2 x 256 columns), so the epilogue of one tile overlaps the MMAs of
-// the next. Warp roles: the first TC_EXP_WARPS expand X stages, the next
-// issues the A bulk copies, the next issues the MMAs, the last four drain
-// accumulators (warp w reads TMEM lanes 32 (w % 4) .. +31).
+// Persistent: one CTA per SM walks the (request tile, key tile) list. The MMA
+// is D[request][key row] = sum_k X[request][k] Key[row][k]: M = 128 requests
+// (the A operand, staged in FP8 by the CUDA cores) by N = 256 key rows (the B
+// operand: two 128-row slices of the key's FP8 image per stage, by bulk copy),
+// so one 16 KB request stage feeds 4 MMAs of 128 x 256 x 32. The request
+// staging is the CUDA-core work around the MMAs; with the requests as the
+// N = 256 side it took twice as much per MMA. The stage ring runs on across
+// tiles, and the FP32 accumulator is double-buffered in tensor memory (2 x 256
+// columns), so the epilogue of one tile overlaps the MMAs of the next.
+// Accumulator lane = request, column = key row: an epilogue thread reads 32
+// columns of its request and packs their parities into one output word.
+// Warp roles: the first TC_EXP_WARPS stage requests, the next issues the key
+// copies, the next issues the MMAs, the last four drain accumulators (warp w
+// reads TMEM lanes 32 (w % 4) .. +31).
+constexpr int TC_REQ = 128;   // requests per tile (MMA M)
+constexpr int TC_KEYN = 256;  // key rows per tile (MMA N): two kTcM-row slices of the key's FP8 image
 constexpr int TC_EXP_WARPS = 8;
 constexpr int TC_THREADS = (TC_EXP_WARPS + 2 + 4) * 32;  // expanders, producer, MMA, 4 epilogue warps
 constexpr int TC_EXP_THREADS = TC_EXP_WARPS * 32;
-constexpr int TC_A_BYTES = kTcM * kTcKB;   // 16 KB per stage
-constexpr int TC_X_BYTES = kTcN * kTcKB;   // 32 KB per stage
-constexpr int tc_smem(int stages) { return stages * (TC_A_BYTES + TC_X_BYTES) + 512; }
-constexpr uint32_t TC_TMEM_COLS = 2 * kTcN;  // two FP32 accumulators of 128 lanes x kTcN columns
-static_assert(kTcN % TC_EXP_THREADS == 0, "whole X rows per expander thread");
+constexpr int TC_A_BYTES = kTcM * kTcKB;    // 16 KB: one 128-row slice of the key image per stage
+constexpr int TC_K_BYTES = 2 * TC_A_BYTES;  // 32 KB: the key stage (N = 256 rows)
+constexpr int TC_X_BYTES = TC_REQ * kTcKB;  // 16 KB: the request stage (M = 128 rows)
+constexpr int tc_smem(int stages) { return stages * (TC_K_BYTES + TC_X_BYTES) + 512; }
+constexpr uint32_t TC_TMEM_COLS = 2 * TC_KEYN;  // two FP32 accumulators of 128 lanes x 256 columns
+static_assert(TC_EXP_THREADS % TC_REQ == 0 && 4 % (TC_EXP_THREADS / TC_REQ) == 0,
+              "expander threads split each request row into equal word ranges");
+static_assert(TC_KEYN == 2 * kTcM, "a key tile is two slices of the FP8 image");
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -161,13 +174,13 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 
 template <int STAGES>
 __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys, const Segs segs, int kstages,
-                                                              int mtiles, long long ntiles,
+                                                              int mtiles, long long rtiles,
                                                               const uint32_t *__restrict__ X, int ldx,
                                                               uint32_t *__restrict__ Out, int ldo, int out_words,
                                                               int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t tsm[];
-  uint8_t *As = tsm;
-  uint8_t *Xs = tsm + STAGES * TC_A_BYTES;
+  uint8_t *Ks = tsm;                        // key stages [STAGES][TC_K_BYTES]
+  uint8_t *Xs = tsm + STAGES * TC_K_BYTES;  // request stages [STAGES][TC_X_BYTES]
   uint64_t *full_a = reinterpret_cast<uint64_t *>(Xs + STAGES * TC_X_BYTES);
   uint64_t *full_x = full_a + STAGES;
   uint64_t *empty = full_x + STAGES;
@@ -179,7 +192,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   int *last_copy = reinterpret_cast<int *>(tmem_slot + 2);  // [STAGES]: last stage copied per buffer
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long ntile_all = (long long)mtiles * ntiles;
+  const int ktiles = (mtiles + 1) >> 1;  // key tiles of 256 rows (the last one half when mtiles is odd)
+  const long long ntile_all = (long long)ktiles * rtiles;
   if (tid == 0) {
     for (int i = 0; i < STAGES; i++) {
       mbar_init(&full_a[i], 1);
@@ -203,68 +217,69 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  constexpr uint32_t idesc = idesc_f8f6f4_e4m3(kTcM, kTcN);
+  constexpr uint32_t idesc = idesc_f8f6f4_e4m3(TC_REQ, TC_KEYN);
 
   if (warp < TC_EXP_WARPS) {
-    // X expanders: thread tid writes whole 128-bit stage rows r = tid + 128 j
-    constexpr int RPT = kTcN / TC_EXP_THREADS;
+    // request stagers: SPLIT threads share each 128-bit stage row; thread tid
+    // takes row r = tid % TC_REQ, request words WPT * part .. + WPT - 1 of the
+    // stage and their 16-bit chunks KCT * part .. + KCT - 1
+    constexpr int SPLIT = TC_EXP_THREADS / TC_REQ;
+    constexpr int WPT = 4 / SPLIT;
+    constexpr int KCT = 8 / SPLIT;
+    const int r = tid % TC_REQ, part = tid / TC_REQ;
     long long g = 0;  // global stage counter of this CTA
     for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x) {
-      const long long op0 = (tile / mtiles) * kTcN;
-      const uint32_t *xrow0 = X + (size_t)(op0 + tid) * ldx;
-      uint4 xnext[RPT];
+      const long long op0 = (tile / ktiles) * TC_REQ;
+      const uint32_t *xrow = X + (size_t)(op0 + r) * ldx + WPT * part;
+      uint32_t xnext[WPT];
 #pragma unroll
-      for (int j = 0; j < RPT; j++)
-        xnext[j] = *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx);
+      for (int w = 0; w < WPT; w++) xnext[w] = xrow[w];
       for (int s = 0; s < kstages; s++, g++) {
         const int buf = (int)(g % STAGES);
         if (g >= STAGES && !mbar_wait(&empty[buf], (uint32_t)(g / STAGES - 1) & 1)) *abort_flag = 1;
         if (*abort_flag) break;
-        uint4 xcur[RPT];
+        uint32_t wv[WPT];
 #pragma unroll
-        for (int j = 0; j < RPT; j++) xcur[j] = xnext[j];
+        for (int w = 0; w < WPT; w++) wv[w] = xnext[w];
         if (s + 1 < kstages) {
 #pragma unroll
-          for (int j = 0; j < RPT; j++)
-            xnext[j] =
-                *reinterpret_cast<const uint4 *>(xrow0 + (size_t)j * TC_EXP_THREADS * ldx + 4 * (s + 1));
+          for (int w = 0; w < WPT; w++) xnext[w] = xrow[4 * (s + 1) + w];
         }
         // request bits -> FP8 core matrices (row r, 16-bit chunk kc at
         // ((r/8)*8 + kc)*128 + (r%8)*16)
-        uint8_t *xb = Xs + buf * TC_X_BYTES;
+        uint8_t *rb = Xs + buf * TC_X_BYTES + (r >> 3) * 1024 + (r & 7) * 16;
 #pragma unroll
-        for (int j = 0; j < RPT; j++) {
-          const int r = tid + j * TC_EXP_THREADS;
-          const uint32_t wv[4] = {xcur[j].x, xcur[j].y, xcur[j].z, xcur[j].w};
-          uint8_t *rb = xb + (r >> 3) * 1024 + (r & 7) * 16;
-#pragma unroll
-          for (int kc = 0; kc < 8; kc++) {
-            const uint32_t bits = (kc & 1) ? (wv[kc >> 1] >> 16) : (wv[kc >> 1] & 0xFFFFu);
-            uint4 v;
-            v.x = expand4_x(bits & 0xFu);
-            v.y = expand4_x((bits >> 4) & 0xFu);
-            v.z = expand4_x((bits >> 8) & 0xFu);
-            v.w = expand4_x((bits >> 12) & 0xFu);
-            *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
-          }
+        for (int c = 0; c < KCT; c++) {
+          const int kc = KCT * part + c;
+          const uint32_t bits = (c & 1) ? (wv[c >> 1] >> 16) : (wv[c >> 1] & 0xFFFFu);
+          uint4 v;
+          v.x = expand4_x(bits & 0xFu);
+          v.y = expand4_x((bits >> 4) & 0xFu);
+          v.z = expand4_x((bits >> 8) & 0xFu);
+          v.w = expand4_x((bits >> 12) & 0xFu);
+          *reinterpret_cast<uint4 *>(rb + kc * 128) = v;
         }
         fence_proxy_async();  // generic-proxy writes visible to the tensor core
         mbar_arrive(&full_x[buf]);
       }
     }
   } else if (warp == TC_EXP_WARPS) {
-    if (lane == 0) {  // A producer: one bulk copy per stage into a free buffer
+    if (lane == 0) {  // key producer: the tile's one or two 128-row slices per stage into a free buffer
       long long g = 0;
       for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x) {
-        const int mtile = (int)(tile % mtiles);
-        const int seg = seg_find(segs, (tile / mtiles) * kTcN);  // a tile never straddles segments
-        const uint8_t *Atile = keys.A8[seg] + (size_t)mtile * kstages * TC_A_BYTES;
+        const int m0 = 2 * (int)(tile % ktiles);
+        const bool two = m0 + 1 < mtiles;
+        const int seg = seg_find(segs, (tile / ktiles) * TC_REQ);  // a tile never straddles segments
+        const uint8_t *A0 = keys.A8[seg] + (size_t)m0 * kstages * TC_A_BYTES;
         for (int s = 0; s < kstages; s++, g++) {
           const int buf = (int)(g % STAGES);
           if (g >= STAGES && !mbar_wait(&empty[buf], (uint32_t)(g / STAGES - 1) & 1)) *abort_flag = 1;
           if (*abort_flag) break;
-          mbar_expect_tx(&full_a[buf], TC_A_BYTES);
-          bulk_g2s(As + buf * TC_A_BYTES, Atile + (size_t)s * TC_A_BYTES, TC_A_BYTES, &full_a[buf]);
+          mbar_expect_tx(&full_a[buf], two ? 2 * TC_A_BYTES : TC_A_BYTES);
+          bulk_g2s(Ks + buf * TC_K_BYTES, A0 + (size_t)s * TC_A_BYTES, TC_A_BYTES, &full_a[buf]);
+          if (two)
+            bulk_g2s(Ks + buf * TC_K_BYTES + TC_A_BYTES, A0 + (size_t)(kstages + s) * TC_A_BYTES, TC_A_BYTES,
+                     &full_a[buf]);
           last_copy[buf] = (int)g;
         }
       }
@@ -279,18 +294,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
         if (i >= 2 && !mbar_wait(&acc_empty[ab], (uint32_t)((i >> 1) - 1) & 1)) *abort_flag = 1;
         if (*abort_flag) break;
         tc_fence_after();
-        const uint32_t dacc = tmem + (uint32_t)(ab * kTcN);
+        const uint32_t dacc = tmem + (uint32_t)(ab * TC_KEYN);
         for (int s = 0; s < kstages; s++, g++) {
           const int buf = (int)(g % STAGES);
           const uint32_t par = (uint32_t)(g / STAGES) & 1;
           if (!mbar_wait(&full_a[buf], par) || !mbar_wait(&full_x[buf], par)) *abort_flag = 1;
           if (*abort_flag) break;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(As + buf * TC_A_BYTES), x0 = smem_u32(Xs + buf * TC_X_BYTES);
+          const uint32_t x0 = smem_u32(Xs + buf * TC_X_BYTES), k0 = smem_u32(Ks + buf * TC_K_BYTES);
 #pragma unroll
           for (int kk = 0; kk < kTcKB / 32; kk++) {
-            const uint64_t ad = smem_desc(a0 + kk * 256, 128, 1024);
-            const uint64_t bd = smem_desc(x0 + kk * 256, 128, 1024);
+            const uint64_t ad = smem_desc(x0 + kk * 256, 128, 1024);  // A: 128 requests
+            const uint64_t bd = smem_desc(k0 + kk * 256, 128, 1024);  // B: 256 key rows
             mma_f8(dacc, ad, bd, idesc, (s > 0 || kk > 0) ? 1u : 0u);
           }
           mma_commit(&empty[buf]);
@@ -301,42 +316,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1) gf2_gemm_tc(const GemmKeys keys
       mma_commit(done);  // arrives once every MMA issued above has completed
     }
   } else {
-    // epilogue: accumulator lanes (rows) 32 (warp % 4) .. +31
+    // epilogue: accumulator lanes 32 (warp % 4) .. +31 = this warp's requests;
+    // lane l packs the parities of its request's 256 key rows into 8 words
     const int quad = warp & 3;
+    const bool vec = (ldo & 3) == 0 && (reinterpret_cast<uintptr_t>(Out) & 15) == 0;
     int i = 0;
     for (long long tile = blockIdx.x; tile < ntile_all && !*abort_flag; tile += gridDim.x, i++) {
       const int ab = i & 1;
       if (!mbar_wait(&acc_full[ab], (uint32_t)(i >> 1) & 1)) *abort_flag = 1;
       if (*abort_flag) break;
       tc_fence_after();
-      const int mtile = (int)(tile % mtiles);
-      const long long op0 = (tile / mtiles) * kTcN;
+      const int kt = (int)(tile % ktiles);
+      const long long op0 = (tile / ktiles) * TC_REQ;
       const int seg = seg_find(segs, op0);
       const long long live_end = segs.row0[seg] + segs.nreq[seg];
+      const long long op = op0 + 32 * quad + lane;
+      const int wd0 = kt * (TC_KEYN / 32);
+      uint32_t *orow = Out + op * ldo + wd0;
+      const bool live = op < live_end, vec_ok = vec && wd0 + TC_KEYN / 32 <= out_words;
+      // two halves of 4 x 32 columns (bounded register use), each stored at once
 #pragma unroll 1
-      for (int cb = 0; cb < kTcN / 32; cb++) {
-        uint32_t r[32];
-        GMC_TMEM_LD32(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(ab * kTcN + 32 * cb), r);
-        tmem_ld_wait();
-        uint32_t mine = 0;
+      for (int h = 0; h < 2; h++) {
+        uint32_t w4[4];
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          // acc * 2^9 + 2^23 = count + 2^23 exactly (count <= 6656 < 2^23): the
-          // float's last mantissa bit is the count's parity, no conversion needed
-          const uint32_t par = __float_as_uint(__fmaf_rn(__uint_as_float(r[j]), kTcXScale, 8388608.0f)) & 1u;
-          const uint32_t word = __ballot_sync(0xffffffffu, par);
-          if (lane == j) mine = word;
+        for (int c = 0; c < 4; c++) {
+          uint32_t rr[32];
+          GMC_TMEM_LD32(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(ab * TC_KEYN + 32 * (4 * h + c)), rr);
+          tmem_ld_wait();
+          uint32_t w = 0;
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            // acc * 2^9 + 2^23 = count + 2^23 exactly (count <= 6656 < 2^23): the
+            // float's last mantissa bit is the count's parity, no conversion needed
+            w |= (__float_as_uint(__fmaf_rn(__uint_as_float(rr[j]), kTcXScale, 8388608.0f)) & 1u) << j;
+          }
+          w4[c] = w;
         }
-        const long long op = op0 + 32 * cb + lane;
-        const int wd = mtile * (kTcM / 32) + quad;
-        if (op < live_end && wd < out_words) Out[op * ldo + wd] = mine;
+        if (live) {
+          if (vec_ok) {
+            reinterpret_cast<uint4 *>(orow)[h] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+              if (wd0 + 4 * h + c < out_words) orow[4 * h + c] = w4[c];
+          }
+        }
       }
       tc_fence_before();
       mbar_arrive(&acc_empty[ab]);
     }
   }
   __syncthreads();
-  // drain: the MMAs (done barrier) and any A copy still landing
+  // drain: the MMAs (done barrier) and any key copy still landing
   bool ok = mbar_wait(done, 0);
   if (warp == TC_EXP_WARPS && lane == 0) {
     for (int b = 0; b < STAGES; b++)
@@ -385,7 +416,7 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
                                int kw_pad, uint32_t *Out, int ldo, int out_words, int *err, cudaStream_t st) {
   const long long rows = seg_rows(segs);
   if (rows <= 0) return cudaSuccess;
-  if (!err || rows_pad % kTcM || kw_pad % (kTcKB / 32) || rows % kTcN || ldx < kw_pad) return cudaErrorInvalidValue;
+  if (!err || rows_pad % kTcM || kw_pad % (kTcKB / 32) || rows % TC_REQ || ldx < kw_pad) return cudaErrorInvalidValue;
   for (int i = 0; i < segs.nseg; i++)
     if (!keys.A8[i]) return cudaErrorInvalidValue;
   // pipeline depth: the set's tuned stage count (2, 3 or 4 buffers of A and X per CTA)
@@ -398,9 +429,9 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int mtiles = rows_pad / kTcM;
-  const long long ntiles = rows / kTcN, tiles = ntiles * mtiles;
+  const long long rtiles = rows / TC_REQ, tiles = rtiles * ((mtiles + 1) / 2);
   const int grid = (int)(tiles < sms ? tiles : sms);  // persistent: one CTA per SM (smem and TMEM bound)
-  kern<<<grid, TC_THREADS, smem, st>>>(keys, segs, kw_pad / (kTcKB / 32), mtiles, ntiles, X, ldx, Out, ldo,
+  kern<<<grid, TC_THREADS, smem, st>>>(keys, segs, kw_pad / (kTcKB / 32), mtiles, rtiles, X, ldx, Out, ldo,
                                        out_words, err);
   return cudaGetLastError();
 }
@@ -414,15 +445,17 @@ cudaError_t launch_gf2_gemm_tc(const GemmKeys &keys, const Segs &segs, int rows_
 // commit; every thread waits (bounded) for it. The denominator of the GEMM's
 // tensor-pipe fraction.
 constexpr int TCP_THREADS = 128;
+constexpr int TCP_A_BYTES = kTcM * kTcKB;  // 16 KB: A, 128 rows of one 128-bit K stage
+constexpr int TCP_B_BYTES = kTcN * kTcKB;  // 32 KB: B, 256 rows
 
 __global__ void __launch_bounds__(TCP_THREADS, 1) tc_f8_peak_kernel(int iters, int *__restrict__ err) {
   extern __shared__ __align__(1024) uint8_t psm[];
   uint8_t *As = psm;
-  uint8_t *Xs = psm + TC_A_BYTES;
-  uint64_t *done = reinterpret_cast<uint64_t *>(Xs + TC_X_BYTES);
+  uint8_t *Xs = psm + TCP_A_BYTES;
+  uint64_t *done = reinterpret_cast<uint64_t *>(Xs + TCP_B_BYTES);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int i = tid; i < (TC_A_BYTES + TC_X_BYTES) / 16; i += TCP_THREADS)
+  for (int i = tid; i < (TCP_A_BYTES + TCP_B_BYTES) / 16; i += TCP_THREADS)
     reinterpret_cast<uint4 *>(psm)[i] = make_uint4(0x38383838u, 0, 0x38383838u, 0);
   if (tid == 0) {
     mbar_init(done, 1);
@@ -458,7 +491,7 @@ cudaError_t time_tc_f8_peak(double *mac_per_s, int *err_dev, cudaStream_t st) {
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int smem = TC_A_BYTES + TC_X_BYTES + 64;
+  const int smem = TCP_A_BYTES + TCP_B_BYTES + 64;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(tc_f8_peak_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
