@@ -63,8 +63,10 @@ constexpr int kGemmKTile = 8;
 // Request-operand buffers (X) are padded to a multiple of kGemmOpPad rows.
 constexpr int kGemmOpPad = 256;
 
-// tcgen05 engine tiling: CTA tile kTcM rows x kTcN requests, kTcKB bits of K
-// per pipeline stage (4 MMAs of K = 32), kTcStages stage buffers.
+// tcgen05 engine tiling: the key's FP8 image is kept in slices of kTcM rows;
+// a CTA tile is 128 requests x 2 kTcM key rows, kTcKB bits of K per pipeline
+// stage (4 MMAs of K = 32), up to kTcStages stage buffers. kTcN is the N of
+// the FP8 peak measurement (128 x 256 x 32, the engine's MMA shape).
 constexpr int kTcM = 128;
 constexpr int kTcN = 256;
 constexpr int kTcKB = 128;
