@@ -157,13 +157,13 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
     };
     // one syndrome of all 32 requests -> M planes in ring entry e (lane b < M stores plane b)
     auto to_ring = [&](uint32_t v, int e) {
-      uint32_t mine = 0;
+      uint32_t pl[M];
 #pragma unroll
-      for (int b = 0; b < M; b++) {
-        const uint32_t pl = __ballot_sync(0xffffffffu, (v >> b) & 1u);
-        mine = (lane == b) ? pl : mine;
+      for (int b = 0; b < M; b++) pl[b] = __ballot_sync(0xffffffffu, (v >> b) & 1u);
+      if (lane == 0) {  // the planes are warp-uniform: one lane stores them (no per-lane selects)
+#pragma unroll
+        for (int b = 0; b < M; b++) SP[e * M + b] = pl[b];
       }
-      if (lane < M) SP[e * M + lane] = mine;
     };
     to_ring(synd(0), 0);
     // C = 1, B = x
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kBMWarps * 32, 1) dec_bm_kernel(const uint32_t
       // this lane's request: f = d / b, the update decision
       uint32_t dq = 0;
 #pragma unroll
-      for (int b = 0; b < M; b++) dq |= ((d[b] >> lane) & 1u) << b;
+      for (int b = 0; b < M; b++) dq += ((d[b] >> lane) & 1u) << b;  // disjoint bits: the add may fuse
       const bool upd = dq != 0 && 2 * L <= n;
       uint32_t fq = 0;
       int ld = 0;
